@@ -1,0 +1,352 @@
+"""Seeded synthetic docking inputs: receptors, ligands, cleft grids, energy matrices, genes.
+
+The shapes follow the docking workloads this package is measured on:
+
+* receptor: N heavy atoms placed by Poisson-disc sampling (minimum separation 2.8 A) in a cube
+  of edge ``40 * (N / 2000) ** (1/3)`` A centred on the origin (2000 atoms at 2.8 A in a 40 A
+  cube is close to the random-sequential-addition jamming limit, so larger receptors scale the
+  cube to keep the density), with a spherical cleft carved out at the centre so the atom count
+  is exact. Types are uniform over 1..40, radii come from the per-type table below.
+* ligand: a seeded tree of heavy atoms with 1.53 A bonds and 109.5 degree angles, with a chosen
+  number of rotatable torsions among the non-terminal tree edges.
+* cleft grid: points of a 0.375 A lattice inside the cleft sphere.
+* energy matrix: symmetric ``ntypes x ntypes`` with N(0, 1) entries in fp32, single-valued
+  (area-weighted) entries.
+* genes: uniform int32 in ``[0, 2**31 - 1]``.
+
+Nothing here reads the reference; everything is reproducible from the seed.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+NTYPES = 40
+
+# Radii (A) per atom type, the SYBYL-derived table of LIB/assign_radii_types.cpp:19-146.
+# Type 2 depends on the number of covalent bonds (1.72 A below three bonds, else 1.61 A).
+# Type 40 (the solvent column of the energy matrix) has no entry in that table; 1.40 A (the
+# probe radius) is used for it here.
+_TYPE_RADIUS = {
+    1: 1.88, 3: 1.88, 4: 1.76, 5: 1.88, 6: 1.64, 7: 1.64, 8: 1.64, 9: 1.64, 10: 1.64,
+    11: 1.64, 12: 1.64, 13: 1.42, 14: 1.46, 15: 1.46, 16: 1.46, 17: 1.782, 18: 1.782,
+    19: 1.782, 20: 1.782, 21: 1.782, 22: 1.871, 23: 1.560, 24: 1.735, 25: 1.978, 26: 2.094,
+    27: 1.9, 28: 0.72, 29: 1.18, 30: 1.18, 31: 0.73, 32: 1.02, 33: 0.95, 34: 0.69, 35: 0.74,
+    36: 1.00, 37: 0.61, 38: 0.65, 39: 2.0, 40: 1.40,
+}
+
+
+def type_radius(t: int, nbonds: int = 0) -> np.float32:
+    if t == 2:
+        return np.float32(1.72 if (3 - nbonds) > 0 else 1.61)
+    return np.float32(_TYPE_RADIUS[int(t)])
+
+
+# --------------------------------------------------------------------------------------------
+# receptor
+# --------------------------------------------------------------------------------------------
+
+@dataclass
+class Receptor:
+    xyz: np.ndarray          # (N, 3) float32
+    type: np.ndarray         # (N,) int32, 1..NTYPES
+    radius: np.ndarray       # (N,) float32
+    cleft_center: np.ndarray  # (3,) float32
+    cleft_radius: float
+
+
+def poisson_disc_receptor(n_atoms: int, cleft_radius: float, seed: int,
+                          min_sep: float = 2.8, edge: float | None = None) -> Receptor:
+    """Poisson-disc sample exactly ``n_atoms`` points in a cube, excluding a central sphere.
+
+    Bridson's active-list algorithm fills the cube (minus the cleft) to a maximal set; the
+    first ``n_atoms`` accepted points are kept. Raises if the cube cannot hold that many.
+    """
+    rng = np.random.default_rng(seed)
+    if edge is None:
+        edge = 40.0 * (n_atoms / 2000.0) ** (1.0 / 3.0)
+    half = edge / 2.0
+    r2min = min_sep * min_sep
+    cell = min_sep / math.sqrt(3.0)
+    ng = int(math.ceil(edge / cell))
+    grid = -np.ones((ng, ng, ng), dtype=np.int64)
+    pts: list[np.ndarray] = []
+
+    def gidx(p):
+        return tuple(np.minimum(((p + half) / cell).astype(np.int64), ng - 1))
+
+    def ok(p):
+        if np.any(np.abs(p) > half) or float(p @ p) < cleft_radius * cleft_radius:
+            return False
+        gi = gidx(p)
+        lo = [max(0, g - 2) for g in gi]
+        hi = [min(ng, g + 3) for g in gi]
+        blk = grid[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]].ravel()
+        blk = blk[blk >= 0]
+        if blk.size == 0:
+            return True
+        q = np.asarray([pts[i] for i in blk])
+        d = q - p
+        return bool(np.all(np.einsum('ij,ij->i', d, d) >= r2min))
+
+    def add(p):
+        grid[gidx(p)] = len(pts)
+        pts.append(p)
+
+    while True:
+        p0 = rng.uniform(-half, half, 3)
+        if ok(p0):
+            add(p0)
+            break
+    active = [0]
+    k = 30
+    while active and len(pts) < n_atoms:
+        ai = int(rng.integers(len(active)))
+        base = pts[active[ai]]
+        found = False
+        # candidates in the spherical shell [r, 2r]
+        dirs = rng.normal(size=(k, 3))
+        dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+        radii = min_sep * (1.0 + rng.uniform(0.0, 1.0, k))
+        for c in base + dirs * radii[:, None]:
+            if ok(c):
+                add(c)
+                active.append(len(pts) - 1)
+                found = True
+                if len(pts) >= n_atoms:
+                    break
+        if not found:
+            active[ai] = active[-1]
+            active.pop()
+    # top up with random darts if the active list ran dry early
+    tries = 0
+    while len(pts) < n_atoms and tries < 200000:
+        c = rng.uniform(-half, half, 3)
+        if ok(c):
+            add(c)
+        tries += 1
+    if len(pts) < n_atoms:
+        raise ValueError(f"cube of edge {edge:.1f} A holds only {len(pts)} atoms at {min_sep} A")
+    xyz = np.asarray(pts[:n_atoms], dtype=np.float64).astype(np.float32)
+    types = rng.integers(1, NTYPES + 1, size=n_atoms).astype(np.int32)
+    radius = np.asarray([type_radius(t, 0) for t in types], dtype=np.float32)
+    return Receptor(xyz=xyz, type=types, radius=radius,
+                    cleft_center=np.zeros(3, np.float32), cleft_radius=float(cleft_radius))
+
+
+# --------------------------------------------------------------------------------------------
+# ligand
+# --------------------------------------------------------------------------------------------
+
+@dataclass
+class Ligand:
+    xyz: np.ndarray            # (n, 3) float32, initial pose
+    type: np.ndarray           # (n,) int32
+    radius: np.ndarray         # (n,) float32
+    bonds: list                # list of (i, j)
+    parent: np.ndarray         # (n,) int32, -1 for the root
+    rec: np.ndarray            # (n, 3) int32 reconstruction references, -1 = reference frame
+    gpa: tuple                 # three global-positioning atoms
+    flex: list = field(default_factory=list)  # per rotatable bond: atoms whose dihedral it sets
+
+
+def _place(a, b, c, bond, ang_deg, dih_deg):
+    """NeRF: position of d with |d-a| = bond, angle(d,a,b) = ang, dihedral(d,a,b,c) = dih."""
+    ang = math.radians(ang_deg)
+    dih = math.radians(dih_deg)
+    bc = a - b
+    bc /= np.linalg.norm(bc)
+    n = np.cross(b - c, bc)
+    n /= np.linalg.norm(n)
+    m = np.cross(n, bc)
+    d2 = np.array([-bond * math.cos(ang), bond * math.sin(ang) * math.cos(dih),
+                   bond * math.sin(ang) * math.sin(dih)])
+    return a + d2[0] * bc + d2[1] * m + d2[2] * n
+
+
+def random_ligand(n_atoms: int, n_torsions: int, seed: int, bond: float = 1.53,
+                  angle: float = 109.5, min_nonbonded: float = 2.6,
+                  center=(0.0, 0.0, 0.0)) -> Ligand:
+    """Seeded random tree ligand with ``n_torsions`` rotatable bonds.
+
+    Atoms 0-1-2 form the global-positioning chain. Reconstruction references follow a
+    Z-matrix: (parent, grandparent, great-grandparent), with atoms 0, 1, 2 standing in where
+    the chain is too short, so that every atom moves rigidly with the positioning frame.
+    A small tree may offer fewer non-terminal bonds than requested; it then gets them all.
+    """
+    if n_atoms < 4:
+        raise ValueError("ligands need at least 4 atoms")
+    rng = np.random.default_rng(seed)
+    for _attempt in range(400):
+        parent = np.full(n_atoms, -1, np.int64)
+        deg = np.zeros(n_atoms, np.int64)
+        parent[1] = 0
+        parent[2] = 1
+        deg[0] = 1
+        deg[1] = 2
+        deg[2] = 1
+        okt = True
+        for i in range(3, n_atoms):
+            # drug-like shapes: at most three heavy neighbours, attachment biased towards
+            # recently added atoms so that large ligands stay elongated rather than bushy
+            cand = np.nonzero(deg[:i] < 3)[0]
+            if cand.size == 0:
+                okt = False
+                break
+            w = 0.6 ** (i - 1 - cand).astype(np.float64)
+            p = int(rng.choice(cand, p=w / w.sum()))
+            parent[i] = p
+            deg[p] += 1
+            deg[i] = 1
+        if not okt:
+            continue
+        children = [[] for _ in range(n_atoms)]
+        for i in range(1, n_atoms):
+            children[parent[i]].append(i)
+        # rotatable bonds (G, P): P a non-terminal child of G, excluding the 0-1 bond whose
+        # torsion is a rigid-body gene.
+        eligible = [(int(parent[p]), p) for p in range(2, n_atoms)
+                    if children[p] and not (parent[p] == 0 and p == 1)]
+        if len(eligible) < n_torsions and _attempt < 100:
+            continue
+        n_tor = min(n_torsions, len(eligible))
+        # reconstruction references
+        rec = np.full((n_atoms, 3), -1, np.int64)
+        rec[1] = (0, -1, -1)
+        rec[2] = (1, 0, -1)
+        for x in range(3, n_atoms):
+            p = parent[x]
+            if p == 0:
+                rec[x] = (0, 1, 2)
+            elif parent[p] == 0:
+                rec[x] = (1, 0, 2) if p == 1 else (p, 0, 1)
+            else:
+                g = parent[p]
+                rec[x] = (p, g, parent[g])
+        # coordinates: BFS order guarantees references are placed first
+        order = [0]
+        head = 0
+        while head < len(order):
+            for c in children[order[head]]:
+                order.append(c)
+            head += 1
+        adj = [set() for _ in range(n_atoms)]
+        for i in range(1, n_atoms):
+            adj[i].add(int(parent[i]))
+            adj[int(parent[i])].add(i)
+        near = [set([i]) | adj[i] | set().union(*[adj[j] for j in adj[i]]) for i in range(n_atoms)]
+        placed_ok = False
+        for _geo in range(8):
+            xyz = np.zeros((n_atoms, 3))
+            xyz[0] = center
+            xyz[1] = xyz[0] + np.array([bond, 0.0, 0.0])
+            th = math.radians(angle)
+            xyz[2] = xyz[1] + bond * np.array([-math.cos(th), math.sin(th), 0.0])
+            placed = [0, 1, 2]
+            failed = False
+            # place the children of each parent together, retrying the sibling base dihedral
+            # until none of them comes closer than min_nonbonded to an already placed atom
+            for p in order:
+                kids = [x for x in children[p] if x >= 3]
+                if not kids:
+                    continue
+                good = None
+                for _try in range(16):
+                    if p == 0:
+                        dset = [60.0, 180.0, 300.0]
+                    elif p == 1:
+                        dset = [120.0, 240.0]
+                    else:
+                        b0 = float(rng.choice([60.0, 180.0, 300.0])) + float(rng.uniform(-30, 30))
+                        dset = [b0, b0 + 120.0, b0 + 240.0]
+                    pos = []
+                    for s, x in enumerate(kids):
+                        r0, r1, r2 = rec[x]
+                        dih = dset[s % len(dset)] + float(rng.uniform(-8.0, 8.0))
+                        pos.append(_place(xyz[r0], xyz[r1], xyz[r2], bond, angle, dih))
+                    clash = False
+                    for s, x in enumerate(kids):
+                        others = [q for q in placed if q not in near[x]]
+                        others += [kids[t] for t in range(s) if kids[t] not in near[x]]
+                        if others:
+                            q = np.asarray([xyz[o] if o in placed else pos[kids.index(o)] for o in others])
+                            if np.min(np.linalg.norm(q - pos[s], axis=1)) < min_nonbonded:
+                                clash = True
+                                break
+                    if not clash:
+                        good = pos
+                        break
+                if good is None:
+                    failed = True
+                    break
+                for s, x in enumerate(kids):
+                    xyz[x] = good[s]
+                    placed.append(x)
+            if not failed:
+                placed_ok = True
+                break
+        if not placed_ok:
+            continue
+        pick = rng.choice(len(eligible), size=n_tor, replace=False) if n_tor else []
+        flex = []
+        for k in sorted(int(i) for i in pick):
+            g, p = eligible[k]
+            flex.append(sorted(children[p])[:3])
+        bonds = [(int(parent[i]), i) for i in range(1, n_atoms)]
+        nb = np.bincount(np.asarray([b for e in bonds for b in e]), minlength=n_atoms)
+        types = rng.integers(1, NTYPES + 1, size=n_atoms).astype(np.int32)
+        radius = np.asarray([type_radius(t, int(nb[i])) for i, t in enumerate(types)], np.float32)
+        return Ligand(xyz=xyz.astype(np.float32), type=types, radius=radius, bonds=bonds,
+                      parent=parent.astype(np.int32), rec=rec.astype(np.int32), gpa=(0, 1, 2),
+                      flex=flex)
+    raise RuntimeError("could not generate a ligand with the requested torsions")
+
+
+# --------------------------------------------------------------------------------------------
+# cleft grid, energy matrix, genes
+# --------------------------------------------------------------------------------------------
+
+def cleft_grid(center, radius: float, spacing: float = 0.375) -> np.ndarray:
+    """Lattice points strictly inside one cleft sphere, in the reference's scan order.
+
+    Follows LIB/generate_grid.cpp:32-95 for a single sphere: the lattice starts at
+    ``(int)((c - r) / s) * s`` per axis and runs while below ``((int)((c + r) / s) + 1) * s``,
+    x fastest, keeping points with float squared distance below ``r * r``.
+    """
+    s = np.float32(spacing)
+    c = np.asarray(center, np.float32)
+    r = np.float32(radius)
+    inv = np.float32(1.0) / s
+    if float(inv - np.float32(int(inv))) <= 0.001:
+        raise NotImplementedError("integer 1/spacing lattices are not generated here")
+    lo = np.asarray([np.float32(int((float(c[k]) - float(r)) / float(s))) * s for k in range(3)], np.float32)
+    hi = np.asarray([np.float32(int((float(c[k]) + float(r)) / float(s)) + 1.0) * s for k in range(3)], np.float32)
+    axes = []
+    for k in range(3):
+        vals = []
+        v = lo[k]
+        while v < hi[k]:
+            vals.append(v)
+            v = np.float32(v + s)
+        axes.append(np.asarray(vals, np.float32))
+    z, y, x = np.meshgrid(axes[2], axes[1], axes[0], indexing='ij')
+    pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1).astype(np.float32)
+    d = pts - c
+    d2 = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]).astype(np.float32)
+    d2 = (d2 + d[:, 2] * d[:, 2]).astype(np.float32)
+    keep = d2 < np.float32(r * r)
+    return pts[keep]
+
+
+def energy_matrix(seed: int, ntypes: int = NTYPES) -> np.ndarray:
+    """Symmetric ntypes x ntypes matrix of N(0, 1) fp32 single values."""
+    rng = np.random.default_rng(seed)
+    m = rng.normal(size=(ntypes, ntypes)).astype(np.float32)
+    return np.triu(m) + np.triu(m, 1).T
+
+
+def random_genes(n_chrom: int, n_genes: int, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    return rng.integers(0, 2 ** 31, size=(n_chrom, n_genes), dtype=np.int64).astype(np.int32)

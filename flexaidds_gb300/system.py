@@ -1,0 +1,167 @@
+"""Docking-system descriptors: everything the evaluation path reads, as flat arrays.
+
+A ``Descriptor`` is the packed form of the reference's set-up state for one receptor, one
+ligand and one energy matrix (the FA / atoms / residue / cleft-grid / gene-limit data that
+LIB/ic2cf.cpp, LIB/buildcc.cpp, LIB/vcfunction.cpp and LIB/Vcontacts.cpp read). It crosses the
+C ABI as ``fxe_receptor_desc`` / ``fxe_ligand_desc`` / ``fxe_emat_desc`` (include/fxe.h).
+
+Atom numbering follows the reference's ``Calc`` order (LIB/Vcontacts.cpp:1600-1630): receptor
+atoms first in residue order, then the ligand atoms. Ligand-local indices are used inside the
+ligand arrays, with -1 standing for the reference frame (``rec == 0`` in the reference).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import synth
+
+# gene types (optmap.typ, LIB/flexaid.h:175-180 / LIB/ic2cf.cpp:56-105)
+GENE_GRID = -1
+GENE_DIS = 0
+GENE_ANG = 1
+GENE_DIH = 2
+GENE_ROTAMER = 4
+
+
+@dataclass
+class SystemInputs:
+    """Raw generator output for one docking system (no set-up applied yet)."""
+    receptor: synth.Receptor
+    ligand: synth.Ligand
+    grid_xyz: np.ndarray                 # (M, 3) float32, cleft points (entry 0 not included)
+    emat: np.ndarray                     # (T, T) float32 single values
+    emat_weight: np.ndarray = None       # (T, T) int32, 1 = single value, 0 = density curve
+    emat_curves: dict = None             # {(i, j): [(x, y), ...]} for density entries (0-based types)
+    permeability: float = 1.0
+    dee_clash: float = 0.5
+    intramolecular: int = 1
+    solventterm: float = 0.0
+
+    def __post_init__(self):
+        t = self.emat.shape[0]
+        if self.emat_weight is None:
+            self.emat_weight = np.ones((t, t), np.int32)
+        if self.emat_curves is None:
+            self.emat_curves = {}
+
+    def emat_tables(self):
+        """Flat (weight, offsets, x, y) arrays in the reference's energy_values layout."""
+        t = self.emat.shape[0]
+        off = [0]
+        xs, ys = [], []
+        for i in range(t):
+            for j in range(t):
+                if self.emat_weight[i, j]:
+                    xs.append(-1.0)
+                    ys.append(float(self.emat[i, j]))
+                else:
+                    pts = self.emat_curves[(min(i, j), max(i, j))]
+                    for x, y in pts:
+                        xs.append(float(x))
+                        ys.append(float(y))
+                off.append(len(xs))
+        return (np.ascontiguousarray(self.emat_weight.reshape(-1), np.int32),
+                np.asarray(off, np.int32), np.asarray(xs, np.float32), np.asarray(ys, np.float32))
+
+
+@dataclass
+class Descriptor:
+    """Packed set-up state (the evaluation path's whole input besides the chromosomes)."""
+    # receptor (Calc order)
+    rec_xyz: np.ndarray
+    rec_radius: np.ndarray
+    rec_type: np.ndarray
+    ori: np.ndarray
+    globalmin: np.ndarray
+    globalmax: np.ndarray
+    maxwidth: float
+    grid_ic: np.ndarray          # (n_grid, 3) dis, ang, dih; entry 0 = initial anchor
+    # ligand
+    lig_radius: np.ndarray
+    lig_type: np.ndarray
+    lig_rec: np.ndarray          # (n, 4) int32, -1 = reference frame / no cascade
+    lig_shift: np.ndarray
+    lig_ic: np.ndarray           # (n, 3) base dis, ang, dih
+    build_order: np.ndarray      # (n_mov,) int32 (FA->mov[0])
+    bonded: np.ndarray           # (n, n) int8
+    gene_typ: np.ndarray
+    gene_atm: np.ndarray
+    gene_min: np.ndarray
+    gene_max: np.ndarray
+    gene_del: np.ndarray
+    gene_map: np.ndarray
+    opt_par: np.ndarray          # initial ICs
+    # energy matrix
+    ntypes: int
+    emat_weight: np.ndarray
+    emat_off: np.ndarray
+    emat_x: np.ndarray
+    emat_y: np.ndarray
+    # scoring parameters
+    permeability: float = 1.0
+    dee_clash: float = 0.5
+    intramolecular: int = 1
+    solventterm: float = 0.0
+    decode: list = field(default_factory=list)
+
+    @property
+    def n_rec(self):
+        return int(self.rec_xyz.shape[0])
+
+    @property
+    def n_lig(self):
+        return int(self.lig_radius.shape[0])
+
+    @property
+    def n_genes(self):
+        return int(self.gene_typ.shape[0])
+
+    def decode_tables(self):
+        """Cumulative-bin tables for genetoic, one per gene (see ``gene_bins``)."""
+        if not self.decode:
+            self.decode = [gene_bins(self.gene_min[g], self.gene_max[g], self.gene_del[g],
+                                     int(self.gene_map[g])) for g in range(self.n_genes)]
+        return self.decode
+
+    def genes_to_ic(self, genes: np.ndarray) -> np.ndarray:
+        """Decode int32 genes to ICs exactly as LIB/gaboom.cpp:2887-2906 (genetoic) does."""
+        genes = np.asarray(genes, np.int32)
+        out = np.empty(genes.shape, np.float64)
+        for g, tab in enumerate(self.decode_tables()):
+            u = genes[..., g].astype(np.float64) / (2147483647.0 + 1.0)
+            i = np.searchsorted(tab, u, side='left')
+            out[..., g] = self.gene_min[g] + self.gene_del[g] * i.astype(np.float64)
+        return out
+
+
+def gene_bins(gmin: float, gmax: float, gdel: float, gmap: int) -> np.ndarray:
+    """Running bin totals of genetoic: T[0] = bin, T[k+1] = T[k] + bin (double, in order).
+
+    ``set_bins`` (LIB/gaboom.cpp:2295-2308) gives ``nbin = (max - min) / del``, rounded up,
+    plus one for mapped (index) genes, and ``bin = 1 / nbin``. genetoic walks ``tot += bin``
+    while ``tot < u``; the index it stops at is the first k with ``T[k] >= u``. The table is
+    extended until it reaches 1.0 so that every u in [0, 1) lands inside it.
+    """
+    nbin = (gmax - gmin) / gdel
+    if nbin - int(nbin) > 0.0:
+        nbin += 1.0
+    if gmap:
+        nbin += 1.0
+    b = 1.0 / nbin
+    n = int(nbin) + 4
+    t = np.cumsum(np.full(n, b, np.float64))   # numpy cumsum adds strictly left to right
+    while t[-1] < 1.0:
+        t = np.concatenate([t, t[-1] + np.cumsum(np.full(4, b))])
+    return t
+
+
+def make_inputs(n_rec: int, cleft_radius: float, n_lig: int, n_tor: int, seed: int,
+                spacing: float = 0.375) -> SystemInputs:
+    """One seeded docking system of the given shape."""
+    rec = synth.poisson_disc_receptor(n_rec, cleft_radius, seed=seed)
+    lig = synth.random_ligand(n_lig, n_tor, seed=seed + 1)
+    grid = synth.cleft_grid(rec.cleft_center, cleft_radius, spacing)
+    emat = synth.energy_matrix(seed + 2)
+    return SystemInputs(receptor=rec, ligand=lig, grid_xyz=grid, emat=emat)

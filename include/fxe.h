@@ -1,0 +1,168 @@
+/* fxe.h — C ABI of the GB300 fitness-evaluation backend for FlexAID∆S-style docking.
+ *
+ * One call scores a batch of chromosomes: gene decode -> pose build -> receptor cell list ->
+ * Voronoi contact surfaces -> energy-matrix complementarity with wall/clash terms, returning
+ * the reference's complementarity-function record (cfstr) per pose; a second entry point
+ * reduces an ensemble of pose energies to its canonical-ensemble thermodynamics in FP64.
+ *
+ * Plain C: plain pointers and sizes, status codes, no exceptions cross this boundary.
+ * All entry points are thread-safe except that one fxe_context must not be used by two
+ * threads at once (it owns one CUDA stream).
+ */
+#ifndef FXE_H
+#define FXE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes; mirror hw::DispatchError (LIB/UnifiedHardwareDispatch.h:63-72) in place of
+ * the exceptions the reference's CUDA backend throws from CUDA_CHECK
+ * (LIB/cuda_eval.cu:38-45, 318-326). */
+typedef enum fxe_status {
+    FXE_OK = 0,
+    FXE_ERR_INVALID_ARGS = 1,
+    FXE_ERR_ALLOC = 2,
+    FXE_ERR_LAUNCH = 3,
+    FXE_ERR_TIMEOUT = 4,
+    FXE_ERR_OVER_BUDGET = 5,
+    FXE_ERR_CAPACITY = 6,   /* a pose exceeded a fixed per-atom capacity; see fxe_cf.status */
+    FXE_ERR_NO_DEVICE = 7,
+    FXE_ERR_INTERNAL = 8
+} fxe_status;
+
+/* Receptor, in the reference's Calc order (residue order, LIB/Vcontacts.cpp:1600-1630),
+ * plus the state LIB/calc_center.cpp:8-61 leaves in FA and the cleft grid of
+ * LIB/generate_grid.cpp / LIB/calc_cleftic.cpp. */
+typedef struct fxe_receptor_desc {
+    int32_t n_atoms;
+    const float* xyz;          /* n_atoms * 3 */
+    const float* radius;       /* n_atoms */
+    const int32_t* type;       /* n_atoms, 1..ntypes */
+    float ori[3];              /* FA->ori: frame origin for unreferenced build atoms */
+    float globalmin[3];        /* FA->globalmin */
+    float globalmax[3];        /* FA->globalmax */
+    float maxwidth;            /* FA->maxwidth */
+    int32_t n_grid;            /* cleft grid entries including entry 0 (initial anchor) */
+    const float* grid_ic;      /* n_grid * 3: dis, ang, dih of each grid point */
+} fxe_receptor_desc;
+
+/* Ligand build tree and genes (atoms/residue/FA->map_par after the reference set-up:
+ * LIB/read_lig.cpp, LIB/assign_shift.cpp, LIB/add2_optimiz_vec.cpp, LIB/create_rebuild_list.cpp).
+ * Atom indices are ligand-local (0..n_atoms-1); -1 stands for the reference frame
+ * (rec == 0 in the reference) or, in rec[3], for "no dihedral cascade". */
+typedef struct fxe_ligand_desc {
+    int32_t n_atoms;
+    const float* radius;       /* n_atoms */
+    const int32_t* type;       /* n_atoms */
+    const int32_t* rec;        /* n_atoms * 4: rec[0..2] build references, rec[3] cascade */
+    const float* shift;        /* n_atoms: dihedral shift along the rec[3] cycle */
+    const float* ic;           /* n_atoms * 3: base dis, ang, dih */
+    int32_t n_build;
+    const int32_t* build_order;/* n_build: FA->mov[0] */
+    const int8_t* bonded;      /* n_atoms * n_atoms: residue.bonded (-1: not within bloops) */
+    int32_t n_genes;
+    const int32_t* gene_type;  /* optmap.typ: -1 grid index, 0 dis, 1 ang, 2 dih */
+    const int32_t* gene_atom;  /* optmap.atm, ligand-local */
+    const double* gene_min;    /* genlim.min / max / del / map (LIB/gaboom.cpp:2491-2507) */
+    const double* gene_max;
+    const double* gene_del;
+    const int32_t* gene_map;
+} fxe_ligand_desc;
+
+/* Energy matrix (LIB/flexaid.h:155-166, read by LIB/read_emat.cpp): per ordered type pair a
+ * weight flag and a piecewise-linear curve; single-valued (weight = 1) entries use curve_y of
+ * their one point. */
+typedef struct fxe_emat_desc {
+    int32_t ntypes;
+    const int32_t* weight;     /* ntypes * ntypes */
+    const int32_t* offset;     /* ntypes * ntypes + 1 */
+    const float* x;
+    const float* y;
+} fxe_emat_desc;
+
+/* Scoring switches read by LIB/vcfunction.cpp (FA->permeability, dee_clash, intramolecular,
+ * solventterm). The optional terms (useacs, normalize_area, electrostatics, H-bonds, GIST,
+ * metal coordination, constraints) are off, as in the reference defaults (LIB/top.cpp:233-330). */
+typedef struct fxe_params {
+    float permeability;
+    float dee_clash;
+    int32_t intramolecular;
+    float solventterm;
+} fxe_params;
+
+/* Per-pose outcome: the reference's cfstr (LIB/flexaid.h:122-135) plus the evalue of
+ * get_cf_evalue (LIB/ic2cf.cpp:396-401) and how the pose ended. */
+typedef struct fxe_cf {
+    double com, con, wal, sas, elec, gist, hbond, gist_desolv, metal_coord, totsas;
+    double evalue;
+    int32_t rclash;
+    int32_t status;            /* FXE_POSE_* */
+} fxe_cf;
+
+enum {
+    FXE_POSE_SCORED = 0,
+    FXE_POSE_POLYHEDRON_FAILED = 1, /* LIB/vcfunction.cpp:68-71: wal = 1e6 */
+    FXE_POSE_CLASHED = 2,           /* LIB/vcfunction.cpp:72-74: wal = clash sum >= 1e4 */
+    FXE_POSE_CAPACITY = 3           /* exceeded a fixed per-atom workspace; not scored */
+};
+
+/* Canonical-ensemble thermodynamics (LIB/statmech.h:36-48, LIB/statmech.cpp:73-174). */
+typedef struct fxe_thermo {
+    double temperature, log_Z, free_energy, mean_energy, mean_energy_sq, heat_capacity,
+           entropy, std_energy;
+} fxe_thermo;
+
+typedef struct fxe_context fxe_context;
+
+/* Creates an evaluation context on the current CUDA device: copies the descriptors into
+ * device memory, builds the receptor cell list and the gene decode tables, and reserves
+ * workspace for up to max_poses poses per call. Replaces cuda_eval_init
+ * (LIB/cuda_eval.cuh:46-58) and GPUContextPool::acquire_cuda (LIB/GPUContextPool.h:56-100). */
+fxe_status fxe_context_create(const fxe_receptor_desc* receptor, const fxe_ligand_desc* ligand,
+                              const fxe_emat_desc* emat, const fxe_params* params,
+                              int32_t max_poses, fxe_context** out);
+
+/* Scores n chromosomes given as int32 genes (n * n_genes, host memory), writing n records to
+ * host memory. Synchronous, like cuda_eval_batch (LIB/cuda_eval.cuh:60-70). */
+fxe_status fxe_eval_genes(fxe_context* ctx, int32_t n, const int32_t* genes, fxe_cf* out);
+
+/* Same, for chromosomes given as decoded internal coordinates (n * n_genes doubles), the
+ * icv vector that eval_chromosome hands to ic2cf (LIB/gaboom.cpp:1845-1866). */
+fxe_status fxe_eval_ic(fxe_context* ctx, int32_t n, const double* ic, fxe_cf* out);
+
+/* Device-resident form: genes and out are device pointers; work is queued on `stream`
+ * (a cudaStream_t, or NULL for the context's own stream) and not waited for. */
+fxe_status fxe_eval_genes_device(fxe_context* ctx, int32_t n, const int32_t* d_genes,
+                                 fxe_cf* d_out, void* stream);
+
+/* Contacts recorded for the last evaluated batch (the ca_rec lists vcfunction walks), for
+ * inspection and parity checks: for pose p and ligand atom a, up to cap entries of
+ * (partner Calc index, area). Returns the count through *n_out. */
+fxe_status fxe_last_contacts(fxe_context* ctx, int32_t pose, int32_t ligand_atom, int32_t cap,
+                             int32_t* partner, float* area, int32_t* n_out);
+
+/* Thermodynamics of an ensemble of n energies (kcal/mol) with multiplicities (NULL = all 1)
+ * at temperature T (K), reduced on the device in FP64: StatMechEngine::compute. The arrays
+ * are host memory. */
+fxe_status fxe_thermo_compute(const double* energies, const int32_t* multiplicity, int64_t n,
+                              double temperature, fxe_thermo* out);
+
+/* Boltzmann weights p_i = n_i exp(-beta E_i) / Z of the same ensemble
+ * (StatMechEngine::boltzmann_weights, LIB/statmech.cpp:178-201). */
+fxe_status fxe_thermo_weights(const double* energies, const int32_t* multiplicity, int64_t n,
+                              double temperature, double* weights);
+
+void fxe_context_destroy(fxe_context* ctx);
+
+/* Message describing the last error on the calling thread ("" if none). */
+const char* fxe_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FXE_H */
