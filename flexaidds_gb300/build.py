@@ -1,0 +1,55 @@
+"""Builds the CUDA backend in-tree: flexaidds_gb300/libfxe.so (sm_103a)."""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libfxe.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# (source, extra flags): the pose build is evaluated without fused multiply-adds, like the
+# reference's single-precision build
+UNITS = [("fxe_build.cu", ["--fmad=false"]), ("fxe_voronoi.cu", []), ("fxe_thermo.cu", []),
+         ("fxe_capi.cu", [])]
+
+
+def nvcc() -> str:
+    p = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(p):
+        raise FileNotFoundError("nvcc not found")
+    return p
+
+
+def _compile(unit):
+    src, extra = unit
+    obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+           "-Xptxas", "-v" if os.environ.get("FXE_PTXAS_VERBOSE") else "-O3", *extra,
+           "-c", os.path.join(CSRC, src), "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+    return obj, r.stderr
+
+
+def build(verbose: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        res = list(ex.map(_compile, UNITS))
+    if verbose:
+        for _, log in res:
+            sys.stderr.write(log)
+    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *[o for o, _ in res], "-cudart", "static"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,236 @@
+// fxe_build.cu — gene decode, IC assignment and pose build, one warp per pose.
+//
+// Compiled with --fmad=false: the single-precision build arithmetic is evaluated exactly as
+// written (no fused multiply-adds), like the reference's buildcc (LIB/buildcc.cpp:6-134).
+//
+// Per pose:
+//   1. genes -> ICs: genetoic (LIB/gaboom.cpp:2887-2906) as a binary search in the running
+//      bin totals the host precomputes, then the clamp of eval_chromosome
+//      (LIB/gaboom.cpp:1845-1866);
+//   2. IC assignment of ic2cf (LIB/ic2cf.cpp:53-105): grid index, angle, dihedral with the
+//      rec[3] cascade;
+//   3. buildcc over the rebuild list;
+//   4. the cell grid of index_protein for this pose (LIB/Vcontacts.cpp:1584-1645: the
+//      receptor's steady grid, re-derived when a ligand atom leaves the receptor's box), the
+//      ligand atoms' cells and their position in Calclist order (cell, then Calc index).
+#include "fxe_common.cuh"
+
+namespace fxe {
+
+constexpr int kBuildWarps = 4;
+
+struct BuildShared {
+    float ic[kMaxLig][3];
+    float pos[kMaxLig][3];
+    int cell[kMaxLig];
+    double icv[64];
+    int bad;
+};
+
+__global__ void __launch_bounds__(kBuildWarps * 32)
+build_kernel(DevSystem S, DevWork W, int n, const int32_t* __restrict__ genes,
+             const double* __restrict__ ic_in) {
+    __shared__ BuildShared sh_all[kBuildWarps];
+    const int wib = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int p = blockIdx.x * kBuildWarps + wib;
+    if (p >= n) return;
+    BuildShared& sh = sh_all[wib];
+    const int ng = S.n_genes, nl = S.n_lig;
+
+    // 1. decode + clamp
+    for (int g = lane; g < ng; g += 32) {
+        double v;
+        if (genes) {
+            const double u = genes[(size_t)p * ng + g] / (2147483647.0 + 1.0);
+            int lo = S.dec_off[g], hi = S.dec_off[g + 1];
+            const int base = lo;
+            while (lo < hi) {  // first entry >= u
+                const int mid = (lo + hi) >> 1;
+                if (S.dec_tab[mid] < u) lo = mid + 1; else hi = mid;
+            }
+            v = S.gene_min[g] + S.gene_del[g] * (double)(lo - base);
+        } else {
+            v = ic_in[(size_t)p * ng + g];
+        }
+        if (v > S.gene_max[g]) v = S.gene_max[g];
+        else if (v < S.gene_min[g]) v = S.gene_min[g];
+        W.ic[(size_t)p * ng + g] = v;
+        if (g < 64) sh.icv[g] = v;
+    }
+    for (int l = lane; l < nl; l += 32) {
+        const float4 b = S.lig_ic[l];
+        sh.ic[l][0] = b.x;
+        sh.ic[l][1] = b.y;
+        sh.ic[l][2] = b.z;
+    }
+    if (lane == 0) sh.bad = 0;
+    __syncwarp();
+
+    if (lane == 0) {
+        // 2. IC assignment, genes in order
+        for (int g = 0; g < ng; ++g) {
+            const double v = g < 64 ? sh.icv[g] : W.ic[(size_t)p * ng + g];
+            const int atm = S.gene_atom[g];
+            switch (S.gene_type[g]) {
+            case -1: {
+                const unsigned gi = (unsigned)v;
+                if (gi >= (unsigned)S.n_grid) { sh.bad = 1; break; }
+                const float4 c = S.grid_ic[gi];
+                sh.ic[atm][0] = c.x;
+                sh.ic[atm][1] = c.y;
+                sh.ic[atm][2] = c.z;
+                break;
+            }
+            case 0: sh.ic[atm][0] = (float)v; break;
+            case 1: sh.ic[atm][1] = (float)v; break;
+            case 2: {
+                sh.ic[atm][2] = (float)v;
+                int j = atm, cat = S.lig_rec[atm].w, guard = 0;
+                if (cat >= 0) {
+                    while (cat != atm && guard++ <= nl) {
+                        sh.ic[cat][2] = sh.ic[j][2] + S.lig_shift[cat];
+                        j = cat;
+                        cat = S.lig_rec[j].w;
+                    }
+                }
+                break;
+            }
+            default: break;
+            }
+        }
+        // 3. buildcc over the rebuild list
+        const float* ori = S.ori;
+        for (int an = 0; an < S.n_build; ++an) {
+            const int l = S.build_order[an];
+            const int4 r = S.lig_rec[l];
+            const int ref[3] = {r.x, r.y, r.z};
+            float x[4], y[4], z[4];
+            for (int i = 1; i <= 3; ++i) {
+                const int j = ref[i - 1];
+                if (j >= 0) {
+                    x[i] = sh.pos[j][0];
+                    y[i] = sh.pos[j][1];
+                    z[i] = sh.pos[j][2];
+                } else if (i == 1) {
+                    x[i] = 1.0f + ori[0];
+                    y[i] = 0.0f + ori[1];
+                    z[i] = 0.0f + ori[2];
+                } else if (i == 3) {
+                    x[i] = 0.0f + ori[0];
+                    y[i] = 1.0f + ori[1];
+                    z[i] = 0.0f + ori[2];
+                } else {
+                    x[i] = 0.0f + ori[0];
+                    y[i] = 0.0f + ori[1];
+                    z[i] = 0.0f + ori[2];
+                }
+                x[i] += 1e-10f;
+                y[i] += 1e-10f;
+                z[i] += 1e-10f;
+            }
+            float a = y[1] * (z[2] - z[3]) + y[2] * (z[3] - z[1]) + y[3] * (z[1] - z[2]);
+            float b = z[1] * (x[2] - x[3]) + z[2] * (x[3] - x[1]) + z[3] * (x[1] - x[2]);
+            float c = x[1] * (y[2] - y[3]) + x[2] * (y[3] - y[1]) + x[3] * (y[1] - y[2]);
+            float op = sqrtf(a * a + b * b + c * c);
+            float cx = a / op, cy = b / op, cz = c / op;
+            a = x[2] - x[1];
+            b = y[2] - y[1];
+            c = z[2] - z[1];
+            const float d = 1.0f / sqrtf(a * a + b * b + c * c);
+            op = sh.ic[l][0] * d;
+            const float xn = a * op, yn = b * op, zn = c * op;
+            a = cx * cx;
+            b = cy * cy;
+            c = cz * cz;
+            const float angPI = (float)(sh.ic[l][1] * kPi / 180.0f);
+            float ct = cosf(angPI), st = -sinf(angPI);
+            op = 1.0f - ct;
+            const float xk = (cx * cz * op - cy * st) * zn + ((1.0f - a) * ct + a) * xn + (cx * cy * op + cz * st) * yn;
+            const float yk = (cy * cx * op - cz * st) * xn + ((1.0f - b) * ct + b) * yn + (cy * cz * op + cx * st) * zn;
+            const float zk = (cz * cy * op - cx * st) * yn + ((1.0f - c) * ct + c) * zn + (cz * cx * op + cy * st) * xn;
+            const float dihPI = (float)(sh.ic[l][2] * kPi / 180.0f);
+            ct = cosf(dihPI);
+            st = sinf(dihPI);
+            op = 1.0f - ct;
+            cx = (x[2] - x[1]) * d;
+            cy = (y[2] - y[1]) * d;
+            cz = (z[2] - z[1]) * d;
+            a = cx * cx;
+            b = cy * cy;
+            c = cz * cz;
+            sh.pos[l][0] = (cx * cz * op - cy * st) * zk + ((1.0f - a) * ct + a) * xk + (cx * cy * op + cz * st) * yk + x[1];
+            sh.pos[l][1] = (cy * cx * op - cz * st) * xk + ((1.0f - b) * ct + b) * yk + (cy * cz * op + cx * st) * zk + y[1];
+            sh.pos[l][2] = (cz * cy * op - cx * st) * yk + ((1.0f - c) * ct + c) * zk + (cz * cx * op + cy * st) * xk + z[1];
+        }
+    }
+    __syncwarp();
+
+    // 4. cell grid of this pose
+    bool below[3] = {false, false, false}, above[3] = {false, false, false};
+    float mn[3] = {S.gmin[0], S.gmin[1], S.gmin[2]};
+    float mx[3] = {S.gmax[0], S.gmax[1], S.gmax[2]};
+    for (int l = lane; l < nl; l += 32)
+        for (int k = 0; k < 3; ++k) {
+            const float v = sh.pos[l][k];
+            if (v < mn[k]) { mn[k] = v; below[k] = true; }
+            else if (v > mx[k]) { mx[k] = v; above[k] = true; }
+        }
+    bool alter = false;
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+            mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+        }
+        alter |= __any_sync(0xffffffffu, below[k] || above[k]);
+    }
+    float gmin[3];
+    int dim;
+    if (alter) {
+        float mw = S.maxwidth;
+        for (int k = 0; k < 3; ++k) {
+            gmin[k] = mn[k] < 0.0f ? (float)((int)mn[k] - 1.0) : (float)((int)mn[k] + 1.0);
+            const float gmx = mx[k] < 0.0f ? (float)((int)mx[k] - 1.0) : (float)((int)mx[k] + 1.0);
+            const float diff = gmx - gmin[k];
+            if (diff > mw) mw = diff;
+        }
+        dim = (int)(mw / kCell) + 1;
+    } else {
+        gmin[0] = S.gmin[0];
+        gmin[1] = S.gmin[1];
+        gmin[2] = S.gmin[2];
+        dim = S.dim;
+    }
+    const int dim2 = dim * dim, dim3 = dim2 * dim;
+    for (int l = lane; l < nl; l += 32) {
+        const int bi = (int)((sh.pos[l][0] - gmin[0]) / kCell) * dim2 + (int)((sh.pos[l][1] - gmin[1]) / kCell) * dim +
+                       (int)((sh.pos[l][2] - gmin[2]) / kCell);
+        if (bi < 0 || bi >= dim3) sh.bad = 2;
+        sh.cell[l] = bi;
+    }
+    __syncwarp();
+    const size_t base = (size_t)p * nl;
+    for (int l = lane; l < nl; l += 32) {
+        const int c = sh.cell[l];
+        int rank = 0;
+        for (int m = 0; m < nl; ++m) {
+            const int cm = sh.cell[m];
+            rank += (cm < c) || (cm == c && m < l);
+        }
+        W.lig_pos[base + l] = make_float4(sh.pos[l][0], sh.pos[l][1], sh.pos[l][2], S.lig_radius[l]);
+        W.lig_cell[base + l] = c;
+        W.lig_rank[base + l] = rank;
+    }
+    if (lane == 0) {
+        W.pose_grid[p] = make_int4(alter ? 1 : 0, dim, sh.bad, 0);
+        W.pose_gmin[p] = make_float4(gmin[0], gmin[1], gmin[2], 0.0f);
+    }
+}
+
+void launch_build(const DevSystem& S, const DevWork& W, int n, const int32_t* genes,
+                  const double* ic, cudaStream_t st) {
+    const int blocks = (n + kBuildWarps - 1) / kBuildWarps;
+    build_kernel<<<blocks, kBuildWarps * 32, 0, st>>>(S, W, n, genes, ic);
+}
+
+}  // namespace fxe

@@ -1,0 +1,475 @@
+// fxe_capi.cu — host side of the C ABI declared in include/fxe.h.
+//
+// A context owns the device copies of one receptor (with its cell list), one ligand (build
+// tree, genes, decode tables) and one energy matrix, a workspace for max_poses poses and one
+// CUDA stream. Batches larger than max_poses are scored in chunks.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "fxe_common.cuh"
+
+namespace fxe {
+void launch_build(const DevSystem&, const DevWork&, int, const int32_t*, const double*, cudaStream_t);
+void launch_contacts(const DevSystem&, const DevWork&, int, cudaStream_t);
+void launch_voronoi(const DevSystem&, const DevWork&, int, cudaStream_t);
+void launch_score(const DevSystem&, const DevWork&, int, cudaStream_t);
+cudaError_t configure_voronoi();
+int thermo_blocks(long, int);
+void launch_thermo_partial(const double*, const int32_t*, long, double, LsePart*, int, cudaStream_t);
+void launch_thermo_weights(const double*, const int32_t*, long, double, double, double*, int, cudaStream_t);
+void thermo_finish(const LsePart*, int, double, fxe_thermo*);
+}  // namespace fxe
+
+namespace {
+
+thread_local std::string g_err;
+
+fxe_status fail(fxe_status s, const std::string& msg) {
+    g_err = msg;
+    return s;
+}
+
+fxe_status cuda_fail(cudaError_t e, const char* what) {
+    return fail(e == cudaErrorMemoryAllocation ? FXE_ERR_ALLOC : FXE_ERR_LAUNCH,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace
+
+struct fxe_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    fxe::DevSystem S{};
+    fxe::DevWork W{};
+    std::vector<void*> allocs;
+    int32_t* d_genes = nullptr;
+    double* d_icin = nullptr;
+    int last_n = 0;
+    int counters[4] = {0, 0, 0, 0};
+
+    template <typename T>
+    cudaError_t alloc(T** p, size_t count) {
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, count * sizeof(T) + 16);
+        if (e == cudaSuccess) {
+            allocs.push_back(q);
+            *p = reinterpret_cast<T*>(q);
+        }
+        return e;
+    }
+    template <typename T>
+    cudaError_t upload(const T** dst, const T* src, size_t count) {
+        T* d = nullptr;
+        cudaError_t e = alloc(&d, count);
+        if (e != cudaSuccess) return e;
+        if (count) e = cudaMemcpy(d, src, count * sizeof(T), cudaMemcpyHostToDevice);
+        *dst = d;
+        return e;
+    }
+    ~fxe_context() {
+        for (void* p : allocs) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+extern "C" const char* fxe_last_error(void) { return g_err.c_str(); }
+
+#define FXE_TRY(expr, what)                      \
+    do {                                         \
+        cudaError_t _e = (expr);                 \
+        if (_e != cudaSuccess) return cuda_fail(_e, what); \
+    } while (0)
+
+extern "C" fxe_status fxe_context_create(const fxe_receptor_desc* rec, const fxe_ligand_desc* lig,
+                                         const fxe_emat_desc* em, const fxe_params* prm,
+                                         int32_t max_poses, fxe_context** out) {
+    g_err.clear();
+    if (!rec || !lig || !em || !prm || !out || max_poses <= 0)
+        return fail(FXE_ERR_INVALID_ARGS, "null argument or max_poses <= 0");
+    *out = nullptr;
+    if (rec->n_atoms <= 0 || !rec->xyz || !rec->radius || !rec->type || rec->n_grid <= 0 || !rec->grid_ic)
+        return fail(FXE_ERR_INVALID_ARGS, "receptor descriptor incomplete");
+    if (lig->n_atoms < 3 || lig->n_atoms > fxe::kMaxLig)
+        return fail(FXE_ERR_INVALID_ARGS, "ligand must have 3.." + std::to_string(fxe::kMaxLig) + " atoms");
+    if (!lig->radius || !lig->type || !lig->rec || !lig->shift || !lig->ic || !lig->build_order ||
+        !lig->bonded || lig->n_build <= 0 || lig->n_build > lig->n_atoms)
+        return fail(FXE_ERR_INVALID_ARGS, "ligand descriptor incomplete");
+    if (lig->n_genes < 0 || lig->n_genes > 1024 || (lig->n_genes && (!lig->gene_type || !lig->gene_atom ||
+        !lig->gene_min || !lig->gene_max || !lig->gene_del || !lig->gene_map)))
+        return fail(FXE_ERR_INVALID_ARGS, "gene arrays incomplete");
+    for (int g = 0; g < lig->n_genes; ++g) {
+        const int t = lig->gene_type[g];
+        if (t != -1 && t != 0 && t != 1 && t != 2)
+            return fail(FXE_ERR_INVALID_ARGS, "gene type " + std::to_string(t) + " is not supported (grid, distance, angle, dihedral only)");
+        if (lig->gene_atom[g] < 0 || lig->gene_atom[g] >= lig->n_atoms)
+            return fail(FXE_ERR_INVALID_ARGS, "gene atom out of range");
+        if (!(lig->gene_del[g] > 0.0) || !(lig->gene_max[g] >= lig->gene_min[g]))
+            return fail(FXE_ERR_INVALID_ARGS, "gene limits invalid");
+    }
+    for (int i = 0; i < lig->n_build; ++i)
+        if (lig->build_order[i] < 0 || lig->build_order[i] >= lig->n_atoms)
+            return fail(FXE_ERR_INVALID_ARGS, "build order entry out of range");
+    for (int i = 0; i < lig->n_atoms * 4; ++i)
+        if (lig->rec[i] < -1 || lig->rec[i] >= lig->n_atoms)
+            return fail(FXE_ERR_INVALID_ARGS, "ligand rec entry out of range");
+    if (em->ntypes <= 0 || !em->weight || !em->offset || !em->y || !em->x)
+        return fail(FXE_ERR_INVALID_ARGS, "energy matrix incomplete");
+    const int T = em->ntypes;
+    for (int i = 0; i < rec->n_atoms; ++i)
+        if (rec->type[i] < 1 || rec->type[i] > T) return fail(FXE_ERR_INVALID_ARGS, "receptor atom type out of range");
+    for (int i = 0; i < lig->n_atoms; ++i)
+        if (lig->type[i] < 1 || lig->type[i] > T) return fail(FXE_ERR_INVALID_ARGS, "ligand atom type out of range");
+    for (int k = 0; k < T * T; ++k)
+        if (em->offset[k + 1] <= em->offset[k]) return fail(FXE_ERR_INVALID_ARGS, "energy matrix entry without values");
+
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
+        return fail(FXE_ERR_NO_DEVICE, "no CUDA device");
+
+    auto* ctx = new fxe_context();
+    fxe_status st = [&]() -> fxe_status {
+        FXE_TRY(cudaGetDevice(&ctx->device), "cudaGetDevice");
+        FXE_TRY(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        FXE_TRY(fxe::configure_voronoi(), "cudaFuncSetAttribute");
+        fxe::DevSystem& S = ctx->S;
+        const int N = rec->n_atoms, n = lig->n_atoms;
+        // receptor atoms
+        std::vector<float4> pos(N);
+        for (int i = 0; i < N; ++i) pos[i] = make_float4(rec->xyz[3 * i], rec->xyz[3 * i + 1], rec->xyz[3 * i + 2], rec->radius[i]);
+        S.n_rec = N;
+        FXE_TRY(ctx->upload(&S.rec_pos, pos.data(), N), "receptor upload");
+        FXE_TRY(ctx->upload(&S.rec_type, rec->type, N), "receptor upload");
+        for (int k = 0; k < 3; ++k) {
+            S.ori[k] = rec->ori[k];
+            S.globalmin[k] = rec->globalmin[k];
+            S.globalmax[k] = rec->globalmax[k];
+            // index_protein's starting bounds once the receptor is indexed (LIB/Vcontacts.cpp:1596-1599)
+            S.gmin[k] = (float)((int)rec->globalmin[k] + 1.0);
+            S.gmax[k] = (float)((int)rec->globalmax[k] + 1.0);
+        }
+        S.maxwidth = rec->maxwidth;
+        S.dim = (int)(rec->maxwidth / fxe::kCell) + 1;
+        if (S.dim < 3) return fail(FXE_ERR_INVALID_ARGS, "receptor narrower than three cells");
+        const int dim = S.dim, dim2 = dim * dim;
+        const long dim3 = (long)dim2 * dim;
+        std::vector<int> cell(N), start(dim3 + 1, 0);
+        for (int i = 0; i < N; ++i) {
+            const long bi = (long)(int)((pos[i].x - S.gmin[0]) / fxe::kCell) * dim2 +
+                            (long)(int)((pos[i].y - S.gmin[1]) / fxe::kCell) * dim +
+                            (int)((pos[i].z - S.gmin[2]) / fxe::kCell);
+            if (bi < 0 || bi >= dim3) return fail(FXE_ERR_INVALID_ARGS, "receptor atom outside its own cell grid");
+            cell[i] = (int)bi;
+            ++start[bi + 1];
+        }
+        for (long b = 0; b < dim3; ++b) start[b + 1] += start[b];
+        std::vector<int> fill(start.begin(), start.end() - 1), catom(N);
+        std::vector<float4> cpos(N);
+        for (int i = 0; i < N; ++i) {
+            const int w = fill[cell[i]]++;
+            catom[w] = i;
+            cpos[w] = pos[i];
+        }
+        FXE_TRY(ctx->upload(&S.cell_start, start.data(), dim3 + 1), "cell list upload");
+        FXE_TRY(ctx->upload(&S.cell_atom, catom.data(), N), "cell list upload");
+        FXE_TRY(ctx->upload(&S.cell_pos, cpos.data(), N), "cell list upload");
+        // cleft grid
+        std::vector<float4> gic(rec->n_grid);
+        for (int g = 0; g < rec->n_grid; ++g)
+            gic[g] = make_float4(rec->grid_ic[3 * g], rec->grid_ic[3 * g + 1], rec->grid_ic[3 * g + 2], 0.0f);
+        S.n_grid = rec->n_grid;
+        FXE_TRY(ctx->upload(&S.grid_ic, gic.data(), rec->n_grid), "grid upload");
+        // ligand
+        S.n_lig = n;
+        std::vector<int4> lrec(n);
+        std::vector<float4> lic(n);
+        for (int l = 0; l < n; ++l) {
+            lrec[l] = make_int4(lig->rec[4 * l], lig->rec[4 * l + 1], lig->rec[4 * l + 2], lig->rec[4 * l + 3]);
+            lic[l] = make_float4(lig->ic[3 * l], lig->ic[3 * l + 1], lig->ic[3 * l + 2], 0.0f);
+        }
+        FXE_TRY(ctx->upload(&S.lig_radius, lig->radius, n), "ligand upload");
+        FXE_TRY(ctx->upload(&S.lig_type, lig->type, n), "ligand upload");
+        FXE_TRY(ctx->upload(&S.lig_rec, lrec.data(), n), "ligand upload");
+        FXE_TRY(ctx->upload(&S.lig_shift, lig->shift, n), "ligand upload");
+        FXE_TRY(ctx->upload(&S.lig_ic, lic.data(), n), "ligand upload");
+        S.n_build = lig->n_build;
+        FXE_TRY(ctx->upload(&S.build_order, lig->build_order, lig->n_build), "ligand upload");
+        FXE_TRY(ctx->upload(&S.bonded, lig->bonded, (size_t)n * n), "ligand upload");
+        // genes and genetoic decode tables (running bin totals, LIB/gaboom.cpp:2295-2308, 2887-2906)
+        const int ng = lig->n_genes;
+        S.n_genes = ng;
+        std::vector<int> doff(ng + 1, 0);
+        std::vector<double> dtab;
+        for (int g = 0; g < ng; ++g) {
+            double nbin = (lig->gene_max[g] - lig->gene_min[g]) / lig->gene_del[g];
+            if (nbin - (int)nbin > 0.0) nbin += 1.0;
+            if (lig->gene_map[g]) nbin += 1.0;
+            if (!(nbin >= 1.0) || nbin > 5e7) return fail(FXE_ERR_INVALID_ARGS, "gene bin count out of range");
+            const double bin = 1.0 / nbin;
+            double tot = bin;
+            dtab.push_back(tot);
+            while (tot < 1.0) {
+                tot += bin;
+                dtab.push_back(tot);
+            }
+            doff[g + 1] = (int)dtab.size();
+        }
+        if (dtab.empty()) dtab.push_back(1.0);
+        FXE_TRY(ctx->upload(&S.gene_type, lig->gene_type, ng), "gene upload");
+        FXE_TRY(ctx->upload(&S.gene_atom, lig->gene_atom, ng), "gene upload");
+        FXE_TRY(ctx->upload(&S.gene_min, lig->gene_min, ng), "gene upload");
+        FXE_TRY(ctx->upload(&S.gene_max, lig->gene_max, ng), "gene upload");
+        FXE_TRY(ctx->upload(&S.gene_del, lig->gene_del, ng), "gene upload");
+        FXE_TRY(ctx->upload(&S.dec_off, doff.data(), ng + 1), "gene upload");
+        FXE_TRY(ctx->upload(&S.dec_tab, dtab.data(), dtab.size()), "gene upload");
+        // energy matrix
+        S.ntypes = T;
+        const int npts = em->offset[T * T];
+        FXE_TRY(ctx->upload(&S.em_weight, em->weight, (size_t)T * T), "emat upload");
+        FXE_TRY(ctx->upload(&S.em_off, em->offset, (size_t)T * T + 1), "emat upload");
+        FXE_TRY(ctx->upload(&S.em_x, em->x, npts), "emat upload");
+        FXE_TRY(ctx->upload(&S.em_y, em->y, npts), "emat upload");
+        S.permeability = prm->permeability;
+        S.dee_clash = prm->dee_clash;
+        S.intramolecular = prm->intramolecular;
+        S.solventterm = prm->solventterm;
+        // workspace
+        fxe::DevWork& W = ctx->W;
+        const size_t P = (size_t)max_poses, PL = P * n, PLC = PL * fxe::kMaxCand;
+        W.max_poses = max_poses;
+        FXE_TRY(ctx->alloc(&W.ic, P * (ng > 0 ? ng : 1)), "workspace");
+        FXE_TRY(ctx->alloc(&W.lig_pos, PL), "workspace");
+        FXE_TRY(ctx->alloc(&W.lig_cell, PL), "workspace");
+        FXE_TRY(ctx->alloc(&W.lig_rank, PL), "workspace");
+        FXE_TRY(ctx->alloc(&W.pose_grid, P), "workspace");
+        FXE_TRY(ctx->alloc(&W.pose_gmin, P), "workspace");
+        FXE_TRY(ctx->alloc(&W.cand_idx, PLC), "workspace");
+        FXE_TRY(ctx->alloc(&W.cand_d2, PLC), "workspace");
+        FXE_TRY(ctx->alloc(&W.cand_area, PLC), "workspace");
+        FXE_TRY(ctx->alloc(&W.cand_flag, PLC), "workspace");
+        FXE_TRY(ctx->alloc(&W.cand_n, PL), "workspace");
+        FXE_TRY(ctx->alloc(&W.clash_part, PL), "workspace");
+        FXE_TRY(ctx->alloc(&W.atom_status, PL), "workspace");
+        FXE_TRY(ctx->alloc(&W.rec0, PL * fxe::kMaskWords), "workspace");
+        FXE_TRY(ctx->alloc(&W.out, P), "workspace");
+        FXE_TRY(ctx->alloc(&W.counters, 4), "workspace");
+        FXE_TRY(ctx->alloc(&ctx->d_genes, P * (ng > 0 ? ng : 1)), "staging");
+        FXE_TRY(ctx->alloc(&ctx->d_icin, P * (ng > 0 ? ng : 1)), "staging");
+        FXE_TRY(cudaDeviceSynchronize(), "context set-up");
+        return FXE_OK;
+    }();
+    if (st != FXE_OK) {
+        delete ctx;
+        return st;
+    }
+    *out = ctx;
+    return FXE_OK;
+}
+
+namespace {
+
+fxe_status run_chunk(fxe_context* ctx, int nb, const int32_t* d_genes, const double* d_ic,
+                     cudaStream_t s) {
+    fxe::launch_build(ctx->S, ctx->W, nb, d_genes, d_ic, s);
+    fxe::launch_contacts(ctx->S, ctx->W, nb, s);
+    fxe::launch_voronoi(ctx->S, ctx->W, nb, s);
+    fxe::launch_score(ctx->S, ctx->W, nb, s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    return FXE_OK;
+}
+
+fxe_status eval_host(fxe_context* ctx, int32_t n, const int32_t* genes, const double* ic, fxe_cf* out) {
+    g_err.clear();
+    if (!ctx || n < 0 || (n > 0 && (!out || (!genes && !ic)))) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
+    const int ng = ctx->S.n_genes;
+    const int P = ctx->W.max_poses;
+    cudaStream_t s = ctx->stream;
+    FXE_TRY(cudaMemsetAsync(ctx->W.counters, 0, 4 * sizeof(int), s), "counters");
+    for (int off = 0; off < n; off += P) {
+        const int nb = n - off < P ? n - off : P;
+        if (genes) {
+            FXE_TRY(cudaMemcpyAsync(ctx->d_genes, genes + (size_t)off * ng, (size_t)nb * ng * sizeof(int32_t),
+                                    cudaMemcpyHostToDevice, s), "genes to device");
+        } else {
+            FXE_TRY(cudaMemcpyAsync(ctx->d_icin, ic + (size_t)off * ng, (size_t)nb * ng * sizeof(double),
+                                    cudaMemcpyHostToDevice, s), "ICs to device");
+        }
+        fxe_status st = run_chunk(ctx, nb, genes ? ctx->d_genes : nullptr, genes ? nullptr : ctx->d_icin, s);
+        if (st != FXE_OK) return st;
+        FXE_TRY(cudaMemcpyAsync(out + off, ctx->W.out, (size_t)nb * sizeof(fxe_cf), cudaMemcpyDeviceToHost, s),
+                "results to host");
+    }
+    FXE_TRY(cudaMemcpyAsync(ctx->counters, ctx->W.counters, 4 * sizeof(int), cudaMemcpyDeviceToHost, s), "counters");
+    FXE_TRY(cudaStreamSynchronize(s), "evaluation");
+    ctx->last_n = n < P ? n : P;
+    return FXE_OK;
+}
+
+}  // namespace
+
+extern "C" fxe_status fxe_eval_genes(fxe_context* ctx, int32_t n, const int32_t* genes, fxe_cf* out) {
+    if (n > 0 && !genes) return fail(FXE_ERR_INVALID_ARGS, "genes is NULL");
+    return eval_host(ctx, n, genes, nullptr, out);
+}
+
+extern "C" fxe_status fxe_eval_ic(fxe_context* ctx, int32_t n, const double* ic, fxe_cf* out) {
+    if (n > 0 && !ic) return fail(FXE_ERR_INVALID_ARGS, "ic is NULL");
+    return eval_host(ctx, n, nullptr, ic, out);
+}
+
+extern "C" fxe_status fxe_eval_genes_device(fxe_context* ctx, int32_t n, const int32_t* d_genes,
+                                            fxe_cf* d_out, void* stream) {
+    g_err.clear();
+    if (!ctx || n < 0 || (n > 0 && (!d_genes || !d_out))) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    if (n > ctx->W.max_poses) return fail(FXE_ERR_INVALID_ARGS, "n exceeds the context's max_poses");
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    if (n == 0) return FXE_OK;
+    fxe_status st = run_chunk(ctx, n, d_genes, nullptr, s);
+    if (st != FXE_OK) return st;
+    FXE_TRY(cudaMemcpyAsync(d_out, ctx->W.out, (size_t)n * sizeof(fxe_cf), cudaMemcpyDeviceToDevice, s), "results");
+    ctx->last_n = n;
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_last_contacts(fxe_context* ctx, int32_t pose, int32_t atom, int32_t cap,
+                                        int32_t* partner, float* area, int32_t* n_out) {
+    g_err.clear();
+    if (!ctx || !n_out || pose < 0 || pose >= ctx->last_n || atom < 0 || atom >= ctx->S.n_lig || cap < 0)
+        return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    const size_t lb = (size_t)pose * ctx->S.n_lig + atom;
+    int nc = 0;
+    FXE_TRY(cudaMemcpy(&nc, ctx->W.cand_n + lb, sizeof(int), cudaMemcpyDeviceToHost), "contacts");
+    *n_out = 0;
+    if (nc <= 0) return FXE_OK;
+    std::vector<int> idx(nc);
+    std::vector<float> ar(nc);
+    std::vector<uint8_t> fl(nc);
+    const size_t cb = lb * fxe::kMaxCand;
+    FXE_TRY(cudaMemcpy(idx.data(), ctx->W.cand_idx + cb, nc * sizeof(int), cudaMemcpyDeviceToHost), "contacts");
+    FXE_TRY(cudaMemcpy(ar.data(), ctx->W.cand_area + cb, nc * sizeof(float), cudaMemcpyDeviceToHost), "contacts");
+    FXE_TRY(cudaMemcpy(fl.data(), ctx->W.cand_flag + cb, nc, cudaMemcpyDeviceToHost), "contacts");
+    int k = 0;
+    for (int c = nc - 1; c >= 0; --c) {  // newest record first, as vcfunction walks them
+        if (!(fl[c] & fxe::kRecorded)) continue;
+        if (k < cap) {
+            if (partner) partner[k] = idx[c];
+            if (area) area[k] = ar[c];
+        }
+        ++k;
+    }
+    *n_out = k;
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_last_stats(fxe_context* ctx, int32_t* out4) {
+    if (!ctx || !out4) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    for (int i = 0; i < 4; ++i) out4[i] = ctx->counters[i];
+    return FXE_OK;
+}
+
+extern "C" void fxe_context_destroy(fxe_context* ctx) { delete ctx; }
+
+namespace {
+
+struct ThermoScratch {
+    std::mutex mu;
+    fxe::LsePart* part = nullptr;
+    int cap = 0;
+};
+ThermoScratch g_thermo;
+
+fxe_status thermo_run(const double* d_e, const int32_t* d_m, long n, double T, fxe_thermo* out,
+                      double* d_w, cudaStream_t s) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int nb = fxe::thermo_blocks(n, sms);
+    std::lock_guard<std::mutex> lk(g_thermo.mu);
+    if (g_thermo.cap < nb) {
+        if (g_thermo.part) cudaFree(g_thermo.part);
+        g_thermo.part = nullptr;
+        FXE_TRY(cudaMalloc(&g_thermo.part, nb * sizeof(fxe::LsePart)), "thermo scratch");
+        g_thermo.cap = nb;
+    }
+    const double beta = 1.0 / (0.001987206 * T);
+    fxe::launch_thermo_partial(d_e, d_m, n, beta, g_thermo.part, nb, s);
+    FXE_TRY(cudaGetLastError(), "thermo launch");
+    std::vector<fxe::LsePart> part(nb);
+    FXE_TRY(cudaMemcpyAsync(part.data(), g_thermo.part, nb * sizeof(fxe::LsePart), cudaMemcpyDeviceToHost, s), "thermo");
+    FXE_TRY(cudaStreamSynchronize(s), "thermo");
+    fxe_thermo th;
+    fxe::thermo_finish(part.data(), nb, T, &th);
+    if (out) *out = th;
+    if (d_w) {
+        fxe::launch_thermo_weights(d_e, d_m, n, beta, th.log_Z, d_w, nb, s);
+        FXE_TRY(cudaGetLastError(), "thermo weights launch");
+    }
+    return FXE_OK;
+}
+
+fxe_status thermo_host(const double* e, const int32_t* mult, int64_t n, double T, fxe_thermo* out, double* w) {
+    g_err.clear();
+    if (!e || n <= 0 || !(T > 0.0)) return fail(FXE_ERR_INVALID_ARGS, "empty ensemble or T <= 0");
+    if (mult)
+        for (int64_t i = 0; i < n; ++i)
+            if (mult[i] <= 0) return fail(FXE_ERR_INVALID_ARGS, "multiplicities must be positive");
+    int dc = 0;
+    if (cudaGetDeviceCount(&dc) != cudaSuccess || dc == 0) return fail(FXE_ERR_NO_DEVICE, "no CUDA device");
+    double *d_e = nullptr, *d_w = nullptr;
+    int32_t* d_m = nullptr;
+    cudaStream_t s = nullptr;
+    auto cleanup = [&]() {
+        if (d_e) cudaFree(d_e);
+        if (d_w) cudaFree(d_w);
+        if (d_m) cudaFree(d_m);
+        if (s) cudaStreamDestroy(s);
+    };
+    fxe_status st = [&]() -> fxe_status {
+        FXE_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
+        FXE_TRY(cudaMalloc(&d_e, n * sizeof(double)), "thermo input");
+        FXE_TRY(cudaMemcpyAsync(d_e, e, n * sizeof(double), cudaMemcpyHostToDevice, s), "thermo input");
+        if (mult) {
+            FXE_TRY(cudaMalloc(&d_m, n * sizeof(int32_t)), "thermo input");
+            FXE_TRY(cudaMemcpyAsync(d_m, mult, n * sizeof(int32_t), cudaMemcpyHostToDevice, s), "thermo input");
+        }
+        if (w) FXE_TRY(cudaMalloc(&d_w, n * sizeof(double)), "thermo output");
+        fxe_status r = thermo_run(d_e, d_m, n, T, out, d_w, s);
+        if (r != FXE_OK) return r;
+        if (w) {
+            FXE_TRY(cudaMemcpyAsync(w, d_w, n * sizeof(double), cudaMemcpyDeviceToHost, s), "thermo output");
+            FXE_TRY(cudaStreamSynchronize(s), "thermo output");
+        }
+        return FXE_OK;
+    }();
+    cleanup();
+    return st;
+}
+
+}  // namespace
+
+extern "C" fxe_status fxe_thermo_compute(const double* energies, const int32_t* multiplicity, int64_t n,
+                                         double temperature, fxe_thermo* out) {
+    if (!out) return fail(FXE_ERR_INVALID_ARGS, "out is NULL");
+    return thermo_host(energies, multiplicity, n, temperature, out, nullptr);
+}
+
+extern "C" fxe_status fxe_thermo_weights(const double* energies, const int32_t* multiplicity, int64_t n,
+                                         double temperature, double* weights) {
+    if (!weights) return fail(FXE_ERR_INVALID_ARGS, "weights is NULL");
+    return thermo_host(energies, multiplicity, n, temperature, nullptr, weights);
+}
+
+extern "C" fxe_status fxe_thermo_compute_device(const double* d_energies, const int32_t* d_multiplicity,
+                                                int64_t n, double temperature, fxe_thermo* out, void* stream) {
+    g_err.clear();
+    if (!d_energies || n <= 0 || !(temperature > 0.0) || !out)
+        return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    return thermo_run(d_energies, d_multiplicity, n, temperature, out, nullptr, (cudaStream_t)stream);
+}

@@ -1,0 +1,128 @@
+// fxe_common.cuh — device-side layout shared by the evaluation kernels.
+//
+// Layout in HBM (one evaluation context, resident for the context's lifetime):
+//   receptor atoms as float4 (x, y, z, radius) in Calc order, and a second copy sorted by cell
+//   of the receptor's steady cell grid (the 6.5 A grid index_protein builds once the receptor
+//   atoms are indexed, LIB/Vcontacts.cpp:1570-1715) with CSR offsets per cell;
+//   ligand build tree, genes and decode tables; energy matrix; cleft-grid ICs as float4.
+// Per batch of poses (workspace sized at context creation for max_poses):
+//   ligand coordinates, cells and processing ranks per pose; candidate lists (Calc index,
+//   squared distance) and Voronoi results (area, flags) per (pose, ligand atom, slot).
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/fxe.h"
+
+namespace fxe {
+
+constexpr float kRw = 1.4f;              // LIB/flexaid.h:88
+constexpr double kPi = 3.141592;         // LIB/flexaid.h:86
+constexpr float kKwall = 1.0e6f;         // LIB/flexaid.h:78
+constexpr float kCell = 6.5f;            // LIB/Vcontacts.h:56
+constexpr double kClashThreshold = 1e4;  // LIB/flexaid.h:70
+constexpr float kPolyPenalty = 1e6f;     // LIB/flexaid.h:69
+
+// Per-atom workspace capacities of the Voronoi warp. Poses whose atoms exceed them are
+// reported with FXE_POSE_CAPACITY rather than scored.
+constexpr int kMaxCand = 96;    // contact candidates of one atom
+constexpr int kMaxPlanes = kMaxCand + 4;
+constexpr int kMaxEdges = 200;  // the reference aborts the hull walk at 200 edges
+constexpr int kMaxVerts = 255;  // vertex indices are bytes; 255 means "none"
+constexpr int kMaxFacePts = 640;
+constexpr int kMaxLig = 128;    // ligand atoms per pose (bit masks, shared staging)
+constexpr int kMaskWords = kMaxLig / 32;
+
+// candidate flag bits
+constexpr uint8_t kOnHull = 1;    // plane flag != 'X'
+constexpr uint8_t kEngulf = 2;    // plane flag 'E'
+constexpr uint8_t kTouches = 4;   // face reaches the atom's sphere (points or area)
+constexpr uint8_t kRecorded = 8;  // contact kept in the atom's record list
+
+// atom status
+constexpr int kAtomOk = 0;
+constexpr int kAtomHullFail = 1;
+constexpr int kAtomCapacity = 2;
+constexpr int kAtomSkipped = 3;   // pose rejected before the polyhedra
+
+struct DevSystem {
+    // receptor
+    int n_rec;
+    const float4* rec_pos;       // [n_rec] x, y, z, radius (Calc order)
+    const int* rec_type;         // [n_rec]
+    float ori[3];
+    float globalmin[3], globalmax[3], maxwidth;
+    // steady cell grid of the receptor
+    float gmin[3];
+    float gmax[3];
+    int dim;
+    const int* cell_start;       // [dim^3 + 1]
+    const int* cell_atom;        // [n_rec] Calc index, cell order
+    const float4* cell_pos;      // [n_rec] positions in cell order
+    // cleft grid
+    int n_grid;
+    const float4* grid_ic;       // dis, ang, dih, 0
+    // ligand
+    int n_lig;
+    const float* lig_radius;
+    const int* lig_type;
+    const int4* lig_rec;         // rec[0..3], -1 = frame / no cascade
+    const float* lig_shift;
+    const float4* lig_ic;        // base dis, ang, dih
+    int n_build;
+    const int* build_order;
+    const int8_t* bonded;        // [n_lig * n_lig]
+    int n_genes;
+    const int* gene_type;
+    const int* gene_atom;
+    const double* gene_min;
+    const double* gene_max;
+    const double* gene_del;
+    const int* dec_off;          // [n_genes + 1] offsets into dec_tab
+    const double* dec_tab;       // running bin totals per gene
+    // energy matrix
+    int ntypes;
+    const int* em_weight;
+    const int* em_off;
+    const float* em_x;
+    const float* em_y;
+    // scoring switches
+    float permeability;
+    float dee_clash;
+    int intramolecular;
+    float solventterm;
+};
+
+struct DevWork {
+    int max_poses;
+    double* ic;            // [P * n_genes]
+    float4* lig_pos;       // [P * n_lig] x, y, z, radius
+    int* lig_cell;         // [P * n_lig]
+    int* lig_rank;         // [P * n_lig] position among the ligand atoms in Calclist order
+    int4* pose_grid;       // [P] (altered, dim, 0, 0)
+    float4* pose_gmin;     // [P]
+    int* cand_idx;         // [P * n_lig * kMaxCand]
+    float* cand_d2;        // [P * n_lig * kMaxCand]
+    float* cand_area;      // [P * n_lig * kMaxCand]
+    uint8_t* cand_flag;    // [P * n_lig * kMaxCand]
+    int* cand_n;           // [P * n_lig]
+    double* clash_part;    // [P * n_lig]
+    int* atom_status;      // [P * n_lig]
+    uint32_t* rec0;        // [P * n_lig * kMaskWords] ligand partners kept in the record list
+    fxe_cf* out;           // [P]
+    int* counters;         // [4]: fix-up recomputes, hull failures, capacity, no-partner faces
+};
+
+// one block's share of the ensemble reduction: running max of the log-weights and the sums
+// of exp(lw - m), E exp(lw - m), E^2 exp(lw - m)
+struct LsePart {
+    double m, s, e1, e2;
+};
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+}  // namespace fxe

@@ -1,0 +1,184 @@
+"""Host-side interface of the GB300 evaluation backend (ctypes over libfxe.so).
+
+Mirrors the reference's evaluation entry points for this path:
+  * ``GPUEvaluator``   — the CUDA backend of calculate_fitness (cuda_eval_init / cuda_eval_batch /
+                         cuda_eval_shutdown, LIB/cuda_eval.cuh:46-75), scoring whole batches and
+                         returning the full cfstr per pose instead of the surrogate's com/wal/sas;
+  * ``ic2cf``          — single-pose scoring with the signature's meaning (LIB/ic2cf.cpp:18);
+  * ``StatMechEngine`` — add_sample / compute / boltzmann_weights / delta_G / helmholtz
+                         (LIB/statmech.h:67-135) with the reduction on the device in FP64.
+
+There is no CPU fallback: without the built library or a CUDA device these raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .capi import CF_DTYPE, STATUS_NAMES, Packed, Thermo, _d, _f, _i, ptr
+from .system import Descriptor
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libfxe.so")
+_lib = None
+
+
+class FxeError(RuntimeError):
+    pass
+
+
+def load_library():
+    """Loads flexaidds_gb300/libfxe.so (built by flexaidds_gb300/build.py)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FxeError(f"CUDA backend not built: {LIB_PATH} is missing (run flexaidds_gb300/build.py)")
+        lib = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        lib.fxe_context_create.argtypes = [vp, vp, vp, vp, C.c_int32, C.POINTER(vp)]
+        lib.fxe_eval_genes.argtypes = [vp, C.c_int32, _i, vp]
+        lib.fxe_eval_ic.argtypes = [vp, C.c_int32, _d, vp]
+        lib.fxe_eval_genes_device.argtypes = [vp, C.c_int32, vp, vp, vp]
+        lib.fxe_last_contacts.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, _i, _f, _i]
+        lib.fxe_last_stats.argtypes = [vp, _i]
+        lib.fxe_thermo_compute.argtypes = [_d, _i, C.c_int64, C.c_double, vp]
+        lib.fxe_thermo_compute_device.argtypes = [vp, vp, C.c_int64, C.c_double, vp, vp]
+        lib.fxe_thermo_weights.argtypes = [_d, _i, C.c_int64, C.c_double, _d]
+        lib.fxe_context_destroy.argtypes = [vp]
+        lib.fxe_context_destroy.restype = None
+        lib.fxe_last_error.restype = C.c_char_p
+        _lib = lib
+    return _lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        msg = load_library().fxe_last_error().decode()
+        raise FxeError(f"{STATUS_NAMES.get(rc, rc)}: {msg}")
+
+
+class GPUEvaluator:
+    """Evaluation context for one receptor, ligand and energy matrix."""
+
+    def __init__(self, desc: Descriptor, max_poses: int = 2048):
+        self.lib = load_library()
+        self.desc = desc
+        self._packed = Packed(desc)
+        self.max_poses = int(max_poses)
+        h = C.c_void_p()
+        pk = self._packed
+        _check(self.lib.fxe_context_create(C.byref(pk.rec), C.byref(pk.lig), C.byref(pk.emat),
+                                           C.byref(pk.params), self.max_poses, C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.fxe_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def eval_genes(self, genes: np.ndarray) -> np.ndarray:
+        genes = np.ascontiguousarray(genes, np.int32)
+        out = np.zeros(genes.shape[0], CF_DTYPE)
+        _check(self.lib.fxe_eval_genes(self.handle, genes.shape[0], ptr(genes, _i),
+                                       out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def eval_ic(self, ic: np.ndarray) -> np.ndarray:
+        ic = np.ascontiguousarray(ic, np.float64)
+        out = np.zeros(ic.shape[0], CF_DTYPE)
+        _check(self.lib.fxe_eval_ic(self.handle, ic.shape[0], ptr(ic, _d), out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def eval_genes_device(self, d_genes: int, n: int, d_out: int, stream: int = 0):
+        """Queues a batch whose genes and records are device pointers (not waited for)."""
+        _check(self.lib.fxe_eval_genes_device(self.handle, n, C.c_void_p(d_genes), C.c_void_p(d_out),
+                                              C.c_void_p(stream) if stream else None))
+
+    def contacts(self, pose: int, atom: int):
+        cap = 512
+        part = np.zeros(cap, np.int32)
+        area = np.zeros(cap, np.float32)
+        n = C.c_int32(0)
+        _check(self.lib.fxe_last_contacts(self.handle, pose, atom, cap, ptr(part, _i), ptr(area, _f),
+                                          C.byref(n)))
+        return part[:n.value].copy(), area[:n.value].copy()
+
+    def stats(self) -> dict:
+        o = np.zeros(4, np.int32)
+        _check(self.lib.fxe_last_stats(self.handle, ptr(o, _i)))
+        return {"recomputed_atoms": int(o[0]), "hull_failures": int(o[1]), "capacity": int(o[2]),
+                "no_partner_faces": int(o[3])}
+
+
+def ic2cf(evaluator: GPUEvaluator, icv) -> np.void:
+    """Scores one pose from its IC vector, as ic2cf(FA, VC, atoms, residue, cleftgrid, npar, icv)."""
+    return evaluator.eval_ic(np.asarray(icv, np.float64)[None, :])[0]
+
+
+def thermo(energies, multiplicity=None, temperature=300.0) -> dict:
+    lib = load_library()
+    e = np.ascontiguousarray(energies, np.float64)
+    m = None if multiplicity is None else np.ascontiguousarray(multiplicity, np.int32)
+    t = Thermo()
+    _check(lib.fxe_thermo_compute(ptr(e, _d), ptr(m, _i) if m is not None else None, e.shape[0],
+                                  float(temperature), C.byref(t)))
+    return {k: getattr(t, k) for k, _ in Thermo._fields_}
+
+
+def boltzmann_weights(energies, multiplicity=None, temperature=300.0) -> np.ndarray:
+    lib = load_library()
+    e = np.ascontiguousarray(energies, np.float64)
+    m = None if multiplicity is None else np.ascontiguousarray(multiplicity, np.int32)
+    w = np.zeros_like(e)
+    _check(lib.fxe_thermo_weights(ptr(e, _d), ptr(m, _i) if m is not None else None, e.shape[0],
+                                  float(temperature), ptr(w, _d)))
+    return w
+
+
+class StatMechEngine:
+    """Canonical ensemble over docking poses (LIB/statmech.h:67-135), reduced on the GPU."""
+
+    kB_kcal = 0.001987206   # LIB/statmech.h:26
+
+    def __init__(self, temperature_K: float):
+        self.T = float(temperature_K)
+        self.beta = 1.0 / (self.kB_kcal * self.T)
+        self._e: list[float] = []
+        self._n: list[int] = []
+
+    def add_sample(self, energy: float, multiplicity: int = 1):
+        self._e.append(float(energy))
+        self._n.append(int(multiplicity))
+
+    def size(self) -> int:
+        return len(self._e)
+
+    def clear(self):
+        self._e.clear()
+        self._n.clear()
+
+    def compute(self) -> dict:
+        if not self._e:
+            raise RuntimeError("StatMechEngine::compute: empty ensemble")
+        return thermo(np.asarray(self._e), np.asarray(self._n, np.int32), self.T)
+
+    def boltzmann_weights(self) -> np.ndarray:
+        if not self._e:
+            return np.zeros(0)
+        return boltzmann_weights(np.asarray(self._e), np.asarray(self._n, np.int32), self.T)
+
+    def delta_G(self, reference: "StatMechEngine") -> float:
+        kT = self.kB_kcal * self.T
+        return -kT * (self.compute()["log_Z"] - reference.compute()["log_Z"])
+
+    @staticmethod
+    def helmholtz(energies, temperature_K: float) -> float:
+        return thermo(np.asarray(energies, np.float64), None, temperature_K)["free_energy"]

@@ -55,18 +55,29 @@ class Receptor:
     radius: np.ndarray       # (N,) float32
     cleft_center: np.ndarray  # (3,) float32
     cleft_radius: float
+    edge: float = 0.0         # cube edge used (A)
 
 
 def poisson_disc_receptor(n_atoms: int, cleft_radius: float, seed: int,
                           min_sep: float = 2.8, edge: float | None = None) -> Receptor:
     """Poisson-disc sample exactly ``n_atoms`` points in a cube, excluding a central sphere.
 
-    Bridson's active-list algorithm fills the cube (minus the cleft) to a maximal set; the
-    first ``n_atoms`` accepted points are kept. Raises if the cube cannot hold that many.
+    The cube edge is ``40 * (n_atoms / 2000) ** (1/3)`` A unless given. Near the jamming
+    density a larger cleft can leave too little room; the edge then grows in 1% steps until
+    the maximal set holds ``n_atoms`` (the edge used is recorded on the result).
     """
-    rng = np.random.default_rng(seed)
     if edge is None:
         edge = 40.0 * (n_atoms / 2000.0) ** (1.0 / 3.0)
+    for _ in range(40):
+        try:
+            return _poisson_disc(n_atoms, cleft_radius, seed, min_sep, edge)
+        except ValueError:
+            edge *= 1.01
+    raise ValueError(f"could not place {n_atoms} atoms")
+
+
+def _poisson_disc(n_atoms, cleft_radius, seed, min_sep, edge):
+    rng = np.random.default_rng(seed)
     half = edge / 2.0
     r2min = min_sep * min_sep
     cell = min_sep / math.sqrt(3.0)
@@ -122,7 +133,7 @@ def poisson_disc_receptor(n_atoms: int, cleft_radius: float, seed: int,
             active.pop()
     # top up with random darts if the active list ran dry early
     tries = 0
-    while len(pts) < n_atoms and tries < 200000:
+    while len(pts) < n_atoms and tries < 20000:
         c = rng.uniform(-half, half, 3)
         if ok(c):
             add(c)
@@ -133,7 +144,8 @@ def poisson_disc_receptor(n_atoms: int, cleft_radius: float, seed: int,
     types = rng.integers(1, NTYPES + 1, size=n_atoms).astype(np.int32)
     radius = np.asarray([type_radius(t, 0) for t in types], dtype=np.float32)
     return Receptor(xyz=xyz, type=types, radius=radius,
-                    cleft_center=np.zeros(3, np.float32), cleft_radius=float(cleft_radius))
+                    cleft_center=np.zeros(3, np.float32), cleft_radius=float(cleft_radius),
+                    edge=float(edge))
 
 
 # --------------------------------------------------------------------------------------------

@@ -145,11 +145,21 @@ fxe_status fxe_eval_genes_device(fxe_context* ctx, int32_t n, const int32_t* d_g
 fxe_status fxe_last_contacts(fxe_context* ctx, int32_t pose, int32_t ligand_atom, int32_t cap,
                              int32_t* partner, float* area, int32_t* n_out);
 
+/* Work counters of the last evaluation call: out4[0] atoms recomputed with the candidate list
+ * the reference would have seen, [1] poses whose hull walk reached 200 edges, [2] poses over
+ * capacity, [3] faces whose first vertex had no neighbour on its second plane. */
+fxe_status fxe_last_stats(fxe_context* ctx, int32_t* out4);
+
 /* Thermodynamics of an ensemble of n energies (kcal/mol) with multiplicities (NULL = all 1)
  * at temperature T (K), reduced on the device in FP64: StatMechEngine::compute. The arrays
  * are host memory. */
 fxe_status fxe_thermo_compute(const double* energies, const int32_t* multiplicity, int64_t n,
                               double temperature, fxe_thermo* out);
+
+/* Device-resident form of fxe_thermo_compute: d_energies / d_multiplicity are device
+ * pointers; the reduction runs on `stream` (cudaStream_t or NULL) and is waited for. */
+fxe_status fxe_thermo_compute_device(const double* d_energies, const int32_t* d_multiplicity,
+                                     int64_t n, double temperature, fxe_thermo* out, void* stream);
 
 /* Boltzmann weights p_i = n_i exp(-beta E_i) / Z of the same ensemble
  * (StatMechEngine::boltzmann_weights, LIB/statmech.cpp:178-201). */
