@@ -14,8 +14,13 @@ LIB = os.path.join(HERE, "libfxe.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # (source, extra flags): the pose build is evaluated without fused multiply-adds, like the
 # reference's single-precision build
-UNITS = [("fxe_build.cu", ["--fmad=false"]), ("fxe_voronoi.cu", []), ("fxe_thermo.cu", []),
-         ("fxe_capi.cu", [])]
+UNITS = [("fxe_build.cu", ["--fmad=false"]), ("fxe_contacts.cu", []), ("fxe_thermo.cu", []),
+         ("fxe_capi.cu", []),
+         # the polyhedron kernel twice: single precision, and double precision with the
+         # reference's expressions and every operation rounded separately
+         ("fxe_voronoi.cu", ["-DFXE_REAL=float", "-DFXE_VARIANT=f32"], "fxe_voronoi_f32.o"),
+         ("fxe_voronoi.cu", ["-DFXE_REAL=double", "-DFXE_VARIANT=f64", "-DFXE_REFERENCE_FORMULAS=1",
+                             "--fmad=false"], "fxe_voronoi_f64.o")]
 
 
 def nvcc() -> str:
@@ -26,8 +31,8 @@ def nvcc() -> str:
 
 
 def _compile(unit):
-    src, extra = unit
-    obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+    src, extra = unit[0], unit[1]
+    obj = os.path.join(BUILD, unit[2] if len(unit) > 2 else src.replace(".cu", ".o"))
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
            "-Xptxas", "-v" if os.environ.get("FXE_PTXAS_VERBOSE") else "-O3", *extra,
            "-c", os.path.join(CSRC, src), "-o", obj]

@@ -143,15 +143,17 @@ build_kernel(DevSystem S, DevWork W, int n, const int32_t* __restrict__ genes,
             a = cx * cx;
             b = cy * cy;
             c = cz * cz;
+            // cos/sin of the single-precision angle, rounded from double: the correctly rounded
+            // values, which is what the C library's cosf/sinf return for these arguments
             const float angPI = (float)(sh.ic[l][1] * kPi / 180.0f);
-            float ct = cosf(angPI), st = -sinf(angPI);
+            float ct = (float)cos((double)angPI), st = -(float)sin((double)angPI);
             op = 1.0f - ct;
             const float xk = (cx * cz * op - cy * st) * zn + ((1.0f - a) * ct + a) * xn + (cx * cy * op + cz * st) * yn;
             const float yk = (cy * cx * op - cz * st) * xn + ((1.0f - b) * ct + b) * yn + (cy * cz * op + cx * st) * zn;
             const float zk = (cz * cy * op - cx * st) * yn + ((1.0f - c) * ct + c) * zn + (cz * cx * op + cy * st) * xn;
             const float dihPI = (float)(sh.ic[l][2] * kPi / 180.0f);
-            ct = cosf(dihPI);
-            st = sinf(dihPI);
+            ct = (float)cos((double)dihPI);
+            st = (float)sin((double)dihPI);
             op = 1.0f - ct;
             cx = (x[2] - x[1]) * d;
             cy = (y[2] - y[1]) * d;

@@ -17,9 +17,14 @@
 namespace fxe {
 void launch_build(const DevSystem&, const DevWork&, int, const int32_t*, const double*, cudaStream_t);
 void launch_contacts(const DevSystem&, const DevWork&, int, cudaStream_t);
-void launch_voronoi(const DevSystem&, const DevWork&, int, cudaStream_t);
-void launch_score(const DevSystem&, const DevWork&, int, cudaStream_t);
+namespace f32 {
+void launch_poses(const DevSystem&, const DevWork&, int, cudaStream_t);
 cudaError_t configure_voronoi();
+}
+namespace f64 {
+void launch_poses(const DevSystem&, const DevWork&, int, cudaStream_t);
+cudaError_t configure_voronoi();
+}
 int thermo_blocks(long, int);
 void launch_thermo_partial(const double*, const int32_t*, long, double, LsePart*, int, cudaStream_t);
 void launch_thermo_weights(const double*, const int32_t*, long, double, double, double*, int, cudaStream_t);
@@ -52,6 +57,7 @@ struct fxe_context {
     double* d_icin = nullptr;
     int last_n = 0;
     int counters[4] = {0, 0, 0, 0};
+    int precision = FXE_PRECISION_REFERENCE;
 
     template <typename T>
     cudaError_t alloc(T** p, size_t count) {
@@ -136,7 +142,8 @@ extern "C" fxe_status fxe_context_create(const fxe_receptor_desc* rec, const fxe
     fxe_status st = [&]() -> fxe_status {
         FXE_TRY(cudaGetDevice(&ctx->device), "cudaGetDevice");
         FXE_TRY(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "cudaStreamCreate");
-        FXE_TRY(fxe::configure_voronoi(), "cudaFuncSetAttribute");
+        FXE_TRY(fxe::f32::configure_voronoi(), "cudaFuncSetAttribute");
+        FXE_TRY(fxe::f64::configure_voronoi(), "cudaFuncSetAttribute");
         fxe::DevSystem& S = ctx->S;
         const int N = rec->n_atoms, n = lig->n_atoms;
         // receptor atoms
@@ -254,8 +261,6 @@ extern "C" fxe_status fxe_context_create(const fxe_receptor_desc* rec, const fxe
         FXE_TRY(ctx->alloc(&W.cand_flag, PLC), "workspace");
         FXE_TRY(ctx->alloc(&W.cand_n, PL), "workspace");
         FXE_TRY(ctx->alloc(&W.clash_part, PL), "workspace");
-        FXE_TRY(ctx->alloc(&W.atom_status, PL), "workspace");
-        FXE_TRY(ctx->alloc(&W.rec0, PL * fxe::kMaskWords), "workspace");
         FXE_TRY(ctx->alloc(&W.out, P), "workspace");
         FXE_TRY(ctx->alloc(&W.counters, 4), "workspace");
         FXE_TRY(ctx->alloc(&ctx->d_genes, P * (ng > 0 ? ng : 1)), "staging");
@@ -277,8 +282,8 @@ fxe_status run_chunk(fxe_context* ctx, int nb, const int32_t* d_genes, const dou
                      cudaStream_t s) {
     fxe::launch_build(ctx->S, ctx->W, nb, d_genes, d_ic, s);
     fxe::launch_contacts(ctx->S, ctx->W, nb, s);
-    fxe::launch_voronoi(ctx->S, ctx->W, nb, s);
-    fxe::launch_score(ctx->S, ctx->W, nb, s);
+    if (ctx->precision == FXE_PRECISION_FAST) fxe::f32::launch_poses(ctx->S, ctx->W, nb, s);
+    else fxe::f64::launch_poses(ctx->S, ctx->W, nb, s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
     return FXE_OK;
@@ -349,18 +354,18 @@ extern "C" fxe_status fxe_last_contacts(fxe_context* ctx, int32_t pose, int32_t 
     *n_out = 0;
     if (nc <= 0) return FXE_OK;
     std::vector<int> idx(nc);
-    std::vector<float> ar(nc);
+    std::vector<double> ar(nc);
     std::vector<uint8_t> fl(nc);
     const size_t cb = lb * fxe::kMaxCand;
     FXE_TRY(cudaMemcpy(idx.data(), ctx->W.cand_idx + cb, nc * sizeof(int), cudaMemcpyDeviceToHost), "contacts");
-    FXE_TRY(cudaMemcpy(ar.data(), ctx->W.cand_area + cb, nc * sizeof(float), cudaMemcpyDeviceToHost), "contacts");
+    FXE_TRY(cudaMemcpy(ar.data(), ctx->W.cand_area + cb, nc * sizeof(double), cudaMemcpyDeviceToHost), "contacts");
     FXE_TRY(cudaMemcpy(fl.data(), ctx->W.cand_flag + cb, nc, cudaMemcpyDeviceToHost), "contacts");
     int k = 0;
     for (int c = nc - 1; c >= 0; --c) {  // newest record first, as vcfunction walks them
         if (!(fl[c] & fxe::kRecorded)) continue;
         if (k < cap) {
             if (partner) partner[k] = idx[c];
-            if (area) area[k] = ar[c];
+            if (area) area[k] = (float)ar[c];
         }
         ++k;
     }
@@ -368,9 +373,32 @@ extern "C" fxe_status fxe_last_contacts(fxe_context* ctx, int32_t pose, int32_t 
     return FXE_OK;
 }
 
+extern "C" fxe_status fxe_last_ligand_xyz(fxe_context* ctx, int32_t pose, float* xyz) {
+    g_err.clear();
+    if (!ctx || !xyz || pose < 0 || pose >= ctx->last_n) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    const int n = ctx->S.n_lig;
+    std::vector<float4> v(n);
+    FXE_TRY(cudaMemcpy(v.data(), ctx->W.lig_pos + (size_t)pose * n, n * sizeof(float4), cudaMemcpyDeviceToHost),
+            "ligand coordinates");
+    for (int l = 0; l < n; ++l) {
+        xyz[3 * l] = v[l].x;
+        xyz[3 * l + 1] = v[l].y;
+        xyz[3 * l + 2] = v[l].z;
+    }
+    return FXE_OK;
+}
+
 extern "C" fxe_status fxe_last_stats(fxe_context* ctx, int32_t* out4) {
     if (!ctx || !out4) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
     for (int i = 0; i < 4; ++i) out4[i] = ctx->counters[i];
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_context_set_precision(fxe_context* ctx, int32_t precision) {
+    g_err.clear();
+    if (!ctx || (precision != FXE_PRECISION_REFERENCE && precision != FXE_PRECISION_FAST))
+        return fail(FXE_ERR_INVALID_ARGS, "invalid precision mode");
+    ctx->precision = precision;
     return FXE_OK;
 }
 

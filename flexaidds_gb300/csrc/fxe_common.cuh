@@ -36,14 +36,12 @@ constexpr int kMaskWords = kMaxLig / 32;
 // candidate flag bits
 constexpr uint8_t kOnHull = 1;    // plane flag != 'X'
 constexpr uint8_t kEngulf = 2;    // plane flag 'E'
-constexpr uint8_t kTouches = 4;   // face reaches the atom's sphere (points or area)
 constexpr uint8_t kRecorded = 8;  // contact kept in the atom's record list
 
 // atom status
 constexpr int kAtomOk = 0;
 constexpr int kAtomHullFail = 1;
 constexpr int kAtomCapacity = 2;
-constexpr int kAtomSkipped = 3;   // pose rejected before the polyhedra
 
 struct DevSystem {
     // receptor
@@ -103,14 +101,12 @@ struct DevWork {
     float4* pose_gmin;     // [P]
     int* cand_idx;         // [P * n_lig * kMaxCand]
     float* cand_d2;        // [P * n_lig * kMaxCand]
-    float* cand_area;      // [P * n_lig * kMaxCand]
+    double* cand_area;     // [P * n_lig * kMaxCand]
     uint8_t* cand_flag;    // [P * n_lig * kMaxCand]
     int* cand_n;           // [P * n_lig]
     double* clash_part;    // [P * n_lig]
-    int* atom_status;      // [P * n_lig]
-    uint32_t* rec0;        // [P * n_lig * kMaskWords] ligand partners kept in the record list
     fxe_cf* out;           // [P]
-    int* counters;         // [4]: fix-up recomputes, hull failures, capacity, no-partner faces
+    int* counters;         // [4]: unused, hull failures, capacity, no-partner faces
 };
 
 // one block's share of the ensemble reduction: running max of the log-weights and the sums

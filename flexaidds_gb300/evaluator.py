@@ -43,9 +43,11 @@ def load_library():
         lib.fxe_eval_genes_device.argtypes = [vp, C.c_int32, vp, vp, vp]
         lib.fxe_last_contacts.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, _i, _f, _i]
         lib.fxe_last_stats.argtypes = [vp, _i]
+        lib.fxe_last_ligand_xyz.argtypes = [vp, C.c_int32, _f]
         lib.fxe_thermo_compute.argtypes = [_d, _i, C.c_int64, C.c_double, vp]
         lib.fxe_thermo_compute_device.argtypes = [vp, vp, C.c_int64, C.c_double, vp, vp]
         lib.fxe_thermo_weights.argtypes = [_d, _i, C.c_int64, C.c_double, _d]
+        lib.fxe_context_set_precision.argtypes = [vp, C.c_int32]
         lib.fxe_context_destroy.argtypes = [vp]
         lib.fxe_context_destroy.restype = None
         lib.fxe_last_error.restype = C.c_char_p
@@ -62,7 +64,9 @@ def _check(rc: int):
 class GPUEvaluator:
     """Evaluation context for one receptor, ligand and energy matrix."""
 
-    def __init__(self, desc: Descriptor, max_poses: int = 2048):
+    REFERENCE, FAST = 0, 1
+
+    def __init__(self, desc: Descriptor, max_poses: int = 2048, precision: int = 0):
         self.lib = load_library()
         self.desc = desc
         self._packed = Packed(desc)
@@ -72,6 +76,7 @@ class GPUEvaluator:
         _check(self.lib.fxe_context_create(C.byref(pk.rec), C.byref(pk.lig), C.byref(pk.emat),
                                            C.byref(pk.params), self.max_poses, C.byref(h)))
         self.handle = h
+        _check(self.lib.fxe_context_set_precision(self.handle, int(precision)))
 
     def close(self):
         if getattr(self, "handle", None):
@@ -111,11 +116,15 @@ class GPUEvaluator:
                                           C.byref(n)))
         return part[:n.value].copy(), area[:n.value].copy()
 
+    def ligand_xyz(self, pose: int) -> np.ndarray:
+        out = np.zeros((self.desc.n_lig, 3), np.float32)
+        _check(self.lib.fxe_last_ligand_xyz(self.handle, pose, ptr(out, _f)))
+        return out
+
     def stats(self) -> dict:
         o = np.zeros(4, np.int32)
         _check(self.lib.fxe_last_stats(self.handle, ptr(o, _i)))
-        return {"recomputed_atoms": int(o[0]), "hull_failures": int(o[1]), "capacity": int(o[2]),
-                "no_partner_faces": int(o[3])}
+        return {"hull_failures": int(o[1]), "capacity": int(o[2]), "no_partner_faces": int(o[3])}
 
 
 def ic2cf(evaluator: GPUEvaluator, icv) -> np.void:

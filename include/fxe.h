@@ -126,6 +126,17 @@ fxe_status fxe_context_create(const fxe_receptor_desc* receptor, const fxe_ligan
                               const fxe_emat_desc* emat, const fxe_params* params,
                               int32_t max_poses, fxe_context** out);
 
+/* Arithmetic of the Voronoi polyhedra and contact areas.
+ * FXE_PRECISION_REFERENCE (default): double precision with the reference's own expressions and
+ *   no fused multiply-adds, so that every operation rounds as in the reference's double
+ *   arithmetic; the reference's areas are sensitive to last-bit rounding on degenerate faces
+ *   (coincident projected vertices, antipodal arc points), and this mode reproduces them.
+ * FXE_PRECISION_FAST: single precision with well-conditioned equivalents of the area
+ *   expressions; agrees with the reference to about 1e-6 on typical poses and differs where the
+ *   reference's result is decided by rounding. */
+enum { FXE_PRECISION_REFERENCE = 0, FXE_PRECISION_FAST = 1 };
+fxe_status fxe_context_set_precision(fxe_context* ctx, int32_t precision);
+
 /* Scores n chromosomes given as int32 genes (n * n_genes, host memory), writing n records to
  * host memory. Synchronous, like cuda_eval_batch (LIB/cuda_eval.cuh:60-70). */
 fxe_status fxe_eval_genes(fxe_context* ctx, int32_t n, const int32_t* genes, fxe_cf* out);
@@ -145,9 +156,12 @@ fxe_status fxe_eval_genes_device(fxe_context* ctx, int32_t n, const int32_t* d_g
 fxe_status fxe_last_contacts(fxe_context* ctx, int32_t pose, int32_t ligand_atom, int32_t cap,
                              int32_t* partner, float* area, int32_t* n_out);
 
-/* Work counters of the last evaluation call: out4[0] atoms recomputed with the candidate list
- * the reference would have seen, [1] poses whose hull walk reached 200 edges, [2] poses over
- * capacity, [3] faces whose first vertex had no neighbour on its second plane. */
+/* Built ligand coordinates of pose `pose` of the last evaluated batch (n_atoms * 3). */
+fxe_status fxe_last_ligand_xyz(fxe_context* ctx, int32_t pose, float* xyz);
+
+/* Work counters of the last evaluation call: out4[0] reserved (0), [1] poses whose hull walk
+ * reached 200 edges, [2] poses over capacity, [3] faces whose first vertex had no neighbour on
+ * its second plane. */
 fxe_status fxe_last_stats(fxe_context* ctx, int32_t* out4);
 
 /* Thermodynamics of an ensemble of n energies (kcal/mol) with multiplicities (NULL = all 1)

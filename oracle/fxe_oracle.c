@@ -451,6 +451,16 @@ static int voronoi_poly2(State* S, int az, float rado, int NC) {
     return vn;
 }
 
+/* First position 1..n-1 of the face list whose vertex lies on plane pY (n if none). */
+static int find_partner(const Vert* poly, const int* pt, int n, int pY) {
+    int vi;
+    for (vi = 1; vi < n; ++vi) {
+        const Vert* p = &poly[pt[vi]];
+        if (p->plane[0] == pY || p->plane[1] == pY || p->plane[2] == pY) break;
+    }
+    return vi;
+}
+
 /* order_faces, LIB/Vcontacts.cpp:699-831: per contact plane, the polygon's vertices in
  * angular order (plus an antipodal arc point so no arc exceeds 180 degrees). */
 static void order_faces(State* S, float rado, int NC, int NV) {
@@ -491,21 +501,27 @@ static void order_faces(State* S, float rado, int NC, int NV) {
         }
         po[X].numpts = sc;
         if (sc > 3) {
-            int pY;
-            if (poly[po[X].pt[0]].plane[0] == X) pY = poly[po[X].pt[0]].plane[1];
-            else pY = poly[po[X].pt[0]].plane[0];
-            int vi;
-            for (vi = 1; vi < sc; ++vi) {
-                const Vert* p = &poly[po[X].pt[vi]];
-                if (p->plane[0] == pY || p->plane[1] == pY || p->plane[2] == pY) break;
+            const Vert* p0 = &poly[po[X].pt[0]];
+            int pY = (p0->plane[0] == X) ? p0->plane[1] : p0->plane[0];
+            int vi = find_partner(poly, po[X].pt, sc, pY);
+            if (vi == sc) {
+                if (S->counts) S->counts->no_partner++;
+                /* No vertex shares pt[0]'s second plane. The reference then swaps pt[1] with
+                   the slot past the face's end, which holds whatever an earlier face left
+                   there. Reference-compat mode replays that read (on a workspace zeroed at the
+                   start of every pose, as the test harness arranges). By default pt[0]'s other
+                   plane is tried instead, so that pt[0] and pt[1] are still neighbours on the
+                   face and the angular sort orders the face's points correctly. */
+                if (g_compat) {
+                    if (sc >= O_MAX_CONT) vi = 1;
+                } else {
+                    int pZ = (p0->plane[0] == X || p0->plane[1] == X) ? p0->plane[2] : p0->plane[1];
+                    if (p0->plane[0] != X && p0->plane[1] != X) pZ = p0->plane[1];
+                    vi = pZ >= 0 ? find_partner(poly, po[X].pt, sc, pZ) : sc;
+                    if (vi == sc) vi = 1;
+                }
             }
-            if (vi == sc && S->counts) S->counts->no_partner++;
-            /* When no vertex shares pt[0]'s second plane the reference swaps pt[1] with the
-               slot past the face's end, which holds whatever an earlier face left there.
-               Default: leave the collection order (what the reference does when that slot
-               holds this face's own pt[1]). Reference-compat mode replays the read on a
-               workspace zeroed at the start of every pose, as the test harness arranges. */
-            if (vi < sc || (g_compat && sc < O_MAX_CONT)) {
+            {
                 int t = po[X].pt[vi];
                 po[X].pt[vi] = po[X].pt[1];
                 po[X].pt[1] = t;
