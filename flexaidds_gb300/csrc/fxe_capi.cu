@@ -58,6 +58,11 @@ struct fxe_context {
     int last_n = 0;
     int counters[4] = {0, 0, 0, 0};
     int precision = FXE_PRECISION_REFERENCE;
+    // per-stage timing (fxe_context_enable_timing) and the count of kernels launched
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    double stage_ms[3] = {0.0, 0.0, 0.0};
+    int64_t launches = 0;
 
     template <typename T>
     cudaError_t alloc(T** p, size_t count) {
@@ -79,6 +84,8 @@ struct fxe_context {
         return e;
     }
     ~fxe_context() {
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
         for (void* p : allocs) cudaFree(p);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -280,12 +287,26 @@ namespace {
 
 fxe_status run_chunk(fxe_context* ctx, int nb, const int32_t* d_genes, const double* d_ic,
                      cudaStream_t s) {
+    const bool t = ctx->timing;
+    if (t) cudaEventRecord(ctx->ev[0], s);
     fxe::launch_build(ctx->S, ctx->W, nb, d_genes, d_ic, s);
+    if (t) cudaEventRecord(ctx->ev[1], s);
     fxe::launch_contacts(ctx->S, ctx->W, nb, s);
+    if (t) cudaEventRecord(ctx->ev[2], s);
     if (ctx->precision == FXE_PRECISION_FAST) fxe::f32::launch_poses(ctx->S, ctx->W, nb, s);
     else fxe::f64::launch_poses(ctx->S, ctx->W, nb, s);
+    if (t) cudaEventRecord(ctx->ev[3], s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    ctx->launches += 3;
+    if (t) {
+        FXE_TRY(cudaEventSynchronize(ctx->ev[3]), "timing");
+        for (int k = 0; k < 3; ++k) {
+            float ms = 0.0f;
+            FXE_TRY(cudaEventElapsedTime(&ms, ctx->ev[k], ctx->ev[k + 1]), "timing");
+            ctx->stage_ms[k] += ms;
+        }
+    }
     return FXE_OK;
 }
 
@@ -336,10 +357,34 @@ extern "C" fxe_status fxe_eval_genes_device(fxe_context* ctx, int32_t n, const i
     if (n > ctx->W.max_poses) return fail(FXE_ERR_INVALID_ARGS, "n exceeds the context's max_poses");
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
     if (n == 0) return FXE_OK;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
+    FXE_TRY(cudaMemsetAsync(ctx->W.counters, 0, 4 * sizeof(int), s), "counters");
     fxe_status st = run_chunk(ctx, n, d_genes, nullptr, s);
     if (st != FXE_OK) return st;
     FXE_TRY(cudaMemcpyAsync(d_out, ctx->W.out, (size_t)n * sizeof(fxe_cf), cudaMemcpyDeviceToDevice, s), "results");
     ctx->last_n = n;
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_context_enable_timing(fxe_context* ctx, int32_t on) {
+    g_err.clear();
+    if (!ctx) return fail(FXE_ERR_INVALID_ARGS, "ctx is NULL");
+    if (on && !ctx->ev[0]) {
+        for (auto& e : ctx->ev) FXE_TRY(cudaEventCreate(&e), "timing events");
+    }
+    ctx->timing = on != 0;
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_context_take_timing(fxe_context* ctx, double* ms3, int64_t* launches) {
+    g_err.clear();
+    if (!ctx) return fail(FXE_ERR_INVALID_ARGS, "ctx is NULL");
+    for (int k = 0; k < 3; ++k) {
+        if (ms3) ms3[k] = ctx->stage_ms[k];
+        ctx->stage_ms[k] = 0.0;
+    }
+    if (launches) *launches = ctx->launches;
+    ctx->launches = 0;
     return FXE_OK;
 }
 

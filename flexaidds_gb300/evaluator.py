@@ -48,6 +48,8 @@ def load_library():
         lib.fxe_thermo_compute_device.argtypes = [vp, vp, C.c_int64, C.c_double, vp, vp]
         lib.fxe_thermo_weights.argtypes = [_d, _i, C.c_int64, C.c_double, _d]
         lib.fxe_context_set_precision.argtypes = [vp, C.c_int32]
+        lib.fxe_context_enable_timing.argtypes = [vp, C.c_int32]
+        lib.fxe_context_take_timing.argtypes = [vp, _d, C.POINTER(C.c_int64)]
         lib.fxe_context_destroy.argtypes = [vp]
         lib.fxe_context_destroy.restype = None
         lib.fxe_last_error.restype = C.c_char_p
@@ -115,6 +117,16 @@ class GPUEvaluator:
         _check(self.lib.fxe_last_contacts(self.handle, pose, atom, cap, ptr(part, _i), ptr(area, _f),
                                           C.byref(n)))
         return part[:n.value].copy(), area[:n.value].copy()
+
+    def enable_timing(self, on: bool = True):
+        _check(self.lib.fxe_context_enable_timing(self.handle, 1 if on else 0))
+
+    def take_timing(self):
+        """(ms per stage [build, candidates, polyhedra+scoring], kernels launched) since the last call."""
+        ms = np.zeros(3, np.float64)
+        n = C.c_int64(0)
+        _check(self.lib.fxe_context_take_timing(self.handle, ptr(ms, _d), C.byref(n)))
+        return ms, int(n.value)
 
     def ligand_xyz(self, pose: int) -> np.ndarray:
         out = np.zeros((self.desc.n_lig, 3), np.float32)

@@ -84,6 +84,7 @@ def _poisson_disc(n_atoms, cleft_radius, seed, min_sep, edge):
     ng = int(math.ceil(edge / cell))
     grid = -np.ones((ng, ng, ng), dtype=np.int64)
     pts: list[np.ndarray] = []
+    arr = np.zeros((n_atoms + 1, 3), np.float64)   # pts as one array, for the distance checks
 
     def gidx(p):
         return tuple(np.minimum(((p + half) / cell).astype(np.int64), ng - 1))
@@ -98,12 +99,12 @@ def _poisson_disc(n_atoms, cleft_radius, seed, min_sep, edge):
         blk = blk[blk >= 0]
         if blk.size == 0:
             return True
-        q = np.asarray([pts[i] for i in blk])
-        d = q - p
+        d = arr[blk] - p
         return bool(np.all(np.einsum('ij,ij->i', d, d) >= r2min))
 
     def add(p):
         grid[gidx(p)] = len(pts)
+        arr[len(pts)] = p
         pts.append(p)
 
     while True:

@@ -125,6 +125,26 @@ class Descriptor:
                                      int(self.gene_map[g])) for g in range(self.n_genes)]
         return self.decode
 
+    _ARRAYS = ("rec_xyz", "rec_radius", "rec_type", "ori", "globalmin", "globalmax", "grid_ic",
+               "lig_radius", "lig_type", "lig_rec", "lig_shift", "lig_ic", "build_order", "bonded",
+               "gene_typ", "gene_atm", "gene_min", "gene_max", "gene_del", "gene_map", "opt_par",
+               "emat_weight", "emat_off", "emat_x", "emat_y")
+    _SCALARS = ("maxwidth", "ntypes", "permeability", "dee_clash", "intramolecular", "solventterm")
+
+    def to_arrays(self, prefix: str = "") -> dict:
+        """Flat name -> array mapping (for np.savez)."""
+        out = {prefix + k: np.asarray(getattr(self, k)) for k in self._ARRAYS}
+        out.update({prefix + k: np.asarray(getattr(self, k)) for k in self._SCALARS})
+        return out
+
+    @classmethod
+    def from_arrays(cls, arrs, prefix: str = "") -> "Descriptor":
+        kw = {k: np.asarray(arrs[prefix + k]).copy() for k in cls._ARRAYS}
+        for k in cls._SCALARS:
+            v = np.asarray(arrs[prefix + k]).item()
+            kw[k] = int(v) if k in ("ntypes", "intramolecular") else float(v)
+        return cls(**kw)
+
     def genes_to_ic(self, genes: np.ndarray) -> np.ndarray:
         """Decode int32 genes to ICs exactly as LIB/gaboom.cpp:2887-2906 (genetoic) does."""
         genes = np.asarray(genes, np.int32)
@@ -158,9 +178,9 @@ def gene_bins(gmin: float, gmax: float, gdel: float, gmap: int) -> np.ndarray:
 
 
 def make_inputs(n_rec: int, cleft_radius: float, n_lig: int, n_tor: int, seed: int,
-                spacing: float = 0.375) -> SystemInputs:
-    """One seeded docking system of the given shape."""
-    rec = synth.poisson_disc_receptor(n_rec, cleft_radius, seed=seed)
+                spacing: float = 0.375, edge: float | None = None) -> SystemInputs:
+    """One seeded docking system of the given shape (``edge``: receptor cube edge to start from)."""
+    rec = synth.poisson_disc_receptor(n_rec, cleft_radius, seed=seed, edge=edge)
     lig = synth.random_ligand(n_lig, n_tor, seed=seed + 1)
     grid = synth.cleft_grid(rec.cleft_center, cleft_radius, spacing)
     emat = synth.energy_matrix(seed + 2)

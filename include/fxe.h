@@ -180,6 +180,18 @@ fxe_status fxe_thermo_compute_device(const double* d_energies, const int32_t* d_
 fxe_status fxe_thermo_weights(const double* energies, const int32_t* multiplicity, int64_t n,
                               double temperature, double* weights);
 
+/* Per-stage device time of the evaluation calls. When enabled, every batch records CUDA events
+ * around its three kernels (pose build, contact candidates, polyhedra and scoring) on the
+ * batch's stream and waits for the last one, so fxe_eval_genes_device returns only after its
+ * work is done. No reference counterpart (the reference times nothing below gaboom's
+ * generation loop). */
+fxe_status fxe_context_enable_timing(fxe_context* ctx, int32_t on);
+
+/* Milliseconds per stage accumulated since the previous call (ms3[0] build, [1] contact
+ * candidates, [2] polyhedra and scoring), and the number of kernels launched (counted whether
+ * or not timing is enabled); resets both. */
+fxe_status fxe_context_take_timing(fxe_context* ctx, double* ms3, int64_t* launches);
+
 void fxe_context_destroy(fxe_context* ctx);
 
 /* Message describing the last error on the calling thread ("" if none). */

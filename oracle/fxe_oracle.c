@@ -32,6 +32,17 @@ static int g_compat = 0;
 
 void fxo_set_reference_compat(int on) { g_compat = on; }
 
+/* Trigonometry of the pose build. The reference calls the C library's cosf/sinf
+   (LIB/buildcc.cpp:80-100), whose last bit is not correctly rounded for about 1% of
+   arguments and differs between C libraries. Mode 1 uses the correctly rounded values
+   (double-precision cos/sin rounded once to float), the values the CUDA build kernel uses. */
+static int g_trig_cr = 0;
+
+void fxo_set_trig_rounding(int correctly_rounded) { g_trig_cr = correctly_rounded; }
+
+static float o_cosf(float x) { return g_trig_cr ? (float)cos((double)x) : cosf(x); }
+static float o_sinf(float x) { return g_trig_cr ? (float)sin((double)x) : sinf(x); }
+
 typedef struct { double Ai[4]; double dist; int index; double area; char flag; } Plane;
 typedef struct { double xi[3]; double dist; int plane[3]; } Vert;
 typedef struct { double V[3]; int startpt, endpt, plane[2], startplane, endplane; char arc; } Edge;
@@ -405,7 +416,10 @@ static int voronoi_poly2(State* S, int az, float rado, int NC) {
         ++vn;
         if (vn >= O_MAX_POLY - 4 || edgenum >= O_MAX_POLY - 4) return -1;
     }
-    if (S->counts) S->counts->edges += edgenum;
+    if (S->counts) {
+        S->counts->edges += edgenum;
+        S->counts->plane_tests += (int64_t)edgenum * NC;
+    }
 
     for (int ei = 0; ei < edgenum; ++ei) {
         if ((rado < poly[ve[ei].startpt].dist) || (rado < poly[ve[ei].endpt].dist)) ve[ei].arc = '?';
@@ -962,14 +976,14 @@ static void buildcc(State* S, const fxe_receptor_desc* rec, const fxe_ligand_des
         b = cy * cy;
         c = cz * cz;
         float angPI = (float)(S->lic[l][1] * O_PI / 180.0f);
-        float ct = cosf(angPI), st = -sinf(angPI);
+        float ct = o_cosf(angPI), st = -o_sinf(angPI);
         op = 1.0f - ct;
         float xk = (cx * cz * op - cy * st) * zn + ((1.0f - a) * ct + a) * xn + (cx * cy * op + cz * st) * yn;
         float yk = (cy * cx * op - cz * st) * xn + ((1.0f - b) * ct + b) * yn + (cy * cz * op + cx * st) * zn;
         float zk = (cz * cy * op - cx * st) * yn + ((1.0f - c) * ct + c) * zn + (cz * cx * op + cy * st) * xn;
         float dihPI = (float)(S->lic[l][2] * O_PI / 180.0f);
-        ct = cosf(dihPI);
-        st = sinf(dihPI);
+        ct = o_cosf(dihPI);
+        st = o_sinf(dihPI);
         op = 1.0f - ct;
         cx = (x[2] - x[1]) * d;
         cy = (y[2] - y[1]) * d;

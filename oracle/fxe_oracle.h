@@ -31,12 +31,17 @@ typedef struct fxo_contact {
 typedef struct fxo_counts {
     int64_t atoms, candidates, contacts, edges, arc_edges, triangles, vertices, built_atoms;
     int64_t no_partner;  /* faces whose first vertex has no neighbour on its second plane */
+    int64_t plane_tests; /* sum over atoms of contacts x hull edges walked */
 } fxo_counts;
 
 /* Reference-compat mode: reproduce the reference's read of the slot past a face's vertex list
  * in order_faces (see fxe_oracle.c), on a workspace zeroed at the start of every pose. Used
  * only to pin this restatement against the compiled reference; off by default. */
 void fxo_set_reference_compat(int on);
+
+/* 0 (default): cosf/sinf of the C library in the pose build, as the reference;
+   1: correctly rounded single-precision cos/sin. */
+void fxo_set_trig_rounding(int correctly_rounded);
 
 /* Scores n poses given as decoded ICs (n * n_genes). xyz_out (n * n_lig * 3) receives the
  * built ligand coordinates when non-NULL; contacts_out (capacity cap) the recorded contacts,

@@ -30,7 +30,8 @@ CONTACT_DTYPE = np.dtype([("pose", np.int32), ("atom", np.int32), ("partner", np
 
 class Counts(C.Structure):
     _fields_ = [(k, C.c_int64) for k in ("atoms", "candidates", "contacts", "edges", "arc_edges",
-                                         "triangles", "vertices", "built_atoms", "no_partner")]
+                                         "triangles", "vertices", "built_atoms", "no_partner",
+                                         "plane_tests")]
 
 
 def build():
@@ -50,6 +51,7 @@ def _load():
         _lib.fxo_thermo.argtypes = [_d, _i, C.c_int64, C.c_double, C.c_void_p]
         _lib.fxo_thermo_weights.argtypes = [_d, _i, C.c_int64, C.c_double, _d]
         _lib.fxo_set_reference_compat.argtypes = [C.c_int]
+        _lib.fxo_set_trig_rounding.argtypes = [C.c_int]
         _lib.fxo_solve_3x3.argtypes = [_d, _d, _d, _d]
         _lib.fxo_solve_2xS.argtypes = [_d, _d, C.c_float, _d, _d]
         _lib.fxo_cosPQR.argtypes = [_d, _d, _d]
@@ -108,6 +110,12 @@ class Oracle:
 def set_reference_compat(on: bool):
     """Replays the reference's stale-slot read in order_faces (for pinning against it)."""
     _load().fxo_set_reference_compat(1 if on else 0)
+
+
+def set_trig_rounding(correctly_rounded: bool):
+    """Pose-build trigonometry: the C library's cosf/sinf (False, as the reference) or the
+    correctly rounded values the CUDA build kernel computes (True)."""
+    _load().fxo_set_trig_rounding(1 if correctly_rounded else 0)
 
 
 def thermo(e, mult=None, temperature=300.0) -> dict:

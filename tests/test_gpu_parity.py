@@ -1,0 +1,135 @@
+"""CUDA path against the oracle and the reference's golden fixtures, through the C ABI.
+
+Tolerances (per pose, relative to max(1, |E|)):
+  * reference precision (FP64 polyhedra, the reference's expressions), identical inputs:
+    every scored pose within 1e-6; status classes identical; ligand coordinates bit-identical;
+  * against the golden fixtures of the compiled reference: the same, except on poses where the
+    reference reads the stale face slot (counted and printed) and poses whose coordinates differ
+    in the last bit because the C library's cosf/sinf are not correctly rounded (counted);
+  * fast precision (FP32 polyhedra): median within 1e-5, 1e-4 on most poses; the rest are
+    poses where the area formulas are ill-conditioned (counted and printed).
+"""
+import numpy as np
+import pytest
+
+from flexaidds_gb300 import evaluator, prepare, synth, system
+from oracle import port
+
+pytestmark = pytest.mark.gpu
+
+REF, FAST = evaluator.GPUEvaluator.REFERENCE, evaluator.GPUEvaluator.FAST
+
+
+def rel_err(a, b):
+    return np.abs(a - b) / np.maximum(1.0, np.abs(b))
+
+
+def oracle_eval(d, ic, **kw):
+    port.set_reference_compat(False)
+    port.set_trig_rounding(True)
+    try:
+        return port.Oracle(d).eval_ic(ic, **kw)
+    finally:
+        port.set_trig_rounding(False)
+
+
+@pytest.fixture(scope="module")
+def c0():
+    inp = system.make_inputs(2000, 8.0, 24, 6, seed=41)
+    d = prepare.prepare(inp)
+    # uniform chromosomes clash nine times in ten: enrich with poses that get scored
+    pool = synth.random_genes(12000, d.n_genes, seed=42)
+    ic = d.genes_to_ic(pool)
+    st = oracle_eval(d, ic)["cf"]["status"]
+    sel = np.concatenate([np.nonzero(st == 0)[0][:400], np.nonzero(st != 0)[0][:200]])
+    return d, pool[np.sort(sel)]
+
+
+@pytest.mark.parametrize("prec", [REF, FAST])
+def test_random_chromosomes_against_oracle(c0, prec):
+    d, genes = c0
+    r = oracle_eval(d, d.genes_to_ic(genes), want_xyz=True)
+    ev = evaluator.GPUEvaluator(d, max_poses=1024, precision=prec)
+    g = ev.eval_genes(genes)
+    np.testing.assert_array_equal(g["status"], r["cf"]["status"])
+    ok = g["status"] == 0
+    assert ok.sum() >= 300
+    for p in range(len(genes)):
+        np.testing.assert_array_equal(ev.ligand_xyz(p), r["xyz"][p])
+    e = rel_err(g["evalue"], r["cf"]["evalue"])
+    assert np.all(e[~ok] <= 1e-6)          # sentinels and clash sums
+    np.testing.assert_array_equal(g["rclash"][ok], r["cf"]["rclash"][ok])
+    if prec == REF:
+        assert e[ok].max() <= 1e-6, e[ok].max()
+        for k in ("com", "wal", "sas"):
+            assert rel_err(g[k][ok], r["cf"][k][ok]).max() <= 1e-6, k
+    else:
+        bad = (e[ok] > 1e-4).sum()
+        print(f"fast precision: {ok.sum()} scored, median {np.median(e[ok]):.1e}, {bad} beyond 1e-4")
+        assert np.median(e[ok]) <= 1e-5
+        assert bad <= 0.2 * ok.sum()
+    assert ev.stats()["capacity"] == 0
+    ev.close()
+
+
+def test_contact_lists_against_oracle(c0):
+    d, genes = c0
+    genes = genes[:120]
+    r = oracle_eval(d, d.genes_to_ic(genes), want_contacts=True)
+    ev = evaluator.GPUEvaluator(d, max_poses=256, precision=REF)
+    g = ev.eval_genes(genes)
+    c = r["contacts"]
+    want = {}
+    for p, a, q, s in zip(c["pose"], c["atom"], c["partner"], c["area"]):
+        want.setdefault((int(p), int(a)), []).append((int(q), float(s)))
+    n_checked = 0
+    for p in np.nonzero(g["status"] == 0)[0]:
+        for a in range(d.n_lig):
+            part, area = ev.contacts(int(p), a)
+            mine = sorted(zip(part.tolist(), area.tolist()))
+            theirs = sorted(want.get((int(p), a), []))
+            assert [m[0] for m in mine] == [t[0] for t in theirs], (p, a)
+            np.testing.assert_allclose([m[1] for m in mine], [t[1] for t in theirs], rtol=1e-5, atol=1e-5)
+            n_checked += len(mine)
+    assert n_checked > 1000
+    ev.close()
+
+
+def test_golden_fixtures(golden):
+    """Against the compiled reference's own results (made by tests/golden/make_golden.py)."""
+    name, d, g = golden
+    port.set_reference_compat(False)
+    o = port.Oracle(d)
+    stale = np.array([o.eval_ic(g["ic"][p:p + 1], counts=True)["counts"]["no_partner"] > 0
+                      for p in range(g["ic"].shape[0])])
+    ev = evaluator.GPUEvaluator(d, max_poses=512, precision=REF)
+    out = ev.eval_genes(g["genes"])
+    np.testing.assert_array_equal(out["status"], g["status"])
+    ok = g["status"] == 0
+    same_xyz = np.array([np.array_equal(ev.ligand_xyz(p), g["xyz"][p]) for p in range(len(ok))])
+    e = rel_err(out["evalue"], g["cf"][:, 9])
+    clean = ok & ~stale & same_xyz
+    print(f"{name}: {ok.sum()} scored; {(ok & stale).sum()} with stale-slot faces; "
+          f"{(ok & ~same_xyz).sum()} with last-bit coordinate differences; "
+          f"{(e[ok] > 1e-4).sum()} beyond 1e-4 in all, {(e[clean] > 1e-6).sum()} of the others beyond 1e-6")
+    assert clean.sum() >= 0.6 * ok.sum()
+    assert e[clean].max() <= 1e-6
+    assert np.all(e[~ok] <= 1e-6)
+    ev.close()
+
+
+def test_scale_system_against_oracle():
+    """6,000-atom receptor, 12 A cleft, 48-atom ligand with 12 torsions."""
+    inp = system.make_inputs(6000, 12.0, 48, 12, seed=61)
+    d = prepare.prepare(inp)
+    pool = synth.random_genes(6000, d.n_genes, seed=62)
+    ic = d.genes_to_ic(pool)
+    r = oracle_eval(d, ic)["cf"]
+    sel = np.concatenate([np.nonzero(r["status"] == 0)[0][:150], np.nonzero(r["status"] != 0)[0][:50]])
+    ev = evaluator.GPUEvaluator(d, max_poses=256, precision=REF)
+    g = ev.eval_genes(pool[sel])
+    np.testing.assert_array_equal(g["status"], r["status"][sel])
+    ok = g["status"] == 0
+    assert ok.sum() >= 20
+    assert rel_err(g["evalue"], r["evalue"][sel]).max() <= 1e-6
+    ev.close()

@@ -1,0 +1,132 @@
+"""Host-side pieces that need no GPU: generators, set-up, gene decode, the C ABI's library."""
+import ctypes as C
+import importlib.util
+import os
+import re
+
+import numpy as np
+import pytest
+
+from flexaidds_gb300 import capi, prepare, synth, system
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _make_golden():
+    spec = importlib.util.spec_from_file_location(
+        "make_golden", os.path.join(ROOT, "tests", "golden", "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+# --- generators -----------------------------------------------------------------------------
+
+def test_receptor_generator_is_seeded_and_poisson():
+    a = synth.poisson_disc_receptor(600, 6.0, seed=3)
+    b = synth.poisson_disc_receptor(600, 6.0, seed=3)
+    np.testing.assert_array_equal(a.xyz, b.xyz)
+    np.testing.assert_array_equal(a.type, b.type)
+    assert a.xyz.shape == (600, 3) and a.type.min() >= 1 and a.type.max() <= 40
+    d2 = ((a.xyz[:, None, :] - a.xyz[None, :, :]) ** 2).sum(-1)
+    d2[np.arange(600), np.arange(600)] = 1e9
+    assert np.sqrt(d2.min()) >= 2.8 - 1e-4
+    assert np.linalg.norm(a.xyz - a.cleft_center, axis=1).min() >= 6.0
+
+
+def test_ligand_generator_geometry():
+    lig = synth.random_ligand(24, 6, seed=7)
+    assert lig.xyz.shape == (24, 3)
+    for i, j in lig.bonds:
+        assert abs(np.linalg.norm(lig.xyz[i] - lig.xyz[j]) - 1.53) < 1e-3
+    assert sum(1 for f in lig.flex if len(f)) == 6
+
+
+# --- set-up restatement against the reference's own set-up (golden descriptors) ---------------
+
+@pytest.mark.parametrize("name", ["c0_2000_24", "curves_900_16"])
+def test_prepare_matches_reference_setup(name):
+    from conftest import load_golden
+    dref, _ = load_golden(name)
+    d = prepare.prepare(_make_golden().inputs_for(name))
+    for k in ("lig_rec", "build_order", "bonded", "gene_typ", "gene_atm", "gene_map", "rec_type",
+              "lig_type", "emat_weight", "emat_off"):
+        np.testing.assert_array_equal(getattr(d, k), getattr(dref, k), err_msg=k)
+    for k in ("gene_min", "gene_max", "gene_del", "emat_x", "emat_y", "rec_xyz", "rec_radius",
+              "lig_radius"):
+        np.testing.assert_array_equal(getattr(d, k), getattr(dref, k), err_msg=k)
+    # float geometry of buildic / calc_center / calc_cleftic: the restatement rounds the same
+    # expressions in a different order in places
+    for k, tol in (("ori", 1e-5), ("globalmin", 1e-5), ("globalmax", 1e-5), ("lig_ic", 1e-3),
+                   ("lig_shift", 1e-3), ("grid_ic", 1e-3)):
+        np.testing.assert_allclose(getattr(d, k), getattr(dref, k), atol=tol, err_msg=k)
+
+
+# --- gene decode (genetoic, LIB/gaboom.cpp:2887-2906) ------------------------------------------
+
+def _genetoic_walk(gmin, gmax, gdel, gmap, gene):
+    """The reference's linear walk, written out: tot += bin until tot >= u."""
+    nbin = (gmax - gmin) / gdel
+    if nbin - int(nbin) > 0.0:
+        nbin += 1.0
+    if gmap:
+        nbin += 1.0
+    b = 1.0 / nbin
+    u = gene / (2147483647.0 + 1.0)
+    tot, i = b, 0
+    while tot < u:
+        tot += b
+        i += 1
+    return gmin + gdel * i
+
+
+@pytest.mark.parametrize("lim", [(-180.0, 180.0, 10.0, 0), (0.0, 180.0, 5.0, 0), (1.0, 4095.0, 1.0, 1),
+                                 (-180.0, 175.0, 5.0, 0)])
+def test_gene_decode_matches_linear_walk(lim):
+    tab = system.gene_bins(*lim)
+    rng = np.random.default_rng(1)
+    genes = np.concatenate([[0, 1, 2147483647, 1073741824], rng.integers(0, 2 ** 31, 3000)])
+    u = genes.astype(np.float64) / 2147483648.0
+    got = lim[0] + lim[2] * np.searchsorted(tab, u, side="left")
+    want = np.array([_genetoic_walk(*lim, int(g)) for g in genes])
+    np.testing.assert_array_equal(got, want)
+
+
+# --- the C ABI's library ------------------------------------------------------------------------
+
+def _declared_symbols():
+    hdr = open(os.path.join(ROOT, "include", "fxe.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    hdr = re.sub(r"//[^\n]*", "", hdr)
+    return sorted(set(re.findall(r"\b(fxe_[a-z0-9_]+)\s*\(", hdr)))
+
+
+@pytest.fixture(scope="module")
+def libfxe():
+    from flexaidds_gb300 import build
+    if not os.path.exists(build.LIB):
+        build.build()
+    return C.CDLL(build.LIB)
+
+
+def test_library_exports_every_declared_symbol(libfxe):
+    names = _declared_symbols()
+    assert len(names) >= 12
+    missing = [n for n in names if not hasattr(libfxe, n)]
+    assert not missing, missing
+
+
+def test_library_reports_errors_without_device(libfxe):
+    """Entry points validate their arguments before touching a device."""
+    libfxe.fxe_last_error.restype = C.c_char_p
+    libfxe.fxe_context_create.argtypes = [C.c_void_p] * 4 + [C.c_int32, C.c_void_p]
+    out = C.c_void_p()
+    rc = libfxe.fxe_context_create(None, None, None, None, 16, C.byref(out))
+    assert rc == 1 and out.value is None
+    assert b"null" in libfxe.fxe_last_error().lower()
+
+
+def test_struct_layouts_match_header():
+    assert C.sizeof(capi.CF) == 11 * 8 + 2 * 4
+    assert capi.CF_DTYPE.itemsize == C.sizeof(capi.CF)
+    assert C.sizeof(capi.Thermo) == 8 * 8
