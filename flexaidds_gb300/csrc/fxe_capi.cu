@@ -5,6 +5,7 @@
 // CUDA stream. Batches larger than max_poses are scored in chunks.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -545,4 +546,45 @@ extern "C" fxe_status fxe_thermo_compute_device(const double* d_energies, const 
     if (!d_energies || n <= 0 || !(temperature > 0.0) || !out)
         return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
     return thermo_run(d_energies, d_multiplicity, n, temperature, out, nullptr, (cudaStream_t)stream);
+}
+
+// ------------------------------------------------------------------------------------------
+// fxe_thermo_compute_device_fixed: the reduction with library-owned scratch, no allocation.
+// ------------------------------------------------------------------------------------------
+namespace fxe {
+cudaError_t fixed_scratch_address(LsePart** p);
+void launch_thermo_fixed(const double*, const int32_t*, long, double, double, LsePart*, fxe_thermo*,
+                         cudaStream_t);
+}  // namespace fxe
+
+namespace {
+constexpr int kFixedMaxDevices = 64;
+std::atomic<fxe::LsePart*> g_fixed_scratch[kFixedMaxDevices];
+}  // namespace
+
+extern "C" fxe_status fxe_thermo_compute_device_fixed(const double* d_energies, const int32_t* d_multiplicity,
+                                                      int64_t n, double temperature, fxe_thermo* d_out,
+                                                      void* stream) {
+    g_err.clear();
+    if (!d_energies || !d_out || n <= 0 || !(temperature > 0.0))
+        return fail(FXE_ERR_INVALID_ARGS, "invalid arguments (NULL pointer, n <= 0 or T <= 0)");
+    if (n > FXE_THERMO_FIXED_MAX_N)
+        return fail(FXE_ERR_INVALID_ARGS, "n = " + std::to_string(n) + " exceeds FXE_THERMO_FIXED_MAX_N = " +
+                                              std::to_string((long long)FXE_THERMO_FIXED_MAX_N) +
+                                              " (the fixed scratch holds " +
+                                              std::to_string(FXE_THERMO_FIXED_MAX_BLOCKS) + " block partials)");
+    int dev = 0;
+    FXE_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= kFixedMaxDevices) return fail(FXE_ERR_NO_DEVICE, "device ordinal out of range");
+    fxe::LsePart* scratch = g_fixed_scratch[dev].load(std::memory_order_acquire);
+    if (!scratch) {
+        // set-up, once per device, with that device current
+        FXE_TRY(fxe::fixed_scratch_address(&scratch), "cudaGetSymbolAddress of the fixed scratch");
+        g_fixed_scratch[dev].store(scratch, std::memory_order_release);
+    }
+    const double beta = 1.0 / (0.001987206 * temperature);  // LIB/statmech.h:26
+    fxe::launch_thermo_fixed(d_energies, d_multiplicity, (long)n, beta, temperature, scratch, d_out,
+                             (cudaStream_t)stream);
+    FXE_TRY(cudaGetLastError(), "fixed-scratch thermo launch");
+    return FXE_OK;
 }

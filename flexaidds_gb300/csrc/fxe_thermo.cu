@@ -123,3 +123,95 @@ void thermo_finish(const LsePart* part, int nb, double T, fxe_thermo* out) {
 }
 
 }  // namespace fxe
+
+// ------------------------------------------------------------------------------------------
+// Fixed-scratch variant: the same reduction with the block partials in a file-scope device
+// array and the merge on the device, for callers that may not allocate (see
+// fxe_thermo_compute_device_fixed in include/fxe.h).
+// ------------------------------------------------------------------------------------------
+namespace fxe {
+
+constexpr long kFixedPerBlock = (long)kThermoThreads * FXE_THERMO_FIXED_PER_THREAD;
+
+// One partial per block; every slot a call reads is written by that call first, so nothing
+// here needs to start at zero.
+static __device__ __align__(256) LsePart g_fixed_part[FXE_THERMO_FIXED_MAX_BLOCKS];
+
+cudaError_t fixed_scratch_address(LsePart** p) {
+    return cudaGetSymbolAddress(reinterpret_cast<void**>(p), g_fixed_part);
+}
+
+__global__ void __launch_bounds__(kThermoThreads)
+thermo_fixed_partial_kernel(const double* __restrict__ e, const int32_t* __restrict__ mult, long n,
+                            double beta, LsePart* __restrict__ part) {
+    LseState st{-INFINITY, 0.0, 0.0, 0.0};
+    const long lo = (long)blockIdx.x * kFixedPerBlock;
+    const long hi = lo + kFixedPerBlock < n ? lo + kFixedPerBlock : n;
+    for (long i = lo + threadIdx.x; i < hi; i += kThermoThreads) {
+        const double ei = e[i];
+        const double lw = (mult ? log((double)mult[i]) : 0.0) - beta * ei;
+        lse_push(st, lw, ei);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        LseState other{__shfl_xor_sync(0xffffffffu, st.m, o), __shfl_xor_sync(0xffffffffu, st.s, o),
+                       __shfl_xor_sync(0xffffffffu, st.e1, o), __shfl_xor_sync(0xffffffffu, st.e2, o)};
+        st = lse_merge(st, other);
+    }
+    __shared__ LseState ws[kThermoThreads / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = st;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        LseState t = ws[0];
+        for (int w = 1; w < kThermoThreads / 32; ++w) t = lse_merge(t, ws[w]);
+        part[blockIdx.x] = {t.m, t.s, t.e1, t.e2};
+    }
+}
+
+// One block merges the partials and writes the record (the host merge of thermo_finish, done
+// as a tree).
+__global__ void __launch_bounds__(kThermoThreads)
+thermo_fixed_finish_kernel(const LsePart* __restrict__ part, int nb, double T, fxe_thermo* __restrict__ out) {
+    LseState st{-INFINITY, 0.0, 0.0, 0.0};
+    for (int b = threadIdx.x; b < nb; b += kThermoThreads) {
+        const LsePart q = part[b];
+        st = lse_merge(st, LseState{q.m, q.s, q.e1, q.e2});
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        LseState other{__shfl_xor_sync(0xffffffffu, st.m, o), __shfl_xor_sync(0xffffffffu, st.s, o),
+                       __shfl_xor_sync(0xffffffffu, st.e1, o), __shfl_xor_sync(0xffffffffu, st.e2, o)};
+        st = lse_merge(st, other);
+    }
+    __shared__ LseState ws[kThermoThreads / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = st;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        LseState t = ws[0];
+        for (int w = 1; w < kThermoThreads / 32; ++w) t = lse_merge(t, ws[w]);
+        const double kB = 0.001987206;  // LIB/statmech.h:26
+        const double lnZ = t.m + log(t.s);
+        const double Ea = t.e1 / t.s, E2 = t.e2 / t.s;
+        const double kT = kB * T;
+        const double var = E2 - Ea * Ea;
+        fxe_thermo r;
+        r.temperature = T;
+        r.log_Z = lnZ;
+        r.free_energy = -kT * lnZ;
+        r.mean_energy = Ea;
+        r.mean_energy_sq = E2;
+        r.heat_capacity = var / (kT * kT);
+        r.entropy = (Ea - r.free_energy) / T;
+        r.std_energy = sqrt(var > 0.0 ? var : 0.0);
+        *out = r;
+    }
+}
+
+void launch_thermo_fixed(const double* e, const int32_t* mult, long n, double beta, double T,
+                         LsePart* scratch, fxe_thermo* d_out, cudaStream_t st) {
+    const int nb = (int)((n + kFixedPerBlock - 1) / kFixedPerBlock);
+    thermo_fixed_partial_kernel<<<nb, kThermoThreads, 0, st>>>(e, mult, n, beta, scratch);
+    thermo_fixed_finish_kernel<<<1, kThermoThreads, 0, st>>>(scratch, nb, T, d_out);
+}
+
+}  // namespace fxe

@@ -175,6 +175,33 @@ fxe_status fxe_thermo_compute(const double* energies, const int32_t* multiplicit
 fxe_status fxe_thermo_compute_device(const double* d_energies, const int32_t* d_multiplicity,
                                      int64_t n, double temperature, fxe_thermo* out, void* stream);
 
+/* Device-resident thermodynamics that allocates nothing. No reference counterpart.
+ *
+ * Same reduction as fxe_thermo_compute_device, for callers that must not allocate device
+ * memory: code running under a fixed device-memory budget that has handed all free memory to
+ * its own pools (an admission-controlled serving loop), and code that may not synchronise the
+ * device, which every cudaMalloc/cudaFree can do. The block partials live in a fixed array
+ * inside the library (FXE_THERMO_FIXED_MAX_BLOCKS partials of 32 bytes, 2 MiB, one array per
+ * device), the merge runs on the device, and the record is written to d_out (device memory).
+ * Work is queued on `stream` (cudaStream_t or NULL for the legacy default stream) and not
+ * waited for.
+ *
+ * - n may be at most FXE_THERMO_FIXED_MAX_N (each block covers FXE_THERMO_FIXED_PER_THREAD x 256
+ *   energies); larger n is rejected with FXE_ERR_INVALID_ARGS before any work is queued.
+ * - The first call on a device looks up the array's address (cudaGetSymbolAddress, with that
+ *   device current) and loads the library's device code; make that first call before any stream
+ *   capture and before memory is handed out.
+ * - Nothing needs to start at zero: every partial a call reads is written by that call.
+ * - Calls on one device share the array: calls whose work overlaps (different streams, or
+ *   host threads without ordering) race and give wrong results. Serialise them on one stream.
+ * - d_multiplicity entries must be positive (not checked on the device). */
+#define FXE_THERMO_FIXED_PER_THREAD 16
+#define FXE_THERMO_FIXED_MAX_BLOCKS 65536
+#define FXE_THERMO_FIXED_MAX_N ((int64_t)FXE_THERMO_FIXED_MAX_BLOCKS * 256 * FXE_THERMO_FIXED_PER_THREAD)
+fxe_status fxe_thermo_compute_device_fixed(const double* d_energies, const int32_t* d_multiplicity,
+                                           int64_t n, double temperature, fxe_thermo* d_out,
+                                           void* stream);
+
 /* Boltzmann weights p_i = n_i exp(-beta E_i) / Z of the same ensemble
  * (StatMechEngine::boltzmann_weights, LIB/statmech.cpp:178-201). */
 fxe_status fxe_thermo_weights(const double* energies, const int32_t* multiplicity, int64_t n,
