@@ -44,6 +44,12 @@ using real = FXE_REAL;
 #ifndef FXE_REFERENCE_FORMULAS
 #define FXE_REFERENCE_FORMULAS 0
 #endif
+// Double builds decide the hull walk's plane tests in single precision first and redo a test
+// in double only when its single-precision result is within its error bound of deciding the
+// other way (see walk_step).
+#ifndef FXE_FILTER
+#define FXE_FILTER (FXE_REFERENCE_FORMULAS)
+#endif
 struct __align__(4 * sizeof(real)) real4 {
     real x, y, z, w;
 };
@@ -97,9 +103,10 @@ struct VorShared {
     uchar4 vp[kMaxVerts];           // the vertex's planes (kNone = sphere)
     union {
         struct {
-            real4 ev[kMaxEdges];   // edge direction
-            uchar4 ep[kMaxEdges];   // plane0, plane1, start plane, end plane
-            uchar2 es[kMaxEdges];   // start vertex, end vertex
+            // (two spare slots: the step that reaches the 200-edge limit writes up to two edges)
+            real4 ev[kMaxEdges + 2];   // edge direction
+            uchar4 ep[kMaxEdges + 2];   // plane0, plane1, start plane, end plane
+            uchar2 es[kMaxEdges + 2];   // start vertex, end vertex
         } e;
         struct {
             uint8_t pt[kMaxFacePts];
@@ -108,6 +115,12 @@ struct VorShared {
     } u;
     uint16_t foff[kMaxCand + 1];
     uint8_t fnp[kMaxCand];
+    uint16_t toff[kMaxCand + 1];   // per face: first fan triangle / arc segment in the flat lists
+    uint16_t aoff[kMaxCand + 1];
+    real tmp[32];                  // one value per lane, for in-order sums
+#if FXE_FILTER
+    float4 plf[kMaxPlanes];        // the planes rounded to single precision, for pre-tests
+#endif
     uint8_t flag[kMaxPlanes];
     int eng[4];
     int epi;
@@ -258,6 +271,218 @@ __device__ void add_edge(VorShared& sh, int en, int p0, int p1, int tp, int sp) 
     sh.u.e.es[en] = make_uchar2((uint8_t)sp, kNone);
 }
 
+struct WalkStep {
+    real x, y, z;
+    int pc;      // closing plane, -1 if none
+};
+
+#if FXE_FILTER
+// Single-precision value of vt = -(P.s + w) / (P.V) and a bound on its distance from the same
+// expression evaluated in double: every input is rounded once to float and every operation
+// rounds, 16 units of roundoff (2^-20) per sum of absolute terms covers both. den_ok is false
+// when the sign of P.V is not certain (the double test skips P.V == 0 exactly).
+__device__ __forceinline__ float vt_pretest(const float4& P, float sx, float sy, float sz, float Vx,
+                                            float Vy, float Vz, float* err, bool* den_ok) {
+    const float g = 9.5367431640625e-07f;   // 2^-20
+    const float den = P.x * Vx + P.y * Vy + P.z * Vz;
+    const float eden = g * (fabsf(P.x * Vx) + fabsf(P.y * Vy) + fabsf(P.z * Vz));
+    const float num = P.x * sx + P.y * sy + P.z * sz + P.w;
+    const float enm = g * (fabsf(P.x * sx) + fabsf(P.y * sy) + fabsf(P.z * sz) + fabsf(P.w));
+    // an all-zero normal (an excluded candidate's inert plane) has P.V == 0 exactly in double
+    // too, and the double test skips it; report it as a decided non-positive value
+    if (P.x == 0.0f && P.y == 0.0f && P.z == 0.0f) {
+        *den_ok = true;
+        *err = 0.0f;
+        return -1.0f;
+    }
+    *den_ok = fabsf(den) > 2.0f * eden;
+    const float vt = -num / den;
+    *err = (enm + fabsf(vt) * eden) / (fabsf(den) - eden) * 1.0625f + fabsf(vt) * 2.4e-7f;
+    return vt;
+}
+#endif
+
+// The vertex that ends edge e (LIB/Vcontacts.cpp:283-330), in full precision: the plane with
+// the smallest positive vt along the edge (planes spread over the lanes) and, when that point
+// lies outside the sphere, the bounding planes too. The result is uniform across the warp.
+__device__ WalkStep walk_step_exact(const VorShared& sh, int NC, int e, real rr, int lane) {
+    const uchar4 ep = sh.u.e.ep[e];
+    const real4 V = sh.u.e.ev[e];
+    const real4 s = sh.vx[sh.u.e.es[e].x];
+    const int pA = ep.x, pB = ep.y, oldC = ep.z;
+    real vtmin = real(9.9e9);
+    int pC = INT_MAX;
+    for (int c = lane; c < NC; c += 32) {
+        if (c == pA || c == pB || c == oldC) continue;
+        const real4 P = sh.pl[c];
+        const real den = P.x * V.x + P.y * V.y + P.z * V.z;
+        if (den != real(0.0)) {
+            const real vt = -(P.x * s.x + P.y * s.y + P.z * s.z + P.w) / den;
+            if (vt < vtmin && vt > real(0.0)) { vtmin = vt; pC = c; }
+        }
+    }
+    warp_argmin(vtmin, pC);
+    real x = s.x + vtmin * V.x, y = s.y + vtmin * V.y, z = s.z + vtmin * V.z;
+    if (x * x + y * y + z * z > rr) {
+        real bvt = vtmin;
+        int bc = pC;
+        if (lane < 4) {
+            const int c = NC + lane;
+            if (c != pA && c != pB && c != oldC) {
+                const real4 P = sh.pl[c];
+                const real den = P.x * V.x + P.y * V.y + P.z * V.z;
+                if (den != real(0.0)) {
+                    const real vt = -(P.x * s.x + P.y * s.y + P.z * s.z + P.w) / den;
+                    if (vt < bvt && vt > real(0.0)) { bvt = vt; bc = c; }
+                }
+            }
+        }
+        warp_argmin(bvt, bc);
+        vtmin = bvt;
+        pC = bc;
+        x = s.x + vtmin * V.x;
+        y = s.y + vtmin * V.y;
+        z = s.z + vtmin * V.z;
+    }
+    WalkStep r;
+    r.x = x;
+    r.y = y;
+    r.z = z;
+    r.pc = pC == INT_MAX ? -1 : pC;
+    return r;
+}
+
+// The same step with the plane tests decided in single precision (double builds): each lane
+// pre-tests its planes; when the winner is surely positive and every other plane is surely not
+// positive or surely farther, only the winner's vt is evaluated in double. Otherwise, and for
+// the bounding planes when the pre-test cannot rule them out, the step is redone in double.
+__device__ WalkStep walk_step(const VorShared& sh, int NC, int e, real rr, int lane) {
+#if FXE_FILTER
+    const uchar4 ep = sh.u.e.ep[e];
+    const real4 V = sh.u.e.ev[e];
+    const real4 s = sh.vx[sh.u.e.es[e].x];
+    const int pA = ep.x, pB = ep.y, oldC = ep.z;
+    const float sx = (float)s.x, sy = (float)s.y, sz = (float)s.z;
+    const float Vx = (float)V.x, Vy = (float)V.y, Vz = (float)V.z;
+    float best = 9.9e9f, beste = 0.0f;
+    int bi = INT_MAX;
+    bool unsure = false;
+    for (int c = lane; c < NC; c += 32) {
+        if (c == pA || c == pB || c == oldC) continue;
+        float er;
+        bool ok;
+        const float vt = vt_pretest(sh.plf[c], sx, sy, sz, Vx, Vy, Vz, &er, &ok);
+        if (!ok) unsure = true;
+        else if (vt > 0.0f && vt < best) { best = vt; beste = er; bi = c; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float b2 = __shfl_xor_sync(kFull, best, o);
+        const float e2 = __shfl_xor_sync(kFull, beste, o);
+        const int i2 = __shfl_xor_sync(kFull, bi, o);
+        if (b2 < best || (b2 == best && i2 < bi)) { best = b2; beste = e2; bi = i2; }
+    }
+    if (bi != INT_MAX && !(best - beste > 0.0f)) unsure = true;
+    for (int c = lane; c < NC && !unsure; c += 32) {
+        if (c == pA || c == pB || c == oldC || c == bi) continue;
+        float er;
+        bool ok;
+        const float vt = vt_pretest(sh.plf[c], sx, sy, sz, Vx, Vy, Vz, &er, &ok);
+        if (ok && (vt + er <= 0.0f || (bi != INT_MAX && vt - er > best + beste))) continue;
+        unsure = true;
+    }
+    if (__any_sync(kFull, unsure)) return walk_step_exact(sh, NC, e, rr, lane);
+    real vtmin = real(9.9e9);
+    int pC = bi;
+    if (bi != INT_MAX) {
+        const real4 P = sh.pl[bi];
+        const real den = P.x * V.x + P.y * V.y + P.z * V.z;
+        vtmin = -(P.x * s.x + P.y * s.y + P.z * s.z + P.w) / den;
+    }
+    real x = s.x + vtmin * V.x, y = s.y + vtmin * V.y, z = s.z + vtmin * V.z;
+    if (x * x + y * y + z * z > rr) {
+        // the bounding planes lie 10 A out: most of the time surely farther than vtmin
+        bool need = bi == INT_MAX;
+        if (!need && lane < 4) {
+            const int c = NC + lane;
+            if (c != pA && c != pB && c != oldC) {
+                float er;
+                bool ok;
+                const float vt = vt_pretest(sh.plf[c], sx, sy, sz, Vx, Vy, Vz, &er, &ok);
+                need = !(ok && (vt + er <= 0.0f || vt - er > (float)vtmin * 1.0000005f));
+            }
+        }
+        if (__any_sync(kFull, need)) return walk_step_exact(sh, NC, e, rr, lane);
+    }
+    WalkStep r;
+    r.x = x;
+    r.y = y;
+    r.z = z;
+    r.pc = pC == INT_MAX ? -1 : pC;
+    return r;
+#else
+    return walk_step_exact(sh, NC, e, rr, lane);
+#endif
+}
+
+// Face of flat item k: the last face X in [0, NC) whose first item is at or before k.
+__device__ __forceinline__ int face_of(const uint16_t* off, int NC, int k) {
+    int lo = 0, hi = NC;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if ((int)off[mid] <= k) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Whether points vi and vi+1 of a face bound an arc segment: both arc points, of different
+// edges (LIB/Vcontacts.cpp:943-954).
+__device__ __forceinline__ int arc_segment(const VorShared& sh, const uint8_t* pt, int np, int vi) {
+    const uchar4 qa = sh.vp[pt[vi]], qb = sh.vp[pt[(vi + 1) % np]];
+    if (qa.z != kNone || qb.z != kNone) return 0;
+    const int sa = (qa.y == kNone ? -1 : qa.y) + qa.x;
+    const int sb = (qb.y == kNone ? -1 : qb.y) + qb.x;
+    return sa != sb;
+}
+
+// Area of the fan triangle v0 va vb on the sphere of radius rado.
+__device__ __forceinline__ real fan_triangle(const real4& v0, const real4& va, const real4& vb, real rado) {
+#if FXE_REFERENCE_FORMULAS
+    // L'Huilier-type tangent products as the reference writes them (LIB/Vcontacts.cpp:927-940)
+    const real cNN1 = (va.x * vb.x + va.y * vb.y + va.z * vb.z) / (va.w * vb.w);
+    const real cN0a = (v0.x * va.x + v0.y * va.y + v0.z * va.z) / (v0.w * va.w);
+    const real cN0b = (v0.x * vb.x + v0.y * vb.y + v0.z * vb.z) / (v0.w * vb.w);
+    const real U = sqrt((1 + cN0a) * (1 + cNN1) * (1 + cN0b) / real(8.0));
+    const real V = sqrt((1 - cN0a) * (1 - cNN1) * (1 + cN0b) / real(8.0));
+    const real W = sqrt((1 - cN0a) * (1 + cNN1) * (1 - cN0b) / real(8.0));
+    const real Xv = sqrt((1 + cN0a) * (1 - cNN1) * (1 - cN0b) / real(8.0));
+    const real tS = (1 - U + V + W + Xv) / (1 + U - V - W - Xv);
+    const real tSA = (1 - U - V - W + Xv) / (1 + U + V + W - Xv);
+    const real tSB = (1 - U - V + W - Xv) / (1 + U + V - W + Xv);
+    const real tSC = (1 - U + V - W - Xv) / (1 + U - V + W + Xv);
+    const real tanprod = sqrt(tS * tSA * tSB * tSC);
+    return tanprod > real(0.0) ? real(4.0) * rado * rado * atan(sqrt(tanprod)) : real(0.0);
+#else
+    // the same triangle's solid angle, well conditioned in FP32
+    return rado * rado * solid_angle(v0, va, vb);
+#endif
+}
+
+// Adds each lane's value v to the area of face X (X < 0: nothing), lanes of one face in lane
+// order, so that a face's sum is formed in the order of its items.
+__device__ __forceinline__ void add_in_order(VorShared& sh, int X, real v, int lane) {
+    sh.tmp[lane] = v;
+    const unsigned grp = __match_any_sync(kFull, X);
+    __syncwarp();
+    if (X >= 0 && lane == __ffs(grp) - 1) {
+        real acc = sh.area[X];
+        for (unsigned m = grp; m; m &= m - 1) acc += sh.tmp[__ffs(m) - 1];
+        sh.area[X] = acc;
+    }
+    __syncwarp();
+}
+
 // One extended-radical-plane polyhedron and its contact areas. sh.pl/flag/cidx hold the
 // planes of the NC candidates (excluded slots carry a plane that never binds). Returns
 // kAtomOk, kAtomHullFail (the walk reached 200 edges) or kAtomCapacity.
@@ -271,6 +496,9 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         const real by[4] = {real(1.0), -real(1.0), real(0.0), real(0.0)};
         const real bz[4] = {real(0.0), real(0.0), real(1.0), -real(1.0)};
         sh.pl[NC + lane] = make_real4(bx[lane], by[lane], bz[lane], -real(10.0));
+#if FXE_FILTER
+        sh.plf[NC + lane] = make_float4((float)bx[lane], (float)by[lane], (float)bz[lane], -10.0f);
+#endif
         sh.flag[NC + lane] = 0;
     }
     for (int c = lane; c < NC; c += 32) sh.area[c] = real(0.0);
@@ -347,53 +575,19 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     for (;;) {
         while (startedge < edgenum && sh.u.e.es[startedge].y != kNone) ++startedge;
         if (startedge >= edgenum) break;
-        const uchar4 ep = sh.u.e.ep[startedge];
-        const real4 V = sh.u.e.ev[startedge];
-        const real4 s = sh.vx[sh.u.e.es[startedge].x];
-        const int pA = ep.x, pB = ep.y, oldC = ep.z;
-        real vtmin = real(9.9e9);
-        int pC = INT_MAX;
-        for (int c = lane; c < NC; c += 32) {
-            if (c == pA || c == pB || c == oldC) continue;
-            const real4 P = sh.pl[c];
-            const real den = P.x * V.x + P.y * V.y + P.z * V.z;
-            if (den != real(0.0)) {
-                const real vt = -(P.x * s.x + P.y * s.y + P.z * s.z + P.w) / den;
-                if (vt < vtmin && vt > real(0.0)) { vtmin = vt; pC = c; }
-            }
-        }
-        warp_argmin(vtmin, pC);
-        real x = s.x + vtmin * V.x, y = s.y + vtmin * V.y, z = s.z + vtmin * V.z;
-        if (x * x + y * y + z * z > rr) {
-            real bvt = vtmin;
-            int bc = pC;
-            if (lane < 4) {
-                const int c = NC + lane;
-                if (c != pA && c != pB && c != oldC) {
-                    const real4 P = sh.pl[c];
-                    const real den = P.x * V.x + P.y * V.y + P.z * V.z;
-                    if (den != real(0.0)) {
-                        const real vt = -(P.x * s.x + P.y * s.y + P.z * s.z + P.w) / den;
-                        if (vt < bvt && vt > real(0.0)) { bvt = vt; bc = c; }
-                    }
-                }
-            }
-            warp_argmin(bvt, bc);
-            vtmin = bvt;
-            pC = bc;
-            x = s.x + vtmin * V.x;
-            y = s.y + vtmin * V.y;
-            z = s.z + vtmin * V.z;
-        }
-        if (pC == INT_MAX) return kAtomHullFail;
+        const WalkStep r = walk_step(sh, NC, startedge, rr, lane);
+        const int pC = r.pc;
+        if (pC < 0) return kAtomHullFail;
         if (vn >= kMaxVerts - 1) return kAtomCapacity;
+        const uchar4 ep = sh.u.e.ep[startedge];
+        const int pA = ep.x, pB = ep.y;
         // edges (pA, pC) and (pB, pC): the first open match after startedge, else a new edge
         int mAC = INT_MAX, mBC = INT_MAX;
         for (int e0 = startedge + 1; e0 < edgenum; e0 += 32) {
-            const int e = e0 + lane;
+            const int f = e0 + lane;
             bool ac = false, bc = false;
-            if (e < edgenum) {
-                const uchar4 q = sh.u.e.ep[e];
+            if (f < edgenum) {
+                const uchar4 q = sh.u.e.ep[f];
                 ac = (q.x == pA && q.y == pC) || (q.x == pC && q.y == pA);
                 bc = (q.x == pB && q.y == pC) || (q.x == pC && q.y == pB);
             }
@@ -401,37 +595,55 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
             if (ma && mAC == INT_MAX) mAC = e0 + __ffs(ma) - 1;
             if (mb && mBC == INT_MAX) mBC = e0 + __ffs(mb) - 1;
         }
+        __syncwarp();
+        // lane 0 books the vertex and edge (pA, pC), lane 1 edge (pB, pC); a new edge's direction
+        // comes from the vertex just found (its distance is filled in after the walk)
+        // a walk that keeps opening edges past the reference's 200-edge check ends here: as a
+        // hull failure when the reference's check fails it at this step, else over capacity
+        const int n_new = (mAC == INT_MAX) + (mBC == INT_MAX);
+        if (edgenum + n_new > kMaxEdges + 2) return mBC == INT_MAX ? kAtomHullFail : kAtomCapacity;
+        const int eAC = mAC != INT_MAX ? mAC : edgenum;
+        const int eBC = mBC != INT_MAX ? mBC : edgenum + (mAC == INT_MAX ? 1 : 0);
         if (lane == 0) {
-            sh.vx[vn] = make_real4(x, y, z, sqrt(x * x + y * y + z * z));
+            sh.vx[vn] = make_real4(r.x, r.y, r.z, real(0.0));
             sh.vp[vn] = make_uchar4((uint8_t)pA, (uint8_t)pB, (uint8_t)pC, 0);
             sh.u.e.es[startedge].y = (uint8_t)vn;
             sh.u.e.ep[startedge].w = (uint8_t)pC;
             sh.flag[pC] |= kOnHull;
         }
-        __syncwarp();
-        if (mAC != INT_MAX) {
-            if (lane == 0) {
-                sh.u.e.es[mAC].y = (uint8_t)vn;
-                sh.u.e.ep[mAC].w = (uint8_t)pB;
+        if (lane < 2) {
+            const bool match = lane == 0 ? mAC != INT_MAX : mBC != INT_MAX;
+            const int e = lane == 0 ? eAC : eBC;
+            const int p0 = lane == 0 ? pA : pB, tp = lane == 0 ? pB : pA;
+            if (match) {
+                sh.u.e.es[e].y = (uint8_t)vn;
+                sh.u.e.ep[e].w = (uint8_t)tp;
+            } else {
+                const real4 a = sh.pl[p0], b = sh.pl[pC], t = sh.pl[tp];
+                real vx = a.y * b.z - a.z * b.y;
+                real vy = a.z * b.x - a.x * b.z;
+                real vz = a.x * b.y - a.y * b.x;
+                const real tv = t.x * (r.x + vx) + t.y * (r.y + vy) + t.z * (r.z + vz) + t.w;
+                if (tv > real(0.0)) { vx = -vx; vy = -vy; vz = -vz; }
+                sh.u.e.ev[e] = make_real4(vx, vy, vz, real(0.0));
+                sh.u.e.ep[e] = make_uchar4((uint8_t)p0, (uint8_t)pC, (uint8_t)tp, kNone);
+                sh.u.e.es[e] = make_uchar2((uint8_t)vn, kNone);
             }
-        } else {
-            if (lane == 0) add_edge(sh, edgenum, pA, pC, pB, vn);
-            ++edgenum;
         }
-        __syncwarp();
-        if (mBC != INT_MAX) {
-            if (lane == 0) {
-                sh.u.e.es[mBC].y = (uint8_t)vn;
-                sh.u.e.ep[mBC].w = (uint8_t)pA;
-            }
-        } else {
-            if (lane == 0) add_edge(sh, edgenum, pB, pC, pA, vn);
+        if (mAC == INT_MAX) ++edgenum;
+        if (mBC == INT_MAX) {
             ++edgenum;
             if (edgenum >= kMaxEdges) return kAtomHullFail;
         }
-        __syncwarp();
         ++vn;
+        __syncwarp();
     }
+    // vertex distances to the centre, all at once
+    for (int vi = 1 + lane; vi < vn; vi += 32) {
+        const real4 X = sh.vx[vi];
+        sh.vx[vi].w = sqrt(X.x * X.x + X.y * X.y + X.z * X.z);
+    }
+    __syncwarp();
 
     // ---- arc points where edges leave the sphere (LIB/Vcontacts.cpp:418-462) ----
     for (int e0 = 0; e0 < edgenum; e0 += 32) {
@@ -655,54 +867,70 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         __syncwarp();
     }
     const real two_pi_r = real(2.0) * (real)kPi * rado;
-    for (int X = lane; X < NC; X += 32) {
-        if (sh.flag[X] == 0) continue;
-        const int np = sh.fnp[X];
-        const uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
-        const real4 cp = centre_of(sh.pl[X]);
-        real area = real(0.0);
-        if (np == 0) {
-            if (inside_all(sh, NC, X, cp.x, cp.y, cp.z)) area = two_pi_r * (rado - cp.w);
-        } else if (np == 2) {
-            const real arc = sph_arc(cp, sh.vx[pt[0]], sh.vx[pt[1]], rado);
-            if (inside_all(sh, NC, X, cp.x, cp.y, cp.z)) area = two_pi_r * (rado - cp.w) - arc;
-            else area = arc;
-        } else {
-            // fan of spherical triangles from pt[0] (LIB/Vcontacts.cpp:906-940)
-            const real4 v0 = sh.vx[pt[0]];
-#if FXE_REFERENCE_FORMULAS
-            for (int vi = 1; vi < np - 1; ++vi) {
-                const real4 va = sh.vx[pt[vi]], vb = sh.vx[pt[vi + 1]];
-                const real cNN1 = (va.x * vb.x + va.y * vb.y + va.z * vb.z) / (va.w * vb.w);
-                const real cN0a = (v0.x * va.x + v0.y * va.y + v0.z * va.z) / (v0.w * va.w);
-                const real cN0b = (v0.x * vb.x + v0.y * vb.y + v0.z * vb.z) / (v0.w * vb.w);
-                const real U = sqrt((1 + cN0a) * (1 + cNN1) * (1 + cN0b) / real(8.0));
-                const real V = sqrt((1 - cN0a) * (1 - cNN1) * (1 + cN0b) / real(8.0));
-                const real W = sqrt((1 - cN0a) * (1 + cNN1) * (1 - cN0b) / real(8.0));
-                const real Xv = sqrt((1 + cN0a) * (1 - cNN1) * (1 - cN0b) / real(8.0));
-                const real tS = (1 - U + V + W + Xv) / (1 + U - V - W - Xv);
-                const real tSA = (1 - U - V - W + Xv) / (1 + U + V + W - Xv);
-                const real tSB = (1 - U - V + W - Xv) / (1 + U + V - W + Xv);
-                const real tSC = (1 - U + V - W - Xv) / (1 + U - V + W + Xv);
-                const real tanprod = sqrt(tS * tSA * tSB * tSC);
-                if (tanprod > real(0.0)) area += real(4.0) * rado * rado * atan(sqrt(tanprod));
+    // Caps and lenses (faces of 0 and 2 points) one face per lane; the fan triangles and arc
+    // segments of the other faces are laid out flat and spread over the lanes, then added to
+    // their face's area in the reference's order (triangles, then arcs, each in point order).
+    int t_run = 0, a_run = 0;
+    for (int x0 = 0; x0 < NC; x0 += 32) {
+        const int X = x0 + lane;
+        int nt = 0, na = 0;
+        if (X < NC && sh.flag[X] != 0) {
+            const int np = sh.fnp[X];
+            const uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
+            const real4 cp = centre_of(sh.pl[X]);
+            real area = real(0.0);
+            if (np == 0) {
+                if (inside_all(sh, NC, X, cp.x, cp.y, cp.z)) area = two_pi_r * (rado - cp.w);
+            } else if (np == 2) {
+                const real arc = sph_arc(cp, sh.vx[pt[0]], sh.vx[pt[1]], rado);
+                if (inside_all(sh, NC, X, cp.x, cp.y, cp.z)) area = two_pi_r * (rado - cp.w) - arc;
+                else area = arc;
+            } else {
+                // (a face of one point has neither triangles nor arcs)
+                nt = np > 2 ? np - 2 : 0;
+                for (int vi = 0; vi < np; ++vi) na += arc_segment(sh, pt, np, vi);
             }
-#else
-            // the same triangles' solid angles, well conditioned in FP32
-            for (int vi = 1; vi < np - 1; ++vi)
-                area += rado * rado * solid_angle(v0, sh.vx[pt[vi]], sh.vx[pt[vi + 1]]);
-#endif
-            for (int vi = 0; vi < np; ++vi) {
-                const int a = pt[vi], b = pt[(vi + 1) % np];
-                const uchar4 qa = sh.vp[a], qb = sh.vp[b];
-                if (qa.z == kNone && qb.z == kNone) {
-                    const int sa = (qa.y == kNone ? -1 : qa.y) + qa.x;
-                    const int sb = (qb.y == kNone ? -1 : qb.y) + qb.x;
-                    if (sa != sb) area += sph_arc(cp, sh.vx[a], sh.vx[b], rado);
-                }
-            }
+            sh.area[X] = area;
         }
-        sh.area[X] = area;
+        int tt, ta;
+        const int ot = warp_excl_scan(nt, lane, &tt);
+        const int oa = warp_excl_scan(na, lane, &ta);
+        if (X < NC) {
+            sh.toff[X] = (uint16_t)(t_run + ot);
+            sh.aoff[X] = (uint16_t)(a_run + oa);
+        }
+        t_run += tt;
+        a_run += ta;
+    }
+    __syncwarp();
+    // fan of spherical triangles from pt[0] (LIB/Vcontacts.cpp:906-940)
+    for (int k0 = 0; k0 < t_run; k0 += 32) {
+        const int k = k0 + lane;
+        int X = -1;
+        real v = real(0.0);
+        if (k < t_run) {
+            X = face_of(sh.toff, NC, k);
+            const int vi = 1 + k - sh.toff[X];
+            const uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
+            v = fan_triangle(sh.vx[pt[0]], sh.vx[pt[vi]], sh.vx[pt[vi + 1]], rado);
+        }
+        add_in_order(sh, X, v, lane);
+    }
+    // arc segments between consecutive arc points of different edges (:943-954)
+    for (int k0 = 0; k0 < a_run; k0 += 32) {
+        const int k = k0 + lane;
+        int X = -1;
+        real v = real(0.0);
+        if (k < a_run) {
+            X = face_of(sh.aoff, NC, k);
+            const int np = sh.fnp[X];
+            const uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
+            int j = k - sh.aoff[X], vi = 0;
+            for (; vi < np - 1; ++vi)
+                if (arc_segment(sh, pt, np, vi) && j-- == 0) break;
+            v = sph_arc(centre_of(sh.pl[X]), sh.vx[pt[vi]], sh.vx[pt[(vi + 1) % np]], rado);
+        }
+        add_in_order(sh, X, v, lane);
     }
     __syncwarp();
     if (epi > 0) {
@@ -773,6 +1001,9 @@ __device__ void load_planes(VorShared& sh, const DevSystem& S, const DevWork& W,
         const bool ex = ((excl[c >> 5] >> (c & 31)) & 1u) || d2 < 1e-20f;
         if (ex) {
             sh.pl[c] = make_real4(real(0.0), real(0.0), real(0.0), -real(1e30));
+#if FXE_FILTER
+            sh.plf[c] = make_float4(0.0f, 0.0f, 0.0f, -1e30f);
+#endif
             sh.flag[c] = 0;
             continue;
         }
@@ -784,8 +1015,12 @@ __device__ void load_planes(VorShared& sh, const DevSystem& S, const DevWork& W,
         const real num = (dd + (real)rr) - (real)qq;
         bool eng = num < real(0.0);
         if (sizeof(real) < 8 && fabs(num) < real(1e-3)) eng = ((double)d2 + (double)rr) - (double)qq < 0.0;
-        sh.pl[c] = make_real4((real)(pj.x - me.x) / d, (real)(pj.y - me.y) / d, (real)(pj.z - me.z) / d,
-                              -(num / (real(2.0) * d)));
+        const real4 P = make_real4((real)(pj.x - me.x) / d, (real)(pj.y - me.y) / d, (real)(pj.z - me.z) / d,
+                                   -(num / (real(2.0) * d)));
+        sh.pl[c] = P;
+#if FXE_FILTER
+        sh.plf[c] = make_float4((float)P.x, (float)P.y, (float)P.z, (float)P.w);
+#endif
         sh.flag[c] = eng ? kEngulf : 0;
     }
     // project_points' fallback centre for two engulfing planes: the atom's own coordinates + rado
@@ -934,9 +1169,9 @@ pose_kernel(DevSystem S, DevWork W, int n) {
         uint32_t keep_lig[kMaskWords] = {0, 0, 0, 0};
         for (int c = lane; c < NC; c += 32) {
             const bool ex = (excl[c >> 5] >> (c & 31)) & 1u;
-            const float ar = ex ? 0.0f : sh.area[c];
+            const real ar = ex ? real(0.0) : sh.area[c];
             const uint8_t f = ex ? 0 : sh.flag[c];
-            const bool kept = ar > 0.0f && (f & (kOnHull | kEngulf));
+            const bool kept = ar > real(0.0) && (f & (kOnHull | kEngulf));
             W.cand_area[cb + c] = (double)ar;
             W.cand_flag[cb + c] = (uint8_t)(f | (kept ? kRecorded : 0));
             const int j = sh.cidx[c];
