@@ -325,6 +325,8 @@ def run_gpu(args):
         sm_ms.append(a.elapsed_time(b))
     sm_best = min(sm_ms)
 
+    batched = run_batched(args, prec, flush, stream) if args.batched else None
+
     if rank != 0:
         ranks.close()
         return
@@ -372,9 +374,95 @@ def run_gpu(args):
         "statmech": {"poses": STATMECH_N, "ms": sm_best, "poses_per_s": STATMECH_N / (sm_best / 1e3),
                      "roofline": {"bound": "hbm", "achieved": sm_gbs, "peak": hbm, "unit": "GB/s",
                                   "frac": (sm_gbs / hbm) if hbm else None, "traffic": None}},
+        "batched": batched,
     }
     print(json.dumps(out), flush=True)
     ranks.close()
+
+
+# ---------------------------------------------------------------------------------------------
+# batched: many ligands on one receptor, one launch per generation
+# ---------------------------------------------------------------------------------------------
+
+BATCH = dict(n_rec=4000, cleft=10.0, seed=31, edge=51.92391670510951, jobs=256, atoms=(10, 70),
+             torsions=(0, 15), population=(200, 2000))
+BATCH_NAME = ("batched: 4000-atom receptor, 10 A cleft (79501 grid points), 256 seeded ligands of "
+              "U[10,70] heavy atoms and U[0,15] torsions, populations U[200,2000] of uniform "
+              "(initial-generation) chromosomes; one GA generation of every job per step")
+
+
+def make_batch_jobs():
+    from flexaidds_gb300.system import SystemInputs
+    b = BATCH
+    base = system.make_inputs(b["n_rec"], b["cleft"], 12, 3, seed=b["seed"], edge=b["edge"])
+    rng = np.random.default_rng(b["seed"] + 1)
+    out = []
+    for k in range(b["jobs"]):
+        n = int(rng.integers(b["atoms"][0], b["atoms"][1] + 1))
+        t = int(rng.integers(b["torsions"][0], b["torsions"][1] + 1))
+        pop = int(rng.integers(b["population"][0], b["population"][1] + 1))
+        lig = synth.random_ligand(n, t, seed=b["seed"] * 1000 + k)
+        d = prepare.prepare(SystemInputs(receptor=base.receptor, ligand=lig, grid_xyz=base.grid_xyz,
+                                         emat=base.emat))
+        out.append((d, pop, synth.random_genes(pop, d.n_genes, seed=b["seed"] * 5000 + k)))
+    return out
+
+
+def run_batched(args, prec, flush, stream):
+    """Poses/s of one generation of all jobs: one launch sequence per job (the plain path) and
+    one batched launch for all of them, same chromosomes, device-resident, L2 flushed."""
+    import torch
+    from flexaidds_gb300 import evaluator
+    jobs = make_batch_jobs()
+    p = 0 if prec == "reference" else 1
+    first = evaluator.GPUEvaluator(jobs[0][0], max_poses=jobs[0][1], precision=p)
+    evs = [first] + [evaluator.GPUEvaluator(d, max_poses=pop, precision=p, share_receptor_with=first)
+                     for d, pop, _ in jobs[1:]]
+    dg = [torch.from_numpy(np.ascontiguousarray(g)).cuda() for _, _, g in jobs]
+    do = [torch.empty(pop * capi.CF_DTYPE.itemsize, dtype=torch.uint8, device="cuda") for _, pop, _ in jobs]
+    total = sum(pop for _, pop, _ in jobs)
+    batch = evaluator.Batch(max_jobs=len(jobs), max_poses=total, max_genes=64)
+    table = [(ev, pop, g.data_ptr(), o.data_ptr()) for ev, (_, pop, _), g, o in zip(evs, jobs, dg, do)]
+
+    def plain():
+        for ev, pop, g, o in table:
+            ev.eval_genes_device(g, pop, o, stream.cuda_stream)
+
+    def batched():
+        batch.eval_genes_device(table, stream.cuda_stream)
+
+    res = {}
+    steps = max(1, min(args.steps, 5))
+    for name, fn in (("plain", plain), ("batched", batched)):
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                fn()
+        stream.synchronize()
+        ms = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                a.record(stream)
+                fn()
+                b.record(stream)
+            b.synchronize()
+            ms += a.elapsed_time(b)
+        res[name] = {"poses_per_s": total * steps / (ms / 1e3), "ms_per_generation": ms / steps}
+    batched_out = [np.frombuffer(o.cpu().numpy().tobytes(), capi.CF_DTYPE) for o in do]
+    plain()
+    stream.synchronize()
+    plain_out = [np.frombuffer(o.cpu().numpy().tobytes(), capi.CF_DTYPE) for o in do]
+    same = all(np.array_equal(a, b) for a, b in zip(batched_out, plain_out))
+    scored = sum(int((o["status"] == capi.POSE_SCORED).sum()) for o in plain_out)
+    for ev in evs:
+        ev.close()
+    batch.close()
+    return {"workload": BATCH_NAME, "jobs": len(jobs), "poses_per_generation": total,
+            "scored_fraction": scored / total, "precision": prec, "steps": steps,
+            "plain": res["plain"], "batched": res["batched"],
+            "speedup": res["batched"]["poses_per_s"] / res["plain"]["poses_per_s"],
+            "results_identical": same}
 
 
 # ---------------------------------------------------------------------------------------------
@@ -451,6 +539,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["reference", "fast"], default="reference")
+    ap.add_argument("--batched", type=int, default=1,
+                    help="also time the batched many-ligand workload against one launch per job")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -27,15 +27,10 @@ struct BuildShared {
     int bad;
 };
 
-__global__ void __launch_bounds__(kBuildWarps * 32)
-build_kernel(DevSystem S, DevWork W, int n, const int32_t* __restrict__ genes,
-             const double* __restrict__ ic_in) {
-    __shared__ BuildShared sh_all[kBuildWarps];
-    const int wib = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
-    const int p = blockIdx.x * kBuildWarps + wib;
-    if (p >= n) return;
-    BuildShared& sh = sh_all[wib];
+__device__ __forceinline__ void build_pose(const DevSystem& S, const DevWork& W, int p,
+                                           const int32_t* __restrict__ genes,
+                                           const double* __restrict__ ic_in, BuildShared& sh,
+                                           int lane) {
     const int ng = S.n_genes, nl = S.n_lig;
 
     // 1. decode + clamp
@@ -229,10 +224,40 @@ build_kernel(DevSystem S, DevWork W, int n, const int32_t* __restrict__ genes,
     }
 }
 
+__global__ void __launch_bounds__(kBuildWarps * 32)
+build_kernel(DevSystem S, DevWork W, int n, const int32_t* __restrict__ genes,
+             const double* __restrict__ ic_in) {
+    __shared__ BuildShared sh_all[kBuildWarps];
+    const int wib = threadIdx.x >> 5;
+    const int p = blockIdx.x * kBuildWarps + wib;
+    if (p >= n) return;
+    build_pose(S, W, p, genes, ic_in, sh_all[wib], threadIdx.x & 31);
+}
+
+// The same over the poses of several jobs: the warp finds its job, takes the job's system and
+// workspace into shared memory and builds its pose there.
+__global__ void __launch_bounds__(kBuildWarps * 32)
+build_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, int total) {
+    __shared__ BuildShared sh_all[kBuildWarps];
+    __shared__ Job job_all[kBuildWarps];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gp = blockIdx.x * kBuildWarps + wib;
+    if (gp >= total) return;
+    const int j = find_job(jobs, n_jobs, gp, false);
+    Job& job = job_all[wib];
+    copy_job(&job, &jobs[j], lane);
+    build_pose(job.S, job.W, gp - job.pose0, job.genes, nullptr, sh_all[wib], lane);
+}
+
 void launch_build(const DevSystem& S, const DevWork& W, int n, const int32_t* genes,
                   const double* ic, cudaStream_t st) {
     const int blocks = (n + kBuildWarps - 1) / kBuildWarps;
     build_kernel<<<blocks, kBuildWarps * 32, 0, st>>>(S, W, n, genes, ic);
+}
+
+void launch_build_jobs(const Job* jobs, int n_jobs, int total, cudaStream_t st) {
+    const int blocks = (total + kBuildWarps - 1) / kBuildWarps;
+    build_kernel_jobs<<<blocks, kBuildWarps * 32, 0, st>>>(jobs, n_jobs, total);
 }
 
 }  // namespace fxe

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -48,12 +49,23 @@ fxe_status cuda_fail(cudaError_t e, const char* what) {
 
 }  // namespace
 
+// Device allocations freed together; a receptor's block is shared by every context built on it.
+struct DevBlock {
+    std::vector<void*> ptrs;
+    ~DevBlock() {
+        for (void* p : ptrs) cudaFree(p);
+    }
+};
+
 struct fxe_context {
     int device = 0;
     cudaStream_t stream = nullptr;
     fxe::DevSystem S{};
     fxe::DevWork W{};
     std::vector<void*> allocs;
+    std::shared_ptr<DevBlock> receptor = std::make_shared<DevBlock>();
+    int rec_type_max = 0;             // largest receptor atom type (checked against each matrix)
+    const void* rec_key = nullptr;    // identity of the receptor block (contexts sharing it)
     int32_t* d_genes = nullptr;
     double* d_icin = nullptr;
     int last_n = 0;
@@ -84,6 +96,16 @@ struct fxe_context {
         *dst = d;
         return e;
     }
+    template <typename T>
+    cudaError_t upload_receptor(const T** dst, const T* src, size_t count) {
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, count * sizeof(T) + 16);
+        if (e != cudaSuccess) return e;
+        receptor->ptrs.push_back(q);
+        if (count) e = cudaMemcpy(q, src, count * sizeof(T), cudaMemcpyHostToDevice);
+        *dst = reinterpret_cast<const T*>(q);
+        return e;
+    }
     ~fxe_context() {
         for (cudaEvent_t e : ev)
             if (e) cudaEventDestroy(e);
@@ -100,14 +122,16 @@ extern "C" const char* fxe_last_error(void) { return g_err.c_str(); }
         if (_e != cudaSuccess) return cuda_fail(_e, what); \
     } while (0)
 
-extern "C" fxe_status fxe_context_create(const fxe_receptor_desc* rec, const fxe_ligand_desc* lig,
-                                         const fxe_emat_desc* em, const fxe_params* prm,
-                                         int32_t max_poses, fxe_context** out) {
+namespace {
+
+fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share,
+                          const fxe_ligand_desc* lig, const fxe_emat_desc* em, const fxe_params* prm,
+                          int32_t max_poses, fxe_context** out) {
     g_err.clear();
-    if (!rec || !lig || !em || !prm || !out || max_poses <= 0)
+    if ((!rec && !share) || !lig || !em || !prm || !out || max_poses <= 0)
         return fail(FXE_ERR_INVALID_ARGS, "null argument or max_poses <= 0");
     *out = nullptr;
-    if (rec->n_atoms <= 0 || !rec->xyz || !rec->radius || !rec->type || rec->n_grid <= 0 || !rec->grid_ic)
+    if (rec && (rec->n_atoms <= 0 || !rec->xyz || !rec->radius || !rec->type || rec->n_grid <= 0 || !rec->grid_ic))
         return fail(FXE_ERR_INVALID_ARGS, "receptor descriptor incomplete");
     if (lig->n_atoms < 3 || lig->n_atoms > fxe::kMaxLig)
         return fail(FXE_ERR_INVALID_ARGS, "ligand must have 3.." + std::to_string(fxe::kMaxLig) + " atoms");
@@ -135,8 +159,13 @@ extern "C" fxe_status fxe_context_create(const fxe_receptor_desc* rec, const fxe
     if (em->ntypes <= 0 || !em->weight || !em->offset || !em->y || !em->x)
         return fail(FXE_ERR_INVALID_ARGS, "energy matrix incomplete");
     const int T = em->ntypes;
-    for (int i = 0; i < rec->n_atoms; ++i)
-        if (rec->type[i] < 1 || rec->type[i] > T) return fail(FXE_ERR_INVALID_ARGS, "receptor atom type out of range");
+    int rec_type_max = share ? share->rec_type_max : 0;
+    if (rec)
+        for (int i = 0; i < rec->n_atoms; ++i) {
+            if (rec->type[i] < 1) return fail(FXE_ERR_INVALID_ARGS, "receptor atom type out of range");
+            rec_type_max = rec->type[i] > rec_type_max ? rec->type[i] : rec_type_max;
+        }
+    if (rec_type_max > T) return fail(FXE_ERR_INVALID_ARGS, "receptor atom type out of range");
     for (int i = 0; i < lig->n_atoms; ++i)
         if (lig->type[i] < 1 || lig->type[i] > T) return fail(FXE_ERR_INVALID_ARGS, "ligand atom type out of range");
     for (int k = 0; k < T * T; ++k)
@@ -149,17 +178,29 @@ extern "C" fxe_status fxe_context_create(const fxe_receptor_desc* rec, const fxe
     auto* ctx = new fxe_context();
     fxe_status st = [&]() -> fxe_status {
         FXE_TRY(cudaGetDevice(&ctx->device), "cudaGetDevice");
+        if (share && share->device != ctx->device)
+            return fail(FXE_ERR_INVALID_ARGS, "the receptor's context lives on another device");
         FXE_TRY(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         FXE_TRY(fxe::f32::configure_voronoi(), "cudaFuncSetAttribute");
         FXE_TRY(fxe::f64::configure_voronoi(), "cudaFuncSetAttribute");
         fxe::DevSystem& S = ctx->S;
-        const int N = rec->n_atoms, n = lig->n_atoms;
+        ctx->rec_type_max = rec_type_max;
+        const int n = lig->n_atoms;
+        if (share) {
+            // the receptor cache: this context reads the receptor, its cell list and cleft grid
+            // from the device arrays of `share` and keeps them alive
+            ctx->receptor = share->receptor;
+            ctx->rec_key = share->rec_key;
+            S = share->S;
+        } else {
+        ctx->rec_key = ctx->receptor.get();
+        const int N = rec->n_atoms;
         // receptor atoms
         std::vector<float4> pos(N);
         for (int i = 0; i < N; ++i) pos[i] = make_float4(rec->xyz[3 * i], rec->xyz[3 * i + 1], rec->xyz[3 * i + 2], rec->radius[i]);
         S.n_rec = N;
-        FXE_TRY(ctx->upload(&S.rec_pos, pos.data(), N), "receptor upload");
-        FXE_TRY(ctx->upload(&S.rec_type, rec->type, N), "receptor upload");
+        FXE_TRY(ctx->upload_receptor(&S.rec_pos, pos.data(), N), "receptor upload");
+        FXE_TRY(ctx->upload_receptor(&S.rec_type, rec->type, N), "receptor upload");
         for (int k = 0; k < 3; ++k) {
             S.ori[k] = rec->ori[k];
             S.globalmin[k] = rec->globalmin[k];
@@ -190,15 +231,16 @@ extern "C" fxe_status fxe_context_create(const fxe_receptor_desc* rec, const fxe
             catom[w] = i;
             cpos[w] = pos[i];
         }
-        FXE_TRY(ctx->upload(&S.cell_start, start.data(), dim3 + 1), "cell list upload");
-        FXE_TRY(ctx->upload(&S.cell_atom, catom.data(), N), "cell list upload");
-        FXE_TRY(ctx->upload(&S.cell_pos, cpos.data(), N), "cell list upload");
+        FXE_TRY(ctx->upload_receptor(&S.cell_start, start.data(), dim3 + 1), "cell list upload");
+        FXE_TRY(ctx->upload_receptor(&S.cell_atom, catom.data(), N), "cell list upload");
+        FXE_TRY(ctx->upload_receptor(&S.cell_pos, cpos.data(), N), "cell list upload");
         // cleft grid
         std::vector<float4> gic(rec->n_grid);
         for (int g = 0; g < rec->n_grid; ++g)
             gic[g] = make_float4(rec->grid_ic[3 * g], rec->grid_ic[3 * g + 1], rec->grid_ic[3 * g + 2], 0.0f);
         S.n_grid = rec->n_grid;
-        FXE_TRY(ctx->upload(&S.grid_ic, gic.data(), rec->n_grid), "grid upload");
+        FXE_TRY(ctx->upload_receptor(&S.grid_ic, gic.data(), rec->n_grid), "grid upload");
+        }
         // ligand
         S.n_lig = n;
         std::vector<int4> lrec(n);
@@ -282,6 +324,28 @@ extern "C" fxe_status fxe_context_create(const fxe_receptor_desc* rec, const fxe
     }
     *out = ctx;
     return FXE_OK;
+}
+
+}  // namespace
+
+extern "C" fxe_status fxe_context_create(const fxe_receptor_desc* rec, const fxe_ligand_desc* lig,
+                                         const fxe_emat_desc* em, const fxe_params* prm,
+                                         int32_t max_poses, fxe_context** out) {
+    if (!rec) {
+        g_err = "null argument or max_poses <= 0";
+        return FXE_ERR_INVALID_ARGS;
+    }
+    return context_create(rec, nullptr, lig, em, prm, max_poses, out);
+}
+
+extern "C" fxe_status fxe_context_create_shared(const fxe_context* receptor_of, const fxe_ligand_desc* lig,
+                                                const fxe_emat_desc* em, const fxe_params* prm,
+                                                int32_t max_poses, fxe_context** out) {
+    if (!receptor_of) {
+        g_err = "receptor_of is NULL";
+        return FXE_ERR_INVALID_ARGS;
+    }
+    return context_create(nullptr, receptor_of, lig, em, prm, max_poses, out);
 }
 
 namespace {
@@ -586,5 +650,195 @@ extern "C" fxe_status fxe_thermo_compute_device_fixed(const double* d_energies, 
     fxe::launch_thermo_fixed(d_energies, d_multiplicity, (long)n, beta, temperature, scratch, d_out,
                              (cudaStream_t)stream);
     FXE_TRY(cudaGetLastError(), "fixed-scratch thermo launch");
+    return FXE_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// Batched evaluation: the populations of several contexts in one launch of each kernel.
+// ------------------------------------------------------------------------------------------
+namespace fxe {
+void launch_build_jobs(const Job*, int, int, cudaStream_t);
+void launch_contacts_jobs(const Job*, int, long long, cudaStream_t);
+namespace f32 {
+void launch_poses_jobs(const Job*, int, int, cudaStream_t);
+}
+namespace f64 {
+void launch_poses_jobs(const Job*, int, int, cudaStream_t);
+}
+}  // namespace fxe
+
+struct fxe_batch {
+    int device = 0;
+    int max_jobs = 0;
+    int64_t max_poses = 0;
+    int32_t max_genes = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t staged = nullptr;          // the job table's host staging may be rewritten
+    fxe::Job* d_jobs = nullptr;
+    fxe::Job* h_jobs = nullptr;            // pinned
+    int32_t* d_genes = nullptr;            // host-pointer form: staged chromosomes
+    int32_t* h_genes = nullptr;            // pinned
+    fxe_cf* d_out = nullptr;
+    fxe_cf* h_out = nullptr;               // pinned
+    int64_t launches = 0;
+    ~fxe_batch() {
+        if (staged) cudaEventDestroy(staged);
+        if (d_jobs) cudaFree(d_jobs);
+        if (h_jobs) cudaFreeHost(h_jobs);
+        if (d_genes) cudaFree(d_genes);
+        if (h_genes) cudaFreeHost(h_genes);
+        if (d_out) cudaFree(d_out);
+        if (h_out) cudaFreeHost(h_out);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+extern "C" fxe_status fxe_batch_create(int32_t max_jobs, int64_t max_poses, int32_t max_genes, fxe_batch** out) {
+    g_err.clear();
+    if (!out || max_jobs <= 0 || max_poses <= 0 || max_genes <= 0 || max_poses > (int64_t)1 << 30)
+        return fail(FXE_ERR_INVALID_ARGS, "invalid batch limits");
+    *out = nullptr;
+    int dc = 0;
+    if (cudaGetDeviceCount(&dc) != cudaSuccess || dc == 0) return fail(FXE_ERR_NO_DEVICE, "no CUDA device");
+    auto* b = new fxe_batch();
+    fxe_status st = [&]() -> fxe_status {
+        FXE_TRY(cudaGetDevice(&b->device), "cudaGetDevice");
+        b->max_jobs = max_jobs;
+        b->max_poses = max_poses;
+        b->max_genes = max_genes;
+        FXE_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        FXE_TRY(cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming), "cudaEventCreate");
+        FXE_TRY(cudaMalloc(&b->d_jobs, sizeof(fxe::Job) * max_jobs), "batch job table");
+        FXE_TRY(cudaMallocHost(&b->h_jobs, sizeof(fxe::Job) * max_jobs), "batch job table");
+        FXE_TRY(cudaMalloc(&b->d_genes, sizeof(int32_t) * max_poses * max_genes), "batch staging");
+        FXE_TRY(cudaMallocHost(&b->h_genes, sizeof(int32_t) * max_poses * max_genes), "batch staging");
+        FXE_TRY(cudaMalloc(&b->d_out, sizeof(fxe_cf) * max_poses), "batch staging");
+        FXE_TRY(cudaMallocHost(&b->h_out, sizeof(fxe_cf) * max_poses), "batch staging");
+        FXE_TRY(cudaEventRecord(b->staged, b->stream), "cudaEventRecord");
+        return FXE_OK;
+    }();
+    if (st != FXE_OK) {
+        delete b;
+        return st;
+    }
+    *out = b;
+    return FXE_OK;
+}
+
+extern "C" void fxe_batch_destroy(fxe_batch* b) { delete b; }
+
+namespace {
+
+// Fills the job table, uploads it and launches the three kernels over every job's poses.
+// genes_of / out_of give each job's device chromosomes and records.
+template <typename G, typename O>
+fxe_status batch_launch(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, cudaStream_t s, G genes_of, O out_of) {
+    int prec = -1, total = 0;
+    long long items = 0;
+    FXE_TRY(cudaEventSynchronize(b->staged), "batch staging");
+    int k = 0;
+    for (int i = 0; i < n_jobs; ++i) {
+        fxe_context* ctx = jobs[i].ctx;
+        if (jobs[i].n == 0) continue;
+        fxe::Job& J = b->h_jobs[k++];
+        J.S = ctx->S;
+        J.W = ctx->W;
+        J.W.out = out_of(i);
+        J.genes = genes_of(i);
+        J.pose0 = total;
+        J.n = jobs[i].n;
+        J.warp0 = items;
+        total += jobs[i].n;
+        items += (long long)jobs[i].n * ctx->S.n_lig;
+        ctx->last_n = jobs[i].n;
+        prec = ctx->precision;
+    }
+    if (k == 0) return FXE_OK;
+    FXE_TRY(cudaMemcpyAsync(b->d_jobs, b->h_jobs, sizeof(fxe::Job) * k, cudaMemcpyHostToDevice, s), "job table");
+    FXE_TRY(cudaEventRecord(b->staged, s), "cudaEventRecord");
+    fxe::launch_build_jobs(b->d_jobs, k, total, s);
+    fxe::launch_contacts_jobs(b->d_jobs, k, items, s);
+    if (prec == FXE_PRECISION_FAST) fxe::f32::launch_poses_jobs(b->d_jobs, k, total, s);
+    else fxe::f64::launch_poses_jobs(b->d_jobs, k, total, s);
+    FXE_TRY(cudaGetLastError(), "batched kernel launch");
+    b->launches += 3;
+    return FXE_OK;
+}
+
+fxe_status batch_check(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, bool device_ptrs, int64_t* total) {
+    if (!b || (n_jobs > 0 && !jobs) || n_jobs < 0) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    if (n_jobs > b->max_jobs)
+        return fail(FXE_ERR_INVALID_ARGS, "n_jobs = " + std::to_string(n_jobs) + " exceeds the batch's max_jobs");
+    int64_t t = 0;
+    int prec = -1;
+    for (int i = 0; i < n_jobs; ++i) {
+        const fxe_context* ctx = jobs[i].ctx;
+        if (!ctx || jobs[i].n < 0) return fail(FXE_ERR_INVALID_ARGS, "job " + std::to_string(i) + ": no context or n < 0");
+        if (jobs[i].n == 0) continue;
+        if (!jobs[i].genes || !jobs[i].out) return fail(FXE_ERR_INVALID_ARGS, "job " + std::to_string(i) + ": NULL genes or out");
+        if (ctx->device != b->device) return fail(FXE_ERR_INVALID_ARGS, "job " + std::to_string(i) + ": context on another device");
+        if (jobs[i].n > ctx->W.max_poses)
+            return fail(FXE_ERR_INVALID_ARGS, "job " + std::to_string(i) + ": n exceeds its context's max_poses");
+        if (!device_ptrs && ctx->S.n_genes > b->max_genes)
+            return fail(FXE_ERR_INVALID_ARGS, "job " + std::to_string(i) + ": more genes than the batch's max_genes");
+        if (prec >= 0 && ctx->precision != prec)
+            return fail(FXE_ERR_INVALID_ARGS, "jobs of one batch must share one precision");
+        prec = ctx->precision;
+        for (int q = 0; q < i; ++q)
+            if (jobs[q].ctx == ctx && jobs[q].n > 0)
+                return fail(FXE_ERR_INVALID_ARGS, "a context appears twice in one batch (its workspace is per context)");
+        t += jobs[i].n;
+    }
+    if (t > b->max_poses) return fail(FXE_ERR_INVALID_ARGS, "total poses exceed the batch's max_poses");
+    *total = t;
+    return FXE_OK;
+}
+
+}  // namespace
+
+extern "C" fxe_status fxe_batch_eval_genes_device(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, void* stream) {
+    g_err.clear();
+    int64_t total = 0;
+    fxe_status st = batch_check(b, jobs, n_jobs, true, &total);
+    if (st != FXE_OK) return st;
+    if (cudaSetDevice(b->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+    return batch_launch(b, jobs, n_jobs, s, [&](int i) { return (const int32_t*)jobs[i].genes; },
+                        [&](int i) { return jobs[i].out; });
+}
+
+extern "C" fxe_status fxe_batch_eval_genes(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs) {
+    g_err.clear();
+    int64_t total = 0;
+    fxe_status st = batch_check(b, jobs, n_jobs, false, &total);
+    if (st != FXE_OK) return st;
+    if (cudaSetDevice(b->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
+    cudaStream_t s = b->stream;
+    // the previous call's copies from the pinned staging have completed (it synchronised)
+    std::vector<int64_t> goff(n_jobs + 1, 0), poff(n_jobs + 1, 0);
+    for (int i = 0; i < n_jobs; ++i) {
+        const int64_t ng = jobs[i].n > 0 ? jobs[i].ctx->S.n_genes : 0;
+        goff[i + 1] = goff[i] + (int64_t)jobs[i].n * ng;
+        poff[i + 1] = poff[i] + jobs[i].n;
+        if (jobs[i].n > 0) std::memcpy(b->h_genes + goff[i], jobs[i].genes, sizeof(int32_t) * jobs[i].n * ng);
+    }
+    if (total == 0) return FXE_OK;
+    FXE_TRY(cudaMemcpyAsync(b->d_genes, b->h_genes, sizeof(int32_t) * goff[n_jobs], cudaMemcpyHostToDevice, s),
+            "genes to device");
+    st = batch_launch(b, jobs, n_jobs, s, [&](int i) { return (const int32_t*)(b->d_genes + goff[i]); },
+                      [&](int i) { return b->d_out + poff[i]; });
+    if (st != FXE_OK) return st;
+    FXE_TRY(cudaMemcpyAsync(b->h_out, b->d_out, sizeof(fxe_cf) * total, cudaMemcpyDeviceToHost, s), "results to host");
+    FXE_TRY(cudaStreamSynchronize(s), "batched evaluation");
+    for (int i = 0; i < n_jobs; ++i)
+        if (jobs[i].n > 0) std::memcpy(jobs[i].out, b->h_out + poff[i], sizeof(fxe_cf) * jobs[i].n);
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_batch_take_launches(fxe_batch* b, int64_t* launches) {
+    g_err.clear();
+    if (!b || !launches) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    *launches = b->launches;
+    b->launches = 0;
     return FXE_OK;
 }

@@ -109,6 +109,39 @@ struct DevWork {
     int* counters;         // [4]: unused, hull failures, capacity, no-partner faces
 };
 
+// One job of a batched launch: a context's system and workspace (W.out pointing at the job's
+// own output records), the job's chromosomes, and where its poses sit in the launch.
+struct Job {
+    DevSystem S;
+    DevWork W;
+    const int32_t* genes;  // [n * S.n_genes]
+    int pose0;             // first pose of the job in the launch
+    int n;                 // poses of the job
+    long long warp0;       // first (pose, ligand atom) item of the job in the contact launch
+};
+
+// Index of the job holding launch item `key` (a pose, or a (pose, atom) item when by_warp):
+// the last job whose first item is at or before key.
+__device__ __forceinline__ int find_job(const Job* jobs, int n_jobs, long long key, bool by_warp) {
+    int lo = 0, hi = n_jobs;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        const long long first = by_warp ? jobs[mid].warp0 : (long long)jobs[mid].pose0;
+        if (first <= key) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Copies a job descriptor into shared memory with the lanes of one warp.
+__device__ __forceinline__ void copy_job(Job* dst, const Job* src, int lane) {
+    static_assert(sizeof(Job) % 4 == 0, "Job is copied in 4-byte words");
+    const int* s = reinterpret_cast<const int*>(src);
+    int* d = reinterpret_cast<int*>(dst);
+    for (int k = lane; k < (int)(sizeof(Job) / 4); k += 32) d[k] = s[k];
+    __syncwarp();
+}
+
 // one block's share of the ensemble reduction: running max of the log-weights and the sums
 // of exp(lw - m), E exp(lw - m), E^2 exp(lw - m)
 struct LsePart {

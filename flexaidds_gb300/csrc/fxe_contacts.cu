@@ -21,13 +21,8 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // ------------------------------------------------------------------------------------------
 // contacts_kernel
 // ------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(128)
-contacts_kernel(DevSystem S, DevWork W, int n) {
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+__device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork& W, int p, int a, int lane) {
     const int nl = S.n_lig;
-    if (gw >= n * nl) return;
-    const int p = gw / nl, a = gw % nl;
     const size_t lb = (size_t)p * nl;
     const int4 pg = W.pose_grid[p];
     const size_t cb = (lb + a) * kMaxCand;
@@ -135,9 +130,36 @@ contacts_kernel(DevSystem S, DevWork W, int n) {
     }
 }
 
+__global__ void __launch_bounds__(128)
+contacts_kernel(DevSystem S, DevWork W, int n) {
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nl = S.n_lig;
+    if (gw >= n * nl) return;
+    contacts_atom(S, W, gw / nl, gw % nl, threadIdx.x & 31);
+}
+
+// The same over the (pose, ligand atom) items of several jobs.
+__global__ void __launch_bounds__(128)
+contacts_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, long long total) {
+    __shared__ Job job_all[4];
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (gw >= total) return;
+    const int j = find_job(jobs, n_jobs, gw, true);
+    Job& job = job_all[wib];
+    copy_job(&job, &jobs[j], lane);
+    const int nl = job.S.n_lig;
+    const long long r = gw - job.warp0;
+    contacts_atom(job.S, job.W, (int)(r / nl), (int)(r % nl), lane);
+}
+
 void launch_contacts(const DevSystem& S, const DevWork& W, int n, cudaStream_t st) {
     const long warps = (long)n * S.n_lig;
     contacts_kernel<<<(unsigned)((warps + 3) / 4), 128, 0, st>>>(S, W, n);
+}
+
+void launch_contacts_jobs(const Job* jobs, int n_jobs, long long total_items, cudaStream_t st) {
+    contacts_kernel_jobs<<<(unsigned)((total_items + 3) / 4), 128, 0, st>>>(jobs, n_jobs, total_items);
 }
 
 }  // namespace fxe

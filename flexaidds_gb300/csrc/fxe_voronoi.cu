@@ -1071,14 +1071,9 @@ __device__ void finish_failed(const DevWork& W, int p, int lane, int status, dou
     if (lane == 0) W.out[p] = cf;
 }
 
-__global__ void __launch_bounds__(kVorWarps * 32)
-pose_kernel(DevSystem S, DevWork W, int n) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    PoseShared& ps = reinterpret_cast<PoseShared*>(smem)[threadIdx.x >> 5];
+__device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W, int p, int lane,
+                                           PoseShared& ps) {
     VorShared& sh = ps.v;
-    const int p = blockIdx.x * kVorWarps + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (p >= n) return;
     const int nl = S.n_lig;
     const size_t lb = (size_t)p * nl;
     if (W.pose_grid[p].z) {
@@ -1275,14 +1270,51 @@ pose_kernel(DevSystem S, DevWork W, int n) {
     if (lane == 0) W.out[p] = cf;
 }
 
+__global__ void __launch_bounds__(kVorWarps * 32)
+pose_kernel(DevSystem S, DevWork W, int n) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    PoseShared& ps = reinterpret_cast<PoseShared*>(smem)[threadIdx.x >> 5];
+    const int p = blockIdx.x * kVorWarps + (threadIdx.x >> 5);
+    if (p >= n) return;
+    score_pose(S, W, p, threadIdx.x & 31, ps);
+}
+
+// The same over the poses of several jobs; each warp keeps its job's system and workspace in
+// shared memory next to its polyhedron workspace.
+struct PoseSlot {
+    PoseShared ps;
+    Job job;
+};
+
+__global__ void __launch_bounds__(kVorWarps * 32)
+pose_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, int total) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    PoseSlot& slot = reinterpret_cast<PoseSlot*>(smem)[threadIdx.x >> 5];
+    const int gp = blockIdx.x * kVorWarps + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (gp >= total) return;
+    const int j = find_job(jobs, n_jobs, gp, false);
+    copy_job(&slot.job, &jobs[j], lane);
+    score_pose(slot.job.S, slot.job.W, gp - slot.job.pose0, lane, slot.ps);
+}
+
 size_t pose_smem_bytes() { return sizeof(PoseShared) * kVorWarps; }
+size_t pose_jobs_smem_bytes() { return sizeof(PoseSlot) * kVorWarps; }
 
 void launch_poses(const DevSystem& S, const DevWork& W, int n, cudaStream_t st) {
     pose_kernel<<<(unsigned)((n + kVorWarps - 1) / kVorWarps), kVorWarps * 32, pose_smem_bytes(), st>>>(S, W, n);
 }
 
+void launch_poses_jobs(const Job* jobs, int n_jobs, int total, cudaStream_t st) {
+    pose_kernel_jobs<<<(unsigned)((total + kVorWarps - 1) / kVorWarps), kVorWarps * 32, pose_jobs_smem_bytes(),
+                       st>>>(jobs, n_jobs, total);
+}
+
 cudaError_t configure_voronoi() {
-    return cudaFuncSetAttribute(pose_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pose_smem_bytes());
+    cudaError_t e = cudaFuncSetAttribute(pose_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pose_smem_bytes());
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(pose_kernel_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)pose_jobs_smem_bytes());
 }
 
 }  // namespace FXE_VARIANT

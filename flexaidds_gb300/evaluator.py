@@ -50,6 +50,13 @@ def load_library():
         lib.fxe_context_set_precision.argtypes = [vp, C.c_int32]
         lib.fxe_context_enable_timing.argtypes = [vp, C.c_int32]
         lib.fxe_context_take_timing.argtypes = [vp, _d, C.POINTER(C.c_int64)]
+        lib.fxe_context_create_shared.argtypes = [vp, vp, vp, vp, C.c_int32, C.POINTER(vp)]
+        lib.fxe_batch_create.argtypes = [C.c_int32, C.c_int64, C.c_int32, C.POINTER(vp)]
+        lib.fxe_batch_eval_genes.argtypes = [vp, vp, C.c_int32]
+        lib.fxe_batch_eval_genes_device.argtypes = [vp, vp, C.c_int32, vp]
+        lib.fxe_batch_take_launches.argtypes = [vp, C.POINTER(C.c_int64)]
+        lib.fxe_batch_destroy.argtypes = [vp]
+        lib.fxe_batch_destroy.restype = None
         lib.fxe_context_destroy.argtypes = [vp]
         lib.fxe_context_destroy.restype = None
         lib.fxe_last_error.restype = C.c_char_p
@@ -68,15 +75,23 @@ class GPUEvaluator:
 
     REFERENCE, FAST = 0, 1
 
-    def __init__(self, desc: Descriptor, max_poses: int = 2048, precision: int = 0):
+    def __init__(self, desc: Descriptor, max_poses: int = 2048, precision: int = 0,
+                 share_receptor_with: "GPUEvaluator | None" = None):
+        """share_receptor_with: an evaluator on the same receptor whose device copy of the
+        receptor, cell list and cleft grid this one reuses (fxe_context_create_shared)."""
         self.lib = load_library()
         self.desc = desc
         self._packed = Packed(desc)
         self.max_poses = int(max_poses)
         h = C.c_void_p()
         pk = self._packed
-        _check(self.lib.fxe_context_create(C.byref(pk.rec), C.byref(pk.lig), C.byref(pk.emat),
-                                           C.byref(pk.params), self.max_poses, C.byref(h)))
+        if share_receptor_with is not None:
+            _check(self.lib.fxe_context_create_shared(share_receptor_with.handle, C.byref(pk.lig),
+                                                      C.byref(pk.emat), C.byref(pk.params),
+                                                      self.max_poses, C.byref(h)))
+        else:
+            _check(self.lib.fxe_context_create(C.byref(pk.rec), C.byref(pk.lig), C.byref(pk.emat),
+                                               C.byref(pk.params), self.max_poses, C.byref(h)))
         self.handle = h
         _check(self.lib.fxe_context_set_precision(self.handle, int(precision)))
 
@@ -137,6 +152,57 @@ class GPUEvaluator:
         o = np.zeros(4, np.int32)
         _check(self.lib.fxe_last_stats(self.handle, ptr(o, _i)))
         return {"hull_failures": int(o[1]), "capacity": int(o[2]), "no_partner_faces": int(o[3])}
+
+
+class Job(C.Structure):
+    _fields_ = [("ctx", C.c_void_p), ("n", C.c_int32), ("genes", C.c_void_p), ("out", C.c_void_p)]
+
+
+class Batch:
+    """Several evaluators' populations scored in one launch of each kernel (fxe_batch_*)."""
+
+    def __init__(self, max_jobs: int, max_poses: int, max_genes: int = 64):
+        self.lib = load_library()
+        h = C.c_void_p()
+        _check(self.lib.fxe_batch_create(int(max_jobs), int(max_poses), int(max_genes), C.byref(h)))
+        self.handle = h
+
+    def eval_genes(self, jobs) -> list:
+        """jobs: [(GPUEvaluator, int32 genes (n, n_genes)), ...] -> list of record arrays."""
+        arr = (Job * max(1, len(jobs)))()
+        keep, outs = [], []
+        for k, (ev, genes) in enumerate(jobs):
+            g = np.ascontiguousarray(genes, np.int32)
+            out = np.zeros(g.shape[0], CF_DTYPE)
+            keep.append(g)
+            outs.append(out)
+            arr[k] = Job(ev.handle.value, g.shape[0], g.ctypes.data, out.ctypes.data)
+        _check(self.lib.fxe_batch_eval_genes(self.handle, arr, len(jobs)))
+        return outs
+
+    def eval_genes_device(self, jobs, stream: int = 0):
+        """jobs: [(GPUEvaluator, n, device genes pointer, device records pointer), ...]; not waited for."""
+        arr = (Job * max(1, len(jobs)))()
+        for k, (ev, n, dg, do) in enumerate(jobs):
+            arr[k] = Job(ev.handle.value, int(n), int(dg), int(do))
+        _check(self.lib.fxe_batch_eval_genes_device(self.handle, arr, len(jobs),
+                                                    C.c_void_p(stream) if stream else None))
+
+    def take_launches(self) -> int:
+        n = C.c_int64(0)
+        _check(self.lib.fxe_batch_take_launches(self.handle, C.byref(n)))
+        return int(n.value)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.fxe_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def ic2cf(evaluator: GPUEvaluator, icv) -> np.void:

@@ -126,6 +126,14 @@ fxe_status fxe_context_create(const fxe_receptor_desc* receptor, const fxe_ligan
                               const fxe_emat_desc* emat, const fxe_params* params,
                               int32_t max_poses, fxe_context** out);
 
+/* A context for another ligand (or energy matrix, or scoring switches) on the receptor of
+ * `receptor_of`: the receptor atoms, cell list and cleft grid stay where `receptor_of` put them
+ * and are shared, not copied (the receptor cache); they live until the last context using them
+ * is destroyed. No reference counterpart: the reference keeps one receptor per process. */
+fxe_status fxe_context_create_shared(const fxe_context* receptor_of, const fxe_ligand_desc* ligand,
+                                     const fxe_emat_desc* emat, const fxe_params* params,
+                                     int32_t max_poses, fxe_context** out);
+
 /* Arithmetic of the Voronoi polyhedra and contact areas.
  * FXE_PRECISION_REFERENCE (default): double precision with the reference's own expressions and
  *   no fused multiply-adds, so that every operation rounds as in the reference's double
@@ -220,6 +228,37 @@ fxe_status fxe_context_enable_timing(fxe_context* ctx, int32_t on);
 fxe_status fxe_context_take_timing(fxe_context* ctx, double* ms3, int64_t* launches);
 
 void fxe_context_destroy(fxe_context* ctx);
+
+/* Batched evaluation: the populations of several contexts (different ligands, receptors, sizes)
+ * scored by one launch of each kernel over all their poses, in place of one launch sequence per
+ * population (the reference scores one population per cuda_eval_batch call). Each job names a
+ * context, its chromosome count, its int32 genes and its output records; a context may appear
+ * once per batch (its workspace holds that job's poses), all contexts share the batch's device
+ * and one precision, and each job's n is at most its context's max_poses. Results equal those
+ * of fxe_eval_genes on each context alone. */
+typedef struct fxe_batch fxe_batch;
+typedef struct fxe_job {
+    fxe_context* ctx;
+    int32_t n;
+    const int32_t* genes;   /* n * n_genes of ctx */
+    fxe_cf* out;            /* n records */
+} fxe_job;
+
+/* max_jobs jobs per call, max_poses poses in all, max_genes genes per chromosome (for staging
+ * host chromosomes). */
+fxe_status fxe_batch_create(int32_t max_jobs, int64_t max_poses, int32_t max_genes, fxe_batch** out);
+
+/* Host genes and records; synchronous. */
+fxe_status fxe_batch_eval_genes(fxe_batch* batch, const fxe_job* jobs, int32_t n_jobs);
+
+/* Device genes and records; queued on `stream` (cudaStream_t, NULL: the batch's own stream) and
+ * not waited for. A later call waits until this call's job table has been copied. */
+fxe_status fxe_batch_eval_genes_device(fxe_batch* batch, const fxe_job* jobs, int32_t n_jobs, void* stream);
+
+/* Kernels launched by the batch since the previous call (resets the count). */
+fxe_status fxe_batch_take_launches(fxe_batch* batch, int64_t* launches);
+
+void fxe_batch_destroy(fxe_batch* batch);
 
 /* Message describing the last error on the calling thread ("" if none). */
 const char* fxe_last_error(void);
