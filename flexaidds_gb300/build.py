@@ -14,7 +14,7 @@ LIB = os.path.join(HERE, "libfxe.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # (source, extra flags): the pose build is evaluated without fused multiply-adds, like the
 # reference's single-precision build
-UNITS = [("fxe_build.cu", ["--fmad=false"]), ("fxe_contacts.cu", []), ("fxe_thermo.cu", []),
+UNITS = [("fxe_build.cu", ["--fmad=false"]), ("fxe_contacts.cu", []), ("fxe_thermo.cu", []), ("fxe_ga.cu", []),
          ("fxe_capi.cu", []),
          # the polyhedron kernel twice: single precision, and double precision with the
          # reference's expressions and every operation rounded separately

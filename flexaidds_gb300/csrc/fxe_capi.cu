@@ -842,3 +842,289 @@ extern "C" fxe_status fxe_batch_take_launches(fxe_batch* b, int64_t* launches) {
     b->launches = 0;
     return FXE_OK;
 }
+
+// ------------------------------------------------------------------------------------------
+// GA engine: populations resident in HBM; a generation of every running job is one graph of
+// breeding, one batched evaluation and selection.
+// ------------------------------------------------------------------------------------------
+namespace fxe {
+void launch_ga_init(const GaJob*, const int*, int, cudaStream_t);
+void launch_ga_breed(const GaJob*, const int*, int, cudaStream_t);
+void launch_ga_select(GaJob*, const int*, int, bool, cudaStream_t);
+}  // namespace fxe
+
+namespace {
+struct GaSlot {
+    bool used = false, running = false, finished = false;
+    fxe_context* ctx = nullptr;
+    fxe_ga_job job{};
+    int steps = 0;
+    std::vector<void*> mem;
+    fxe::GaJob J{};   // host copy of the pointers as set up (the device copy swaps them)
+};
+}  // namespace
+
+struct fxe_ga {
+    int device = 0;
+    int max_jobs = 0;
+    int precision = FXE_PRECISION_REFERENCE;
+    cudaStream_t stream = nullptr;
+    std::vector<GaSlot> slots;
+    fxe::GaJob* d_all = nullptr;        // [max_jobs] per-slot state (pointers swap on device)
+    int* d_ids = nullptr;               // [max_jobs] 0..max_jobs-1
+    int* d_run = nullptr;               // [max_jobs] running slots of the captured graph
+    fxe::Job* d_eval = nullptr;         // [max_jobs] batched-evaluation table of the running slots
+    std::vector<int> run;               // running slots of the captured graph
+    cudaGraphExec_t exec = nullptr;
+    bool dirty = true;
+    int64_t launches = 0, graph_launches = 0;
+    ~fxe_ga() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (exec) cudaGraphExecDestroy(exec);
+        for (auto& s : slots)
+            for (void* p : s.mem) cudaFree(p);
+        if (d_all) cudaFree(d_all);
+        if (d_ids) cudaFree(d_ids);
+        if (d_run) cudaFree(d_run);
+        if (d_eval) cudaFree(d_eval);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+extern "C" fxe_status fxe_ga_create(int32_t max_jobs, int32_t precision, fxe_ga** out) {
+    g_err.clear();
+    if (!out || max_jobs <= 0 || (precision != FXE_PRECISION_REFERENCE && precision != FXE_PRECISION_FAST))
+        return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    *out = nullptr;
+    int dc = 0;
+    if (cudaGetDeviceCount(&dc) != cudaSuccess || dc == 0) return fail(FXE_ERR_NO_DEVICE, "no CUDA device");
+    auto* e = new fxe_ga();
+    fxe_status st = [&]() -> fxe_status {
+        FXE_TRY(cudaGetDevice(&e->device), "cudaGetDevice");
+        e->max_jobs = max_jobs;
+        e->precision = precision;
+        e->slots.resize(max_jobs);
+        FXE_TRY(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        FXE_TRY(cudaMalloc(&e->d_all, sizeof(fxe::GaJob) * max_jobs), "GA state");
+        FXE_TRY(cudaMalloc(&e->d_ids, sizeof(int) * max_jobs), "GA state");
+        FXE_TRY(cudaMalloc(&e->d_run, sizeof(int) * max_jobs), "GA state");
+        FXE_TRY(cudaMalloc(&e->d_eval, sizeof(fxe::Job) * max_jobs), "GA state");
+        std::vector<int> ids(max_jobs);
+        for (int i = 0; i < max_jobs; ++i) ids[i] = i;
+        FXE_TRY(cudaMemcpy(e->d_ids, ids.data(), sizeof(int) * max_jobs, cudaMemcpyHostToDevice), "GA state");
+        return FXE_OK;
+    }();
+    if (st != FXE_OK) {
+        delete e;
+        return st;
+    }
+    *out = e;
+    return FXE_OK;
+}
+
+extern "C" void fxe_ga_destroy(fxe_ga* e) { delete e; }
+
+extern "C" fxe_status fxe_ga_job_bytes(const fxe_ga_job* job, int64_t* bytes) {
+    g_err.clear();
+    if (!job || !job->ctx || !bytes) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    const int64_t P = job->population, ng = job->ctx->S.n_genes, G = job->generations;
+    *bytes = P * ng * 4 * 3 + P * 8 * 2 + P * (int64_t)sizeof(fxe_cf) + P * (G + 1) * 8 + 16;
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_ga_admit(fxe_ga* e, const fxe_ga_job* job, int32_t* slot_out) {
+    g_err.clear();
+    if (!e || !job || !job->ctx || !slot_out) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    fxe_context* ctx = job->ctx;
+    const int P = job->population, ng = ctx->S.n_genes;
+    if (P < 2 || P > 2048 || P > ctx->W.max_poses)
+        return fail(FXE_ERR_INVALID_ARGS, "population must be 2..2048 and at most the context's max_poses");
+    if (job->generations < 0 || ng < 1 || ng > 64)
+        return fail(FXE_ERR_INVALID_ARGS, "generations < 0, or genes outside 1..64");
+    if (ctx->device != e->device) return fail(FXE_ERR_INVALID_ARGS, "context on another device");
+    for (const auto& s : e->slots)
+        if (s.used && s.ctx == ctx) return fail(FXE_ERR_INVALID_ARGS, "the context already runs a job");
+    int k = -1;
+    for (int i = 0; i < e->max_jobs && k < 0; ++i)
+        if (!e->slots[i].used) k = i;
+    if (k < 0) return fail(FXE_ERR_OVER_BUDGET, "no free job slot");
+    if (cudaSetDevice(e->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
+    GaSlot& s = e->slots[k];
+    auto get = [&](size_t bytes, void** p) -> cudaError_t {
+        cudaError_t r = cudaMalloc(p, bytes + 16);
+        if (r == cudaSuccess) s.mem.push_back(*p);
+        return r;
+    };
+    fxe::GaJob J{};
+    void* q = nullptr;
+    fxe_status st = [&]() -> fxe_status {
+        FXE_TRY(get(sizeof(int32_t) * P * ng, &q), "GA population"); J.pop = (int32_t*)q;
+        FXE_TRY(get(sizeof(int32_t) * P * ng, &q), "GA population"); J.pop_next = (int32_t*)q;
+        FXE_TRY(get(sizeof(double) * P, &q), "GA population"); J.pop_e = (double*)q;
+        FXE_TRY(get(sizeof(double) * P, &q), "GA population"); J.pop_e_next = (double*)q;
+        FXE_TRY(get(sizeof(int32_t) * P * ng, &q), "GA children"); J.child = (int32_t*)q;
+        FXE_TRY(get(sizeof(fxe_cf) * P, &q), "GA children"); J.child_cf = (const fxe_cf*)q;
+        FXE_TRY(get(sizeof(double) * P * ((size_t)job->generations + 1), &q), "GA ensemble"); J.ens = (double*)q;
+        FXE_TRY(get(sizeof(int), &q), "GA counter"); J.gen = (int*)q;
+        FXE_TRY(cudaMemsetAsync(J.gen, 0, sizeof(int), e->stream), "GA counter");
+        J.seed = job->seed;
+        J.cross_rate = job->cross_rate;
+        J.mut_rate = job->mut_rate;
+        J.P = P;
+        J.ng = ng;
+        J.G = job->generations;
+        FXE_TRY(cudaMemcpyAsync(e->d_all + k, &J, sizeof(J), cudaMemcpyHostToDevice, e->stream), "GA state");
+        // generation 0: uniform genes, evaluated on the job's context, sorted
+        fxe::launch_ga_init(e->d_all, e->d_ids + k, 1, e->stream);
+        const int prec = ctx->precision;
+        ctx->precision = e->precision;
+        fxe_status r = run_chunk(ctx, P, J.child, nullptr, e->stream);
+        ctx->precision = prec;
+        if (r != FXE_OK) return r;
+        FXE_TRY(cudaMemcpyAsync((void*)J.child_cf, ctx->W.out, sizeof(fxe_cf) * P, cudaMemcpyDeviceToDevice, e->stream),
+                "GA records");
+        fxe::launch_ga_select(e->d_all, e->d_ids + k, 1, true, e->stream);
+        FXE_TRY(cudaGetLastError(), "GA launch");
+        FXE_TRY(cudaStreamSynchronize(e->stream), "GA admission");   // the host copy of J is not kept alive
+        e->launches += 5;
+        return FXE_OK;
+    }();
+    if (st != FXE_OK) {
+        for (void* p : s.mem) cudaFree(p);
+        s.mem.clear();
+        return st;
+    }
+    s.used = true;
+    s.running = job->generations > 0;
+    s.finished = job->generations == 0;
+    s.ctx = ctx;
+    s.job = *job;
+    s.steps = 0;
+    s.J = J;
+    e->dirty = true;
+    *slot_out = k;
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_ga_step(fxe_ga* e) {
+    g_err.clear();
+    if (!e) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    if (cudaSetDevice(e->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
+    if (e->dirty) {
+        e->run.clear();
+        for (int i = 0; i < e->max_jobs; ++i)
+            if (e->slots[i].running) e->run.push_back(i);
+        if (e->exec) {
+            cudaGraphExecDestroy(e->exec);
+            e->exec = nullptr;
+        }
+        e->dirty = false;
+        if (e->run.empty()) return FXE_OK;
+        const int n = (int)e->run.size();
+        std::vector<fxe::Job> ev(n);
+        int total = 0;
+        long long items = 0;
+        for (int r = 0; r < n; ++r) {
+            GaSlot& s = e->slots[e->run[r]];
+            fxe::Job& J = ev[r];
+            J.S = s.ctx->S;
+            J.W = s.ctx->W;
+            J.W.out = const_cast<fxe_cf*>(s.J.child_cf);
+            J.genes = s.J.child;
+            J.pose0 = total;
+            J.n = s.job.population;
+            J.warp0 = items;
+            total += J.n;
+            items += (long long)J.n * s.ctx->S.n_lig;
+        }
+        FXE_TRY(cudaMemcpyAsync(e->d_run, e->run.data(), sizeof(int) * n, cudaMemcpyHostToDevice, e->stream), "GA table");
+        FXE_TRY(cudaMemcpyAsync(e->d_eval, ev.data(), sizeof(fxe::Job) * n, cudaMemcpyHostToDevice, e->stream), "GA table");
+        FXE_TRY(cudaStreamSynchronize(e->stream), "GA table");
+        cudaGraph_t g = nullptr;
+        FXE_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+        fxe::launch_ga_breed(e->d_all, e->d_run, n, e->stream);
+        fxe::launch_build_jobs(e->d_eval, n, total, e->stream);
+        fxe::launch_contacts_jobs(e->d_eval, n, items, e->stream);
+        if (e->precision == FXE_PRECISION_FAST) fxe::f32::launch_poses_jobs(e->d_eval, n, total, e->stream);
+        else fxe::f64::launch_poses_jobs(e->d_eval, n, total, e->stream);
+        fxe::launch_ga_select(e->d_all, e->d_run, n, false, e->stream);
+        cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+        if (ce != cudaSuccess) return cuda_fail(ce, "graph capture");
+        ce = cudaGraphInstantiate(&e->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return cuda_fail(ce, "graph instantiate");
+    }
+    if (e->run.empty()) return FXE_OK;
+    FXE_TRY(cudaGraphLaunch(e->exec, e->stream), "graph launch");
+    e->launches += 5;
+    e->graph_launches += 1;
+    for (int i : e->run) {
+        GaSlot& s = e->slots[i];
+        if (++s.steps >= s.job.generations) {
+            s.running = false;
+            s.finished = true;
+            e->dirty = true;
+        }
+    }
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_ga_finished(fxe_ga* e, int32_t* slots, int32_t cap, int32_t* n) {
+    g_err.clear();
+    if (!e || !n || cap < 0 || (cap > 0 && !slots)) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    FXE_TRY(cudaStreamSynchronize(e->stream), "GA step");
+    int k = 0;
+    for (int i = 0; i < e->max_jobs; ++i)
+        if (e->slots[i].used && e->slots[i].finished) {
+            if (k < cap) slots[k] = i;
+            ++k;
+        }
+    *n = k;
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_ga_collect(fxe_ga* e, int32_t slot, double temperature, int32_t* best_genes,
+                                     double* best_energy, fxe_thermo* thermo) {
+    g_err.clear();
+    if (!e || slot < 0 || slot >= e->max_jobs || !e->slots[slot].used || !e->slots[slot].finished)
+        return fail(FXE_ERR_INVALID_ARGS, "slot does not hold a finished job");
+    GaSlot& s = e->slots[slot];
+    if (cudaSetDevice(e->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
+    FXE_TRY(cudaStreamSynchronize(e->stream), "GA step");
+    fxe::GaJob J;
+    FXE_TRY(cudaMemcpy(&J, e->d_all + slot, sizeof(J), cudaMemcpyDeviceToHost), "GA state");
+    const int P = s.job.population, ng = s.ctx->S.n_genes;
+    if (best_genes) FXE_TRY(cudaMemcpy(best_genes, J.pop, sizeof(int32_t) * ng, cudaMemcpyDeviceToHost), "GA result");
+    if (best_energy) FXE_TRY(cudaMemcpy(best_energy, J.pop_e, sizeof(double), cudaMemcpyDeviceToHost), "GA result");
+    if (thermo) {
+        fxe_status st = thermo_run(J.ens, nullptr, (long)P * (s.job.generations + 1), temperature, thermo, nullptr,
+                                   e->stream);
+        if (st != FXE_OK) return st;
+    }
+    for (void* p : s.mem) cudaFree(p);
+    s = GaSlot();
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_ga_take_launches(fxe_ga* e, int64_t* launches, int64_t* graphs) {
+    g_err.clear();
+    if (!e) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    if (launches) *launches = e->launches;
+    if (graphs) *graphs = e->graph_launches;
+    e->launches = e->graph_launches = 0;
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_ga_population(fxe_ga* e, int32_t slot, int32_t* genes, double* energies) {
+    g_err.clear();
+    if (!e || slot < 0 || slot >= e->max_jobs || !e->slots[slot].used) return fail(FXE_ERR_INVALID_ARGS, "empty slot");
+    GaSlot& s = e->slots[slot];
+    if (cudaSetDevice(e->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
+    FXE_TRY(cudaStreamSynchronize(e->stream), "GA step");
+    fxe::GaJob J;
+    FXE_TRY(cudaMemcpy(&J, e->d_all + slot, sizeof(J), cudaMemcpyDeviceToHost), "GA state");
+    const int P = s.job.population, ng = s.ctx->S.n_genes;
+    if (genes) FXE_TRY(cudaMemcpy(genes, J.pop, sizeof(int32_t) * P * ng, cudaMemcpyDeviceToHost), "GA population");
+    if (energies) FXE_TRY(cudaMemcpy(energies, J.pop_e, sizeof(double) * P, cudaMemcpyDeviceToHost), "GA population");
+    return FXE_OK;
+}

@@ -142,6 +142,23 @@ __device__ __forceinline__ void copy_job(Job* dst, const Job* src, int lane) {
     __syncwarp();
 }
 
+// One job's GA state in HBM. The population is double-buffered: selection writes the next
+// population into pop_next / pop_e_next and swaps the pointers here, in device memory, so a
+// captured generation can be replayed without the host.
+struct GaJob {
+    int32_t* pop;            // [P * ng] current population, sorted by energy
+    int32_t* pop_next;
+    double* pop_e;           // [P]
+    double* pop_e_next;
+    int32_t* child;          // [P * ng] chromosomes evaluated this generation
+    const fxe_cf* child_cf;  // [P] their records
+    double* ens;             // [P * (G + 1)] energies of every evaluated chromosome, for statmech
+    int* gen;                // generation counter (device), advanced by selection
+    uint64_t seed;
+    double cross_rate, mut_rate;
+    int P, ng, G;
+};
+
 // one block's share of the ensemble reduction: running max of the log-weights and the sums
 // of exp(lw - m), E exp(lw - m), E^2 exp(lw - m)
 struct LsePart {

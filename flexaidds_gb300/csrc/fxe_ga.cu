@@ -1,0 +1,211 @@
+// fxe_ga.cu — the GA generation on the device: breeding (roulette selection, crossover,
+// mutation on the int32 genes) and replacement, one block per job, for populations kept in HBM.
+//
+// Semantics follow the reference's operators:
+//   * LINEAR fitness: after sorting by energy, rank i (0 = lowest energy) gets fitness P - i
+//     (LIB/gaboom.cpp:1627-1635);
+//   * roulette_wheel: r = u * sum(fitness), the first index whose running fitness sum exceeds r
+//     (LIB/gaboom.cpp:1158-1186);
+//   * crossover: the reference's two-point bit crossover over the genes' 32-bit strings, with
+//     its choice of genes and bit points (LIB/gaboom.cpp:2517-2614, intragenes = 1);
+//   * mutate: every bit of every gene flipped with probability mut_rate (LIB/gaboom.cpp:2620-2641);
+//   * BOOM replacement: parents and children merged, sorted by energy, the best P kept
+//     (LIB/gaboom.cpp:1023-1033).
+// The reference draws from a random_device-seeded generator, so its trajectories cannot be
+// replayed; here every draw is a counter-based hash of (job seed, generation, child, draw), so a
+// job's trajectory depends on its seed alone — the same whether it runs alone or among others.
+// Duplicate rejection (hash_genes) is not applied.
+#include <cstdint>
+
+#include "fxe_common.cuh"
+
+namespace fxe {
+
+// SplitMix64 finaliser (Steele, Lea and Flood, OOPSLA 2014) of a 64-bit counter.
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Uniform double in [0, 1) for draw `k` of stream `s` of a job: 53 random bits.
+__device__ __forceinline__ double uniform(uint64_t seed, uint64_t s, uint64_t k) {
+    return (double)(mix64(seed ^ mix64(s * 0x100000001B3ull + k)) >> 11) * 0x1.0p-53;
+}
+
+constexpr int kGaThreads = 256;
+constexpr int kGaMaxSort = 4096;   // 2P entries sorted in shared memory: P <= 2048
+
+// Ascending bitonic sort of (key, index) pairs in shared memory, n a power of two.
+__device__ void bitonic_sort(double* key, int* idx, int n) {
+    for (int k = 2; k <= n; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const bool up = (i & k) == 0;
+                    const double a = key[i], b = key[l];
+                    const int ia = idx[i], ib = idx[l];
+                    // order by key, then by index, so equal energies keep a fixed order
+                    const bool gt = a > b || (a == b && ia > ib);
+                    if (gt == up) {
+                        key[i] = b; key[l] = a;
+                        idx[i] = ib; idx[l] = ia;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Roulette over LINEAR fitness: ranks 0..P-1 with fitness P - i; the first rank whose running
+// sum exceeds r = u * P (P + 1) / 2. The running sum of ranks 0..i is (i + 1) P - i (i + 1) / 2.
+__device__ __forceinline__ int roulette_linear(int P, double u) {
+    const double tot = (double)P * (double)(P + 1) * 0.5;
+    const double r = u * tot;
+    int lo = 0, hi = P - 1;   // smallest i with cum(i) > r
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const double cum = (double)(mid + 1) * P - 0.5 * (double)mid * (double)(mid + 1);
+        if (cum > r) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+// Uniform initial genes, [0, 2^31) like the reference's RandomInt over MAX_RANDOM_VALUE.
+__global__ void ga_init_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
+    const GaJob& J = all[run[blockIdx.x]];
+    const int n = J.P * J.ng;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        J.child[i] = (int32_t)(mix64(J.seed ^ mix64(0xFFFFFFFFull * 977 + (uint64_t)i)) >> 33);
+}
+
+// Children of the running generation: pairs (2k, 2k+1) from two roulette draws, crossed with
+// probability cross_rate and mutated bit by bit.
+__global__ void __launch_bounds__(kGaThreads) ga_breed_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
+    const GaJob& J = all[run[blockIdx.x]];
+    const int P = J.P, ng = J.ng;
+    const int g = *J.gen;
+    const uint64_t sb = (uint64_t)(g + 1) << 32;   // streams of generation g + 1
+    for (int k = threadIdx.x; 2 * k < P; k += blockDim.x) {
+        const uint64_t st = sb + (uint64_t)k;
+        uint64_t d = 0;
+        const int a = roulette_linear(P, uniform(J.seed, st, d++));
+        const int b = roulette_linear(P, uniform(J.seed, st, d++));
+        int32_t* john = J.child + (size_t)(2 * k) * ng;
+        int32_t* mary = 2 * k + 1 < P ? J.child + (size_t)(2 * k + 1) * ng : nullptr;
+        int32_t tmp[64];
+        int32_t* m = mary ? mary : tmp;
+        for (int q = 0; q < ng; ++q) {
+            john[q] = J.pop[(size_t)a * ng + q];
+            m[q] = J.pop[(size_t)b * ng + q];
+        }
+        if (uniform(J.seed, st, d++) < J.cross_rate) {
+            // crossover with intragenes (LIB/gaboom.cpp:2527-2551, 2580-2598)
+            int gen_a = (int)(uniform(J.seed, st, d++) * (double)ng);
+            int gen_b = (int)(uniform(J.seed, st, d++) * (double)ng);
+            if (gen_a >= ng) gen_a = ng - 1;
+            if (gen_b >= ng) gen_b = ng - 1;
+            int pnt_a = (int)(uniform(J.seed, st, d++) * 32.0);
+            int pnt_b = (int)(uniform(J.seed, st, d++) * 32.0);
+            if (gen_a > gen_b) {
+                const int tg = gen_a, tp = pnt_a;
+                gen_a = gen_b; pnt_a = pnt_b;
+                gen_b = tg; pnt_b = tp;
+            }
+            if (gen_a == gen_b && pnt_a < pnt_b) {
+                const int tp = pnt_b;
+                pnt_b = pnt_a;
+                pnt_a = tp;
+            }
+            for (int j = gen_a; j <= gen_b; ++j) {
+                const int np = j == gen_a ? pnt_a : 32;
+                // the reference's mask: 1, then np times optr |= optr << 1
+                const uint32_t optr = np >= 31 ? 0xFFFFFFFFu : ((2u << np) - 1u);
+                const uint32_t uj = (uint32_t)john[j], um = (uint32_t)m[j];
+                john[j] = (int32_t)((uj & ~optr) | (um & optr));
+                m[j] = (int32_t)((uj & optr) | (um & ~optr));
+            }
+            if (pnt_b > 0) {
+                const int np = pnt_b - 1;
+                const uint32_t optr = np >= 31 ? 0xFFFFFFFFu : ((2u << np) - 1u);
+                const uint32_t uj = (uint32_t)john[gen_b], um = (uint32_t)m[gen_b];
+                john[gen_b] = (int32_t)((uj & ~optr) | (um & optr));
+                m[gen_b] = (int32_t)((uj & optr) | (um & ~optr));
+            }
+        }
+        // mutate both children (LIB/gaboom.cpp:2620-2641)
+        for (int c = 0; c < 2; ++c) {
+            int32_t* ch = c == 0 ? john : m;
+            for (int q = 0; q < ng; ++q) {
+                uint32_t optr = 0u;
+                for (int bit = 0; bit < 32; ++bit)
+                    if (uniform(J.seed, st, d++) < J.mut_rate) optr |= 1u << bit;
+                ch[q] ^= (int32_t)optr;
+            }
+        }
+    }
+}
+
+// Selection. kInitial: the evaluated initial population becomes generation 0. Otherwise BOOM
+// replacement: parents and children merged and sorted by energy, the best P kept; the
+// children's energies join the ensemble and the generation counter advances.
+template <bool kInitial>
+__global__ void __launch_bounds__(kGaThreads) ga_select_kernel(GaJob* __restrict__ all, const int* __restrict__ run) {
+    __shared__ double key[kGaMaxSort];
+    __shared__ int idx[kGaMaxSort];
+    GaJob& J = all[run[blockIdx.x]];
+    const int P = J.P, ng = J.ng;
+    const int g = *J.gen;
+    int32_t* const pop = J.pop;
+    int32_t* const nxt = J.pop_next;
+    double* const pe = J.pop_e;
+    double* const nxt_e = J.pop_e_next;
+    const int m = kInitial ? P : 2 * P;   // entries [0, P) parents, [P, 2P) children
+    int n = 1;
+    while (n < m) n <<= 1;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double e = INFINITY;
+        if (i < m) {
+            e = kInitial ? J.child_cf[i].evalue : (i < P ? pe[i] : J.child_cf[i - P].evalue);
+            if (e != e) e = INFINITY;   // a NaN energy sorts last
+        }
+        key[i] = e;
+        idx[i] = i;
+    }
+    const int slot = kInitial ? 0 : g + 1;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) J.ens[(size_t)slot * P + i] = J.child_cf[i].evalue;
+    __syncthreads();
+    bitonic_sort(key, idx, n);
+    for (int t = threadIdx.x; t < P * ng; t += blockDim.x) {
+        const int r = t / ng, q = t - r * ng;
+        const int src = idx[r];
+        nxt[t] = kInitial ? J.child[(size_t)src * ng + q]
+                          : (src < P ? pop[(size_t)src * ng + q] : J.child[(size_t)(src - P) * ng + q]);
+    }
+    for (int r = threadIdx.x; r < P; r += blockDim.x) nxt_e[r] = key[r];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        J.pop = nxt;
+        J.pop_next = pop;
+        J.pop_e = nxt_e;
+        J.pop_e_next = pe;
+        if (!kInitial) *J.gen = g + 1;
+    }
+}
+
+void launch_ga_init(const GaJob* all, const int* run, int n_jobs, cudaStream_t st) {
+    ga_init_kernel<<<n_jobs, kGaThreads, 0, st>>>(all, run);
+}
+void launch_ga_breed(const GaJob* all, const int* run, int n_jobs, cudaStream_t st) {
+    ga_breed_kernel<<<n_jobs, kGaThreads, 0, st>>>(all, run);
+}
+void launch_ga_select(GaJob* all, const int* run, int n_jobs, bool initial, cudaStream_t st) {
+    if (initial) ga_select_kernel<true><<<n_jobs, kGaThreads, 0, st>>>(all, run);
+    else ga_select_kernel<false><<<n_jobs, kGaThreads, 0, st>>>(all, run);
+}
+
+}  // namespace fxe

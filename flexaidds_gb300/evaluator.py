@@ -57,6 +57,16 @@ def load_library():
         lib.fxe_batch_take_launches.argtypes = [vp, C.POINTER(C.c_int64)]
         lib.fxe_batch_destroy.argtypes = [vp]
         lib.fxe_batch_destroy.restype = None
+        lib.fxe_ga_create.argtypes = [C.c_int32, C.c_int32, C.POINTER(vp)]
+        lib.fxe_ga_job_bytes.argtypes = [vp, C.POINTER(C.c_int64)]
+        lib.fxe_ga_admit.argtypes = [vp, vp, C.POINTER(C.c_int32)]
+        lib.fxe_ga_step.argtypes = [vp]
+        lib.fxe_ga_finished.argtypes = [vp, _i, C.c_int32, C.POINTER(C.c_int32)]
+        lib.fxe_ga_collect.argtypes = [vp, C.c_int32, C.c_double, _i, C.POINTER(C.c_double), vp]
+        lib.fxe_ga_population.argtypes = [vp, C.c_int32, _i, _d]
+        lib.fxe_ga_take_launches.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        lib.fxe_ga_destroy.argtypes = [vp]
+        lib.fxe_ga_destroy.restype = None
         lib.fxe_context_destroy.argtypes = [vp]
         lib.fxe_context_destroy.restype = None
         lib.fxe_last_error.restype = C.c_char_p
@@ -196,6 +206,80 @@ class Batch:
     def close(self):
         if getattr(self, "handle", None):
             self.lib.fxe_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GAJob(C.Structure):
+    _fields_ = [("ctx", C.c_void_p), ("population", C.c_int32), ("generations", C.c_int32),
+                ("cross_rate", C.c_double), ("mut_rate", C.c_double), ("seed", C.c_uint64)]
+
+
+class GAEngine:
+    """Docking jobs' genetic algorithms on the device (fxe_ga_*): admit, step, collect."""
+
+    def __init__(self, max_jobs: int, precision: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        _check(self.lib.fxe_ga_create(int(max_jobs), int(precision), C.byref(h)))
+        self.handle = h
+        self.jobs = {}
+
+    @staticmethod
+    def job(ev: GPUEvaluator, population: int, generations: int, seed: int,
+            cross_rate: float = 0.9, mut_rate: float = 0.01) -> GAJob:
+        return GAJob(ev.handle.value, int(population), int(generations), float(cross_rate),
+                     float(mut_rate), int(seed) & 0xFFFFFFFFFFFFFFFF)
+
+    def job_bytes(self, job: GAJob) -> int:
+        b = C.c_int64(0)
+        _check(self.lib.fxe_ga_job_bytes(C.byref(job), C.byref(b)))
+        return int(b.value)
+
+    def admit(self, job: GAJob, ev: GPUEvaluator) -> int:
+        slot = C.c_int32(-1)
+        _check(self.lib.fxe_ga_admit(self.handle, C.byref(job), C.byref(slot)))
+        self.jobs[slot.value] = ev
+        return slot.value
+
+    def step(self):
+        _check(self.lib.fxe_ga_step(self.handle))
+
+    def finished(self) -> list:
+        cap = max(1, len(self.jobs))
+        out = np.zeros(cap, np.int32)
+        n = C.c_int32(0)
+        _check(self.lib.fxe_ga_finished(self.handle, ptr(out, _i), cap, C.byref(n)))
+        return out[:n.value].tolist()
+
+    def read_population(self, slot: int, population: int):
+        ev = self.jobs[slot]
+        g = np.zeros((population, ev.desc.n_genes), np.int32)
+        e = np.zeros(population, np.float64)
+        _check(self.lib.fxe_ga_population(self.handle, slot, ptr(g, _i), ptr(e, _d)))
+        return g, e
+
+    def collect(self, slot: int, temperature: float = 300.0):
+        ev = self.jobs.pop(slot)
+        g = np.zeros(ev.desc.n_genes, np.int32)
+        be = C.c_double(0.0)
+        t = Thermo()
+        _check(self.lib.fxe_ga_collect(self.handle, slot, float(temperature), ptr(g, _i), C.byref(be), C.byref(t)))
+        return g, be.value, {k: getattr(t, k) for k, _ in Thermo._fields_}
+
+    def take_launches(self):
+        a, b = C.c_int64(0), C.c_int64(0)
+        _check(self.lib.fxe_ga_take_launches(self.handle, C.byref(a), C.byref(b)))
+        return int(a.value), int(b.value)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.fxe_ga_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

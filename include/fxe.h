@@ -260,6 +260,44 @@ fxe_status fxe_batch_take_launches(fxe_batch* batch, int64_t* launches);
 
 void fxe_batch_destroy(fxe_batch* batch);
 
+/* GA engine: docking jobs (one context each) run their genetic algorithm with the population in
+ * HBM. A generation of every running job is one CUDA graph: breeding (LINEAR fitness, roulette
+ * selection, the reference's bit crossover and mutation, LIB/gaboom.cpp:909-960), one batched
+ * evaluation of all children, and BOOM replacement (parents and children merged, the best P
+ * kept, LIB/gaboom.cpp:1023-1033). The graph is captured again only when the set of running
+ * jobs changes, so jobs are admitted and retired between generations (continuous batching).
+ * Random draws are counter-based hashes of (seed, generation, child, draw): a job's trajectory
+ * depends on its seed only, whatever else runs. Duplicate rejection is not applied. */
+typedef struct fxe_ga fxe_ga;
+typedef struct fxe_ga_job {
+    fxe_context* ctx;        /* the job's system; one running job per context */
+    int32_t population;      /* 2..2048, at most ctx's max_poses */
+    int32_t generations;
+    double cross_rate;       /* probability of crossover per pair of children */
+    double mut_rate;         /* probability of flipping each gene bit */
+    uint64_t seed;
+} fxe_ga_job;
+
+fxe_status fxe_ga_create(int32_t max_jobs, int32_t precision, fxe_ga** out);
+/* Device bytes a job's GA state takes (populations, children, ensemble), for admission control. */
+fxe_status fxe_ga_job_bytes(const fxe_ga_job* job, int64_t* bytes);
+/* Draws, evaluates and sorts the job's initial population (waits for it); *slot names the job. */
+fxe_status fxe_ga_admit(fxe_ga* ga, const fxe_ga_job* job, int32_t* slot);
+/* One generation of every running job (queued; not waited for). */
+fxe_status fxe_ga_step(fxe_ga* ga);
+/* Waits for the queued generations and lists the slots whose jobs have finished. */
+fxe_status fxe_ga_finished(fxe_ga* ga, int32_t* slots, int32_t cap, int32_t* n);
+/* A finished job's best chromosome and energy, and the FP64 thermodynamics at `temperature` of
+ * every chromosome it evaluated (the ensemble of StatMechEngine, LIB/statmech.cpp:73-174);
+ * frees the slot. */
+fxe_status fxe_ga_collect(fxe_ga* ga, int32_t slot, double temperature, int32_t* best_genes,
+                          double* best_energy, fxe_thermo* thermo);
+/* The current population of a job (sorted by energy): P * n_genes genes and P energies. */
+fxe_status fxe_ga_population(fxe_ga* ga, int32_t slot, int32_t* genes, double* energies);
+/* Kernels launched and graphs replayed since the previous call (resets both). */
+fxe_status fxe_ga_take_launches(fxe_ga* ga, int64_t* launches, int64_t* graphs);
+void fxe_ga_destroy(fxe_ga* ga);
+
 /* Message describing the last error on the calling thread ("" if none). */
 const char* fxe_last_error(void);
 

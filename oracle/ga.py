@@ -1,0 +1,113 @@
+"""Restatement of one GA generation for checking the device GA engine.
+
+TEST INFRASTRUCTURE ONLY: the checker for flexaidds_gb300/csrc/fxe_ga.cu, used by tests/.
+
+Operators as the reference defines them — LINEAR fitness (LIB/gaboom.cpp:1627-1635), roulette
+selection (:1158-1186), the reproduce loop's crossover-then-mutate of each pair (:918-960), the
+bit crossover with intragenes (:2517-2614) and bit mutation (:2620-2641), BOOM replacement
+(:1023-1033) — driven by the counter-based draws the device uses (the reference's own draws come
+from a random_device-seeded generator and cannot be replayed).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+M64 = (1 << 64) - 1
+
+
+def mix64(z: int) -> int:
+    """SplitMix64 finaliser (Steele, Lea and Flood, OOPSLA 2014)."""
+    z = (z + 0x9E3779B97F4A7C15) & M64
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M64
+    return z ^ (z >> 31)
+
+
+def uniform(seed: int, stream: int, k: int) -> float:
+    return (mix64(seed ^ mix64((stream * 0x100000001B3 + k) & M64)) >> 11) * 2.0 ** -53
+
+
+def initial_genes(seed: int, P: int, ng: int) -> np.ndarray:
+    g = [mix64(seed ^ mix64((0xFFFFFFFF * 977 + i) & M64)) >> 33 for i in range(P * ng)]
+    return np.asarray(g, np.int64).astype(np.int32).reshape(P, ng)
+
+
+def roulette_linear(P: int, u: float) -> int:
+    tot = float(P) * float(P + 1) * 0.5
+    r = u * tot
+    lo, hi = 0, P - 1
+    while lo < hi:
+        mid = (lo + hi) >> 1
+        cum = float(mid + 1) * P - 0.5 * float(mid) * float(mid + 1)
+        if cum > r:
+            hi = mid
+        else:
+            lo = mid + 1
+    return lo
+
+
+def _mask(np_: int) -> int:
+    return 0xFFFFFFFF if np_ >= 31 else (2 << np_) - 1
+
+
+def breed(pop: np.ndarray, gen: int, seed: int, cross_rate: float, mut_rate: float) -> np.ndarray:
+    """Children of generation gen + 1 from the sorted population `pop` (P, ng) int32."""
+    P, ng = pop.shape
+    u32 = pop.astype(np.int64) & 0xFFFFFFFF
+    child = np.zeros((P, ng), np.int64)
+    sb = (gen + 1) << 32
+    for k in range((P + 1) // 2):
+        st = sb + k
+        d = 0
+
+        def draw():
+            nonlocal d
+            v = uniform(seed, st, d)
+            d += 1
+            return v
+
+        a = roulette_linear(P, draw())
+        b = roulette_linear(P, draw())
+        john = [int(x) for x in u32[a]]
+        mary = [int(x) for x in u32[b]]
+        if draw() < cross_rate:
+            gen_a = min(int(draw() * ng), ng - 1)
+            gen_b = min(int(draw() * ng), ng - 1)
+            pnt_a = int(draw() * 32.0)
+            pnt_b = int(draw() * 32.0)
+            if gen_a > gen_b:
+                gen_a, gen_b, pnt_a, pnt_b = gen_b, gen_a, pnt_b, pnt_a
+            if gen_a == gen_b and pnt_a < pnt_b:
+                pnt_a, pnt_b = pnt_b, pnt_a
+            for j in range(gen_a, gen_b + 1):
+                m = _mask(pnt_a if j == gen_a else 32)
+                uj, um = john[j], mary[j]
+                john[j] = (uj & ~m & 0xFFFFFFFF) | (um & m)
+                mary[j] = (uj & m) | (um & ~m & 0xFFFFFFFF)
+            if pnt_b > 0:
+                m = _mask(pnt_b - 1)
+                uj, um = john[gen_b], mary[gen_b]
+                john[gen_b] = (uj & ~m & 0xFFFFFFFF) | (um & m)
+                mary[gen_b] = (uj & m) | (um & ~m & 0xFFFFFFFF)
+        for ch in (john, mary):
+            for q in range(ng):
+                m = 0
+                for bit in range(32):
+                    if draw() < mut_rate:
+                        m |= 1 << bit
+                ch[q] ^= m
+        child[2 * k] = john
+        if 2 * k + 1 < P:
+            child[2 * k + 1] = mary
+    return child.astype(np.uint32).astype(np.int32)
+
+
+def boom(pop: np.ndarray, pop_e: np.ndarray, child: np.ndarray, child_e: np.ndarray):
+    """Parents and children merged, sorted by energy (then by position), as many kept as there
+    are children (the initial population: no parents)."""
+    keep = child.shape[0]
+    e = np.concatenate([pop_e, child_e]).astype(np.float64)
+    e = np.where(np.isnan(e), np.inf, e)
+    order = np.lexsort((np.arange(e.shape[0]), e))[:keep]
+    genes = np.concatenate([pop, child])[order]
+    return genes, e[order]

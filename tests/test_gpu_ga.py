@@ -1,0 +1,95 @@
+"""The device GA engine: a generation equals the restated operators on the same draws, a job's
+result is the same alone and among other jobs, and the best energy never rises."""
+import numpy as np
+import pytest
+
+from flexaidds_gb300 import evaluator, prepare, synth, system
+from oracle import ga as ref_ga
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def systems():
+    base = system.make_inputs(1200, 7.0, 14, 4, seed=91)
+    out = [prepare.prepare(base)]
+    for k, (n, t) in enumerate([(20, 6), (10, 2)]):
+        lig = synth.random_ligand(n, t, seed=300 + k)
+        out.append(prepare.prepare(system.SystemInputs(receptor=base.receptor, ligand=lig,
+                                                       grid_xyz=base.grid_xyz, emat=base.emat)))
+    return out
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_generation_matches_restated_operators(systems, prec):
+    d = systems[0]
+    P, seed, pc, pm = 96, 12345, 0.9, 0.02
+    ev = evaluator.GPUEvaluator(d, max_poses=P, precision=prec)
+    check = evaluator.GPUEvaluator(d, max_poses=P, precision=prec)
+    eng = evaluator.GAEngine(max_jobs=2, precision=prec)
+    slot = eng.admit(eng.job(ev, P, 3, seed, pc, pm), ev)
+    # generation 0: the uniform draws, evaluated and sorted
+    init = ref_ga.initial_genes(seed, P, d.n_genes)
+    e0 = check.eval_genes(init)["evalue"]
+    want_g, want_e = ref_ga.boom(init[:0], e0[:0], init, e0)
+    pop, pe = eng.read_population(slot, P)
+    np.testing.assert_array_equal(pop, want_g)
+    np.testing.assert_array_equal(pe, want_e)
+    for gen in range(3):
+        child = ref_ga.breed(pop, gen, seed, pc, pm)
+        ce = check.eval_genes(child)["evalue"]
+        want_g, want_e = ref_ga.boom(pop, pe, child, ce)
+        eng.step()
+        pop, pe = eng.read_population(slot, P)
+        np.testing.assert_array_equal(pop, want_g)
+        np.testing.assert_array_equal(pe, want_e)
+    assert eng.finished() == [slot]
+
+
+def test_job_alone_equals_job_in_a_mix(systems):
+    jobs = [(0, 128, 6, 7), (1, 200, 4, 8), (2, 64, 9, 9)]
+
+    def run(which, stagger):
+        eng = evaluator.GAEngine(max_jobs=4)
+        evs = {k: evaluator.GPUEvaluator(systems[k], max_poses=256) for k, *_ in jobs}
+        slots, results = {}, {}
+        pending = [j for j in jobs if j[0] in which]
+        step = 0
+        while pending or eng.jobs:
+            # admit one waiting job every `stagger` generations (continuous batching)
+            if pending and step % stagger == 0:
+                k, P, G, seed = pending.pop(0)
+                slots[eng.admit(eng.job(evs[k], P, G, seed), evs[k])] = k
+            eng.step()
+            step += 1
+            for s in eng.finished():
+                results[slots[s]] = eng.collect(s, 300.0)
+        return results
+
+    mixed = run({0, 1, 2}, 2)
+    for k in (0, 1, 2):
+        alone = run({k}, 1)[k]
+        g, e, th = mixed[k]
+        np.testing.assert_array_equal(g, alone[0])
+        assert e == alone[1]
+        for key in th:
+            assert th[key] == alone[2][key] or abs(th[key] - alone[2][key]) <= 1e-12 * abs(alone[2][key])
+
+
+def test_best_energy_never_rises(systems):
+    d = systems[1]
+    P = 256
+    ev = evaluator.GPUEvaluator(d, max_poses=P)
+    eng = evaluator.GAEngine(max_jobs=1)
+    slot = eng.admit(eng.job(ev, P, 12, 4242), ev)
+    best = [eng.read_population(slot, P)[1][0]]
+    for _ in range(12):
+        eng.step()
+        best.append(eng.read_population(slot, P)[1][0])
+    assert all(b <= a for a, b in zip(best, best[1:]))
+    assert best[-1] < best[0]
+    g, e, th = eng.collect(slot, 300.0)
+    assert e == best[-1]
+    assert np.isfinite(th["free_energy"])
+    launches, graphs = eng.take_launches()
+    assert graphs == 12 and launches == 5 + 12 * 5
