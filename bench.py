@@ -326,6 +326,13 @@ def run_gpu(args):
     sm_best = min(sm_ms)
 
     batched = run_batched(args, prec, flush, stream) if args.batched else None
+    served = None
+    if args.served:
+        from flexaidds_gb300.system import SystemInputs  # noqa: F401
+        w, b = WORKLOAD, BATCH
+        served = run_served(prec, {
+            "6000": system.make_inputs(w["n_rec"], w["cleft"], 12, 3, seed=w["seed"], edge=w["edge"]),
+            "4000": system.make_inputs(b["n_rec"], b["cleft"], 12, 3, seed=b["seed"], edge=b["edge"])})
 
     if rank != 0:
         ranks.close()
@@ -375,6 +382,7 @@ def run_gpu(args):
                      "roofline": {"bound": "hbm", "achieved": sm_gbs, "peak": hbm, "unit": "GB/s",
                                   "frac": (sm_gbs / hbm) if hbm else None, "traffic": None}},
         "batched": batched,
+        "served": served,
     }
     print(json.dumps(out), flush=True)
     ranks.close()
@@ -466,6 +474,50 @@ def run_batched(args, prec, flush, stream):
 
 
 # ---------------------------------------------------------------------------------------------
+# served: Poisson arrivals of docking jobs, continuous batching on the device GA engine
+# ---------------------------------------------------------------------------------------------
+
+SERVE = dict(rates=(10.0, 50.0, 200.0), jobs=48, population=500, generations=20, budget=150e9,
+             atoms_median=30, atoms=(10, 70), torsions=(0, 15), seed=77)
+SERVE_NAME = ("served: Poisson arrivals at 10, 50 and 200 jobs/s, 48 jobs per rate, receptors from a "
+              "cache of two (6000 and 4000 atoms), ligands lognormal median 30 heavy atoms (10-70) "
+              "with U[0,15] torsions, population 500 for 20 generations, 150 GB admission budget")
+
+
+def run_served(prec, receptors):
+    from flexaidds_gb300 import serve
+    from flexaidds_gb300.system import SystemInputs
+    s = SERVE
+    rng = np.random.default_rng(s["seed"])
+    reqs = []
+    keys = list(receptors)
+    for k in range(s["jobs"]):
+        key = keys[k % len(keys)]
+        base = receptors[key]
+        n = int(np.clip(round(rng.lognormal(np.log(s["atoms_median"]), 0.4)), *s["atoms"]))
+        t = int(rng.integers(s["torsions"][0], s["torsions"][1] + 1))
+        lig = synth.random_ligand(n, t, seed=s["seed"] * 1000 + k)
+        d = prepare.prepare(SystemInputs(receptor=base.receptor, ligand=lig, grid_xyz=base.grid_xyz, emat=base.emat))
+        reqs.append(serve.JobRequest(0.0, key, d, s["population"], s["generations"], seed=s["seed"] * 7919 + k))
+    p = 0 if prec == "reference" else 1
+    out = {"workload": SERVE_NAME, "precision": prec, "rates": []}
+    for rate in s["rates"]:
+        arr = serve.poisson_arrivals(len(reqs), rate, seed=int(rate))
+        for r, t in zip(reqs, arr):
+            r.arrival = float(t)
+        srv = serve.DockingServer(max_jobs=256, hbm_budget=s["budget"], precision=p)
+        res = srv.run(reqs)
+        launches, graphs = srv.engine.take_launches()
+        srv.close()
+        summ = serve.latency_summary(res)
+        poses = len(res) * s["population"] * (s["generations"] + 1)
+        summ.update({"arrival_rate": rate, "poses_per_s": poses / summ["makespan_s"],
+                     "graph_launches": graphs, "kernel_launches": launches})
+        out["rates"].append(summ)
+    return out
+
+
+# ---------------------------------------------------------------------------------------------
 # reference arm: the reference's algorithm on the host cores
 # ---------------------------------------------------------------------------------------------
 
@@ -539,6 +591,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["reference", "fast"], default="reference")
+    ap.add_argument("--served", type=int, default=1,
+                    help="also serve Poisson streams of docking jobs and report latency percentiles")
     ap.add_argument("--batched", type=int, default=1,
                     help="also time the batched many-ligand workload against one launch per job")
     args = ap.parse_args()

@@ -256,9 +256,25 @@ def cleft_ic(grid_xyz, ori):
     return np.stack([dis, ang, dih], axis=1).astype(np.float32)
 
 
+_RECEPTOR_MEMO: list = []   # (receptor xyz, grid xyz, centre, cleft ICs) of recent receptors
+
+
+def _receptor_setup(rec_xyz, grid_xyz):
+    """calc_center and the cleft ICs of a receptor, remembered for the last few receptors (they
+    depend on the receptor and its grid only, not on the ligand)."""
+    for k, (x, g, c, ic) in enumerate(_RECEPTOR_MEMO):
+        if x is rec_xyz and g is grid_xyz:
+            return c, ic
+    c = calc_center(rec_xyz)
+    ic = cleft_ic(grid_xyz, c[0])
+    _RECEPTOR_MEMO.insert(0, (rec_xyz, grid_xyz, c, ic))
+    del _RECEPTOR_MEMO[8:]
+    return c, ic
+
+
 def prepare(inp: SystemInputs) -> Descriptor:
     rec, lig = inp.receptor, inp.ligand
-    ori, gmin, gmax, mw = calc_center(rec.xyz)
+    (ori, gmin, gmax, mw), grid_ic = _receptor_setup(rec.xyz, inp.grid_xyz)
     n = lig.xyz.shape[0]
     adj = [[] for _ in range(n)]
     for a, b in lig.bonds:
@@ -272,7 +288,7 @@ def prepare(inp: SystemInputs) -> Descriptor:
     ic2 = buildic(xyz2, lrec, ori)
     grid = np.zeros((inp.grid_xyz.shape[0] + 1, 3), np.float32)
     grid[0] = ic1[lig.gpa[0]]
-    grid[1:] = cleft_ic(inp.grid_xyz, ori)
+    grid[1:] = grid_ic
     n_grid = grid.shape[0]
     # genes: grid index, three rotations, flexible bonds (LIB/add2_optimiz_vec.cpp)
     typ = [-1, 1, 2, 2] + [2] * len(lig.flex)
