@@ -5,6 +5,7 @@
 // CUDA stream. Batches larger than max_poses are scored in chunks.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -65,6 +66,9 @@ struct fxe_context {
     std::vector<void*> allocs;
     std::shared_ptr<DevBlock> receptor = std::make_shared<DevBlock>();
     int rec_type_max = 0;             // largest receptor atom type (checked against each matrix)
+    // host copies of the gene limits and genetoic tables (decoding snapshots on the host)
+    std::vector<double> h_gmin, h_gmax, h_gdel, h_dtab;
+    std::vector<int> h_doff;
     const void* rec_key = nullptr;    // identity of the receptor block (contexts sharing it)
     int32_t* d_genes = nullptr;
     double* d_icin = nullptr;
@@ -277,6 +281,11 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
             doff[g + 1] = (int)dtab.size();
         }
         if (dtab.empty()) dtab.push_back(1.0);
+        ctx->h_gmin.assign(lig->gene_min, lig->gene_min + ng);
+        ctx->h_gmax.assign(lig->gene_max, lig->gene_max + ng);
+        ctx->h_gdel.assign(lig->gene_del, lig->gene_del + ng);
+        ctx->h_dtab = dtab;
+        ctx->h_doff = doff;
         FXE_TRY(ctx->upload(&S.gene_type, lig->gene_type, ng), "gene upload");
         FXE_TRY(ctx->upload(&S.gene_atom, lig->gene_atom, ng), "gene upload");
         FXE_TRY(ctx->upload(&S.gene_min, lig->gene_min, ng), "gene upload");
@@ -928,7 +937,7 @@ extern "C" fxe_status fxe_ga_job_bytes(const fxe_ga_job* job, int64_t* bytes) {
     g_err.clear();
     if (!job || !job->ctx || !bytes) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
     const int64_t P = job->population, ng = job->ctx->S.n_genes, G = job->generations;
-    *bytes = P * ng * 4 * 3 + P * 8 * 2 + P * (int64_t)sizeof(fxe_cf) + P * (G + 1) * 8 + 16;
+    *bytes = P * ng * 4 * 3 + P * 8 * 2 + P * (int64_t)sizeof(fxe_cf) + G * P * (ng * 4 + 8) + 16;
     return FXE_OK;
 }
 
@@ -964,7 +973,9 @@ extern "C" fxe_status fxe_ga_admit(fxe_ga* e, const fxe_ga_job* job, int32_t* sl
         FXE_TRY(get(sizeof(double) * P, &q), "GA population"); J.pop_e_next = (double*)q;
         FXE_TRY(get(sizeof(int32_t) * P * ng, &q), "GA children"); J.child = (int32_t*)q;
         FXE_TRY(get(sizeof(fxe_cf) * P, &q), "GA children"); J.child_cf = (const fxe_cf*)q;
-        FXE_TRY(get(sizeof(double) * P * ((size_t)job->generations + 1), &q), "GA ensemble"); J.ens = (double*)q;
+        const size_t G = (size_t)job->generations > 0 ? (size_t)job->generations : 1;
+        FXE_TRY(get(sizeof(int32_t) * P * ng * G, &q), "GA snapshots"); J.snap = (int32_t*)q;
+        FXE_TRY(get(sizeof(double) * P * G, &q), "GA snapshots"); J.snap_e = (double*)q;
         FXE_TRY(get(sizeof(int), &q), "GA counter"); J.gen = (int*)q;
         FXE_TRY(cudaMemsetAsync(J.gen, 0, sizeof(int), e->stream), "GA counter");
         J.seed = job->seed;
@@ -1083,8 +1094,19 @@ extern "C" fxe_status fxe_ga_finished(fxe_ga* e, int32_t* slots, int32_t cap, in
     return FXE_OK;
 }
 
+namespace {
+// genetoic on the host (LIB/gaboom.cpp:2887-2906): the first running bin total at or above u.
+double host_genetoic(const fxe_context* ctx, int g, int32_t gene) {
+    const double u = gene / (2147483647.0 + 1.0);
+    const double* lo = ctx->h_dtab.data() + ctx->h_doff[g];
+    const double* hi = ctx->h_dtab.data() + ctx->h_doff[g + 1];
+    const double* it = std::lower_bound(lo, hi, u);
+    return ctx->h_gmin[g] + ctx->h_gdel[g] * (double)(it - lo);
+}
+}  // namespace
+
 extern "C" fxe_status fxe_ga_collect(fxe_ga* e, int32_t slot, double temperature, int32_t* best_genes,
-                                     double* best_energy, fxe_thermo* thermo) {
+                                     double* best_energy, fxe_thermo* thermo, int64_t* n_ensemble) {
     g_err.clear();
     if (!e || slot < 0 || slot >= e->max_jobs || !e->slots[slot].used || !e->slots[slot].finished)
         return fail(FXE_ERR_INVALID_ARGS, "slot does not hold a finished job");
@@ -1096,10 +1118,40 @@ extern "C" fxe_status fxe_ga_collect(fxe_ga* e, int32_t slot, double temperature
     const int P = s.job.population, ng = s.ctx->S.n_genes;
     if (best_genes) FXE_TRY(cudaMemcpy(best_genes, J.pop, sizeof(int32_t) * ng, cudaMemcpyDeviceToHost), "GA result");
     if (best_energy) FXE_TRY(cudaMemcpy(best_energy, J.pop_e, sizeof(double), cudaMemcpyDeviceToHost), "GA result");
-    if (thermo) {
-        fxe_status st = thermo_run(J.ens, nullptr, (long)P * (s.job.generations + 1), temperature, thermo, nullptr,
-                                   e->stream);
-        if (st != FXE_OK) return st;
+    if (thermo || n_ensemble) {
+        // the ensemble of the reference's GA (LIB/gaboom.cpp:520-540): every generation's
+        // population, sorted by energy, chromosomes within 0.1 of the last one kept on every
+        // decoded gene dropped (remove_dups, :2728-2747); ties in energy in snapshot order
+        const int G = s.job.generations;
+        const size_t N = (size_t)G * P;
+        std::vector<int32_t> sg(N * ng);
+        std::vector<double> se(N);
+        if (N) {
+            FXE_TRY(cudaMemcpy(sg.data(), J.snap, sizeof(int32_t) * N * ng, cudaMemcpyDeviceToHost), "GA snapshots");
+            FXE_TRY(cudaMemcpy(se.data(), J.snap_e, sizeof(double) * N, cudaMemcpyDeviceToHost), "GA snapshots");
+        }
+        std::vector<size_t> ord(N);
+        for (size_t i = 0; i < N; ++i) ord[i] = i;
+        std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return se[a] < se[b]; });
+        std::vector<double> kept_e, last(ng), cur(ng);
+        bool have = false;
+        for (size_t i : ord) {
+            for (int g = 0; g < ng; ++g) cur[g] = host_genetoic(s.ctx, g, sg[i * ng + g]);
+            int same = 0;
+            if (have)
+                for (int g = 0; g < ng; ++g) same += std::fabs(cur[g] - last[g]) < 0.1;
+            if (!have || same != ng) {
+                kept_e.push_back(se[i]);
+                last = cur;
+                have = true;
+            }
+        }
+        if (n_ensemble) *n_ensemble = (int64_t)kept_e.size();
+        if (thermo) {
+            if (kept_e.empty()) return fail(FXE_ERR_INVALID_ARGS, "the job ran no generation: empty ensemble");
+            fxe_status st = thermo_host(kept_e.data(), nullptr, (int64_t)kept_e.size(), temperature, thermo, nullptr);
+            if (st != FXE_OK) return st;
+        }
     }
     for (void* p : s.mem) cudaFree(p);
     s = GaSlot();

@@ -152,7 +152,8 @@ struct GaJob {
     double* pop_e_next;
     int32_t* child;          // [P * ng] chromosomes evaluated this generation
     const fxe_cf* child_cf;  // [P] their records
-    double* ens;             // [P * (G + 1)] energies of every evaluated chromosome, for statmech
+    int32_t* snap;           // [G * P * ng] the population after each generation (the snapshot
+    double* snap_e;          // [G * P]       the reference feeds to statmech, LIB/gaboom.cpp:494)
     int* gen;                // generation counter (device), advanced by selection
     uint64_t seed;
     double cross_rate, mut_rate;

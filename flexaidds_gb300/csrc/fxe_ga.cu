@@ -151,8 +151,8 @@ __global__ void __launch_bounds__(kGaThreads) ga_breed_kernel(const GaJob* __res
 }
 
 // Selection. kInitial: the evaluated initial population becomes generation 0. Otherwise BOOM
-// replacement: parents and children merged and sorted by energy, the best P kept; the
-// children's energies join the ensemble and the generation counter advances.
+// replacement: parents and children merged and sorted by energy, the best P kept, saved as the
+// generation's snapshot, and the generation counter advanced.
 template <bool kInitial>
 __global__ void __launch_bounds__(kGaThreads) ga_select_kernel(GaJob* __restrict__ all, const int* __restrict__ run) {
     __shared__ double key[kGaMaxSort];
@@ -176,17 +176,23 @@ __global__ void __launch_bounds__(kGaThreads) ga_select_kernel(GaJob* __restrict
         key[i] = e;
         idx[i] = i;
     }
-    const int slot = kInitial ? 0 : g + 1;
-    for (int i = threadIdx.x; i < P; i += blockDim.x) J.ens[(size_t)slot * P + i] = J.child_cf[i].evalue;
     __syncthreads();
     bitonic_sort(key, idx, n);
+    // the new population, and (after a generation) its snapshot for the ensemble
+    int32_t* const sg = kInitial ? nullptr : J.snap + (size_t)g * P * ng;
+    double* const se = kInitial ? nullptr : J.snap_e + (size_t)g * P;
     for (int t = threadIdx.x; t < P * ng; t += blockDim.x) {
         const int r = t / ng, q = t - r * ng;
         const int src = idx[r];
-        nxt[t] = kInitial ? J.child[(size_t)src * ng + q]
-                          : (src < P ? pop[(size_t)src * ng + q] : J.child[(size_t)(src - P) * ng + q]);
+        const int32_t v = kInitial ? J.child[(size_t)src * ng + q]
+                                   : (src < P ? pop[(size_t)src * ng + q] : J.child[(size_t)(src - P) * ng + q]);
+        nxt[t] = v;
+        if (!kInitial) sg[t] = v;
     }
-    for (int r = threadIdx.x; r < P; r += blockDim.x) nxt_e[r] = key[r];
+    for (int r = threadIdx.x; r < P; r += blockDim.x) {
+        nxt_e[r] = key[r];
+        if (!kInitial) se[r] = key[r];
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         J.pop = nxt;

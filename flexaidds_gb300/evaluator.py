@@ -62,7 +62,8 @@ def load_library():
         lib.fxe_ga_admit.argtypes = [vp, vp, C.POINTER(C.c_int32)]
         lib.fxe_ga_step.argtypes = [vp]
         lib.fxe_ga_finished.argtypes = [vp, _i, C.c_int32, C.POINTER(C.c_int32)]
-        lib.fxe_ga_collect.argtypes = [vp, C.c_int32, C.c_double, _i, C.POINTER(C.c_double), vp]
+        lib.fxe_ga_collect.argtypes = [vp, C.c_int32, C.c_double, _i, C.POINTER(C.c_double), vp,
+                                       C.POINTER(C.c_int64)]
         lib.fxe_ga_population.argtypes = [vp, C.c_int32, _i, _d]
         lib.fxe_ga_take_launches.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         lib.fxe_ga_destroy.argtypes = [vp]
@@ -269,8 +270,12 @@ class GAEngine:
         g = np.zeros(ev.desc.n_genes, np.int32)
         be = C.c_double(0.0)
         t = Thermo()
-        _check(self.lib.fxe_ga_collect(self.handle, slot, float(temperature), ptr(g, _i), C.byref(be), C.byref(t)))
-        return g, be.value, {k: getattr(t, k) for k, _ in Thermo._fields_}
+        n = C.c_int64(0)
+        _check(self.lib.fxe_ga_collect(self.handle, slot, float(temperature), ptr(g, _i), C.byref(be), C.byref(t),
+                                       C.byref(n)))
+        th = {k: getattr(t, k) for k, _ in Thermo._fields_}
+        th["n_ensemble"] = int(n.value)
+        return g, be.value, th
 
     def take_launches(self):
         a, b = C.c_int64(0), C.c_int64(0)

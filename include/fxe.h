@@ -288,10 +288,12 @@ fxe_status fxe_ga_step(fxe_ga* ga);
 /* Waits for the queued generations and lists the slots whose jobs have finished. */
 fxe_status fxe_ga_finished(fxe_ga* ga, int32_t* slots, int32_t cap, int32_t* n);
 /* A finished job's best chromosome and energy, and the FP64 thermodynamics at `temperature` of
- * every chromosome it evaluated (the ensemble of StatMechEngine, LIB/statmech.cpp:73-174);
- * frees the slot. */
+ * its ensemble as the reference assembles it (every generation's population, sorted by energy,
+ * near-duplicates within 0.1 on every decoded gene removed, LIB/gaboom.cpp:494,520-540,
+ * 2728-2747; StatMechEngine::compute, LIB/statmech.cpp:73-174), with the ensemble size in
+ * *n_ensemble; frees the slot. */
 fxe_status fxe_ga_collect(fxe_ga* ga, int32_t slot, double temperature, int32_t* best_genes,
-                          double* best_energy, fxe_thermo* thermo);
+                          double* best_energy, fxe_thermo* thermo, int64_t* n_ensemble);
 /* The current population of a job (sorted by energy): P * n_genes genes and P energies. */
 fxe_status fxe_ga_population(fxe_ga* ga, int32_t slot, int32_t* genes, double* energies);
 /* Kernels launched and graphs replayed since the previous call (resets both). */

@@ -111,3 +111,18 @@ def boom(pop: np.ndarray, pop_e: np.ndarray, child: np.ndarray, child_e: np.ndar
     order = np.lexsort((np.arange(e.shape[0]), e))[:keep]
     genes = np.concatenate([pop, child])[order]
     return genes, e[order]
+
+
+def ensemble(snapshots, desc) -> np.ndarray:
+    """The reference's statmech ensemble (LIB/gaboom.cpp:494,520-540,2728-2747): every
+    generation's population, sorted by energy (ties in snapshot order), a chromosome dropped
+    when every decoded gene is within 0.1 of the last one kept. Returns the kept energies."""
+    g = np.concatenate([s[0] for s in snapshots])
+    e = np.concatenate([s[1] for s in snapshots])
+    ic = desc.genes_to_ic(g)
+    kept, last = [], None
+    for i in np.argsort(e, kind="stable"):
+        if last is None or not np.all(np.abs(ic[i] - last) < 0.1):
+            kept.append(e[i])
+            last = ic[i]
+    return np.asarray(kept)

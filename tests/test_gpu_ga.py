@@ -5,6 +5,7 @@ import pytest
 
 from flexaidds_gb300 import evaluator, prepare, synth, system
 from oracle import ga as ref_ga
+from oracle import port
 
 pytestmark = pytest.mark.gpu
 
@@ -35,6 +36,7 @@ def test_generation_matches_restated_operators(systems, prec):
     pop, pe = eng.read_population(slot, P)
     np.testing.assert_array_equal(pop, want_g)
     np.testing.assert_array_equal(pe, want_e)
+    snaps = []
     for gen in range(3):
         child = ref_ga.breed(pop, gen, seed, pc, pm)
         ce = check.eval_genes(child)["evalue"]
@@ -43,7 +45,18 @@ def test_generation_matches_restated_operators(systems, prec):
         pop, pe = eng.read_population(slot, P)
         np.testing.assert_array_equal(pop, want_g)
         np.testing.assert_array_equal(pe, want_e)
+        snaps.append((want_g, want_e))
     assert eng.finished() == [slot]
+    # the statmech ensemble: snapshots sorted, near-duplicates removed
+    kept = ref_ga.ensemble(snaps, d)
+    g, e, th = eng.collect(slot, 300.0)
+    assert th["n_ensemble"] == len(kept)
+    want = port.thermo(kept, None, 300.0)
+    for k in ("log_Z", "free_energy", "mean_energy", "entropy"):
+        assert abs(th[k] - want[k]) <= 1e-9 * max(1.0, abs(want[k])), k
+    # Cv = (<E^2> - <E>^2) / (kT)^2 cancels: its rounding scales with <E^2> / (kT)^2, not with Cv
+    kT = 0.001987206 * 300.0
+    assert abs(th["heat_capacity"] - want["heat_capacity"]) <= 1e-9 * max(1.0, want["mean_energy_sq"] / kT ** 2)
 
 
 def test_job_alone_equals_job_in_a_mix(systems):
