@@ -58,6 +58,11 @@ SYSTEMS = {
     # 900-atom receptor, 7 A cleft, 16-atom ligand, 4 torsions, density curves, other switches
     "curves_900_16": dict(args=(900, 7.0, 16, 4), seed=23, grid=512, pool=4000, scored=100,
                           clashed=20, contacts=8, tweak="curves"),
+    # 600-atom receptor, 6 A cleft, 10-atom ligand; half the grid points lie outside the
+    # receptor's box, so poses leave it: index_protein re-derives its cell grid for them, and
+    # atoms without contacts take the SAS-only path
+    "outside_600_10": dict(args=(600, 6.0, 10, 2), seed=37, grid=256, pool=3000, scored=120,
+                           clashed=20, contacts=8, tweak="outside"),
 }
 
 
@@ -69,6 +74,18 @@ def inputs_for(name):
     rng = np.random.default_rng(cfg["seed"] + 100)
     keep = np.sort(rng.choice(inp.grid_xyz.shape[0], cfg["grid"], replace=False))
     inp.grid_xyz = np.ascontiguousarray(inp.grid_xyz[keep])
+    if cfg["tweak"] == "outside":
+        # replace half of the grid with points 1-6 A beyond the faces of the receptor's box
+        lo, hi = inp.receptor.xyz.min(axis=0), inp.receptor.xyz.max(axis=0)
+        m = inp.grid_xyz.shape[0] // 2
+        pts = rng.uniform(lo, hi, size=(m, 3))
+        axis = rng.integers(0, 3, size=m)
+        side = rng.integers(0, 2, size=m)
+        off = rng.uniform(1.0, 6.0, size=m)
+        for k in range(m):
+            a = axis[k]
+            pts[k, a] = hi[a] + off[k] if side[k] else lo[a] - off[k]
+        inp.grid_xyz = np.ascontiguousarray(np.concatenate([inp.grid_xyz[m:], pts]).astype(np.float32))
     if cfg["tweak"] == "curves":
         density_curves(inp, cfg["seed"] + 200)
         inp.permeability = 0.9
