@@ -320,6 +320,8 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
         FXE_TRY(ctx->alloc(&W.cand_flag, PLC), "workspace");
         FXE_TRY(ctx->alloc(&W.cand_n, PL), "workspace");
         FXE_TRY(ctx->alloc(&W.clash_part, PL), "workspace");
+        FXE_TRY(ctx->alloc(&W.pose_seed, P * fxe::kMaxLig * 3), "workspace");
+        FXE_TRY(ctx->alloc(&W.pose_rec, P * fxe::kMaxLig * fxe::kMaskWords), "workspace");
         FXE_TRY(ctx->alloc(&W.out, P), "workspace");
         FXE_TRY(ctx->alloc(&W.counters, 4), "workspace");
         FXE_TRY(ctx->alloc(&ctx->d_genes, P * (ng > 0 ? ng : 1)), "staging");

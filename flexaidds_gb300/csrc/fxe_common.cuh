@@ -105,6 +105,8 @@ struct DevWork {
     uint8_t* cand_flag;    // [P * n_lig * kMaxCand]
     int* cand_n;           // [P * n_lig]
     double* clash_part;    // [P * n_lig]
+    int* pose_seed;        // [P * kMaxLig * 3] polyhedron seeds left by earlier atoms
+    uint32_t* pose_rec;    // [P * kMaxLig * kMaskWords] ligand partners each processed atom kept
     fxe_cf* out;           // [P]
     int* counters;         // [4]: unused, hull failures, capacity, no-partner faces
 };

@@ -27,7 +27,9 @@ namespace FXE_VARIANT {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr uint8_t kNone = 255;
-constexpr int kVorWarps = 2;   // poses (warps) per block of pose_kernel
+// Poses (warps) per block of pose_kernel: with about 1 KB of shared memory reserved per block,
+// two 13 KB single-precision workspaces per block fit sixteen warps on an SM.
+constexpr int kVorWarps = 2;
 
 // Floating-point type of the polyhedron arithmetic: single precision by default; building
 // with -DFXE_REAL=double gives the same algorithm in double precision (for comparisons).
@@ -1037,12 +1039,19 @@ __device__ double pose_clash_sum(const DevSystem& S, const DevWork& W, int p, in
 // ------------------------------------------------------------------------------------------
 // pose_kernel: calc_region + vcfunction for one pose per warp
 // ------------------------------------------------------------------------------------------
+// Shared memory per warp sets how many poses an SM holds at once. The single-precision kernel is
+// latency-bound and gains from more warps, so it keeps the per-pose seeds and record masks in the
+// workspace (W.pose_seed, W.pose_rec); the double-precision kernel is bound by the FP64 pipe and
+// keeps them in shared memory.
+#define FXE_SEEDS_SHARED (FXE_REFERENCE_FORMULAS)
 struct PoseShared {
     VorShared v;
-    int order[kMaxLig];              // ligand atoms in Calclist order
-    int seed[kMaxLig][3];            // polyhedron seeds (Calc indices), -1 = none
-    uint32_t rec[kMaxLig][kMaskWords];  // ligand partners each processed atom kept
+    uint8_t order[kMaxLig];          // ligand atoms in Calclist order
     uint32_t done[kMaskWords];       // ligand atoms whose contacts are saved
+#if FXE_SEEDS_SHARED
+    int seed[kMaxLig][3];
+    uint32_t rec[kMaxLig][kMaskWords];
+#endif
 };
 
 __device__ __forceinline__ bool bit(const uint32_t* m, int l) { return (m[l >> 5] >> (l & 31)) & 1u; }
@@ -1075,6 +1084,14 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
                                            PoseShared& ps) {
     VorShared& sh = ps.v;
     const int nl = S.n_lig;
+    // polyhedron seeds (Calc indices, -1 = none) and the ligand partners each processed atom kept
+#if FXE_SEEDS_SHARED
+    int (*const seed)[3] = ps.seed;
+    uint32_t (*const rec)[kMaskWords] = ps.rec;
+#else
+    int (*const seed)[3] = reinterpret_cast<int (*)[3]>(W.pose_seed + (size_t)p * kMaxLig * 3);
+    uint32_t (*const rec)[kMaskWords] = reinterpret_cast<uint32_t (*)[kMaskWords]>(W.pose_rec + (size_t)p * kMaxLig * kMaskWords);
+#endif
     const size_t lb = (size_t)p * nl;
     if (W.pose_grid[p].z) {
         finish_failed(W, p, lane, FXE_POSE_CAPACITY, 0.0);
@@ -1087,10 +1104,10 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         return;
     }
     for (int l = lane; l < nl; l += 32) {
-        ps.order[W.lig_rank[lb + l]] = l;
-        ps.seed[l][0] = ps.seed[l][1] = ps.seed[l][2] = -1;
+        ps.order[W.lig_rank[lb + l]] = (uint8_t)l;
+        seed[l][0] = seed[l][1] = seed[l][2] = -1;
 #pragma unroll
-        for (int w = 0; w < kMaskWords; ++w) ps.rec[l][w] = 0;
+        for (int w = 0; w < kMaskWords; ++w) rec[l][w] = 0;
     }
     if (lane < kMaskWords) ps.done[lane] = 0;
     __syncwarp();
@@ -1115,7 +1132,7 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
                 const int j = W.cand_idx[cb + c];
                 if (j >= S.n_rec) {
                     const int l = j - S.n_rec;
-                    ex = bit(ps.done, l) && !bit(ps.rec[l], a);
+                    ex = bit(ps.done, l) && !bit(rec[l], a);
                 }
             }
             excl[w] = __ballot_sync(kFull, ex);
@@ -1133,8 +1150,8 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         load_planes(sh, S, W, p, a, NC, me, rado, excl, lane);
         // seed vertex left by an earlier atom, if all three of its planes are in the list
         int sA = -1, sB = -1, sC = -1;
-        if (ps.seed[a][0] != -1) {
-            const int s0 = ps.seed[a][0], s1 = ps.seed[a][1], s2 = ps.seed[a][2];
+        if (seed[a][0] != -1) {
+            const int s0 = seed[a][0], s1 = seed[a][1], s2 = seed[a][2];
             for (int c0 = 0; c0 < NC; c0 += 32) {
                 const int c = c0 + lane;
                 int j = -2;
@@ -1180,7 +1197,7 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
             uint32_t m = keep_lig[w];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) m |= __shfl_xor_sync(kFull, m, o);
-            if (lane == 0) ps.rec[a][w] = m;
+            if (lane == 0) rec[a][w] = m;
         }
         // save_seeds (LIB/Vcontacts.cpp:601-629): first vertex naming each later atom's plane
         if (lane == 0) {
@@ -1189,14 +1206,14 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
                 const uchar4 q = sh.vp[vi];
                 if (q.z == kNone || q.x >= NC || q.y >= NC || q.z >= NC) continue;
                 const int j0 = sh.cidx[q.x], j1 = sh.cidx[q.y], j2 = sh.cidx[q.z];
-                if (j0 >= S.n_rec && ps.seed[j0 - S.n_rec][0] == -1) {
-                    ps.seed[j0 - S.n_rec][0] = az; ps.seed[j0 - S.n_rec][1] = j1; ps.seed[j0 - S.n_rec][2] = j2;
+                if (j0 >= S.n_rec && seed[j0 - S.n_rec][0] == -1) {
+                    seed[j0 - S.n_rec][0] = az; seed[j0 - S.n_rec][1] = j1; seed[j0 - S.n_rec][2] = j2;
                 }
-                if (j1 >= S.n_rec && ps.seed[j1 - S.n_rec][0] == -1) {
-                    ps.seed[j1 - S.n_rec][0] = az; ps.seed[j1 - S.n_rec][1] = j0; ps.seed[j1 - S.n_rec][2] = j2;
+                if (j1 >= S.n_rec && seed[j1 - S.n_rec][0] == -1) {
+                    seed[j1 - S.n_rec][0] = az; seed[j1 - S.n_rec][1] = j0; seed[j1 - S.n_rec][2] = j2;
                 }
-                if (j2 >= S.n_rec && ps.seed[j2 - S.n_rec][0] == -1) {
-                    ps.seed[j2 - S.n_rec][0] = az; ps.seed[j2 - S.n_rec][1] = j0; ps.seed[j2 - S.n_rec][2] = j1;
+                if (j2 >= S.n_rec && seed[j2 - S.n_rec][0] == -1) {
+                    seed[j2 - S.n_rec][0] = az; seed[j2 - S.n_rec][1] = j0; seed[j2 - S.n_rec][2] = j1;
                 }
             }
             ps.done[a >> 5] |= 1u << (a & 31);
@@ -1279,27 +1296,20 @@ pose_kernel(DevSystem S, DevWork W, int n) {
     score_pose(S, W, p, threadIdx.x & 31, ps);
 }
 
-// The same over the poses of several jobs; each warp keeps its job's system and workspace in
-// shared memory next to its polyhedron workspace.
-struct PoseSlot {
-    PoseShared ps;
-    Job job;
-};
-
+// The same over the poses of several jobs; the job's system and workspace descriptors are read
+// from the job table (they stay in L1), keeping shared memory for the polyhedron workspace.
 __global__ void __launch_bounds__(kVorWarps * 32)
 pose_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, int total) {
     extern __shared__ __align__(16) unsigned char smem[];
-    PoseSlot& slot = reinterpret_cast<PoseSlot*>(smem)[threadIdx.x >> 5];
+    PoseShared& ps = reinterpret_cast<PoseShared*>(smem)[threadIdx.x >> 5];
     const int gp = blockIdx.x * kVorWarps + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
     if (gp >= total) return;
-    const int j = find_job(jobs, n_jobs, gp, false);
-    copy_job(&slot.job, &jobs[j], lane);
-    score_pose(slot.job.S, slot.job.W, gp - slot.job.pose0, lane, slot.ps);
+    const Job& job = jobs[find_job(jobs, n_jobs, gp, false)];
+    score_pose(job.S, job.W, gp - job.pose0, threadIdx.x & 31, ps);
 }
 
 size_t pose_smem_bytes() { return sizeof(PoseShared) * kVorWarps; }
-size_t pose_jobs_smem_bytes() { return sizeof(PoseSlot) * kVorWarps; }
+size_t pose_jobs_smem_bytes() { return sizeof(PoseShared) * kVorWarps; }
 
 void launch_poses(const DevSystem& S, const DevWork& W, int n, cudaStream_t st) {
     pose_kernel<<<(unsigned)((n + kVorWarps - 1) / kVorWarps), kVorWarps * 32, pose_smem_bytes(), st>>>(S, W, n);
