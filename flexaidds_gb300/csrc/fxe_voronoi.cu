@@ -52,6 +52,13 @@ using real = FXE_REAL;
 #ifndef FXE_FILTER
 #define FXE_FILTER (FXE_REFERENCE_FORMULAS)
 #endif
+// The double build's kernel outgrows the instruction cache (its top stall is instruction
+// fetch): its rarely taken or bulky helpers are called, not inlined.
+#if FXE_REFERENCE_FORMULAS
+#define FXE_COLD __noinline__
+#else
+#define FXE_COLD
+#endif
 struct __align__(4 * sizeof(real)) real4 {
     real x, y, z, w;
 };
@@ -134,7 +141,7 @@ __device__ __forceinline__ real dot3(const real4& a, real x, real y, real z) {
 }
 
 // solve_3x3 (LIB/Vcontacts.cpp:1384-1414) in FP32.
-__device__ bool solve3(const real4& e0, const real4& e1, const real4& e2, real* pt) {
+__device__ FXE_COLD bool solve3(const real4& e0, const real4& e1, const real4& e2, real* pt) {
     const real c00 = e1.y * e2.z - e2.y * e1.z;
     const real c01 = -e1.x * e2.z + e2.x * e1.z;
     const real c02 = e1.x * e2.y - e2.x * e1.y;
@@ -154,7 +161,7 @@ __device__ bool solve3(const real4& e0, const real4& e1, const real4& e2, real* 
 
 // solve_2xS (LIB/Vcontacts.cpp:1427-1476) in FP32.
 // rr is the square of the radius as the reference forms it: a single-precision product.
-__device__ bool solve2s(const real4& a, const real4& b, real rr, real* p0, real* p1) {
+__device__ FXE_COLD bool solve2s(const real4& a, const real4& b, real rr, real* p0, real* p1) {
     const real e2x = a.y * b.z - a.z * b.y;
     const real e2y = a.z * b.x - a.x * b.z;
     const real e2z = a.x * b.y - a.y * b.x;
@@ -177,7 +184,7 @@ __device__ bool solve2s(const real4& a, const real4& b, real rr, real* p0, real*
     return true;
 }
 
-__device__ __forceinline__ real cos_pqr(const real4& p, const real4& q, const real4& r) {
+__device__ FXE_COLD real cos_pqr(const real4& p, const real4& q, const real4& r) {
     const real ax = p.x - q.x, ay = p.y - q.y, az = p.z - q.z;
     const real bx = r.x - q.x, by = r.y - q.y, bz = r.z - q.z;
     return (ax * bx + ay * by + az * bz) / sqrt((ax * ax + ay * ay + az * az) * (bx * bx + by * by + bz * bz));
@@ -215,7 +222,7 @@ __device__ __forceinline__ real angle_between(real ux, real uy, real uz, real vx
 #if FXE_REFERENCE_FORMULAS
 // The reference's own expression (double builds): reproduces its values, including those of
 // nearly degenerate triangles, to rounding.
-__device__ real sph_arc(const real4& ao, const real4& b, const real4& c, real rado) {
+__device__ FXE_COLD real sph_arc(const real4& ao, const real4& b, const real4& c, real rado) {
     const real cosAOB = (ao.x * b.x + ao.y * b.y + ao.z * b.z) / (ao.w * b.w);
     const real cosBOC = (b.x * c.x + b.y * c.y + b.z * c.z) / (b.w * c.w);
     const real U = (1 + cosAOB) * sqrt((1 + cosBOC) / real(8.0));
@@ -236,7 +243,7 @@ __device__ real sph_arc(const real4& ao, const real4& b, const real4& c, real ra
     return rado * (angBAC * (rado - ao.w) - real(4.0) * rado * atan(sqrt(tanprod)));
 }
 #else
-__device__ real sph_arc(const real4& ao, const real4& b, const real4& c, real rado) {
+__device__ FXE_COLD real sph_arc(const real4& ao, const real4& b, const real4& c, real rado) {
     const real sector = angle_between(b.x - ao.x, b.y - ao.y, b.z - ao.z, c.x - ao.x, c.y - ao.y, c.z - ao.z);
     const real th = angle_between(ao.x, ao.y, ao.z, b.x, b.y, b.z);
     const real ph = angle_between(b.x, b.y, b.z, c.x, c.y, c.z);
@@ -251,7 +258,7 @@ __device__ __forceinline__ real4 centre_of(const real4& pl) {
 }
 
 // test_point (LIB/Vcontacts.cpp:1357-1372): true unless x lies behind a contact plane.
-__device__ bool inside_all(const VorShared& sh, int NC, int skip, real x, real y, real z) {
+__device__ FXE_COLD bool inside_all(const VorShared& sh, int NC, int skip, real x, real y, real z) {
     for (int cp = 0; cp < NC; ++cp) {
         if (cp == skip || sh.flag[cp] == 0) continue;
         if (dot3(sh.pl[cp], x, y, z) + sh.pl[cp].w > real(0.0)) return false;
@@ -307,7 +314,7 @@ __device__ __forceinline__ float vt_pretest(const float4& P, float sx, float sy,
 // The vertex that ends edge e (LIB/Vcontacts.cpp:283-330), in full precision: the plane with
 // the smallest positive vt along the edge (planes spread over the lanes) and, when that point
 // lies outside the sphere, the bounding planes too. The result is uniform across the warp.
-__device__ WalkStep walk_step_exact(const VorShared& sh, int NC, int e, real rr, int lane) {
+__device__ FXE_COLD WalkStep walk_step_exact(const VorShared& sh, int NC, int e, real rr, int lane) {
     const uchar4 ep = sh.u.e.ep[e];
     const real4 V = sh.u.e.ev[e];
     const real4 s = sh.vx[sh.u.e.es[e].x];
@@ -483,6 +490,60 @@ __device__ __forceinline__ void add_in_order(VorShared& sh, int X, real v, int l
         sh.area[X] = acc;
     }
     __syncwarp();
+}
+
+// Corrections for engulfing planes (LIB/Vcontacts.cpp:963-1041): arcs of the engulfed faces
+// credited to their neighbours, then the engulfing faces' own areas.
+__device__ FXE_COLD void engulf_corrections(VorShared& sh, int NC, real rado, real rr, real two_pi_r, int epi,
+                                            int lane) {
+    if (epi > 0) {
+        if (lane == 0) {
+            for (int X = 0; X < NC; ++X) {
+                if (!(sh.flag[X] & kEngulf)) continue;
+                const int np = sh.fnp[X];
+                const uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
+                const real4 cp = centre_of(sh.pl[X]);
+                for (int vi = 0; vi < np; ++vi) {
+                    const int cur = pt[vi], nxt = pt[(vi + 1) % np];
+                    const uchar4 qc = sh.vp[cur], qn = sh.vp[nxt];
+                    int pa1, pa2;
+                    if (qc.x == X) { pa1 = qc.y; pa2 = qc.z; }
+                    else { pa1 = qc.x; pa2 = (qc.y == X) ? qc.z : qc.y; }
+                    int comm;
+                    if (pa1 == qn.x || pa1 == qn.y || pa1 == qn.z) comm = pa1;
+                    else if (pa2 == qn.x || pa2 == qn.y || pa2 == qn.z) comm = pa2;
+                    else continue;
+                    if (comm != kNone && !(comm < NC && (sh.flag[comm] & kEngulf))) {
+                        if (comm < NC) sh.area[comm] += sph_arc(cp, sh.vx[cur], sh.vx[nxt], rado);
+                        if (np == 2) break;
+                    }
+                }
+            }
+            if (epi == 1) {
+                sh.area[sh.eng[0]] = two_pi_r * (rado + fabs(sh.pl[sh.eng[0]].w));
+            } else if (epi == 2) {
+                real q0[3], q1[3];
+                const real full = two_pi_r * rado;
+                if (!solve2s(sh.pl[sh.eng[0]], sh.pl[sh.eng[1]], rr, q0, q1)) {
+                    sh.area[sh.eng[0]] = full;
+                    sh.area[sh.eng[1]] = full;
+                } else {
+                    const real4 Bp = make_real4(q0[0], q0[1], q0[2], rado);
+                    const real4 Cp = make_real4(q1[0], q1[1], q1[2], rado);
+                    real m = sph_arc(centre_of(sh.pl[sh.eng[0]]), Bp, Cp, rado);
+                    m += sph_arc(centre_of(sh.pl[sh.eng[1]]), Bp, Cp, rado);
+                    sh.area[sh.eng[0]] = full - real(0.5) * m;
+                    sh.area[sh.eng[1]] = full - real(0.5) * m;
+                }
+            }
+        }
+        __syncwarp();
+        if (epi >= 3) {
+            const real share = real(4.0) * (real)kPi * rado * rado / epi;
+            for (int X = lane; X < NC; X += 32) sh.area[X] = (sh.flag[X] & kEngulf) ? share : real(0.0);
+        }
+        __syncwarp();
+    }
 }
 
 // One extended-radical-plane polyhedron and its contact areas. sh.pl/flag/cidx hold the
@@ -935,54 +996,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         add_in_order(sh, X, v, lane);
     }
     __syncwarp();
-    if (epi > 0) {
-        if (lane == 0) {
-            for (int X = 0; X < NC; ++X) {
-                if (!(sh.flag[X] & kEngulf)) continue;
-                const int np = sh.fnp[X];
-                const uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
-                const real4 cp = centre_of(sh.pl[X]);
-                for (int vi = 0; vi < np; ++vi) {
-                    const int cur = pt[vi], nxt = pt[(vi + 1) % np];
-                    const uchar4 qc = sh.vp[cur], qn = sh.vp[nxt];
-                    int pa1, pa2;
-                    if (qc.x == X) { pa1 = qc.y; pa2 = qc.z; }
-                    else { pa1 = qc.x; pa2 = (qc.y == X) ? qc.z : qc.y; }
-                    int comm;
-                    if (pa1 == qn.x || pa1 == qn.y || pa1 == qn.z) comm = pa1;
-                    else if (pa2 == qn.x || pa2 == qn.y || pa2 == qn.z) comm = pa2;
-                    else continue;
-                    if (comm != kNone && !(comm < NC && (sh.flag[comm] & kEngulf))) {
-                        if (comm < NC) sh.area[comm] += sph_arc(cp, sh.vx[cur], sh.vx[nxt], rado);
-                        if (np == 2) break;
-                    }
-                }
-            }
-            if (epi == 1) {
-                sh.area[sh.eng[0]] = two_pi_r * (rado + fabs(sh.pl[sh.eng[0]].w));
-            } else if (epi == 2) {
-                real q0[3], q1[3];
-                const real full = two_pi_r * rado;
-                if (!solve2s(sh.pl[sh.eng[0]], sh.pl[sh.eng[1]], rr, q0, q1)) {
-                    sh.area[sh.eng[0]] = full;
-                    sh.area[sh.eng[1]] = full;
-                } else {
-                    const real4 Bp = make_real4(q0[0], q0[1], q0[2], rado);
-                    const real4 Cp = make_real4(q1[0], q1[1], q1[2], rado);
-                    real m = sph_arc(centre_of(sh.pl[sh.eng[0]]), Bp, Cp, rado);
-                    m += sph_arc(centre_of(sh.pl[sh.eng[1]]), Bp, Cp, rado);
-                    sh.area[sh.eng[0]] = full - real(0.5) * m;
-                    sh.area[sh.eng[1]] = full - real(0.5) * m;
-                }
-            }
-        }
-        __syncwarp();
-        if (epi >= 3) {
-            const real share = real(4.0) * (real)kPi * rado * rado / epi;
-            for (int X = lane; X < NC; X += 32) sh.area[X] = (sh.flag[X] & kEngulf) ? share : real(0.0);
-        }
-        __syncwarp();
-    }
+    engulf_corrections(sh, NC, rado, rr, two_pi_r, epi, lane);
     sh.nv = NV;
     __syncwarp();
     return kAtomOk;
@@ -1056,7 +1070,7 @@ struct PoseShared {
 
 __device__ __forceinline__ bool bit(const uint32_t* m, int l) { return (m[l >> 5] >> (l & 31)) & 1u; }
 
-__device__ double get_yval(const DevSystem& S, int idx, double rel) {
+__device__ FXE_COLD double get_yval(const DevSystem& S, int idx, double rel) {
     const int o = S.em_off[idx], e = S.em_off[idx + 1];
     if (S.em_weight[idx]) return (double)S.em_y[o];
     int k = o;
