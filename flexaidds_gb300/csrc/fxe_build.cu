@@ -24,8 +24,39 @@ struct BuildShared {
     float pos[kMaxLig][3];
     int cell[kMaxLig];
     double icv[64];
+    int gbin[64];     // bin of each gene's value (its entry in the trigonometry tables)
+    int gi;           // grid index of the pose
     int bad;
 };
+
+// cos and sin of a build angle: the C library's values tabulated by the host for the angles the
+// genes produce (so that coordinates match the reference built on the same host bit for bit),
+// else the correctly rounded values.
+__device__ __forceinline__ void build_trig(const DevSystem& S, const BuildShared& sh, int l, int c, float x,
+                                           float* cs, float* sn) {
+    const int k = 2 * l + c, src = S.trig_src[k];
+    float4 e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    bool have = false;
+    if (src == -2) {
+        if ((unsigned)sh.gi < (unsigned)S.n_grid) {
+            e = c == 0 ? S.grid_trig_a[sh.gi] : S.grid_trig_d[sh.gi];
+            have = true;
+        }
+    } else {
+        const int idx = src < 0 ? 0 : (src < 64 ? sh.gbin[src] : -1);
+        if (idx >= 0 && idx < S.trig_cnt[k]) {
+            e = S.trig_tab[S.trig_off[k] + idx];
+            have = true;
+        }
+    }
+    if (have && __float_as_int(e.x) == __float_as_int(x)) {
+        *cs = e.y;
+        *sn = e.z;
+    } else {
+        *cs = (float)cos((double)x);
+        *sn = (float)sin((double)x);
+    }
+}
 
 __device__ __forceinline__ void build_pose(const DevSystem& S, const DevWork& W, int p,
                                            const int32_t* __restrict__ genes,
@@ -45,8 +76,12 @@ __device__ __forceinline__ void build_pose(const DevSystem& S, const DevWork& W,
                 if (S.dec_tab[mid] < u) lo = mid + 1; else hi = mid;
             }
             v = S.gene_min[g] + S.gene_del[g] * (double)(lo - base);
+            if (g < 64) sh.gbin[g] = lo - base;
         } else {
             v = ic_in[(size_t)p * ng + g];
+            // the bin this value would come from; the table entry is used only if its angle matches
+            const double b = (v - S.gene_min[g]) / S.gene_del[g];
+            if (g < 64) sh.gbin[g] = (b >= 0.0 && b < 2147483647.0) ? (int)rint(b) : -1;
         }
         if (v > S.gene_max[g]) v = S.gene_max[g];
         else if (v < S.gene_min[g]) v = S.gene_min[g];
@@ -59,7 +94,10 @@ __device__ __forceinline__ void build_pose(const DevSystem& S, const DevWork& W,
         sh.ic[l][1] = b.y;
         sh.ic[l][2] = b.z;
     }
-    if (lane == 0) sh.bad = 0;
+    if (lane == 0) {
+        sh.bad = 0;
+        sh.gi = -1;
+    }
     __syncwarp();
 
     if (lane == 0) {
@@ -71,6 +109,7 @@ __device__ __forceinline__ void build_pose(const DevSystem& S, const DevWork& W,
             case -1: {
                 const unsigned gi = (unsigned)v;
                 if (gi >= (unsigned)S.n_grid) { sh.bad = 1; break; }
+                sh.gi = (int)gi;
                 const float4 c = S.grid_ic[gi];
                 sh.ic[atm][0] = c.x;
                 sh.ic[atm][1] = c.y;
@@ -138,17 +177,16 @@ __device__ __forceinline__ void build_pose(const DevSystem& S, const DevWork& W,
             a = cx * cx;
             b = cy * cy;
             c = cz * cz;
-            // cos/sin of the single-precision angle, rounded from double: the correctly rounded
-            // values, which is what the C library's cosf/sinf return for these arguments
             const float angPI = (float)(sh.ic[l][1] * kPi / 180.0f);
-            float ct = (float)cos((double)angPI), st = -(float)sin((double)angPI);
+            float ct, st;
+            build_trig(S, sh, l, 0, angPI, &ct, &st);
+            st = -st;
             op = 1.0f - ct;
             const float xk = (cx * cz * op - cy * st) * zn + ((1.0f - a) * ct + a) * xn + (cx * cy * op + cz * st) * yn;
             const float yk = (cy * cx * op - cz * st) * xn + ((1.0f - b) * ct + b) * yn + (cy * cz * op + cx * st) * zn;
             const float zk = (cz * cy * op - cx * st) * yn + ((1.0f - c) * ct + c) * zn + (cz * cx * op + cy * st) * xn;
             const float dihPI = (float)(sh.ic[l][2] * kPi / 180.0f);
-            ct = (float)cos((double)dihPI);
-            st = (float)sin((double)dihPI);
+            build_trig(S, sh, l, 1, dihPI, &ct, &st);
             op = 1.0f - ct;
             cx = (x[2] - x[1]) * d;
             cy = (y[2] - y[1]) * d;

@@ -53,6 +53,7 @@ fxe_status cuda_fail(cudaError_t e, const char* what) {
 // Device allocations freed together; a receptor's block is shared by every context built on it.
 struct DevBlock {
     std::vector<void*> ptrs;
+    std::vector<float4> grid_ic;   // host copy of the cleft-grid ICs
     ~DevBlock() {
         for (void* p : ptrs) cudaFree(p);
     }
@@ -127,6 +128,10 @@ extern "C" const char* fxe_last_error(void) { return g_err.c_str(); }
     } while (0)
 
 namespace {
+
+// The single-precision angle buildcc takes the sine and cosine of (LIB/buildcc.cpp:80-100),
+// formed as the pose build kernel forms it.
+float build_angle(float deg) { return (float)(deg * fxe::kPi / 180.0f); }
 
 fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share,
                           const fxe_ligand_desc* lig, const fxe_emat_desc* em, const fxe_params* prm,
@@ -244,6 +249,16 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
             gic[g] = make_float4(rec->grid_ic[3 * g], rec->grid_ic[3 * g + 1], rec->grid_ic[3 * g + 2], 0.0f);
         S.n_grid = rec->n_grid;
         FXE_TRY(ctx->upload_receptor(&S.grid_ic, gic.data(), rec->n_grid), "grid upload");
+        // the C library's cosf/sinf of the anchor atom's angle and dihedral at every grid point
+        std::vector<float4> ta(rec->n_grid), td(rec->n_grid);
+        for (int g = 0; g < rec->n_grid; ++g) {
+            const float a = build_angle(gic[g].y), d = build_angle(gic[g].z);
+            ta[g] = make_float4(a, cosf(a), sinf(a), 0.0f);
+            td[g] = make_float4(d, cosf(d), sinf(d), 0.0f);
+        }
+        FXE_TRY(ctx->upload_receptor(&S.grid_trig_a, ta.data(), rec->n_grid), "grid upload");
+        FXE_TRY(ctx->upload_receptor(&S.grid_trig_d, td.data(), rec->n_grid), "grid upload");
+        ctx->receptor->grid_ic = gic;
         }
         // ligand
         S.n_lig = n;
@@ -286,6 +301,69 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
         ctx->h_gdel.assign(lig->gene_del, lig->gene_del + ng);
         ctx->h_dtab = dtab;
         ctx->h_doff = doff;
+        {
+            // which gene sets each atom's angle and dihedral last, and through which cascade
+            // (the IC assignment of ic2cf, LIB/ic2cf.cpp:53-105, replayed symbolically)
+            std::vector<int> src(2 * n, -1), pos(2 * n, 0);
+            std::vector<std::vector<int>> chain(ng);
+            for (int g = 0; g < ng; ++g) {
+                const int atm = lig->gene_atom[g], t = lig->gene_type[g];
+                if (t == -1) {
+                    src[2 * atm] = src[2 * atm + 1] = -2;
+                } else if (t == 1) {
+                    src[2 * atm] = g;
+                    pos[2 * atm] = 0;
+                } else if (t == 2) {
+                    chain[g].push_back(atm);
+                    src[2 * atm + 1] = g;
+                    pos[2 * atm + 1] = 0;
+                    int j = atm, cat = lig->rec[4 * atm + 3], guard = 0;
+                    if (cat >= 0)
+                        while (cat != atm && guard++ <= n) {
+                            chain[g].push_back(cat);
+                            src[2 * cat + 1] = g;
+                            pos[2 * cat + 1] = (int)chain[g].size() - 1;
+                            j = cat;
+                            cat = lig->rec[4 * j + 3];
+                        }
+                }
+            }
+            std::vector<float4> tab;
+            std::vector<int> off(2 * n), cnt(2 * n);
+            for (int l = 0; l < n; ++l)
+                for (int c = 0; c < 2; ++c) {
+                    const int k = 2 * l + c, g = src[k];
+                    off[k] = (int)tab.size();
+                    if (g == -2) {
+                        cnt[k] = 0;   // read from the grid tables
+                        continue;
+                    }
+                    std::vector<float> vals;
+                    if (g == -1) {
+                        vals.push_back(c == 0 ? lig->ic[3 * l + 1] : lig->ic[3 * l + 2]);
+                    } else {
+                        const int nb = doff[g + 1] - doff[g];
+                        for (int i = 0; i < nb; ++i) {
+                            double v = lig->gene_min[g] + lig->gene_del[g] * (double)i;
+                            if (v > lig->gene_max[g]) v = lig->gene_max[g];
+                            else if (v < lig->gene_min[g]) v = lig->gene_min[g];
+                            float f = (float)v;
+                            for (int q = 1; q <= pos[k]; ++q) f = f + lig->shift[chain[g][q]];
+                            vals.push_back(f);
+                        }
+                    }
+                    cnt[k] = (int)vals.size();
+                    for (float a : vals) {
+                        const float x = build_angle(a);
+                        tab.push_back(make_float4(x, cosf(x), sinf(x), 0.0f));
+                    }
+                }
+            if (tab.empty()) tab.push_back(make_float4(0.0f, 1.0f, 0.0f, 0.0f));
+            FXE_TRY(ctx->upload(&S.trig_tab, tab.data(), tab.size()), "trig upload");
+            FXE_TRY(ctx->upload(&S.trig_src, src.data(), 2 * n), "trig upload");
+            FXE_TRY(ctx->upload(&S.trig_off, off.data(), 2 * n), "trig upload");
+            FXE_TRY(ctx->upload(&S.trig_cnt, cnt.data(), 2 * n), "trig upload");
+        }
         FXE_TRY(ctx->upload(&S.gene_type, lig->gene_type, ng), "gene upload");
         FXE_TRY(ctx->upload(&S.gene_atom, lig->gene_atom, ng), "gene upload");
         FXE_TRY(ctx->upload(&S.gene_min, lig->gene_min, ng), "gene upload");

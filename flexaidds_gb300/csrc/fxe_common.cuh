@@ -78,6 +78,16 @@ struct DevSystem {
     const double* gene_del;
     const int* dec_off;          // [n_genes + 1] offsets into dec_tab
     const double* dec_tab;       // running bin totals per gene
+    // cosf/sinf of the host's C library for every single-precision angle the pose build can
+    // meet, as (angle, cos, sin, 0): per grid point (the anchor atom's angle and dihedral), and
+    // per (ligand atom, angle|dihedral) over the bins of the gene that sets it last (trig_src:
+    // -1 no gene, -2 the grid gene, else the gene's index; trig_off/trig_cnt locate its entries)
+    const float4* grid_trig_a;   // [n_grid]
+    const float4* grid_trig_d;   // [n_grid]
+    const float4* trig_tab;
+    const int* trig_src;         // [n_lig * 2]
+    const int* trig_off;         // [n_lig * 2]
+    const int* trig_cnt;         // [n_lig * 2]
     // energy matrix
     int ntypes;
     const int* em_weight;

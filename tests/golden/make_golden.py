@@ -63,6 +63,10 @@ SYSTEMS = {
     # atoms without contacts take the SAS-only path
     "outside_600_10": dict(args=(600, 6.0, 10, 2), seed=37, grid=256, pool=3000, scored=120,
                            clashed=20, contacts=8, tweak="outside"),
+    # the at-scale shape of the benchmark: 6,000-atom receptor, 12 A cleft, 48-atom ligand with
+    # 12 torsions (receptor cube edge given, as the benchmark gives it)
+    "scale_6000_48": dict(args=(6000, 12.0, 48, 12), seed=7, grid=768, pool=40000, scored=60,
+                          clashed=10, contacts=3, tweak=None, edge=60.032427451306646),
 }
 
 
@@ -70,7 +74,7 @@ def inputs_for(name):
     """The generator inputs of fixture ``name`` (seeded; the cleft grid subsampled)."""
     cfg = SYSTEMS[name]
     n_rec, cleft, n_lig, n_tor = cfg["args"]
-    inp = system.make_inputs(n_rec, cleft, n_lig, n_tor, seed=cfg["seed"])
+    inp = system.make_inputs(n_rec, cleft, n_lig, n_tor, seed=cfg["seed"], edge=cfg.get("edge"))
     rng = np.random.default_rng(cfg["seed"] + 100)
     keep = np.sort(rng.choice(inp.grid_xyz.shape[0], cfg["grid"], replace=False))
     inp.grid_xyz = np.ascontiguousarray(inp.grid_xyz[keep])

@@ -44,7 +44,7 @@ def test_ligand_generator_geometry():
 
 # --- set-up restatement against the reference's own set-up (golden descriptors) ---------------
 
-@pytest.mark.parametrize("name", ["c0_2000_24", "curves_900_16", "outside_600_10"])
+@pytest.mark.parametrize("name", ["c0_2000_24", "curves_900_16", "outside_600_10", "scale_6000_48"])
 def test_prepare_matches_reference_setup(name):
     from conftest import load_golden
     dref, _ = load_golden(name)
