@@ -28,7 +28,9 @@ constexpr float kPolyPenalty = 1e6f;     // LIB/flexaid.h:69
 constexpr int kMaxCand = 96;    // contact candidates of one atom
 constexpr int kMaxPlanes = kMaxCand + 4;
 constexpr int kMaxEdges = 200;  // the reference aborts the hull walk at 200 edges
-constexpr int kMaxVerts = 255;  // vertex indices are bytes; 255 means "none"
+// vertex indices are bytes (255 means "none"); a walk that reaches the reference's 200-edge abort
+// has at most about 135 vertices, a complete one with its arc points about 105
+constexpr int kMaxVerts = 176;
 constexpr int kMaxFacePts = 640;
 constexpr int kMaxLig = 128;    // ligand atoms per pose (bit masks, shared staging)
 constexpr int kMaskWords = kMaxLig / 32;

@@ -27,8 +27,9 @@ namespace FXE_VARIANT {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr uint8_t kNone = 255;
-// Poses (warps) per block of pose_kernel: with about 1 KB of shared memory reserved per block,
-// two 13 KB single-precision workspaces per block fit sixteen warps on an SM.
+// Poses (warps) per block of pose_kernel. Two per block fit eight double-precision workspaces
+// (23 KB each) or twenty single-precision ones (10.6 KB) on an SM; the double kernel measured no
+// faster with nine (three per block) than with seven or eight.
 constexpr int kVorWarps = 2;
 
 // Floating-point type of the polyhedron arithmetic: single precision by default; building
@@ -61,6 +62,9 @@ using real = FXE_REAL;
 #endif
 struct __align__(4 * sizeof(real)) real4 {
     real x, y, z, w;
+};
+struct real3 {
+    real x, y, z;
 };
 __device__ __forceinline__ real4 make_real4(real x, real y, real z, real w) { return real4{x, y, z, w}; }
 __device__ __forceinline__ real4 to_real4(const float4& v) { return real4{(real)v.x, (real)v.y, (real)v.z, (real)v.w}; }
@@ -113,7 +117,7 @@ struct VorShared {
     union {
         struct {
             // (two spare slots: the step that reaches the 200-edge limit writes up to two edges)
-            real4 ev[kMaxEdges + 2];   // edge direction
+            real3 ev[kMaxEdges + 2];   // edge direction
             uchar4 ep[kMaxEdges + 2];   // plane0, plane1, start plane, end plane
             uchar2 es[kMaxEdges + 2];   // start vertex, end vertex
         } e;
@@ -275,7 +279,7 @@ __device__ void add_edge(VorShared& sh, int en, int p0, int p1, int tp, int sp) 
     const real4 t = sh.pl[tp];
     const real tv = t.x * (s.x + vx) + t.y * (s.y + vy) + t.z * (s.z + vz) + t.w;
     if (tv > real(0.0)) { vx = -vx; vy = -vy; vz = -vz; }
-    sh.u.e.ev[en] = make_real4(vx, vy, vz, real(0.0));
+    sh.u.e.ev[en] = real3{vx, vy, vz};
     sh.u.e.ep[en] = make_uchar4((uint8_t)p0, (uint8_t)p1, (uint8_t)tp, kNone);
     sh.u.e.es[en] = make_uchar2((uint8_t)sp, kNone);
 }
@@ -316,7 +320,7 @@ __device__ __forceinline__ float vt_pretest(const float4& P, float sx, float sy,
 // lies outside the sphere, the bounding planes too. The result is uniform across the warp.
 __device__ FXE_COLD WalkStep walk_step_exact(const VorShared& sh, int NC, int e, real rr, int lane) {
     const uchar4 ep = sh.u.e.ep[e];
-    const real4 V = sh.u.e.ev[e];
+    const real3 V = sh.u.e.ev[e];
     const real4 s = sh.vx[sh.u.e.es[e].x];
     const int pA = ep.x, pB = ep.y, oldC = ep.z;
     real vtmin = real(9.9e9);
@@ -368,7 +372,7 @@ __device__ FXE_COLD WalkStep walk_step_exact(const VorShared& sh, int NC, int e,
 __device__ WalkStep walk_step(const VorShared& sh, int NC, int e, real rr, int lane) {
 #if FXE_FILTER
     const uchar4 ep = sh.u.e.ep[e];
-    const real4 V = sh.u.e.ev[e];
+    const real3 V = sh.u.e.ev[e];
     const real4 s = sh.vx[sh.u.e.es[e].x];
     const int pA = ep.x, pB = ep.y, oldC = ep.z;
     const float sx = (float)s.x, sy = (float)s.y, sz = (float)s.z;
@@ -688,7 +692,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
                 real vz = a.x * b.y - a.y * b.x;
                 const real tv = t.x * (r.x + vx) + t.y * (r.y + vy) + t.z * (r.z + vz) + t.w;
                 if (tv > real(0.0)) { vx = -vx; vy = -vy; vz = -vz; }
-                sh.u.e.ev[e] = make_real4(vx, vy, vz, real(0.0));
+                sh.u.e.ev[e] = real3{vx, vy, vz};
                 sh.u.e.ep[e] = make_uchar4((uint8_t)p0, (uint8_t)pC, (uint8_t)tp, kNone);
                 sh.u.e.es[e] = make_uchar2((uint8_t)vn, kNone);
             }
