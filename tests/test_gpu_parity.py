@@ -141,3 +141,27 @@ def test_scale_system_against_oracle():
     assert ok.sum() >= 20
     assert rel_err(g["evalue"], r["evalue"][sel]).max() <= 1e-9
     ev.close()
+
+
+def test_large_ligand_against_oracle():
+    """A 120-atom ligand with 15 torsions (the masks and staging hold up to 128 atoms)."""
+    base = system.make_inputs(2000, 8.0, 24, 6, seed=41)
+    lig = synth.random_ligand(120, 15, seed=77)
+    # anchors 4-12 A beyond a face of the receptor's box: the ligand lies against its surface
+    rng = np.random.default_rng(79)
+    lo, hi = base.receptor.xyz.min(axis=0), base.receptor.xyz.max(axis=0)
+    grid = rng.uniform(lo, hi, size=(400, 3))
+    grid[:, 0] = hi[0] + rng.uniform(4.0, 12.0, 400)
+    d = prepare.prepare(system.SystemInputs(receptor=base.receptor, ligand=lig,
+                                            grid_xyz=grid.astype(np.float32), emat=base.emat))
+    pool = synth.random_genes(6000, d.n_genes, seed=78)
+    r = oracle_eval(d, d.genes_to_ic(pool))["cf"]
+    ev = evaluator.GPUEvaluator(d, max_poses=1024, precision=REF)
+    g = ev.eval_genes(pool)
+    np.testing.assert_array_equal(g["status"], r["status"])
+    ok = g["status"] == 0
+    e = rel_err(g["evalue"], r["evalue"])
+    print(f"120-atom ligand: {ok.sum()} scored of {len(pool)}, max rel {e.max():.1e}")
+    assert ok.sum() >= 100
+    assert e.max() <= 1e-9
+    ev.close()
