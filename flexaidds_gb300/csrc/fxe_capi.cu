@@ -1030,6 +1030,9 @@ extern "C" fxe_status fxe_ga_admit(fxe_ga* e, const fxe_ga_job* job, int32_t* sl
         return fail(FXE_ERR_INVALID_ARGS, "population must be 2..2048 and at most the context's max_poses");
     if (job->generations < 0 || ng < 1 || ng > 64)
         return fail(FXE_ERR_INVALID_ARGS, "generations < 0, or genes outside 1..64");
+    const int nnew = job->n_new > 0 ? job->n_new : P;
+    if (nnew > P || (job->steady && job->n_new <= 0))
+        return fail(FXE_ERR_INVALID_ARGS, "n_new must be 1..population (STEADY needs it set)");
     if (ctx->device != e->device) return fail(FXE_ERR_INVALID_ARGS, "context on another device");
     for (const auto& s : e->slots)
         if (s.used && s.ctx == ctx) return fail(FXE_ERR_INVALID_ARGS, "the context already runs a job");
@@ -1064,6 +1067,11 @@ extern "C" fxe_status fxe_ga_admit(fxe_ga* e, const fxe_ga_job* job, int32_t* sl
         J.P = P;
         J.ng = ng;
         J.G = job->generations;
+        J.nnew = nnew;
+        J.steady = job->steady ? 1 : 0;
+        J.intragenes = job->intragenes ? 1 : 0;
+        J.adaptive = job->adaptive ? 1 : 0;
+        for (int q = 0; q < 4; ++q) J.k[q] = job->k[q];
         FXE_TRY(cudaMemcpyAsync(e->d_all + k, &J, sizeof(J), cudaMemcpyHostToDevice, e->stream), "GA state");
         // generation 0: uniform genes, evaluated on the job's context, sorted
         fxe::launch_ga_init(e->d_all, e->d_ids + k, 1, e->stream);
@@ -1123,7 +1131,7 @@ extern "C" fxe_status fxe_ga_step(fxe_ga* e) {
             J.W.out = const_cast<fxe_cf*>(s.J.child_cf);
             J.genes = s.J.child;
             J.pose0 = total;
-            J.n = s.job.population;
+            J.n = s.J.nnew;
             J.warp0 = items;
             total += J.n;
             items += (long long)J.n * s.ctx->S.n_lig;

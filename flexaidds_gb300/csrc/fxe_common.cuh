@@ -171,7 +171,12 @@ struct GaJob {
     int* gen;                // generation counter (device), advanced by selection
     uint64_t seed;
     double cross_rate, mut_rate;
+    double k[4];             // adaptive probabilities (adapt_prob, LIB/gaboom.cpp:848-880)
     int P, ng, G;
+    int nnew;                // children per generation
+    int steady;              // 1: STEADY replacement, 0: BOOM
+    int intragenes;          // crossover points inside genes (1) or at gene boundaries (0)
+    int adaptive;            // adaptive crossover and mutation probabilities
 };
 
 // one block's share of the ensemble reduction: running max of the log-weights and the sums

@@ -6,11 +6,15 @@
 //     (LIB/gaboom.cpp:1627-1635);
 //   * roulette_wheel: r = u * sum(fitness), the first index whose running fitness sum exceeds r
 //     (LIB/gaboom.cpp:1158-1186);
+//   * the reproduce loop (LIB/gaboom.cpp:909-1000): pairs of parents, adaptive probabilities
+//     (adapt_prob, :848-880) when asked, crossover with probability crossprob, both children
+//     mutated, until nnew children exist;
 //   * crossover: the reference's two-point bit crossover over the genes' 32-bit strings, with
-//     its choice of genes and bit points (LIB/gaboom.cpp:2517-2614, intragenes = 1);
-//   * mutate: every bit of every gene flipped with probability mut_rate (LIB/gaboom.cpp:2620-2641);
-//   * BOOM replacement: parents and children merged, sorted by energy, the best P kept
-//     (LIB/gaboom.cpp:1023-1033).
+//     its choice of genes and bit points, inside genes or at gene boundaries
+//     (LIB/gaboom.cpp:2517-2614);
+//   * mutate: every bit of every gene flipped with probability mutprob (LIB/gaboom.cpp:2620-2641);
+//   * replacement (LIB/gaboom.cpp:1023-1033): BOOM merges parents and children and keeps the best
+//     P; STEADY puts the children in place of the worst parents.
 // The reference draws from a random_device-seeded generator, so its trajectories cannot be
 // replayed; here every draw is a counter-based hash of (job seed, generation, child, draw), so a
 // job's trajectory depends on its seed alone — the same whether it runs alone or among others.
@@ -90,36 +94,65 @@ __global__ void __launch_bounds__(kGaThreads) ga_breed_kernel(const GaJob* __res
     const int P = J.P, ng = J.ng;
     const int g = *J.gen;
     const uint64_t sb = (uint64_t)(g + 1) << 32;   // streams of generation g + 1
-    for (int k = threadIdx.x; 2 * k < P; k += blockDim.x) {
+    const int nnew = J.nnew;
+    // fitness statistics of the LINEAR fitness P - rank (fitness_stats, LIB/gaboom.cpp:818-840)
+    const double fit_max = (double)P, fit_avg = 0.5 * (double)(P + 1);
+    for (int k = threadIdx.x; 2 * k < nnew; k += blockDim.x) {
         const uint64_t st = sb + (uint64_t)k;
         uint64_t d = 0;
         const int a = roulette_linear(P, uniform(J.seed, st, d++));
         const int b = roulette_linear(P, uniform(J.seed, st, d++));
+        double crossp = J.cross_rate, mutp = J.mut_rate;
+        if (J.adaptive) {
+            const double f1 = (double)(P - a), f2 = (double)(P - b);
+            const double hi = f1 > f2 ? f1 : f2, lo = f1 > f2 ? f2 : f1;
+            double denom = fit_max - fit_avg;
+            if (denom < 1e-15) denom = 1e-15;   // GA_FITNESS_DENOM_FLOOR, LIB/ga_constants.h:38
+            crossp = hi > fit_avg ? J.k[0] * (fit_max - hi) / denom : J.k[2];
+            mutp = lo > fit_avg ? J.k[1] * (fit_max - lo) / denom : J.k[3];
+        }
         int32_t* john = J.child + (size_t)(2 * k) * ng;
-        int32_t* mary = 2 * k + 1 < P ? J.child + (size_t)(2 * k + 1) * ng : nullptr;
+        int32_t* mary = 2 * k + 1 < nnew ? J.child + (size_t)(2 * k + 1) * ng : nullptr;
         int32_t tmp[64];
         int32_t* m = mary ? mary : tmp;
         for (int q = 0; q < ng; ++q) {
             john[q] = J.pop[(size_t)a * ng + q];
             m[q] = J.pop[(size_t)b * ng + q];
         }
-        if (uniform(J.seed, st, d++) < J.cross_rate) {
-            // crossover with intragenes (LIB/gaboom.cpp:2527-2551, 2580-2598)
+        if (uniform(J.seed, st, d++) < crossp) {
+            // LIB/gaboom.cpp:2527-2598
             int gen_a = (int)(uniform(J.seed, st, d++) * (double)ng);
             int gen_b = (int)(uniform(J.seed, st, d++) * (double)ng);
             if (gen_a >= ng) gen_a = ng - 1;
             if (gen_b >= ng) gen_b = ng - 1;
-            int pnt_a = (int)(uniform(J.seed, st, d++) * 32.0);
-            int pnt_b = (int)(uniform(J.seed, st, d++) * 32.0);
-            if (gen_a > gen_b) {
-                const int tg = gen_a, tp = pnt_a;
-                gen_a = gen_b; pnt_a = pnt_b;
-                gen_b = tg; pnt_b = tp;
-            }
-            if (gen_a == gen_b && pnt_a < pnt_b) {
-                const int tp = pnt_b;
-                pnt_b = pnt_a;
-                pnt_a = tp;
+            int pnt_a, pnt_b;
+            if (J.intragenes) {
+                pnt_a = (int)(uniform(J.seed, st, d++) * 32.0);
+                pnt_b = (int)(uniform(J.seed, st, d++) * 32.0);
+                if (gen_a > gen_b) {
+                    const int tg = gen_a, tp = pnt_a;
+                    gen_a = gen_b; pnt_a = pnt_b;
+                    gen_b = tg; pnt_b = tp;
+                }
+                if (gen_a == gen_b && pnt_a < pnt_b) {
+                    const int tp = pnt_b;
+                    pnt_b = pnt_a;
+                    pnt_a = tp;
+                }
+            } else {
+                if (gen_a > gen_b) {
+                    const int tg = gen_a;
+                    gen_a = gen_b;
+                    gen_b = tg;
+                }
+                if (gen_a != gen_b) {
+                    pnt_a = uniform(J.seed, st, d++) < 0.5 ? 32 : 0;
+                    pnt_b = uniform(J.seed, st, d++) < 0.5 ? 32 : 0;
+                    if (gen_b - gen_a == 1 && pnt_a == 0 && pnt_b == 32) pnt_b = pnt_a;
+                } else {
+                    pnt_a = 32;
+                    pnt_b = 0;
+                }
             }
             for (int j = gen_a; j <= gen_b; ++j) {
                 const int np = j == gen_a ? pnt_a : 32;
@@ -143,38 +176,46 @@ __global__ void __launch_bounds__(kGaThreads) ga_breed_kernel(const GaJob* __res
             for (int q = 0; q < ng; ++q) {
                 uint32_t optr = 0u;
                 for (int bit = 0; bit < 32; ++bit)
-                    if (uniform(J.seed, st, d++) < J.mut_rate) optr |= 1u << bit;
+                    if (uniform(J.seed, st, d++) < mutp) optr |= 1u << bit;
                 ch[q] ^= (int32_t)optr;
             }
         }
     }
 }
 
-// Selection. kInitial: the evaluated initial population becomes generation 0. Otherwise BOOM
-// replacement: parents and children merged and sorted by energy, the best P kept, saved as the
-// generation's snapshot, and the generation counter advanced.
+// Selection. kInitial: the evaluated initial population becomes generation 0. Otherwise the
+// replacement: BOOM merges the P parents and nnew children, STEADY keeps the best P - nnew
+// parents with the children in the places of the worst (child i at place P - 1 - i); the merged
+// set is sorted by energy, the best P kept, saved as the generation's snapshot, and the
+// generation counter advanced.
 template <bool kInitial>
 __global__ void __launch_bounds__(kGaThreads) ga_select_kernel(GaJob* __restrict__ all, const int* __restrict__ run) {
     __shared__ double key[kGaMaxSort];
     __shared__ int idx[kGaMaxSort];
     GaJob& J = all[run[blockIdx.x]];
-    const int P = J.P, ng = J.ng;
+    const int P = J.P, ng = J.ng, nnew = J.nnew;
     const int g = *J.gen;
     int32_t* const pop = J.pop;
     int32_t* const nxt = J.pop_next;
     double* const pe = J.pop_e;
     double* const nxt_e = J.pop_e_next;
-    const int m = kInitial ? P : 2 * P;   // entries [0, P) parents, [P, 2P) children
+    // entries: parents [0, np_), then children; idx >= np_ names a child
+    const int np_ = kInitial ? 0 : (J.steady ? P - nnew : P);
+    const int m = kInitial ? P : np_ + nnew;
     int n = 1;
     while (n < m) n <<= 1;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double e = INFINITY;
+        int id = i;
         if (i < m) {
-            e = kInitial ? J.child_cf[i].evalue : (i < P ? pe[i] : J.child_cf[i - P].evalue);
+            // STEADY: the place P-1-c holds child c
+            const int c = kInitial ? i : (J.steady ? (P - 1 - i) : (i - np_));
+            e = i < np_ ? pe[i] : J.child_cf[c].evalue;
             if (e != e) e = INFINITY;   // a NaN energy sorts last
+            id = i;
         }
         key[i] = e;
-        idx[i] = i;
+        idx[i] = id;
     }
     __syncthreads();
     bitonic_sort(key, idx, n);
@@ -184,8 +225,8 @@ __global__ void __launch_bounds__(kGaThreads) ga_select_kernel(GaJob* __restrict
     for (int t = threadIdx.x; t < P * ng; t += blockDim.x) {
         const int r = t / ng, q = t - r * ng;
         const int src = idx[r];
-        const int32_t v = kInitial ? J.child[(size_t)src * ng + q]
-                                   : (src < P ? pop[(size_t)src * ng + q] : J.child[(size_t)(src - P) * ng + q]);
+        const int c = kInitial ? src : (J.steady ? (P - 1 - src) : (src - np_));
+        const int32_t v = src < np_ ? pop[(size_t)src * ng + q] : J.child[(size_t)c * ng + q];
         nxt[t] = v;
         if (!kInitial) sg[t] = v;
     }

@@ -218,7 +218,9 @@ class Batch:
 
 class GAJob(C.Structure):
     _fields_ = [("ctx", C.c_void_p), ("population", C.c_int32), ("generations", C.c_int32),
-                ("cross_rate", C.c_double), ("mut_rate", C.c_double), ("seed", C.c_uint64)]
+                ("cross_rate", C.c_double), ("mut_rate", C.c_double), ("seed", C.c_uint64),
+                ("n_new", C.c_int32), ("steady", C.c_int32), ("intragenes", C.c_int32),
+                ("adaptive", C.c_int32), ("k", C.c_double * 4)]
 
 
 class GAEngine:
@@ -233,9 +235,13 @@ class GAEngine:
 
     @staticmethod
     def job(ev: GPUEvaluator, population: int, generations: int, seed: int,
-            cross_rate: float = 0.9, mut_rate: float = 0.01) -> GAJob:
+            cross_rate: float = 0.9, mut_rate: float = 0.01, n_new: int = 0, steady: bool = False,
+            intragenes: bool = False, adaptive: bool = False, k=(1.0, 0.5, 1.0, 0.5)) -> GAJob:
+        """Defaults follow the reference's: BOOM with boom_fraction 1, crossover at gene
+        boundaries, fixed probabilities (LIB/config_parser.cpp:135-161)."""
         return GAJob(ev.handle.value, int(population), int(generations), float(cross_rate),
-                     float(mut_rate), int(seed) & 0xFFFFFFFFFFFFFFFF)
+                     float(mut_rate), int(seed) & 0xFFFFFFFFFFFFFFFF, int(n_new), int(bool(steady)),
+                     int(bool(intragenes)), int(bool(adaptive)), (C.c_double * 4)(*k))
 
     def job_bytes(self, job: GAJob) -> int:
         b = C.c_int64(0)

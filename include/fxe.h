@@ -276,6 +276,11 @@ typedef struct fxe_ga_job {
     double cross_rate;       /* probability of crossover per pair of children */
     double mut_rate;         /* probability of flipping each gene bit */
     uint64_t seed;
+    int32_t n_new;           /* children per generation (0: population, BOOM's boom_fraction 1) */
+    int32_t steady;          /* 1: STEADY replacement (n_new is steady_state_num), 0: BOOM */
+    int32_t intragenes;      /* 1: crossover points inside genes, 0: at gene boundaries (default) */
+    int32_t adaptive;        /* 1: adaptive probabilities from k[0..3] (adapt_prob) */
+    double k[4];             /* k1..k4 (the reference's defaults: 1.0, 0.5, 1.0, 0.5) */
 } fxe_ga_job;
 
 fxe_status fxe_ga_create(int32_t max_jobs, int32_t precision, fxe_ga** out);

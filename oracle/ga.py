@@ -50,14 +50,17 @@ def _mask(np_: int) -> int:
     return 0xFFFFFFFF if np_ >= 31 else (2 << np_) - 1
 
 
-def breed(pop: np.ndarray, gen: int, seed: int, cross_rate: float, mut_rate: float) -> np.ndarray:
-    """Children of generation gen + 1 from the sorted population `pop` (P, ng) int32."""
+def breed(pop: np.ndarray, gen: int, seed: int, cross_rate: float, mut_rate: float, nnew: int = 0,
+          intragenes: bool = False, adaptive: bool = False, k=(1.0, 0.5, 1.0, 0.5)) -> np.ndarray:
+    """nnew children of generation gen + 1 from the sorted population `pop` (P, ng) int32."""
     P, ng = pop.shape
+    nnew = nnew or P
     u32 = pop.astype(np.int64) & 0xFFFFFFFF
-    child = np.zeros((P, ng), np.int64)
+    child = np.zeros((nnew, ng), np.int64)
     sb = (gen + 1) << 32
-    for k in range((P + 1) // 2):
-        st = sb + k
+    fit_max, fit_avg = float(P), 0.5 * float(P + 1)
+    for kk in range((nnew + 1) // 2):
+        st = sb + kk
         d = 0
 
         def draw():
@@ -68,17 +71,35 @@ def breed(pop: np.ndarray, gen: int, seed: int, cross_rate: float, mut_rate: flo
 
         a = roulette_linear(P, draw())
         b = roulette_linear(P, draw())
+        crossp, mutp = cross_rate, mut_rate
+        if adaptive:
+            f1, f2 = float(P - a), float(P - b)
+            hi, lo = max(f1, f2), min(f1, f2)
+            denom = max(fit_max - fit_avg, 1e-15)
+            crossp = k[0] * (fit_max - hi) / denom if hi > fit_avg else k[2]
+            mutp = k[1] * (fit_max - lo) / denom if lo > fit_avg else k[3]
         john = [int(x) for x in u32[a]]
         mary = [int(x) for x in u32[b]]
-        if draw() < cross_rate:
+        if draw() < crossp:
             gen_a = min(int(draw() * ng), ng - 1)
             gen_b = min(int(draw() * ng), ng - 1)
-            pnt_a = int(draw() * 32.0)
-            pnt_b = int(draw() * 32.0)
-            if gen_a > gen_b:
-                gen_a, gen_b, pnt_a, pnt_b = gen_b, gen_a, pnt_b, pnt_a
-            if gen_a == gen_b and pnt_a < pnt_b:
-                pnt_a, pnt_b = pnt_b, pnt_a
+            if intragenes:
+                pnt_a = int(draw() * 32.0)
+                pnt_b = int(draw() * 32.0)
+                if gen_a > gen_b:
+                    gen_a, gen_b, pnt_a, pnt_b = gen_b, gen_a, pnt_b, pnt_a
+                if gen_a == gen_b and pnt_a < pnt_b:
+                    pnt_a, pnt_b = pnt_b, pnt_a
+            else:
+                if gen_a > gen_b:
+                    gen_a, gen_b = gen_b, gen_a
+                if gen_a != gen_b:
+                    pnt_a = 32 if draw() < 0.5 else 0
+                    pnt_b = 32 if draw() < 0.5 else 0
+                    if gen_b - gen_a == 1 and pnt_a == 0 and pnt_b == 32:
+                        pnt_b = pnt_a
+                else:
+                    pnt_a, pnt_b = 32, 0
             for j in range(gen_a, gen_b + 1):
                 m = _mask(pnt_a if j == gen_a else 32)
                 uj, um = john[j], mary[j]
@@ -93,19 +114,33 @@ def breed(pop: np.ndarray, gen: int, seed: int, cross_rate: float, mut_rate: flo
             for q in range(ng):
                 m = 0
                 for bit in range(32):
-                    if draw() < mut_rate:
+                    if draw() < mutp:
                         m |= 1 << bit
                 ch[q] ^= m
-        child[2 * k] = john
-        if 2 * k + 1 < P:
-            child[2 * k + 1] = mary
+        child[2 * kk] = john
+        if 2 * kk + 1 < nnew:
+            child[2 * kk + 1] = mary
     return child.astype(np.uint32).astype(np.int32)
 
 
+def steady(pop: np.ndarray, pop_e: np.ndarray, child: np.ndarray, child_e: np.ndarray):
+    """STEADY replacement: child i in the place of parent P-1-i, then sorted by energy (then by
+    place)."""
+    P, nnew = pop.shape[0], child.shape[0]
+    genes = pop.copy()
+    e = pop_e.astype(np.float64).copy()
+    for i in range(nnew):
+        genes[P - 1 - i] = child[i]
+        e[P - 1 - i] = child_e[i]
+    e = np.where(np.isnan(e), np.inf, e)
+    order = np.lexsort((np.arange(P), e))
+    return genes[order], e[order]
+
+
 def boom(pop: np.ndarray, pop_e: np.ndarray, child: np.ndarray, child_e: np.ndarray):
-    """Parents and children merged, sorted by energy (then by position), as many kept as there
-    are children (the initial population: no parents)."""
-    keep = child.shape[0]
+    """Parents and children merged, sorted by energy (then by position), the best P kept (the
+    initial population, which has no parents: all of it)."""
+    keep = pop.shape[0] if pop.shape[0] else child.shape[0]
     e = np.concatenate([pop_e, child_e]).astype(np.float64)
     e = np.where(np.isnan(e), np.inf, e)
     order = np.lexsort((np.arange(e.shape[0]), e))[:keep]

@@ -21,14 +21,22 @@ def systems():
     return out
 
 
-@pytest.mark.parametrize("prec", [0, 1])
-def test_generation_matches_restated_operators(systems, prec):
+# (precision, options): the reference's defaults, then its other operators
+GA_CASES = [
+    (0, dict()),
+    (1, dict(intragenes=True, adaptive=True, n_new=58)),
+    (0, dict(steady=True, n_new=20, adaptive=True, k=(0.8, 0.3, 0.9, 0.2))),
+]
+
+
+@pytest.mark.parametrize("prec,opts", GA_CASES)
+def test_generation_matches_restated_operators(systems, prec, opts):
     d = systems[0]
     P, seed, pc, pm = 96, 12345, 0.9, 0.02
     ev = evaluator.GPUEvaluator(d, max_poses=P, precision=prec)
     check = evaluator.GPUEvaluator(d, max_poses=P, precision=prec)
     eng = evaluator.GAEngine(max_jobs=2, precision=prec)
-    slot = eng.admit(eng.job(ev, P, 3, seed, pc, pm), ev)
+    slot = eng.admit(eng.job(ev, P, 3, seed, pc, pm, **opts), ev)
     # generation 0: the uniform draws, evaluated and sorted
     init = ref_ga.initial_genes(seed, P, d.n_genes)
     e0 = check.eval_genes(init)["evalue"]
@@ -37,10 +45,15 @@ def test_generation_matches_restated_operators(systems, prec):
     np.testing.assert_array_equal(pop, want_g)
     np.testing.assert_array_equal(pe, want_e)
     snaps = []
+    bopts = {k: v for k, v in opts.items() if k in ("intragenes", "adaptive", "k")}
+    nnew = opts.get("n_new", 0)
     for gen in range(3):
-        child = ref_ga.breed(pop, gen, seed, pc, pm)
+        child = ref_ga.breed(pop, gen, seed, pc, pm, nnew=nnew, **bopts)
         ce = check.eval_genes(child)["evalue"]
-        want_g, want_e = ref_ga.boom(pop, pe, child, ce)
+        if opts.get("steady"):
+            want_g, want_e = ref_ga.steady(pop, pe, child, ce)
+        else:
+            want_g, want_e = ref_ga.boom(pop, pe, child, ce)
         eng.step()
         pop, pe = eng.read_population(slot, P)
         np.testing.assert_array_equal(pop, want_g)
