@@ -1013,11 +1013,23 @@ extern "C" fxe_status fxe_ga_create(int32_t max_jobs, int32_t precision, fxe_ga*
 
 extern "C" void fxe_ga_destroy(fxe_ga* e) { delete e; }
 
+namespace {
+// Slots of a job's signature set: a power of two at least twice the chromosomes it can take in.
+unsigned long long seen_slots(const fxe_ga_job& job) {
+    const long long P = job.population, nnew = job.n_new > 0 ? job.n_new : job.population;
+    const long long most = P + (long long)(job.generations > 0 ? job.generations : 0) * nnew;
+    unsigned long long n = 64;
+    while (n < 2ull * (unsigned long long)most) n <<= 1;
+    return n;
+}
+}  // namespace
+
 extern "C" fxe_status fxe_ga_job_bytes(const fxe_ga_job* job, int64_t* bytes) {
     g_err.clear();
     if (!job || !job->ctx || !bytes) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
     const int64_t P = job->population, ng = job->ctx->S.n_genes, G = job->generations;
-    *bytes = P * ng * 4 * 3 + P * 8 * 2 + P * (int64_t)sizeof(fxe_cf) + G * P * (ng * 4 + 8) + 16;
+    *bytes = P * ng * 4 * 3 + P * 8 * 2 + P * (int64_t)sizeof(fxe_cf) + G * P * (ng * 4 + 8) + 16 +
+             2 * (P + 8) * (ng * 4 + 8) + (job->duplicates ? 0 : 8 * (int64_t)seen_slots(*job));
     return FXE_OK;
 }
 
@@ -1059,8 +1071,25 @@ extern "C" fxe_status fxe_ga_admit(fxe_ga* e, const fxe_ga_job* job, int32_t* sl
         const size_t G = (size_t)job->generations > 0 ? (size_t)job->generations : 1;
         FXE_TRY(get(sizeof(int32_t) * P * ng * G, &q), "GA snapshots"); J.snap = (int32_t*)q;
         FXE_TRY(get(sizeof(double) * P * G, &q), "GA snapshots"); J.snap_e = (double*)q;
-        FXE_TRY(get(sizeof(int), &q), "GA counter"); J.gen = (int*)q;
-        FXE_TRY(cudaMemsetAsync(J.gen, 0, sizeof(int), e->stream), "GA counter");
+        // gen[0]: generation, gen[1]: pairs in the first candidate batch, gen[2..3]: duplicate
+        // counts, gen[4]: signature 0 seen
+        FXE_TRY(get(sizeof(int) * 8, &q), "GA counter"); J.gen = (int*)q;
+        J.ncand = P + 8;
+        const int gen0[8] = {0, std::min(J.ncand, P / 2 + P / 16 + 8), 0, 0, 0, 0, 0, 0};
+        FXE_TRY(cudaMemcpyAsync(J.gen, gen0, sizeof(gen0), cudaMemcpyHostToDevice, e->stream), "GA counter");
+        FXE_TRY(get(sizeof(int32_t) * 2 * J.ncand * ng, &q), "GA candidates"); J.cand = (int32_t*)q;
+        FXE_TRY(get(sizeof(uint64_t) * 2 * J.ncand, &q), "GA candidates"); J.cand_sig = (uint64_t*)q;
+        J.reject = job->duplicates ? 0 : 1;
+        if (J.reject) {
+            const unsigned long long slots = seen_slots(*job);
+            FXE_TRY(get(sizeof(uint64_t) * slots, &q), "GA signature set"); J.seen = (uint64_t*)q;
+            FXE_TRY(cudaMemsetAsync(J.seen, 0, sizeof(uint64_t) * slots, e->stream), "GA signature set");
+            J.hmask = slots - 1;
+        }
+        J.dec_off = ctx->S.dec_off;
+        J.dec_tab = ctx->S.dec_tab;
+        J.gene_min = ctx->S.gene_min;
+        J.gene_del = ctx->S.gene_del;
         J.seed = job->seed;
         J.cross_rate = job->cross_rate;
         J.mut_rate = job->mut_rate;
@@ -1084,8 +1113,8 @@ extern "C" fxe_status fxe_ga_admit(fxe_ga* e, const fxe_ga_job* job, int32_t* sl
                 "GA records");
         fxe::launch_ga_select(e->d_all, e->d_ids + k, 1, true, e->stream);
         FXE_TRY(cudaGetLastError(), "GA launch");
-        FXE_TRY(cudaStreamSynchronize(e->stream), "GA admission");   // the host copy of J is not kept alive
-        e->launches += 5;
+        FXE_TRY(cudaStreamSynchronize(e->stream), "GA admission");   // gen0 and the host copy of J die here
+        e->launches += 6;
         return FXE_OK;
     }();
     if (st != FXE_OK) {
@@ -1155,7 +1184,7 @@ extern "C" fxe_status fxe_ga_step(fxe_ga* e) {
     }
     if (e->run.empty()) return FXE_OK;
     FXE_TRY(cudaGraphLaunch(e->exec, e->stream), "graph launch");
-    e->launches += 5;
+    e->launches += 6;
     e->graph_launches += 1;
     for (int i : e->run) {
         GaSlot& s = e->slots[i];
@@ -1243,6 +1272,18 @@ extern "C" fxe_status fxe_ga_collect(fxe_ga* e, int32_t slot, double temperature
     }
     for (void* p : s.mem) cudaFree(p);
     s = GaSlot();
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_ga_duplicates(fxe_ga* e, int32_t slot, int64_t* rejected, int64_t* forced) {
+    g_err.clear();
+    if (!e || slot < 0 || slot >= e->max_jobs || !e->slots[slot].used) return fail(FXE_ERR_INVALID_ARGS, "empty slot");
+    if (cudaSetDevice(e->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
+    FXE_TRY(cudaStreamSynchronize(e->stream), "GA step");
+    int gen[4];
+    FXE_TRY(cudaMemcpy(gen, e->slots[slot].J.gen, sizeof(gen), cudaMemcpyDeviceToHost), "GA counter");
+    if (rejected) *rejected = gen[3];
+    if (forced) *forced = gen[2];
     return FXE_OK;
 }
 

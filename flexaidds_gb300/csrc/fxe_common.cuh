@@ -168,7 +168,8 @@ struct GaJob {
     const fxe_cf* child_cf;  // [P] their records
     int32_t* snap;           // [G * P * ng] the population after each generation (the snapshot
     double* snap_e;          // [G * P]       the reference feeds to statmech, LIB/gaboom.cpp:494)
-    int* gen;                // generation counter (device), advanced by selection
+    int* gen;                // [8] device counters: generation (advanced by selection), first
+                             // candidate batch, duplicates forced / rejected, signature 0 seen
     uint64_t seed;
     double cross_rate, mut_rate;
     double k[4];             // adaptive probabilities (adapt_prob, LIB/gaboom.cpp:848-880)
@@ -177,6 +178,19 @@ struct GaJob {
     int steady;              // 1: STEADY replacement, 0: BOOM
     int intragenes;          // crossover points inside genes (1) or at gene boundaries (0)
     int adaptive;            // adaptive crossover and mutation probabilities
+    // duplicate rejection (hash_genes, LIB/gaboom.cpp:977-1018, 1040-1045): candidates are bred
+    // in parallel and accepted in the reference's order against the set of every signature seen
+    int reject;              // 1: reject duplicates (the reference's default, duplicates = false)
+    int ncand;               // candidate pairs bred per generation
+    int32_t* cand;           // [2 * ncand * ng]
+    uint64_t* cand_sig;      // [2 * ncand]
+    uint64_t* seen;          // open-addressing set of signatures (0 = empty), hmask + 1 slots
+    unsigned long long hmask;
+    // genetoic tables of the job's context (signatures are taken on decoded ICs)
+    const int* dec_off;
+    const double* dec_tab;
+    const double* gene_min;
+    const double* gene_del;
 };
 
 // one block's share of the ensemble reduction: running max of the log-weights and the sums

@@ -18,7 +18,9 @@
 // The reference draws from a random_device-seeded generator, so its trajectories cannot be
 // replayed; here every draw is a counter-based hash of (job seed, generation, child, draw), so a
 // job's trajectory depends on its seed alone — the same whether it runs alone or among others.
-// Duplicate rejection (hash_genes) is not applied.
+// Duplicate rejection (LIB/gaboom.cpp:977-1018 and the populate loop, :1936-1978): children and
+// initial chromosomes whose hash_genes signature the job has seen are dropped, as by the
+// reference's default (duplicates = false).
 #include <cstdint>
 
 #include "fxe_common.cuh"
@@ -79,107 +81,229 @@ __device__ __forceinline__ int roulette_linear(int P, double u) {
     return lo;
 }
 
-// Uniform initial genes, [0, 2^31) like the reference's RandomInt over MAX_RANDOM_VALUE.
-__global__ void ga_init_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
-    const GaJob& J = all[run[blockIdx.x]];
-    const int n = J.P * J.ng;
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-        J.child[i] = (int32_t)(mix64(J.seed ^ mix64(0xFFFFFFFFull * 977 + (uint64_t)i)) >> 33);
+// genetoic (LIB/gaboom.cpp:2887-2906): the first running bin total at or above u.
+__device__ __forceinline__ double gene_ic(const GaJob& J, int g, int32_t gene) {
+    const double u = gene / (2147483647.0 + 1.0);
+    int lo = J.dec_off[g], hi = J.dec_off[g + 1];
+    const int base = lo;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (J.dec_tab[mid] < u) lo = mid + 1;
+        else hi = mid;
+    }
+    return J.gene_min[g] + J.gene_del[g] * (double)(lo - base);
 }
 
-// Children of the running generation: pairs (2k, 2k+1) from two roulette draws, crossed with
-// probability cross_rate and mutated bit by bit.
-__global__ void __launch_bounds__(kGaThreads) ga_breed_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
+// hash_genes (LIB/gaboom.cpp:1040-1045) with the C++ library's identity hash of int32.
+__device__ __forceinline__ uint64_t signature(const GaJob& J, const int32_t* genes) {
+    uint64_t h = 0;
+    for (int i = 0; i < J.ng; ++i) {
+        const int32_t v = (int32_t)(gene_ic(J, i, genes[i]) + 0.5);
+        h ^= (uint64_t)(int64_t)v + 0x9e3779b9ull + (h << 6) + (h >> 2);
+    }
+    return h;
+}
+
+// Inserts a signature; false if it was there already. 0 marks an empty slot of the open-addressing
+// table, so the signature 0 is kept in gen[4] instead.
+__device__ bool seen_insert(const GaJob& J, uint64_t h) {
+    if (h == 0) {
+        if (J.gen[4]) return false;
+        J.gen[4] = 1;
+        return true;
+    }
+    unsigned long long i = mix64(h) & J.hmask;
+    for (unsigned long long n = 0; n <= J.hmask; ++n, i = (i + 1) & J.hmask) {
+        const uint64_t v = J.seen[i];
+        if (v == h) return false;
+        if (v == 0) {
+            J.seen[i] = h;
+            return true;
+        }
+    }
+    return true;   // full table: cannot happen, it has twice the slots of the chromosomes a job makes
+}
+
+__device__ __forceinline__ int32_t uniform_gene(const GaJob& J, uint64_t i) {
+    return (int32_t)(mix64(J.seed ^ mix64(0xFFFFFFFFull * 977 + i)) >> 33);
+}
+
+// Initial candidates c0 .. c0 + 2 npairs - 1: uniform genes in [0, 2^31) like the reference's
+// RandomInt over MAX_RANDOM_VALUE; candidate c's gene q is draw c * ng + q.
+__device__ void initial_candidates(const GaJob& J, long long c0, int npairs) {
+    const int ng = J.ng;
+    for (int c = threadIdx.x; c < 2 * npairs; c += blockDim.x) {
+        int32_t* g = J.cand + (size_t)c * ng;
+        for (int q = 0; q < ng; ++q) g[q] = uniform_gene(J, (uint64_t)(c0 + c) * ng + q);
+        J.cand_sig[c] = signature(J, g);
+    }
+}
+
+__global__ void __launch_bounds__(kGaThreads) ga_init_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
     const GaJob& J = all[run[blockIdx.x]];
+    initial_candidates(J, 0, min(J.ncand, J.gen[1]));
+}
+
+// One pair of children of generation g + 1 (pair k of the generation's draw stream): two roulette
+// draws, optional adaptive probabilities, crossover with probability crossp, both children
+// mutated bit by bit.
+__device__ void breed_pair(const GaJob& J, int g, int k, int32_t* john, int32_t* mary) {
     const int P = J.P, ng = J.ng;
-    const int g = *J.gen;
     const uint64_t sb = (uint64_t)(g + 1) << 32;   // streams of generation g + 1
-    const int nnew = J.nnew;
     // fitness statistics of the LINEAR fitness P - rank (fitness_stats, LIB/gaboom.cpp:818-840)
     const double fit_max = (double)P, fit_avg = 0.5 * (double)(P + 1);
-    for (int k = threadIdx.x; 2 * k < nnew; k += blockDim.x) {
-        const uint64_t st = sb + (uint64_t)k;
-        uint64_t d = 0;
-        const int a = roulette_linear(P, uniform(J.seed, st, d++));
-        const int b = roulette_linear(P, uniform(J.seed, st, d++));
-        double crossp = J.cross_rate, mutp = J.mut_rate;
-        if (J.adaptive) {
-            const double f1 = (double)(P - a), f2 = (double)(P - b);
-            const double hi = f1 > f2 ? f1 : f2, lo = f1 > f2 ? f2 : f1;
-            double denom = fit_max - fit_avg;
-            if (denom < 1e-15) denom = 1e-15;   // GA_FITNESS_DENOM_FLOOR, LIB/ga_constants.h:38
-            crossp = hi > fit_avg ? J.k[0] * (fit_max - hi) / denom : J.k[2];
-            mutp = lo > fit_avg ? J.k[1] * (fit_max - lo) / denom : J.k[3];
-        }
-        int32_t* john = J.child + (size_t)(2 * k) * ng;
-        int32_t* mary = 2 * k + 1 < nnew ? J.child + (size_t)(2 * k + 1) * ng : nullptr;
-        int32_t tmp[64];
-        int32_t* m = mary ? mary : tmp;
-        for (int q = 0; q < ng; ++q) {
-            john[q] = J.pop[(size_t)a * ng + q];
-            m[q] = J.pop[(size_t)b * ng + q];
-        }
-        if (uniform(J.seed, st, d++) < crossp) {
-            // LIB/gaboom.cpp:2527-2598
-            int gen_a = (int)(uniform(J.seed, st, d++) * (double)ng);
-            int gen_b = (int)(uniform(J.seed, st, d++) * (double)ng);
-            if (gen_a >= ng) gen_a = ng - 1;
-            if (gen_b >= ng) gen_b = ng - 1;
-            int pnt_a, pnt_b;
-            if (J.intragenes) {
-                pnt_a = (int)(uniform(J.seed, st, d++) * 32.0);
-                pnt_b = (int)(uniform(J.seed, st, d++) * 32.0);
-                if (gen_a > gen_b) {
-                    const int tg = gen_a, tp = pnt_a;
-                    gen_a = gen_b; pnt_a = pnt_b;
-                    gen_b = tg; pnt_b = tp;
-                }
-                if (gen_a == gen_b && pnt_a < pnt_b) {
-                    const int tp = pnt_b;
-                    pnt_b = pnt_a;
-                    pnt_a = tp;
-                }
+    const uint64_t st = sb + (uint64_t)k;
+    uint64_t d = 0;
+    const int a = roulette_linear(P, uniform(J.seed, st, d++));
+    const int b = roulette_linear(P, uniform(J.seed, st, d++));
+    double crossp = J.cross_rate, mutp = J.mut_rate;
+    if (J.adaptive) {
+        const double f1 = (double)(P - a), f2 = (double)(P - b);
+        const double hi = f1 > f2 ? f1 : f2, lo = f1 > f2 ? f2 : f1;
+        double denom = fit_max - fit_avg;
+        if (denom < 1e-15) denom = 1e-15;   // GA_FITNESS_DENOM_FLOOR, LIB/ga_constants.h:38
+        crossp = hi > fit_avg ? J.k[0] * (fit_max - hi) / denom : J.k[2];
+        mutp = lo > fit_avg ? J.k[1] * (fit_max - lo) / denom : J.k[3];
+    }
+    int32_t* m = mary;
+    for (int q = 0; q < ng; ++q) {
+        john[q] = J.pop[(size_t)a * ng + q];
+        m[q] = J.pop[(size_t)b * ng + q];
+    }
+    if (uniform(J.seed, st, d++) < crossp) {
+        // LIB/gaboom.cpp:2527-2598
+        int gen_a = (int)(uniform(J.seed, st, d++) * (double)ng);
+        int gen_b = (int)(uniform(J.seed, st, d++) * (double)ng);
+        if (gen_a >= ng) gen_a = ng - 1;
+        if (gen_b >= ng) gen_b = ng - 1;
+        int pnt_a, pnt_b;
+        if (J.intragenes) {
+            pnt_a = (int)(uniform(J.seed, st, d++) * 32.0);
+            pnt_b = (int)(uniform(J.seed, st, d++) * 32.0);
+            if (gen_a > gen_b) {
+                const int tg = gen_a, tp = pnt_a;
+                gen_a = gen_b; pnt_a = pnt_b;
+                gen_b = tg; pnt_b = tp;
+            }
+            if (gen_a == gen_b && pnt_a < pnt_b) {
+                const int tp = pnt_b;
+                pnt_b = pnt_a;
+                pnt_a = tp;
+            }
+        } else {
+            if (gen_a > gen_b) {
+                const int tg = gen_a;
+                gen_a = gen_b;
+                gen_b = tg;
+            }
+            if (gen_a != gen_b) {
+                pnt_a = uniform(J.seed, st, d++) < 0.5 ? 32 : 0;
+                pnt_b = uniform(J.seed, st, d++) < 0.5 ? 32 : 0;
+                if (gen_b - gen_a == 1 && pnt_a == 0 && pnt_b == 32) pnt_b = pnt_a;
             } else {
-                if (gen_a > gen_b) {
-                    const int tg = gen_a;
-                    gen_a = gen_b;
-                    gen_b = tg;
-                }
-                if (gen_a != gen_b) {
-                    pnt_a = uniform(J.seed, st, d++) < 0.5 ? 32 : 0;
-                    pnt_b = uniform(J.seed, st, d++) < 0.5 ? 32 : 0;
-                    if (gen_b - gen_a == 1 && pnt_a == 0 && pnt_b == 32) pnt_b = pnt_a;
+                pnt_a = 32;
+                pnt_b = 0;
+            }
+        }
+        for (int j = gen_a; j <= gen_b; ++j) {
+            const int np = j == gen_a ? pnt_a : 32;
+            // the reference's mask: 1, then np times optr |= optr << 1
+            const uint32_t optr = np >= 31 ? 0xFFFFFFFFu : ((2u << np) - 1u);
+            const uint32_t uj = (uint32_t)john[j], um = (uint32_t)m[j];
+            john[j] = (int32_t)((uj & ~optr) | (um & optr));
+            m[j] = (int32_t)((uj & optr) | (um & ~optr));
+        }
+        if (pnt_b > 0) {
+            const int np = pnt_b - 1;
+            const uint32_t optr = np >= 31 ? 0xFFFFFFFFu : ((2u << np) - 1u);
+            const uint32_t uj = (uint32_t)john[gen_b], um = (uint32_t)m[gen_b];
+            john[gen_b] = (int32_t)((uj & ~optr) | (um & optr));
+            m[gen_b] = (int32_t)((uj & optr) | (um & ~optr));
+        }
+    }
+    // mutate both children (LIB/gaboom.cpp:2620-2641)
+    for (int c = 0; c < 2; ++c) {
+        int32_t* ch = c == 0 ? john : m;
+        for (int q = 0; q < ng; ++q) {
+            uint32_t optr = 0u;
+            for (int bit = 0; bit < 32; ++bit)
+                if (uniform(J.seed, st, d++) < mutp) optr |= 1u << bit;
+            ch[q] ^= (int32_t)optr;
+        }
+    }
+}
+
+// Pairs k0 .. k0 + npairs - 1 of the running generation's children as candidates, with their
+// signatures.
+__device__ void bred_candidates(const GaJob& J, int g, long long k0, int npairs) {
+    const int ng = J.ng;
+    for (int k = threadIdx.x; k < npairs; k += blockDim.x) {
+        int32_t* john = J.cand + (size_t)(2 * k) * ng;
+        int32_t* mary = john + ng;
+        breed_pair(J, g, (int)(k0 + k), john, mary);
+        J.cand_sig[2 * k] = signature(J, john);
+        J.cand_sig[2 * k + 1] = signature(J, mary);
+    }
+}
+
+__global__ void __launch_bounds__(kGaThreads) ga_breed_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
+    const GaJob& J = all[run[blockIdx.x]];
+    bred_candidates(J, J.gen[0], 0, min(J.ncand, J.gen[1]));
+}
+
+constexpr int kGaMaxBatches = 16;   // candidate batches before duplicates are let through
+
+// Acceptance in the reference's order (child 1, then child 2 of each pair, until the generation
+// has nnew children; the initial population: P chromosomes): a candidate is taken unless its
+// signature was seen before in the job, and taken signatures join the set. Thread 0 walks the
+// batch; when it runs out, the block breeds the next batch of pairs. After kGaMaxBatches batches
+// candidates are taken as they come (counted in gen[2]), where the reference would loop until
+// mutation finds new genes. gen[1] sizes the next generation's first batch from what this one
+// used; gen[3] counts rejected candidates.
+template <bool kInitial>
+__global__ void __launch_bounds__(kGaThreads) ga_accept_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
+    __shared__ int s_done;
+    const GaJob& J = all[run[blockIdx.x]];
+    const int ng = J.ng, g = J.gen[0];
+    const int need = kInitial ? J.P : J.nnew;
+    int npairs = min(J.ncand, J.gen[1]);
+    long long base = 0;   // candidate index of the batch's first entry
+    int i = 0, used = 0, forced = 0, rejected = 0;
+    for (int batch = 0;; ++batch) {
+        if (threadIdx.x == 0) {
+            const bool force = !J.reject || batch >= kGaMaxBatches;
+            int c = 0;
+            for (; c < 2 * npairs; ++c) {
+                if (force || seen_insert(J, J.cand_sig[c])) {
+                    for (int q = 0; q < ng; ++q) J.child[(size_t)i * ng + q] = J.cand[(size_t)c * ng + q];
+                    if (J.reject && force) ++forced;
+                    if (++i == need) break;
                 } else {
-                    pnt_a = 32;
-                    pnt_b = 0;
+                    ++rejected;
                 }
             }
-            for (int j = gen_a; j <= gen_b; ++j) {
-                const int np = j == gen_a ? pnt_a : 32;
-                // the reference's mask: 1, then np times optr |= optr << 1
-                const uint32_t optr = np >= 31 ? 0xFFFFFFFFu : ((2u << np) - 1u);
-                const uint32_t uj = (uint32_t)john[j], um = (uint32_t)m[j];
-                john[j] = (int32_t)((uj & ~optr) | (um & optr));
-                m[j] = (int32_t)((uj & optr) | (um & ~optr));
-            }
-            if (pnt_b > 0) {
-                const int np = pnt_b - 1;
-                const uint32_t optr = np >= 31 ? 0xFFFFFFFFu : ((2u << np) - 1u);
-                const uint32_t uj = (uint32_t)john[gen_b], um = (uint32_t)m[gen_b];
-                john[gen_b] = (int32_t)((uj & ~optr) | (um & optr));
-                m[gen_b] = (int32_t)((uj & optr) | (um & ~optr));
-            }
+            used = (int)(base + c + 1);
+            s_done = i == need;
         }
-        // mutate both children (LIB/gaboom.cpp:2620-2641)
-        for (int c = 0; c < 2; ++c) {
-            int32_t* ch = c == 0 ? john : m;
-            for (int q = 0; q < ng; ++q) {
-                uint32_t optr = 0u;
-                for (int bit = 0; bit < 32; ++bit)
-                    if (uniform(J.seed, st, d++) < mutp) optr |= 1u << bit;
-                ch[q] ^= (int32_t)optr;
-            }
+        __syncthreads();
+        if (s_done) break;
+        base += 2 * npairs;
+        npairs = J.ncand;
+        if (kInitial) initial_candidates(J, base, npairs);
+        else bred_candidates(J, g, base >> 1, npairs);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        int next;
+        if (kInitial) {
+            next = (J.nnew + 1) / 2 + J.nnew / 16 + 8;
+        } else {
+            const int pairs = (used + 1) / 2;
+            next = pairs + pairs / 4 + 8;
         }
+        J.gen[1] = min(J.ncand, next);
+        J.gen[2] += forced;
+        J.gen[3] += rejected;
     }
 }
 
@@ -194,7 +318,7 @@ __global__ void __launch_bounds__(kGaThreads) ga_select_kernel(GaJob* __restrict
     __shared__ int idx[kGaMaxSort];
     GaJob& J = all[run[blockIdx.x]];
     const int P = J.P, ng = J.ng, nnew = J.nnew;
-    const int g = *J.gen;
+    const int g = J.gen[0];
     int32_t* const pop = J.pop;
     int32_t* const nxt = J.pop_next;
     double* const pe = J.pop_e;
@@ -240,15 +364,17 @@ __global__ void __launch_bounds__(kGaThreads) ga_select_kernel(GaJob* __restrict
         J.pop_next = pop;
         J.pop_e = nxt_e;
         J.pop_e_next = pe;
-        if (!kInitial) *J.gen = g + 1;
+        if (!kInitial) J.gen[0] = g + 1;
     }
 }
 
 void launch_ga_init(const GaJob* all, const int* run, int n_jobs, cudaStream_t st) {
     ga_init_kernel<<<n_jobs, kGaThreads, 0, st>>>(all, run);
+    ga_accept_kernel<true><<<n_jobs, kGaThreads, 0, st>>>(all, run);
 }
 void launch_ga_breed(const GaJob* all, const int* run, int n_jobs, cudaStream_t st) {
     ga_breed_kernel<<<n_jobs, kGaThreads, 0, st>>>(all, run);
+    ga_accept_kernel<false><<<n_jobs, kGaThreads, 0, st>>>(all, run);
 }
 void launch_ga_select(GaJob* all, const int* run, int n_jobs, bool initial, cudaStream_t st) {
     if (initial) ga_select_kernel<true><<<n_jobs, kGaThreads, 0, st>>>(all, run);

@@ -66,6 +66,7 @@ def load_library():
                                        C.POINTER(C.c_int64)]
         lib.fxe_ga_population.argtypes = [vp, C.c_int32, _i, _d]
         lib.fxe_ga_take_launches.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        lib.fxe_ga_duplicates.argtypes = [vp, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         lib.fxe_ga_destroy.argtypes = [vp]
         lib.fxe_ga_destroy.restype = None
         lib.fxe_context_destroy.argtypes = [vp]
@@ -220,7 +221,7 @@ class GAJob(C.Structure):
     _fields_ = [("ctx", C.c_void_p), ("population", C.c_int32), ("generations", C.c_int32),
                 ("cross_rate", C.c_double), ("mut_rate", C.c_double), ("seed", C.c_uint64),
                 ("n_new", C.c_int32), ("steady", C.c_int32), ("intragenes", C.c_int32),
-                ("adaptive", C.c_int32), ("k", C.c_double * 4)]
+                ("adaptive", C.c_int32), ("k", C.c_double * 4), ("duplicates", C.c_int32)]
 
 
 class GAEngine:
@@ -236,12 +237,15 @@ class GAEngine:
     @staticmethod
     def job(ev: GPUEvaluator, population: int, generations: int, seed: int,
             cross_rate: float = 0.9, mut_rate: float = 0.01, n_new: int = 0, steady: bool = False,
-            intragenes: bool = False, adaptive: bool = False, k=(1.0, 0.5, 1.0, 0.5)) -> GAJob:
+            intragenes: bool = False, adaptive: bool = False, k=(1.0, 0.5, 1.0, 0.5),
+            duplicates: bool = False) -> GAJob:
         """Defaults follow the reference's: BOOM with boom_fraction 1, crossover at gene
-        boundaries, fixed probabilities (LIB/config_parser.cpp:135-161)."""
+        boundaries, fixed probabilities, duplicate chromosomes rejected
+        (LIB/config_parser.cpp:135-161)."""
         return GAJob(ev.handle.value, int(population), int(generations), float(cross_rate),
                      float(mut_rate), int(seed) & 0xFFFFFFFFFFFFFFFF, int(n_new), int(bool(steady)),
-                     int(bool(intragenes)), int(bool(adaptive)), (C.c_double * 4)(*k))
+                     int(bool(intragenes)), int(bool(adaptive)), (C.c_double * 4)(*k),
+                     int(bool(duplicates)))
 
     def job_bytes(self, job: GAJob) -> int:
         b = C.c_int64(0)
@@ -263,6 +267,12 @@ class GAEngine:
         n = C.c_int32(0)
         _check(self.lib.fxe_ga_finished(self.handle, ptr(out, _i), cap, C.byref(n)))
         return out[:n.value].tolist()
+
+    def duplicates(self, slot: int):
+        """(rejected, forced): candidates dropped as duplicates, and duplicates let through."""
+        a, b = C.c_int64(0), C.c_int64(0)
+        _check(self.lib.fxe_ga_duplicates(self.handle, int(slot), C.byref(a), C.byref(b)))
+        return int(a.value), int(b.value)
 
     def read_population(self, slot: int, population: int):
         ev = self.jobs[slot]

@@ -281,6 +281,9 @@ typedef struct fxe_ga_job {
     int32_t intragenes;      /* 1: crossover points inside genes, 0: at gene boundaries (default) */
     int32_t adaptive;        /* 1: adaptive probabilities from k[0..3] (adapt_prob) */
     double k[4];             /* k1..k4 (the reference's defaults: 1.0, 0.5, 1.0, 0.5) */
+    int32_t duplicates;      /* 0 (the reference's default): a chromosome whose hash_genes
+                                signature the job has produced before is dropped and another bred
+                                (LIB/gaboom.cpp:977-1018, 1040-1045); 1: duplicates allowed */
 } fxe_ga_job;
 
 fxe_status fxe_ga_create(int32_t max_jobs, int32_t precision, fxe_ga** out);
@@ -301,6 +304,9 @@ fxe_status fxe_ga_collect(fxe_ga* ga, int32_t slot, double temperature, int32_t*
                           double* best_energy, fxe_thermo* thermo, int64_t* n_ensemble);
 /* The current population of a job (sorted by energy): P * n_genes genes and P energies. */
 fxe_status fxe_ga_population(fxe_ga* ga, int32_t slot, int32_t* genes, double* energies);
+/* Candidates a job has dropped as duplicates so far, and those taken although seen before
+ * (when 16 batches of candidates in a row held too few new ones; 0 in practice). */
+fxe_status fxe_ga_duplicates(fxe_ga* ga, int32_t slot, int64_t* rejected, int64_t* forced);
 /* Kernels launched and graphs replayed since the previous call (resets both). */
 fxe_status fxe_ga_take_launches(fxe_ga* ga, int64_t* launches, int64_t* graphs);
 void fxe_ga_destroy(fxe_ga* ga);

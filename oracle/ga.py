@@ -4,9 +4,13 @@ TEST INFRASTRUCTURE ONLY: the checker for flexaidds_gb300/csrc/fxe_ga.cu, used b
 
 Operators as the reference defines them — LINEAR fitness (LIB/gaboom.cpp:1627-1635), roulette
 selection (:1158-1186), the reproduce loop's crossover-then-mutate of each pair (:918-960), the
-bit crossover with intragenes (:2517-2614) and bit mutation (:2620-2641), BOOM replacement
+bit crossover with intragenes (:2517-2614) and bit mutation (:2620-2641), duplicate rejection by
+hash_genes signature (:977-1018, 1040-1045, and the populate loop :1936-1978), BOOM replacement
 (:1023-1033) — driven by the counter-based draws the device uses (the reference's own draws come
 from a random_device-seeded generator and cannot be replayed).
+
+Not restated: the device lets duplicates through after 16 batches of candidates in a row without
+enough new ones (the reference loops on); the tests check that this never happened.
 """
 from __future__ import annotations
 
@@ -27,9 +31,44 @@ def uniform(seed: int, stream: int, k: int) -> float:
     return (mix64(seed ^ mix64((stream * 0x100000001B3 + k) & M64)) >> 11) * 2.0 ** -53
 
 
-def initial_genes(seed: int, P: int, ng: int) -> np.ndarray:
-    g = [mix64(seed ^ mix64((0xFFFFFFFF * 977 + i) & M64)) >> 33 for i in range(P * ng)]
-    return np.asarray(g, np.int64).astype(np.int32).reshape(P, ng)
+def signature(ic_row) -> int:
+    """hash_genes (LIB/gaboom.cpp:1040-1045) of one chromosome's decoded ICs; std::hash<int32_t>
+    is the identity, sign-extended to 64 bits."""
+    h = 0
+    for v in ic_row:
+        x = int(float(v) + 0.5) & M64          # (int32_t)(to_ic + 0.5): truncation toward zero
+        h ^= (x + 0x9E3779B9 + ((h << 6) & M64) + (h >> 2)) & M64
+    return h
+
+
+class Rejector:
+    """The set of signatures a job has produced (duplicates = false): `take` says whether a
+    chromosome is new, and remembers it."""
+
+    def __init__(self, desc, allow: bool = False):
+        self.desc, self.allow, self.seen, self.rejected = desc, allow, set(), 0
+
+    def take(self, genes) -> bool:
+        if self.allow:
+            return True
+        sig = signature(self.desc.genes_to_ic(np.asarray(genes, np.uint32).astype(np.int32)[None])[0])
+        if sig in self.seen:
+            self.rejected += 1
+            return False
+        self.seen.add(sig)
+        return True
+
+
+def initial_genes(seed: int, P: int, ng: int, rej: Rejector | None = None) -> np.ndarray:
+    """Uniform chromosomes; candidate c's gene q is draw c * ng + q. With `rej`, candidates whose
+    signature was seen are skipped (the populate loop)."""
+    out, c = [], 0
+    while len(out) < P:
+        g = [mix64(seed ^ mix64((0xFFFFFFFF * 977 + c * ng + q) & M64)) >> 33 for q in range(ng)]
+        c += 1
+        if rej is None or rej.take(g):
+            out.append(g)
+    return np.asarray(out, np.int64).astype(np.int32).reshape(P, ng)
 
 
 def roulette_linear(P: int, u: float) -> int:
@@ -51,76 +90,89 @@ def _mask(np_: int) -> int:
 
 
 def breed(pop: np.ndarray, gen: int, seed: int, cross_rate: float, mut_rate: float, nnew: int = 0,
-          intragenes: bool = False, adaptive: bool = False, k=(1.0, 0.5, 1.0, 0.5)) -> np.ndarray:
-    """nnew children of generation gen + 1 from the sorted population `pop` (P, ng) int32."""
+          intragenes: bool = False, adaptive: bool = False, k=(1.0, 0.5, 1.0, 0.5),
+          rej: Rejector | None = None) -> np.ndarray:
+    """nnew children of generation gen + 1 from the sorted population `pop` (P, ng) int32: pair
+    kk's child 1, then its child 2, each kept unless `rej` has seen it, until there are nnew."""
     P, ng = pop.shape
     nnew = nnew or P
+    out = []
+    kk = 0
+    while len(out) < nnew:
+        for ch in pair(pop, gen, seed, kk, cross_rate, mut_rate, intragenes, adaptive, k):
+            if rej is None or rej.take(ch):
+                out.append(ch)
+                if len(out) == nnew:
+                    break
+        kk += 1
+    return np.asarray(out, np.int64).astype(np.uint32).astype(np.int32)
+
+
+def pair(pop: np.ndarray, gen: int, seed: int, kk: int, cross_rate: float, mut_rate: float,
+         intragenes: bool, adaptive: bool, k):
+    """Pair kk of generation gen + 1's children (two lists of uint32 genes)."""
+    P, ng = pop.shape
     u32 = pop.astype(np.int64) & 0xFFFFFFFF
-    child = np.zeros((nnew, ng), np.int64)
     sb = (gen + 1) << 32
     fit_max, fit_avg = float(P), 0.5 * float(P + 1)
-    for kk in range((nnew + 1) // 2):
-        st = sb + kk
-        d = 0
+    st = sb + kk
+    d = 0
 
-        def draw():
-            nonlocal d
-            v = uniform(seed, st, d)
-            d += 1
-            return v
+    def draw():
+        nonlocal d
+        v = uniform(seed, st, d)
+        d += 1
+        return v
 
-        a = roulette_linear(P, draw())
-        b = roulette_linear(P, draw())
-        crossp, mutp = cross_rate, mut_rate
-        if adaptive:
-            f1, f2 = float(P - a), float(P - b)
-            hi, lo = max(f1, f2), min(f1, f2)
-            denom = max(fit_max - fit_avg, 1e-15)
-            crossp = k[0] * (fit_max - hi) / denom if hi > fit_avg else k[2]
-            mutp = k[1] * (fit_max - lo) / denom if lo > fit_avg else k[3]
-        john = [int(x) for x in u32[a]]
-        mary = [int(x) for x in u32[b]]
-        if draw() < crossp:
-            gen_a = min(int(draw() * ng), ng - 1)
-            gen_b = min(int(draw() * ng), ng - 1)
-            if intragenes:
-                pnt_a = int(draw() * 32.0)
-                pnt_b = int(draw() * 32.0)
-                if gen_a > gen_b:
-                    gen_a, gen_b, pnt_a, pnt_b = gen_b, gen_a, pnt_b, pnt_a
-                if gen_a == gen_b and pnt_a < pnt_b:
-                    pnt_a, pnt_b = pnt_b, pnt_a
+    a = roulette_linear(P, draw())
+    b = roulette_linear(P, draw())
+    crossp, mutp = cross_rate, mut_rate
+    if adaptive:
+        f1, f2 = float(P - a), float(P - b)
+        hi, lo = max(f1, f2), min(f1, f2)
+        denom = max(fit_max - fit_avg, 1e-15)
+        crossp = k[0] * (fit_max - hi) / denom if hi > fit_avg else k[2]
+        mutp = k[1] * (fit_max - lo) / denom if lo > fit_avg else k[3]
+    john = [int(x) for x in u32[a]]
+    mary = [int(x) for x in u32[b]]
+    if draw() < crossp:
+        gen_a = min(int(draw() * ng), ng - 1)
+        gen_b = min(int(draw() * ng), ng - 1)
+        if intragenes:
+            pnt_a = int(draw() * 32.0)
+            pnt_b = int(draw() * 32.0)
+            if gen_a > gen_b:
+                gen_a, gen_b, pnt_a, pnt_b = gen_b, gen_a, pnt_b, pnt_a
+            if gen_a == gen_b and pnt_a < pnt_b:
+                pnt_a, pnt_b = pnt_b, pnt_a
+        else:
+            if gen_a > gen_b:
+                gen_a, gen_b = gen_b, gen_a
+            if gen_a != gen_b:
+                pnt_a = 32 if draw() < 0.5 else 0
+                pnt_b = 32 if draw() < 0.5 else 0
+                if gen_b - gen_a == 1 and pnt_a == 0 and pnt_b == 32:
+                    pnt_b = pnt_a
             else:
-                if gen_a > gen_b:
-                    gen_a, gen_b = gen_b, gen_a
-                if gen_a != gen_b:
-                    pnt_a = 32 if draw() < 0.5 else 0
-                    pnt_b = 32 if draw() < 0.5 else 0
-                    if gen_b - gen_a == 1 and pnt_a == 0 and pnt_b == 32:
-                        pnt_b = pnt_a
-                else:
-                    pnt_a, pnt_b = 32, 0
-            for j in range(gen_a, gen_b + 1):
-                m = _mask(pnt_a if j == gen_a else 32)
-                uj, um = john[j], mary[j]
-                john[j] = (uj & ~m & 0xFFFFFFFF) | (um & m)
-                mary[j] = (uj & m) | (um & ~m & 0xFFFFFFFF)
-            if pnt_b > 0:
-                m = _mask(pnt_b - 1)
-                uj, um = john[gen_b], mary[gen_b]
-                john[gen_b] = (uj & ~m & 0xFFFFFFFF) | (um & m)
-                mary[gen_b] = (uj & m) | (um & ~m & 0xFFFFFFFF)
-        for ch in (john, mary):
-            for q in range(ng):
-                m = 0
-                for bit in range(32):
-                    if draw() < mutp:
-                        m |= 1 << bit
-                ch[q] ^= m
-        child[2 * kk] = john
-        if 2 * kk + 1 < nnew:
-            child[2 * kk + 1] = mary
-    return child.astype(np.uint32).astype(np.int32)
+                pnt_a, pnt_b = 32, 0
+        for j in range(gen_a, gen_b + 1):
+            m = _mask(pnt_a if j == gen_a else 32)
+            uj, um = john[j], mary[j]
+            john[j] = (uj & ~m & 0xFFFFFFFF) | (um & m)
+            mary[j] = (uj & m) | (um & ~m & 0xFFFFFFFF)
+        if pnt_b > 0:
+            m = _mask(pnt_b - 1)
+            uj, um = john[gen_b], mary[gen_b]
+            john[gen_b] = (uj & ~m & 0xFFFFFFFF) | (um & m)
+            mary[gen_b] = (uj & m) | (um & ~m & 0xFFFFFFFF)
+    for ch in (john, mary):
+        for q in range(ng):
+            m = 0
+            for bit in range(32):
+                if draw() < mutp:
+                    m |= 1 << bit
+            ch[q] ^= m
+    return john, mary
 
 
 def steady(pop: np.ndarray, pop_e: np.ndarray, child: np.ndarray, child_e: np.ndarray):

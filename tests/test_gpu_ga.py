@@ -21,24 +21,29 @@ def systems():
     return out
 
 
-# (precision, options): the reference's defaults, then its other operators
+# (precision, mutation rate, options): the reference's defaults, then its other operators; the
+# low mutation rate makes children that repeat a chromosome the job has made (dropped unless
+# duplicates are allowed)
 GA_CASES = [
-    (0, dict()),
-    (1, dict(intragenes=True, adaptive=True, n_new=58)),
-    (0, dict(steady=True, n_new=20, adaptive=True, k=(0.8, 0.3, 0.9, 0.2))),
+    (0, 0.02, dict()),
+    (1, 0.02, dict(intragenes=True, adaptive=True, n_new=58)),
+    (0, 0.02, dict(steady=True, n_new=20, adaptive=True, k=(0.8, 0.3, 0.9, 0.2))),
+    (0, 0.001, dict()),
+    (1, 0.001, dict(duplicates=True, n_new=31)),
 ]
 
 
-@pytest.mark.parametrize("prec,opts", GA_CASES)
-def test_generation_matches_restated_operators(systems, prec, opts):
+@pytest.mark.parametrize("prec,pm,opts", GA_CASES)
+def test_generation_matches_restated_operators(systems, prec, pm, opts):
     d = systems[0]
-    P, seed, pc, pm = 96, 12345, 0.9, 0.02
+    P, seed, pc = 96, 12345, 0.9
     ev = evaluator.GPUEvaluator(d, max_poses=P, precision=prec)
     check = evaluator.GPUEvaluator(d, max_poses=P, precision=prec)
     eng = evaluator.GAEngine(max_jobs=2, precision=prec)
     slot = eng.admit(eng.job(ev, P, 3, seed, pc, pm, **opts), ev)
+    rej = ref_ga.Rejector(d, allow=opts.get("duplicates", False))
     # generation 0: the uniform draws, evaluated and sorted
-    init = ref_ga.initial_genes(seed, P, d.n_genes)
+    init = ref_ga.initial_genes(seed, P, d.n_genes, rej)
     e0 = check.eval_genes(init)["evalue"]
     want_g, want_e = ref_ga.boom(init[:0], e0[:0], init, e0)
     pop, pe = eng.read_population(slot, P)
@@ -48,7 +53,7 @@ def test_generation_matches_restated_operators(systems, prec, opts):
     bopts = {k: v for k, v in opts.items() if k in ("intragenes", "adaptive", "k")}
     nnew = opts.get("n_new", 0)
     for gen in range(3):
-        child = ref_ga.breed(pop, gen, seed, pc, pm, nnew=nnew, **bopts)
+        child = ref_ga.breed(pop, gen, seed, pc, pm, nnew=nnew, rej=rej, **bopts)
         ce = check.eval_genes(child)["evalue"]
         if opts.get("steady"):
             want_g, want_e = ref_ga.steady(pop, pe, child, ce)
@@ -59,6 +64,9 @@ def test_generation_matches_restated_operators(systems, prec, opts):
         np.testing.assert_array_equal(pop, want_g)
         np.testing.assert_array_equal(pe, want_e)
         snaps.append((want_g, want_e))
+        assert eng.duplicates(slot) == (rej.rejected, 0)
+    if pm < 0.01 and not opts.get("duplicates"):
+        assert rej.rejected > 0, "the case was meant to make duplicates"
     assert eng.finished() == [slot]
     # the statmech ensemble: snapshots sorted, near-duplicates removed
     kept = ref_ga.ensemble(snaps, d)
@@ -118,4 +126,4 @@ def test_best_energy_never_rises(systems):
     assert e == best[-1]
     assert np.isfinite(th["free_energy"])
     launches, graphs = eng.take_launches()
-    assert graphs == 12 and launches == 5 + 12 * 5
+    assert graphs == 12 and launches == 6 + 12 * 6

@@ -130,3 +130,39 @@ def test_struct_layouts_match_header():
     assert C.sizeof(capi.CF) == 11 * 8 + 2 * 4
     assert capi.CF_DTYPE.itemsize == C.sizeof(capi.CF)
     assert C.sizeof(capi.Thermo) == 8 * 8
+
+
+# --- GA restatement ---------------------------------------------------------------------------
+
+def test_ga_job_layout_matches_header():
+    from flexaidds_gb300 import evaluator
+    assert C.sizeof(evaluator.GAJob) == 96
+    assert evaluator.GAJob.duplicates.offset == 88
+
+
+def test_hash_genes_signature_known_answers():
+    """hash_genes folds (int32_t)(to_ic + 0.5), sign-extended, into h with the boost-style mix."""
+    from oracle import ga
+    assert ga.signature([0.0]) == 0x9E3779B9
+    assert ga.signature([-1.7]) == 0x9E3779B8            # (int32_t)(-1.2) = -1 wraps to 2^64 - 1
+    h1 = 0x9E3779B9 + 3
+    assert ga.signature([2.6, 0.2]) == h1 ^ ((0x9E3779B9 + (h1 << 6) + (h1 >> 2)) & ga.M64)
+
+
+def test_ga_rejection_keeps_signatures_unique():
+    from oracle import ga
+    d = prepare.prepare(system.make_inputs(600, 6.0, 10, 2, seed=4))
+    rej = ga.Rejector(d)
+    pop = ga.initial_genes(77, 64, d.n_genes, rej)
+    sigs = {ga.signature(r) for r in d.genes_to_ic(pop)}
+    assert len(sigs) == 64
+    for gen in range(3):
+        child = ga.breed(pop, gen, 77, 0.9, 0.001, rej=rej)
+        csig = [ga.signature(r) for r in d.genes_to_ic(child)]
+        assert len(set(csig)) == len(csig) and not sigs.intersection(csig)
+        sigs.update(csig)
+        pop = child
+    assert rej.rejected > 0 and len(rej.seen) == len(sigs)
+    # allowing duplicates takes the candidates in order
+    free = ga.breed(pop, 5, 77, 0.9, 0.001, rej=ga.Rejector(d, allow=True))
+    np.testing.assert_array_equal(free, ga.breed(pop, 5, 77, 0.9, 0.001))
