@@ -267,7 +267,8 @@ void fxe_batch_destroy(fxe_batch* batch);
  * kept, LIB/gaboom.cpp:1023-1033). The graph is captured again only when the set of running
  * jobs changes, so jobs are admitted and retired between generations (continuous batching).
  * Random draws are counter-based hashes of (seed, generation, child, draw): a job's trajectory
- * depends on its seed only, whatever else runs. Duplicate rejection is not applied. */
+ * depends on its seed only, whatever else runs. Chromosomes the job has produced before are
+ * dropped unless the job allows duplicates (fxe_ga_job.duplicates). */
 typedef struct fxe_ga fxe_ga;
 typedef struct fxe_ga_job {
     fxe_context* ctx;        /* the job's system; one running job per context */
