@@ -20,10 +20,16 @@ STATUS_NAMES = {0: "FXE_OK", 1: "FXE_ERR_INVALID_ARGS", 2: "FXE_ERR_ALLOC", 3: "
 POSE_SCORED, POSE_POLYHEDRON_FAILED, POSE_CLASHED, POSE_CAPACITY = 0, 1, 2, 3
 
 
+class FlexResidue(C.Structure):
+    _fields_ = [("first", C.c_int32), ("n_atoms", C.c_int32), ("n_rot", C.c_int32),
+                ("backbone", _b), ("rot_xyz", _f), ("bonded", _b)]
+
+
 class ReceptorDesc(C.Structure):
     _fields_ = [("n_atoms", C.c_int32), ("xyz", _f), ("radius", _f), ("type", _i),
                 ("ori", C.c_float * 3), ("globalmin", C.c_float * 3), ("globalmax", C.c_float * 3),
-                ("maxwidth", C.c_float), ("n_grid", C.c_int32), ("grid_ic", _f)]
+                ("maxwidth", C.c_float), ("n_grid", C.c_int32), ("grid_ic", _f),
+                ("n_flex", C.c_int32), ("flex", C.POINTER(FlexResidue))]
 
 
 class LigandDesc(C.Structure):
@@ -87,6 +93,21 @@ class Packed:
         r.maxwidth = d.maxwidth
         r.n_grid = d.grid_ic.shape[0]
         r.grid_ic = ptr(k(d.grid_ic, np.float32), _f)
+        r.n_flex = d.n_flex
+        if d.n_flex:
+            fr = (FlexResidue * d.n_flex)()
+            a0 = r0 = b0 = 0
+            for i in range(d.n_flex):
+                na, nr = int(d.flex_natm[i]), int(d.flex_nrot[i])
+                fr[i].first = int(d.flex_first[i])
+                fr[i].n_atoms = na
+                fr[i].n_rot = nr
+                fr[i].backbone = ptr(k(d.flex_isbb[a0:a0 + na], np.int8), _b)
+                fr[i].rot_xyz = ptr(k(d.flex_xyz[r0:r0 + nr * na], np.float32), _f)
+                fr[i].bonded = ptr(k(d.flex_bonded[b0:b0 + na * na], np.int8), _b)
+                a0, r0, b0 = a0 + na, r0 + nr * na, b0 + na * na
+            self.keep.append(fr)
+            r.flex = fr
         lg = LigandDesc()
         lg.n_atoms = d.n_lig
         lg.radius = ptr(k(d.lig_radius, np.float32), _f)

@@ -10,9 +10,11 @@
 //   2. IC assignment of ic2cf (LIB/ic2cf.cpp:53-105): grid index, angle, dihedral with the
 //      rec[3] cascade;
 //   3. buildcc over the rebuild list;
-//   4. the cell grid of index_protein for this pose (LIB/Vcontacts.cpp:1584-1645: the
-//      receptor's steady grid, re-derived when a ligand atom leaves the receptor's box), the
-//      ligand atoms' cells and their position in Calclist order (cell, then Calc index).
+//   4. the side-chain atoms of the rotamers the rotamer genes select (LIB/ic2cf.cpp:90-94 and
+//      index_protein's refill of the scored Calc slots, LIB/Vcontacts.cpp:1600-1625);
+//   5. the cell grid of index_protein for this pose (LIB/Vcontacts.cpp:1584-1645: the
+//      receptor's steady grid, re-derived when a mobile atom leaves the receptor's box), the
+//      mobile atoms' cells and their position in Calclist order (cell, then Calc index).
 #include "fxe_common.cuh"
 
 namespace fxe {
@@ -22,7 +24,9 @@ constexpr int kBuildWarps = 4;
 struct BuildShared {
     float ic[kMaxLig][3];
     float pos[kMaxLig][3];
-    int cell[kMaxLig];
+    int cell[kMaxLig];          // per mobile atom
+    float sc[kMaxSc][4];        // side-chain atoms: x, y, z, radius
+    int rot[kMaxFlex];          // rotamer of each flexible residue
     double icv[64];
     int gbin[64];     // bin of each gene's value (its entry in the trigonometry tables)
     int gi;           // grid index of the pose
@@ -98,6 +102,7 @@ __device__ __forceinline__ void build_pose(const DevSystem& S, const DevWork& W,
         sh.bad = 0;
         sh.gi = -1;
     }
+    if (lane < kMaxFlex) sh.rot[lane] = 0;
     __syncwarp();
 
     if (lane == 0) {
@@ -128,6 +133,11 @@ __device__ __forceinline__ void build_pose(const DevSystem& S, const DevWork& W,
                         cat = S.lig_rec[j].w;
                     }
                 }
+                break;
+            }
+            case 4: {
+                const unsigned r = (unsigned)(v + 0.5);
+                if (atm >= 0 && atm < S.n_flex) sh.rot[atm] = (int)r;
                 break;
             }
             default: break;
@@ -201,13 +211,28 @@ __device__ __forceinline__ void build_pose(const DevSystem& S, const DevWork& W,
     }
     __syncwarp();
 
-    // 4. cell grid of this pose
+    // 4. side-chain atoms of the selected rotamers
+    const int nsc = S.n_sc, nm = nsc + nl;
+    if (lane < nsc) {
+        const int r = S.sc_res[lane];
+        const int4 fi = S.flex_info[r];
+        const int rot = sh.rot[r];
+        const float4 q = S.sc_rot[fi.x + rot * fi.z + (lane - fi.y)];
+        sh.sc[lane][0] = q.x;
+        sh.sc[lane][1] = q.y;
+        sh.sc[lane][2] = q.z;
+        sh.sc[lane][3] = q.w;
+    }
+    __syncwarp();
+    auto mpos = [&](int m, int k) -> float { return m < nsc ? sh.sc[m][k] : sh.pos[m - nsc][k]; };
+
+    // 5. cell grid of this pose
     bool below[3] = {false, false, false}, above[3] = {false, false, false};
     float mn[3] = {S.gmin[0], S.gmin[1], S.gmin[2]};
     float mx[3] = {S.gmax[0], S.gmax[1], S.gmax[2]};
-    for (int l = lane; l < nl; l += 32)
+    for (int m = lane; m < nm; m += 32)
         for (int k = 0; k < 3; ++k) {
-            const float v = sh.pos[l][k];
+            const float v = mpos(m, k);
             if (v < mn[k]) { mn[k] = v; below[k] = true; }
             else if (v > mx[k]) { mx[k] = v; above[k] = true; }
         }
@@ -237,24 +262,25 @@ __device__ __forceinline__ void build_pose(const DevSystem& S, const DevWork& W,
         dim = S.dim;
     }
     const int dim2 = dim * dim, dim3 = dim2 * dim;
-    for (int l = lane; l < nl; l += 32) {
-        const int bi = (int)((sh.pos[l][0] - gmin[0]) / kCell) * dim2 + (int)((sh.pos[l][1] - gmin[1]) / kCell) * dim +
-                       (int)((sh.pos[l][2] - gmin[2]) / kCell);
+    for (int m = lane; m < nm; m += 32) {
+        const int bi = (int)((mpos(m, 0) - gmin[0]) / kCell) * dim2 + (int)((mpos(m, 1) - gmin[1]) / kCell) * dim +
+                       (int)((mpos(m, 2) - gmin[2]) / kCell);
         if (bi < 0 || bi >= dim3) sh.bad = 2;
-        sh.cell[l] = bi;
+        sh.cell[m] = bi;
     }
     __syncwarp();
-    const size_t base = (size_t)p * nl;
-    for (int l = lane; l < nl; l += 32) {
-        const int c = sh.cell[l];
+    const size_t base = (size_t)p * nm;
+    for (int m = lane; m < nm; m += 32) {
+        const int c = sh.cell[m];
         int rank = 0;
-        for (int m = 0; m < nl; ++m) {
-            const int cm = sh.cell[m];
-            rank += (cm < c) || (cm == c && m < l);
+        for (int q = 0; q < nm; ++q) {
+            const int cq = sh.cell[q];
+            rank += (cq < c) || (cq == c && q < m);
         }
-        W.lig_pos[base + l] = make_float4(sh.pos[l][0], sh.pos[l][1], sh.pos[l][2], S.lig_radius[l]);
-        W.lig_cell[base + l] = c;
-        W.lig_rank[base + l] = rank;
+        const float rad = m < nsc ? sh.sc[m][3] : S.lig_radius[m - nsc];
+        W.mob_pos[base + m] = make_float4(mpos(m, 0), mpos(m, 1), mpos(m, 2), rad);
+        W.mob_cell[base + m] = c;
+        W.mob_rank[base + m] = rank;
     }
     if (lane == 0) {
         W.pose_grid[p] = make_int4(alter ? 1 : 0, dim, sh.bad, 0);

@@ -54,6 +54,7 @@ fxe_status cuda_fail(cudaError_t e, const char* what) {
 struct DevBlock {
     std::vector<void*> ptrs;
     std::vector<float4> grid_ic;   // host copy of the cleft-grid ICs
+    std::vector<int> flex_nrot;    // rotamers of each flexible side chain
     ~DevBlock() {
         for (void* p : ptrs) cudaFree(p);
     }
@@ -150,15 +151,57 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
     if (lig->n_genes < 0 || lig->n_genes > 1024 || (lig->n_genes && (!lig->gene_type || !lig->gene_atom ||
         !lig->gene_min || !lig->gene_max || !lig->gene_del || !lig->gene_map)))
         return fail(FXE_ERR_INVALID_ARGS, "gene arrays incomplete");
+    // flexible side chains: the receptor's own, or those of the receptor shared
+    std::vector<int> flex_nrot;
+    int n_sc = 0;
+    if (rec) {
+        if (rec->n_flex < 0 || rec->n_flex > fxe::kMaxFlex || (rec->n_flex && !rec->flex))
+            return fail(FXE_ERR_INVALID_ARGS, "at most " + std::to_string(fxe::kMaxFlex) + " flexible side chains");
+        int next = 0;
+        for (int r = 0; r < rec->n_flex; ++r) {
+            const fxe_flex_residue& f = rec->flex[r];
+            if (f.first < next || f.n_atoms < 1 || f.n_atoms > 255 || f.first + f.n_atoms > rec->n_atoms ||
+                f.n_rot < 2 || !f.backbone || !f.rot_xyz || !f.bonded)
+                return fail(FXE_ERR_INVALID_ARGS, "flexible side chain " + std::to_string(r) +
+                                                      ": atoms out of order or range, or fewer than two rotamers");
+            next = f.first + f.n_atoms;
+            int ns = 0;
+            for (int k = 0; k < f.n_atoms; ++k) ns += f.backbone[k] ? 0 : 1;
+            if (ns == 0) return fail(FXE_ERR_INVALID_ARGS, "flexible side chain without side-chain atoms");
+            for (int k = 0; k < f.n_atoms * 3; ++k)
+                if (f.rot_xyz[k] != rec->xyz[(size_t)f.first * 3 + k])
+                    return fail(FXE_ERR_INVALID_ARGS, "rotamer 0 must be the receptor's own coordinates");
+            n_sc += ns;
+            flex_nrot.push_back(f.n_rot);
+        }
+    } else {
+        flex_nrot = share->receptor->flex_nrot;
+        n_sc = share->S.n_sc;
+    }
+    if (n_sc > fxe::kMaxSc)
+        return fail(FXE_ERR_INVALID_ARGS, "more than " + std::to_string(fxe::kMaxSc) + " side-chain atoms");
+    if (n_sc + lig->n_atoms > fxe::kMaxLig)
+        return fail(FXE_ERR_INVALID_ARGS, "side-chain and ligand atoms exceed " + std::to_string(fxe::kMaxLig));
+    std::vector<int> flex_gene(flex_nrot.size(), -1);
     for (int g = 0; g < lig->n_genes; ++g) {
         const int t = lig->gene_type[g];
-        if (t != -1 && t != 0 && t != 1 && t != 2)
-            return fail(FXE_ERR_INVALID_ARGS, "gene type " + std::to_string(t) + " is not supported (grid, distance, angle, dihedral only)");
-        if (lig->gene_atom[g] < 0 || lig->gene_atom[g] >= lig->n_atoms)
-            return fail(FXE_ERR_INVALID_ARGS, "gene atom out of range");
+        if (t != -1 && t != 0 && t != 1 && t != 2 && t != 4)
+            return fail(FXE_ERR_INVALID_ARGS, "gene type " + std::to_string(t) + " is not supported (grid, distance, angle, dihedral, rotamer only)");
         if (!(lig->gene_del[g] > 0.0) || !(lig->gene_max[g] >= lig->gene_min[g]))
             return fail(FXE_ERR_INVALID_ARGS, "gene limits invalid");
+        if (t == 4) {
+            const int r = lig->gene_atom[g];
+            if (r < 0 || r >= (int)flex_nrot.size() || flex_gene[r] >= 0)
+                return fail(FXE_ERR_INVALID_ARGS, "rotamer gene names no flexible side chain, or one twice");
+            if (!(lig->gene_min[g] >= 0.0) || !(lig->gene_max[g] + 0.5 < (double)flex_nrot[r]))
+                return fail(FXE_ERR_INVALID_ARGS, "rotamer gene limits outside the residue's rotamers");
+            flex_gene[r] = g;
+        } else if (lig->gene_atom[g] < 0 || lig->gene_atom[g] >= lig->n_atoms) {
+            return fail(FXE_ERR_INVALID_ARGS, "gene atom out of range");
+        }
     }
+    for (size_t r = 0; r < flex_gene.size(); ++r)
+        if (flex_gene[r] < 0) return fail(FXE_ERR_INVALID_ARGS, "flexible side chain without a rotamer gene");
     for (int i = 0; i < lig->n_build; ++i)
         if (lig->build_order[i] < 0 || lig->build_order[i] >= lig->n_atoms)
             return fail(FXE_ERR_INVALID_ARGS, "build order entry out of range");
@@ -221,10 +264,53 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
         S.maxwidth = rec->maxwidth;
         S.dim = (int)(rec->maxwidth / fxe::kCell) + 1;
         if (S.dim < 3) return fail(FXE_ERR_INVALID_ARGS, "receptor narrower than three cells");
+        // flexible side chains: side-chain atoms leave the steady cell list (they move with the
+        // pose); their rotamers, residue bonded matrices and Calc places go to the device
+        std::vector<int> rec_mob(N, -1), rec_res(N, -1), sc_slot, sc_res, sc_local, bond_off;
+        std::vector<float4> sc_rot;
+        std::vector<int4> finfo;
+        std::vector<int8_t> fbonded;
+        for (int r = 0; r < rec->n_flex; ++r) {
+            const fxe_flex_residue& f = rec->flex[r];
+            const int sc0 = (int)sc_slot.size();
+            for (int k = 0; k < f.n_atoms; ++k) {
+                rec_res[f.first + k] = (r << 8) | k;
+                if (f.backbone[k]) continue;
+                rec_mob[f.first + k] = (int)sc_slot.size();
+                sc_slot.push_back(f.first + k);
+                sc_res.push_back(r);
+                sc_local.push_back(k);
+            }
+            const int nsr = (int)sc_slot.size() - sc0;
+            finfo.push_back(make_int4((int)sc_rot.size(), sc0, nsr, f.n_atoms));
+            for (int q = 0; q < f.n_rot; ++q)
+                for (int k = 0; k < f.n_atoms; ++k) {
+                    if (f.backbone[k]) continue;
+                    const float* x = f.rot_xyz + ((size_t)q * f.n_atoms + k) * 3;
+                    sc_rot.push_back(make_float4(x[0], x[1], x[2], rec->radius[f.first + k]));
+                }
+            bond_off.push_back((int)fbonded.size());
+            fbonded.insert(fbonded.end(), f.bonded, f.bonded + (size_t)f.n_atoms * f.n_atoms);
+        }
+        S.n_flex = rec->n_flex;
+        S.n_sc = (int)sc_slot.size();
+        ctx->receptor->flex_nrot = flex_nrot;
+        if (S.n_flex) {
+            FXE_TRY(ctx->upload_receptor(&S.sc_slot, sc_slot.data(), sc_slot.size()), "side-chain upload");
+            FXE_TRY(ctx->upload_receptor(&S.sc_res, sc_res.data(), sc_res.size()), "side-chain upload");
+            FXE_TRY(ctx->upload_receptor(&S.sc_local, sc_local.data(), sc_local.size()), "side-chain upload");
+            FXE_TRY(ctx->upload_receptor(&S.rec_mob, rec_mob.data(), N), "side-chain upload");
+            FXE_TRY(ctx->upload_receptor(&S.rec_res, rec_res.data(), N), "side-chain upload");
+            FXE_TRY(ctx->upload_receptor(&S.sc_rot, sc_rot.data(), sc_rot.size()), "side-chain upload");
+            FXE_TRY(ctx->upload_receptor(&S.flex_info, finfo.data(), finfo.size()), "side-chain upload");
+            FXE_TRY(ctx->upload_receptor(&S.flex_bond_off, bond_off.data(), bond_off.size()), "side-chain upload");
+            FXE_TRY(ctx->upload_receptor(&S.flex_bonded, fbonded.data(), fbonded.size()), "side-chain upload");
+        }
         const int dim = S.dim, dim2 = dim * dim;
         const long dim3 = (long)dim2 * dim;
         std::vector<int> cell(N), start(dim3 + 1, 0);
         for (int i = 0; i < N; ++i) {
+            if (rec_mob[i] >= 0) continue;
             const long bi = (long)(int)((pos[i].x - S.gmin[0]) / fxe::kCell) * dim2 +
                             (long)(int)((pos[i].y - S.gmin[1]) / fxe::kCell) * dim +
                             (int)((pos[i].z - S.gmin[2]) / fxe::kCell);
@@ -233,16 +319,18 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
             ++start[bi + 1];
         }
         for (long b = 0; b < dim3; ++b) start[b + 1] += start[b];
-        std::vector<int> fill(start.begin(), start.end() - 1), catom(N);
-        std::vector<float4> cpos(N);
+        const int n_rigid = N - S.n_sc;
+        std::vector<int> fill(start.begin(), start.end() - 1), catom(n_rigid);
+        std::vector<float4> cpos(n_rigid);
         for (int i = 0; i < N; ++i) {
+            if (rec_mob[i] >= 0) continue;
             const int w = fill[cell[i]]++;
             catom[w] = i;
             cpos[w] = pos[i];
         }
         FXE_TRY(ctx->upload_receptor(&S.cell_start, start.data(), dim3 + 1), "cell list upload");
-        FXE_TRY(ctx->upload_receptor(&S.cell_atom, catom.data(), N), "cell list upload");
-        FXE_TRY(ctx->upload_receptor(&S.cell_pos, cpos.data(), N), "cell list upload");
+        FXE_TRY(ctx->upload_receptor(&S.cell_atom, catom.data(), n_rigid), "cell list upload");
+        FXE_TRY(ctx->upload_receptor(&S.cell_pos, cpos.data(), n_rigid), "cell list upload");
         // cleft grid
         std::vector<float4> gic(rec->n_grid);
         for (int g = 0; g < rec->n_grid; ++g)
@@ -364,6 +452,7 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
             FXE_TRY(ctx->upload(&S.trig_off, off.data(), 2 * n), "trig upload");
             FXE_TRY(ctx->upload(&S.trig_cnt, cnt.data(), 2 * n), "trig upload");
         }
+        if (!flex_gene.empty()) FXE_TRY(ctx->upload(&S.flex_gene, flex_gene.data(), flex_gene.size()), "gene upload");
         FXE_TRY(ctx->upload(&S.gene_type, lig->gene_type, ng), "gene upload");
         FXE_TRY(ctx->upload(&S.gene_atom, lig->gene_atom, ng), "gene upload");
         FXE_TRY(ctx->upload(&S.gene_min, lig->gene_min, ng), "gene upload");
@@ -384,12 +473,12 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
         S.solventterm = prm->solventterm;
         // workspace
         fxe::DevWork& W = ctx->W;
-        const size_t P = (size_t)max_poses, PL = P * n, PLC = PL * fxe::kMaxCand;
+        const size_t P = (size_t)max_poses, PL = P * (size_t)(S.n_sc + n), PLC = PL * fxe::kMaxCand;
         W.max_poses = max_poses;
         FXE_TRY(ctx->alloc(&W.ic, P * (ng > 0 ? ng : 1)), "workspace");
-        FXE_TRY(ctx->alloc(&W.lig_pos, PL), "workspace");
-        FXE_TRY(ctx->alloc(&W.lig_cell, PL), "workspace");
-        FXE_TRY(ctx->alloc(&W.lig_rank, PL), "workspace");
+        FXE_TRY(ctx->alloc(&W.mob_pos, PL), "workspace");
+        FXE_TRY(ctx->alloc(&W.mob_cell, PL), "workspace");
+        FXE_TRY(ctx->alloc(&W.mob_rank, PL), "workspace");
         FXE_TRY(ctx->alloc(&W.pose_grid, P), "workspace");
         FXE_TRY(ctx->alloc(&W.pose_gmin, P), "workspace");
         FXE_TRY(ctx->alloc(&W.cand_idx, PLC), "workspace");
@@ -545,9 +634,9 @@ extern "C" fxe_status fxe_context_take_timing(fxe_context* ctx, double* ms3, int
 extern "C" fxe_status fxe_last_contacts(fxe_context* ctx, int32_t pose, int32_t atom, int32_t cap,
                                         int32_t* partner, float* area, int32_t* n_out) {
     g_err.clear();
-    if (!ctx || !n_out || pose < 0 || pose >= ctx->last_n || atom < 0 || atom >= ctx->S.n_lig || cap < 0)
+    if (!ctx || !n_out || pose < 0 || pose >= ctx->last_n || atom < 0 || atom >= ctx->S.n_sc + ctx->S.n_lig || cap < 0)
         return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
-    const size_t lb = (size_t)pose * ctx->S.n_lig + atom;
+    const size_t lb = (size_t)pose * (ctx->S.n_sc + ctx->S.n_lig) + atom;
     int nc = 0;
     FXE_TRY(cudaMemcpy(&nc, ctx->W.cand_n + lb, sizeof(int), cudaMemcpyDeviceToHost), "contacts");
     *n_out = 0;
@@ -577,7 +666,8 @@ extern "C" fxe_status fxe_last_ligand_xyz(fxe_context* ctx, int32_t pose, float*
     if (!ctx || !xyz || pose < 0 || pose >= ctx->last_n) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
     const int n = ctx->S.n_lig;
     std::vector<float4> v(n);
-    FXE_TRY(cudaMemcpy(v.data(), ctx->W.lig_pos + (size_t)pose * n, n * sizeof(float4), cudaMemcpyDeviceToHost),
+    FXE_TRY(cudaMemcpy(v.data(), ctx->W.mob_pos + (size_t)pose * (ctx->S.n_sc + n) + ctx->S.n_sc, n * sizeof(float4),
+                       cudaMemcpyDeviceToHost),
             "ligand coordinates");
     for (int l = 0; l < n; ++l) {
         xyz[3 * l] = v[l].x;
@@ -838,7 +928,7 @@ fxe_status batch_launch(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, cudaS
         J.n = jobs[i].n;
         J.warp0 = items;
         total += jobs[i].n;
-        items += (long long)jobs[i].n * ctx->S.n_lig;
+        items += (long long)jobs[i].n * (ctx->S.n_sc + ctx->S.n_lig);
         ctx->last_n = jobs[i].n;
         prec = ctx->precision;
     }
@@ -1163,7 +1253,7 @@ extern "C" fxe_status fxe_ga_step(fxe_ga* e) {
             J.n = s.J.nnew;
             J.warp0 = items;
             total += J.n;
-            items += (long long)J.n * s.ctx->S.n_lig;
+            items += (long long)J.n * (s.ctx->S.n_sc + s.ctx->S.n_lig);
         }
         FXE_TRY(cudaMemcpyAsync(e->d_run, e->run.data(), sizeof(int) * n, cudaMemcpyHostToDevice, e->stream), "GA table");
         FXE_TRY(cudaMemcpyAsync(e->d_eval, ev.data(), sizeof(fxe::Job) * n, cudaMemcpyHostToDevice, e->stream), "GA table");

@@ -32,8 +32,10 @@ constexpr int kMaxEdges = 200;  // the reference aborts the hull walk at 200 edg
 // has at most about 135 vertices, a complete one with its arc points about 105
 constexpr int kMaxVerts = 176;
 constexpr int kMaxFacePts = 640;
-constexpr int kMaxLig = 128;    // ligand atoms per pose (bit masks, shared staging)
+constexpr int kMaxLig = 128;    // scored atoms per pose: ligand + side chains (bit masks, staging)
 constexpr int kMaskWords = kMaxLig / 32;
+constexpr int kMaxSc = 32;      // scored side-chain atoms per pose (one per lane)
+constexpr int kMaxFlex = 8;     // flexible side chains
 
 // candidate flag bits
 constexpr uint8_t kOnHull = 1;    // plane flag != 'X'
@@ -90,6 +92,22 @@ struct DevSystem {
     const int* trig_src;         // [n_lig * 2]
     const int* trig_off;         // [n_lig * 2]
     const int* trig_cnt;         // [n_lig * 2]
+    // flexible side chains. Their non-backbone atoms ("side-chain atoms") are scored: with the
+    // ligand atoms they form the pose's mobile atoms, side-chain atoms first (Calc order), then
+    // the ligand (mobile index n_sc + l). Mobile atoms are re-placed every pose; the other
+    // receptor atoms, the backbone of flexible residues included, stay where they are.
+    int n_sc;
+    int n_flex;
+    const int* sc_slot;          // [n_sc] Calc index
+    const int* sc_res;           // [n_sc] residue (0..n_flex-1)
+    const int* sc_local;         // [n_sc] index among the residue's atoms
+    const int* rec_mob;          // [n_rec] mobile index of a side-chain atom, -1 for the others
+    const int* rec_res;          // [n_rec] residue << 8 | index in it, for atoms of flexible residues, else -1
+    const float4* sc_rot;        // per residue: [n_rot][its side-chain atoms] x, y, z, radius
+    const int4* flex_info;       // [n_flex] (first sc_rot entry, first mobile index, side-chain atoms, atoms)
+    const int* flex_gene;        // [n_flex] the residue's rotamer gene
+    const int* flex_bond_off;    // [n_flex] offset of the residue's bonded matrix
+    const int8_t* flex_bonded;
     // energy matrix
     int ntypes;
     const int* em_weight;
@@ -106,32 +124,60 @@ struct DevSystem {
 struct DevWork {
     int max_poses;
     double* ic;            // [P * n_genes]
-    float4* lig_pos;       // [P * n_lig] x, y, z, radius
-    int* lig_cell;         // [P * n_lig]
-    int* lig_rank;         // [P * n_lig] position among the ligand atoms in Calclist order
+    // per (pose, mobile atom): P * (n_sc + n_lig) entries
+    float4* mob_pos;       // x, y, z, radius
+    int* mob_cell;
+    int* mob_rank;         // position among the mobile atoms in Calclist order
     int4* pose_grid;       // [P] (altered, dim, 0, 0)
     float4* pose_gmin;     // [P]
-    int* cand_idx;         // [P * n_lig * kMaxCand]
-    float* cand_d2;        // [P * n_lig * kMaxCand]
-    double* cand_area;     // [P * n_lig * kMaxCand]
-    uint8_t* cand_flag;    // [P * n_lig * kMaxCand]
-    int* cand_n;           // [P * n_lig]
-    double* clash_part;    // [P * n_lig]
+    int* cand_idx;         // [P * n_mob * kMaxCand]
+    float* cand_d2;        // [P * n_mob * kMaxCand]
+    double* cand_area;     // [P * n_mob * kMaxCand]
+    uint8_t* cand_flag;    // [P * n_mob * kMaxCand]
+    int* cand_n;           // [P * n_mob]
+    double* clash_part;    // [P * n_mob]
     int* pose_seed;        // [P * kMaxLig * 3] polyhedron seeds left by earlier atoms
-    uint32_t* pose_rec;    // [P * kMaxLig * kMaskWords] ligand partners each processed atom kept
+    uint32_t* pose_rec;    // [P * kMaxLig * kMaskWords] mobile partners each processed atom kept
     fxe_cf* out;           // [P]
     int* counters;         // [4]: unused, hull failures, capacity, no-partner faces
 };
 
 // One job of a batched launch: a context's system and workspace (W.out pointing at the job's
 // own output records), the job's chromosomes, and where its poses sit in the launch.
+// Mobile atoms: the side-chain atoms (0 .. n_sc-1, Calc order), then the ligand atoms.
+__device__ __forceinline__ int n_mobile(const DevSystem& S) { return S.n_sc + S.n_lig; }
+
+// Calc index -> mobile index, or -1 for a receptor atom that stays in place.
+__device__ __forceinline__ int mobile_of(const DevSystem& S, int j) {
+    return j >= S.n_rec ? S.n_sc + (j - S.n_rec) : (S.n_sc ? S.rec_mob[j] : -1);
+}
+
+// Mobile index -> Calc index.
+__device__ __forceinline__ int slot_of(const DevSystem& S, int m) {
+    return m < S.n_sc ? S.sc_slot[m] : S.n_rec + (m - S.n_sc);
+}
+
+// How mobile atom m and the atom at Calc index j relate through their residue: 0 other
+// residues, 1 one residue and at most bloops bonds apart (residue.bonded >= 0), 2 one residue
+// and further apart.
+__device__ __forceinline__ int residue_pair(const DevSystem& S, int m, int j) {
+    if (m >= S.n_sc) {
+        if (j < S.n_rec) return 0;
+        return S.bonded[(m - S.n_sc) * S.n_lig + (j - S.n_rec)] >= 0 ? 1 : 2;
+    }
+    if (j >= S.n_rec) return 0;
+    const int rr = S.rec_res[j], r = S.sc_res[m];
+    if (rr < 0 || (rr >> 8) != r) return 0;
+    return S.flex_bonded[S.flex_bond_off[r] + S.sc_local[m] * S.flex_info[r].w + (rr & 255)] >= 0 ? 1 : 2;
+}
+
 struct Job {
     DevSystem S;
     DevWork W;
     const int32_t* genes;  // [n * S.n_genes]
     int pose0;             // first pose of the job in the launch
     int n;                 // poses of the job
-    long long warp0;       // first (pose, ligand atom) item of the job in the contact launch
+    long long warp0;       // first (pose, mobile atom) item of the job in the contact launch
 };
 
 // Index of the job holding launch item `key` (a pose, or a (pose, atom) item when by_warp):

@@ -1,11 +1,13 @@
-// fxe_contacts.cu — contact candidates of every (pose, ligand atom).
+// fxe_contacts.cu — contact candidates of every (pose, mobile atom).
 //
-// contacts_kernel, one warp per (pose, ligand atom): the 27-cell scan of get_contlist4
-// (LIB/Vcontacts.cpp:1725-1839) over the receptor's cell list and the pose's ligand atoms, in
-// the reference's candidate order (cells in scan order, atoms in Calc order within a cell),
+// contacts_kernel, one warp per (pose, mobile atom): the 27-cell scan of get_contlist4
+// (LIB/Vcontacts.cpp:1725-1839) over the receptor's cell list of rigid atoms and the pose's
+// mobile atoms (side-chain atoms at their Calc places among the rigid atoms, then the ligand),
+// in the reference's candidate order (cells in scan order, atoms in Calc order within a cell),
 // with the reference's single-precision squared distance and its double-precision cut-off test,
-// plus the atom's share of the clash pre-filter (LIB/Vcontacts.cpp:36-51): receptor partners
-// and the ligand partners processed after it in Calclist order.
+// plus the atom's share of the clash pre-filter (LIB/Vcontacts.cpp:36-51): rigid partners and
+// the mobile partners processed after it in Calclist order, pairs of one residue within bloops
+// bonds left out.
 #include "fxe_common.cuh"
 
 namespace fxe {
@@ -22,8 +24,8 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // contacts_kernel
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork& W, int p, int a, int lane) {
-    const int nl = S.n_lig;
-    const size_t lb = (size_t)p * nl;
+    const int nsc = S.n_sc, nm = nsc + S.n_lig;
+    const size_t lb = (size_t)p * nm;
     const int4 pg = W.pose_grid[p];
     const size_t cb = (lb + a) * kMaxCand;
     if (pg.z) {  // the pose left the grid the reference can index
@@ -33,28 +35,30 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
         }
         return;
     }
-    const float4 me = W.lig_pos[lb + a];
+    const float4 me = W.mob_pos[lb + a];
     const float rado = me.w + kRw;
-    const int my_rank = W.lig_rank[lb + a];
+    const int my_rank = W.mob_rank[lb + a];
     const int dim = pg.y, dim2 = dim * dim, dim3 = dim2 * dim;
-    const int box0 = W.lig_cell[lb + a];
-    // ligand atoms held by this lane (atom lane + 32 * slot): cell offset key 0..26 or -1
+    const int box0 = W.mob_cell[lb + a];
+    // mobile atoms held by this lane (atom lane + 32 * slot): cell offset key 0..26 or -1; the
+    // side-chain atoms (fewer than 33) are the lanes of slot 0
     int key[kMaxLig / 32];
     float4 lpos[kMaxLig / 32];
 #pragma unroll
     for (int s = 0; s < kMaxLig / 32; ++s) {
-        const int l = lane + 32 * s;
+        const int m = lane + 32 * s;
         key[s] = -1;
         lpos[s] = make_float4(0, 0, 0, 0);
-        if (l < nl) {
-            lpos[s] = W.lig_pos[lb + l];
-            const int o = W.lig_cell[lb + l] - box0 + dim2 + dim + 1;
+        if (m < nm) {
+            lpos[s] = W.mob_pos[lb + m];
+            const int o = W.mob_cell[lb + m] - box0 + dim2 + dim + 1;
             if (o >= 0) {
                 const int di = o / dim2, rem = o - di * dim2, dj = rem / dim, dk = rem - dj * dim;
                 if (di <= 2 && dj <= 2 && dk <= 2) key[s] = di * 9 + dj * 3 + dk;
             }
         }
     }
+    const int my_slot = lane < nsc ? S.sc_slot[lane] : 0;
     const float4 gm = W.pose_gmin[p];
     int nc = 0;
     double clash = 0.0;
@@ -75,52 +79,79 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
                 W.cand_idx[cb + w] = j;
                 W.cand_d2[cb + w] = sq;
             }
-            // clash pre-filter share: receptor partners, and ligand partners processed later
-            const bool later = j < S.n_rec || W.lig_rank[lb + (j - S.n_rec)] > my_rank;
+            // clash pre-filter share: rigid partners, and mobile partners processed later
+            const int mj = mobile_of(S, j);
+            const bool later = mj < 0 || W.mob_rank[lb + mj] > my_rank;
             if (later) {
                 const double rAB = (double)__fadd_rn(me.w, pj.w);
                 const double cd = permea * rAB;
                 const double dist = sqrt((double)sq);
-                if (dist < cd) {
-                    const bool intra = j >= S.n_rec;
-                    if (!intra || S.bonded[a * nl + (j - S.n_rec)] < 0)
-                        clash += (double)kKwall * (pow(dist, -12.0) - pow(cd, -12.0));
-                }
+                if (dist < cd && residue_pair(S, a, j) != 1)
+                    clash += (double)kKwall * (pow(dist, -12.0) - pow(cd, -12.0));
             }
         }
         nc += __popc(m);
     };
+    // rigid atoms of one cell in Calc order, entries [k0, k1) of the cell list (or, on a grid
+    // re-derived for this pose, Calc indices [k0, k1) that fall into cell bi)
+    auto scan_rigid = [&](int k0, int k1, int bi) {
+        for (int kb = k0; kb < k1; kb += 32) {
+            const int k = kb + lane;
+            bool in = k < k1;
+            int j = 0;
+            float4 pj = make_float4(0, 0, 0, 0);
+            if (!pg.x) {
+                if (in) {
+                    j = S.cell_atom[k];
+                    pj = S.cell_pos[k];
+                }
+            } else if (in) {
+                j = k;
+                pj = S.rec_pos[k];
+                const int cb2 = (int)((pj.x - gm.x) / kCell) * dim2 + (int)((pj.y - gm.y) / kCell) * dim +
+                                (int)((pj.z - gm.z) / kCell);
+                in = cb2 == bi && (nsc == 0 || S.rec_mob[k] < 0);
+            }
+            consider(in, j, pj);
+        }
+    };
     for (int i = 0; i < 27; ++i) {
         const int bi = box0 + dim2 * ((i / 9) - 1) + dim * (((i / 3) % 3) - 1) + (i % 3) - 1;
         if (bi < 0 || bi >= dim3) continue;
+        int k0, k1;
         if (!pg.x) {
-            const int s0 = S.cell_start[bi], s1 = S.cell_start[bi + 1];
-            for (int k0 = s0; k0 < s1; k0 += 32) {
-                const int k = k0 + lane;
-                const bool in = k < s1;
-                const int j = in ? S.cell_atom[k] : 0;
-                const float4 pj = in ? S.cell_pos[k] : make_float4(0, 0, 0, 0);
-                consider(in, j, pj);
-            }
+            k0 = S.cell_start[bi];
+            k1 = S.cell_start[bi + 1];
         } else {
-            // a grid re-derived for this pose: scan every receptor atom for cell bi
-            for (int k0 = 0; k0 < S.n_rec; k0 += 32) {
-                const int k = k0 + lane;
-                bool in = false;
-                float4 pj = make_float4(0, 0, 0, 0);
-                if (k < S.n_rec) {
-                    pj = S.rec_pos[k];
-                    const int cb2 = (int)((pj.x - gm.x) / kCell) * dim2 + (int)((pj.y - gm.y) / kCell) * dim +
-                                    (int)((pj.z - gm.z) / kCell);
-                    in = cb2 == bi;
-                }
-                consider(in, k, pj);
-            }
+            k0 = 0;
+            k1 = S.n_rec;
         }
+        // side-chain atoms in this cell take their Calc places among the rigid atoms
+        unsigned scm = __ballot_sync(kFull, lane < nsc && key[0] == i);
+        while (scm) {
+            const int q = __ffs(scm) - 1;
+            scm &= scm - 1;
+            const int qs = __shfl_sync(kFull, my_slot, q);
+            int split = qs;
+            if (!pg.x) {   // rigid entries of the cell before Calc index qs
+                split = k0;
+                for (int kb = k0; kb < k1; kb += 32) {
+                    const int k = kb + lane;
+                    const unsigned lt = __ballot_sync(kFull, k < k1 && S.cell_atom[k] < qs);
+                    split += __popc(lt);
+                    if (lt != kFull) break;
+                }
+            }
+            scan_rigid(k0, split, bi);
+            consider(lane == q, qs, lpos[0]);
+            k0 = split;
+        }
+        scan_rigid(k0, k1, bi);
 #pragma unroll
         for (int s = 0; s < kMaxLig / 32; ++s) {
-            if (32 * s >= nl) break;
-            consider(key[s] == i, S.n_rec + lane + 32 * s, lpos[s]);
+            if (32 * s >= nm) break;
+            const int m = lane + 32 * s;
+            consider(key[s] == i && m >= nsc, S.n_rec + (m - nsc), lpos[s]);
         }
     }
     clash = warp_sum_d(clash);
@@ -133,12 +164,12 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
 __global__ void __launch_bounds__(128)
 contacts_kernel(DevSystem S, DevWork W, int n) {
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nl = S.n_lig;
-    if (gw >= n * nl) return;
-    contacts_atom(S, W, gw / nl, gw % nl, threadIdx.x & 31);
+    const int nm = n_mobile(S);
+    if (gw >= n * nm) return;
+    contacts_atom(S, W, gw / nm, gw % nm, threadIdx.x & 31);
 }
 
-// The same over the (pose, ligand atom) items of several jobs.
+// The same over the (pose, mobile atom) items of several jobs.
 __global__ void __launch_bounds__(128)
 contacts_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, long long total) {
     __shared__ Job job_all[4];
@@ -148,13 +179,13 @@ contacts_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, long long total) 
     const int j = find_job(jobs, n_jobs, gw, true);
     Job& job = job_all[wib];
     copy_job(&job, &jobs[j], lane);
-    const int nl = job.S.n_lig;
+    const int nm = n_mobile(job.S);
     const long long r = gw - job.warp0;
-    contacts_atom(job.S, job.W, (int)(r / nl), (int)(r % nl), lane);
+    contacts_atom(job.S, job.W, (int)(r / nm), (int)(r % nm), lane);
 }
 
 void launch_contacts(const DevSystem& S, const DevWork& W, int n, cudaStream_t st) {
-    const long warps = (long)n * S.n_lig;
+    const long warps = (long)n * (S.n_sc + S.n_lig);
     contacts_kernel<<<(unsigned)((warps + 3) / 4), 128, 0, st>>>(S, W, n);
 }
 

@@ -1011,13 +1011,15 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
 // leaves the order of the remaining planes, and so every tie-break, as in the shorter list.
 __device__ void load_planes(VorShared& sh, const DevSystem& S, const DevWork& W, int p, int a,
                             int NC, float4 me, float rado, const uint32_t* excl, int lane) {
-    const size_t cb = ((size_t)p * S.n_lig + a) * kMaxCand;
+    const int nm = n_mobile(S);
+    const size_t cb = ((size_t)p * nm + a) * kMaxCand;
     const float rr = rado * rado;          // single-precision products, as in the reference
     for (int c = lane; c < NC; c += 32) {
         const int j = W.cand_idx[cb + c];
         const float d2 = W.cand_d2[cb + c];
         sh.cidx[c] = j;
-        const float4 pj = j < S.n_rec ? S.rec_pos[j] : W.lig_pos[(size_t)p * S.n_lig + (j - S.n_rec)];
+        const int mj = mobile_of(S, j);
+        const float4 pj = mj < 0 ? S.rec_pos[j] : W.mob_pos[(size_t)p * nm + mj];
         const bool ex = ((excl[c >> 5] >> (c & 31)) & 1u) || d2 < 1e-20f;
         if (ex) {
             sh.pl[c] = make_real4(real(0.0), real(0.0), real(0.0), -real(1e30));
@@ -1049,8 +1051,9 @@ __device__ void load_planes(VorShared& sh, const DevSystem& S, const DevWork& W,
 }
 
 __device__ double pose_clash_sum(const DevSystem& S, const DevWork& W, int p, int lane) {
+    const int nm = n_mobile(S);
     double s = 0.0;
-    for (int l = lane; l < S.n_lig; l += 32) s += W.clash_part[(size_t)p * S.n_lig + l];
+    for (int m = lane; m < nm; m += 32) s += W.clash_part[(size_t)p * nm + m];
     return warp_sum(s);
 }
 
@@ -1064,8 +1067,8 @@ __device__ double pose_clash_sum(const DevSystem& S, const DevWork& W, int p, in
 #define FXE_SEEDS_SHARED (FXE_REFERENCE_FORMULAS)
 struct PoseShared {
     VorShared v;
-    uint8_t order[kMaxLig];          // ligand atoms in Calclist order
-    uint32_t done[kMaskWords];       // ligand atoms whose contacts are saved
+    uint8_t order[kMaxLig];          // mobile atoms in Calclist order
+    uint32_t done[kMaskWords];       // mobile atoms whose contacts are saved
 #if FXE_SEEDS_SHARED
     int seed[kMaxLig][3];
     uint32_t rec[kMaxLig][kMaskWords];
@@ -1101,8 +1104,8 @@ __device__ void finish_failed(const DevWork& W, int p, int lane, int status, dou
 __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W, int p, int lane,
                                            PoseShared& ps) {
     VorShared& sh = ps.v;
-    const int nl = S.n_lig;
-    // polyhedron seeds (Calc indices, -1 = none) and the ligand partners each processed atom kept
+    const int nl = n_mobile(S);      // the scored atoms: side-chain atoms, then the ligand
+    // polyhedron seeds (Calc indices, -1 = none) and the mobile partners each processed atom kept
 #if FXE_SEEDS_SHARED
     int (*const seed)[3] = ps.seed;
     uint32_t (*const rec)[kMaskWords] = ps.rec;
@@ -1122,7 +1125,7 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         return;
     }
     for (int l = lane; l < nl; l += 32) {
-        ps.order[W.lig_rank[lb + l]] = (uint8_t)l;
+        ps.order[W.mob_rank[lb + l]] = (uint8_t)l;
         seed[l][0] = seed[l][1] = seed[l][2] = -1;
 #pragma unroll
         for (int w = 0; w < kMaskWords; ++w) rec[l][w] = 0;
@@ -1147,11 +1150,8 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
             const int c = w * 32 + lane;
             bool ex = false;
             if (c < NC) {
-                const int j = W.cand_idx[cb + c];
-                if (j >= S.n_rec) {
-                    const int l = j - S.n_rec;
-                    ex = bit(ps.done, l) && !bit(rec[l], a);
-                }
+                const int l = mobile_of(S, W.cand_idx[cb + c]);
+                if (l >= 0) ex = bit(ps.done, l) && !bit(rec[l], a);
             }
             excl[w] = __ballot_sync(kFull, ex);
             kept_n += __popc(__ballot_sync(kFull, c < NC && !ex));
@@ -1163,7 +1163,7 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
             }
             continue;
         }
-        const float4 me = W.lig_pos[lb + a];
+        const float4 me = W.mob_pos[lb + a];
         const float rado = me.w + kRw;
         load_planes(sh, S, W, p, a, NC, me, rado, excl, lane);
         // seed vertex left by an earlier atom, if all three of its planes are in the list
@@ -1204,11 +1204,8 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
             const bool kept = ar > real(0.0) && (f & (kOnHull | kEngulf));
             W.cand_area[cb + c] = (double)ar;
             W.cand_flag[cb + c] = (uint8_t)(f | (kept ? kRecorded : 0));
-            const int j = sh.cidx[c];
-            if (kept && j >= S.n_rec) {
-                const int l = j - S.n_rec;
-                keep_lig[l >> 5] |= 1u << (l & 31);
-            }
+            const int l = kept ? mobile_of(S, sh.cidx[c]) : -1;
+            if (l >= 0) keep_lig[l >> 5] |= 1u << (l & 31);
         }
 #pragma unroll
         for (int w = 0; w < kMaskWords; ++w) {
@@ -1219,50 +1216,74 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         }
         // save_seeds (LIB/Vcontacts.cpp:601-629): first vertex naming each later atom's plane
         if (lane == 0) {
-            const int az = S.n_rec + a;
+            const int az = slot_of(S, a);
             for (int vi = 0; vi < sh.nv; ++vi) {
                 const uchar4 q = sh.vp[vi];
                 if (q.z == kNone || q.x >= NC || q.y >= NC || q.z >= NC) continue;
                 const int j0 = sh.cidx[q.x], j1 = sh.cidx[q.y], j2 = sh.cidx[q.z];
-                if (j0 >= S.n_rec && seed[j0 - S.n_rec][0] == -1) {
-                    seed[j0 - S.n_rec][0] = az; seed[j0 - S.n_rec][1] = j1; seed[j0 - S.n_rec][2] = j2;
+                const int m0 = mobile_of(S, j0), m1 = mobile_of(S, j1), m2 = mobile_of(S, j2);
+                if (m0 >= 0 && seed[m0][0] == -1) {
+                    seed[m0][0] = az; seed[m0][1] = j1; seed[m0][2] = j2;
                 }
-                if (j1 >= S.n_rec && seed[j1 - S.n_rec][0] == -1) {
-                    seed[j1 - S.n_rec][0] = az; seed[j1 - S.n_rec][1] = j0; seed[j1 - S.n_rec][2] = j2;
+                if (m1 >= 0 && seed[m1][0] == -1) {
+                    seed[m1][0] = az; seed[m1][1] = j0; seed[m1][2] = j2;
                 }
-                if (j2 >= S.n_rec && seed[j2 - S.n_rec][0] == -1) {
-                    seed[j2 - S.n_rec][0] = az; seed[j2 - S.n_rec][1] = j0; seed[j2 - S.n_rec][2] = j1;
+                if (m2 >= 0 && seed[m2][0] == -1) {
+                    seed[m2][0] = az; seed[m2][1] = j0; seed[m2][2] = j1;
                 }
             }
             ps.done[a >> 5] |= 1u << (a & 31);
         }
         __syncwarp();
     }
-    // vcfunction (LIB/vcfunction.cpp:84-513): atoms in Calc order, their kept contacts
-    const int T = S.ntypes;
+    // vcfunction (LIB/vcfunction.cpp:84-513): scored atoms in Calc order (side-chain atoms,
+    // then the ligand), their kept contacts; each residue's terms are summed on their own and the
+    // records added up ligand first, then the side chains in order (LIB/ic2cf.cpp:133-245)
+    const int T = S.ntypes, nsc = S.n_sc;
     const double permea = (double)S.permeability;
     double com = 0.0, wal = 0.0, sas = 0.0, totsas = 0.0;
+    double res_com[kMaxFlex], res_wal[kMaxFlex], res_sas[kMaxFlex];
+#pragma unroll
+    for (int r = 0; r < kMaxFlex; ++r) res_com[r] = res_wal[r] = res_sas[r] = 0.0;
+    int cur_res = -1;
     for (int i = 0; i < nl; ++i) {
         const int NC = W.cand_n[lb + i];
         const size_t cb = (lb + i) * kMaxCand;
-        const double radA = (double)S.lig_radius[i];
+        const bool side = i < nsc;
+        const int res = side ? S.sc_res[i] : kMaxFlex;
+        if (res != cur_res) {
+            if (cur_res >= 0 && cur_res < kMaxFlex) {
+                res_com[cur_res] = com;
+                res_wal[cur_res] = wal;
+                res_sas[cur_res] = sas;
+            }
+            com = wal = sas = 0.0;
+            cur_res = res;
+        }
+        const double radA = (double)W.mob_pos[lb + i].w;
         const double radoA = radA + (double)kRw;
         const double surfA = 4.0 * kPi * radoA * radoA;
-        const int ti = S.lig_type[i];
+        const int ti = side ? S.rec_type[S.sc_slot[i]] : S.lig_type[i - nsc];
         double c_com = 0.0, c_wal = 0.0, c_area = 0.0;
         for (int c = lane; c < NC; c += 32) {
             if (!(W.cand_flag[cb + c] & kRecorded)) continue;
             const int j = W.cand_idx[cb + c];
             const double area = (double)W.cand_area[cb + c];
             c_area += area;
-            const bool lig = j >= S.n_rec;
-            const int l = j - S.n_rec;
-            if (lig && (S.bonded[l * nl + i] >= 0 || l < i)) continue;
-            const float rj = lig ? S.lig_radius[l] : S.rec_pos[j].w;
-            const int tj = lig ? S.lig_type[l] : S.rec_type[j];
+            const int rel = residue_pair(S, i, j);
+            if (rel == 1) continue;                      // bonded within the residue
+            const int mj = mobile_of(S, j);
+            if (mj >= 0 && mj < i) continue;             // FA->contacts: scored from that atom
+            const bool lig_j = j >= S.n_rec;
+            const float rj = lig_j ? S.lig_radius[j - S.n_rec] : (mj >= 0 ? W.mob_pos[lb + mj].w : S.rec_pos[j].w);
+            const int tj = lig_j ? S.lig_type[j - S.n_rec] : S.rec_type[j];
             const int eidx = (ti - 1) * T + (tj - 1);
-            const double yval = get_yval(S, eidx, area / surfA);
-            c_com += S.em_weight[eidx] ? yval * area : yval;
+            // intramolecular: one residue, or two protein residues (LIB/vcfunction.cpp:283-291)
+            const bool intra = rel != 0 || (side && !lig_j);
+            if (S.intramolecular || !intra) {
+                const double yval = get_yval(S, eidx, area / surfA);
+                c_com += S.em_weight[eidx] ? yval * area : yval;
+            }
             const double rAB = radA + (double)rj;
             const float clash_distance = (float)(permea * rAB);
             const float d2 = W.cand_d2[cb + c];
@@ -1281,7 +1302,7 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         c_area = warp_sum(c_area);
         double SAS = surfA - c_area;
         if (SAS < 0.0) SAS = 0.0;
-        totsas += SAS;
+        if (!side) totsas += SAS;
         double contribution;
         if (S.solventterm != 0.0f) {
             contribution = (double)S.solventterm * SAS;
@@ -1293,6 +1314,12 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         com += c_com;
         wal += c_wal;
         sas += contribution;
+    }
+    // the ligand's record (com/wal/sas hold it now), then each side chain's
+    for (int r = 0; r < S.n_flex; ++r) {
+        com += res_com[r];
+        wal += res_wal[r];
+        sas += res_sas[r];
     }
     fxe_cf cf;
     memset(&cf, 0, sizeof(cf));

@@ -12,7 +12,11 @@ Restates the reference's set-up steps that produce what the evaluation path read
     then buildic again inside add2_optimiz_vec)
   * cleft-grid ICs: calc_cleftic (LIB/calc_cleftic.cpp:5-33), entry 0 the initial anchor
   * genes: add2_optimiz_vec for the grid index, the three rotations and every flexible bond
-    (LIB/add2_optimiz_vec.cpp:93-196) with the reference's default deltas (LIB/top.cpp:266-270)
+    (LIB/add2_optimiz_vec.cpp:93-196) with the reference's default deltas (LIB/top.cpp:266-270),
+    then one rotamer gene per flexible side chain (LIB/add2_optimiz_vec.cpp:28-60)
+  * flexible side chains: the residue's bonded matrix (bondedlist + update_bonded, as
+    build_rotamers makes it, LIB/build_rotamers.cpp:309-345); the rotamer coordinates are
+    generator output here (the reference builds them from a rotamer library with buildcc)
 
 The integer structure (rebuild order, cycles, bonded matrix, genes) is the reference's exactly;
 the single-precision ICs agree to within a few units in the last place (transcendental
@@ -299,10 +303,36 @@ def prepare(inp: SystemInputs) -> Descriptor:
     gmap = [1, 0, 0, 0] + [0] * len(lig.flex)
     opt = [0.0, float(ic2[lig.gpa[1]][1]), float(ic2[lig.gpa[1]][2]), float(ic2[lig.gpa[2]][2])] + \
           [float(ic2[b][2]) for b in bond]
+    # rotamer genes of the flexible side chains, last (add2_optimiz_vec "SC",
+    # LIB/add2_optimiz_vec.cpp:28-60): 0 .. trot with the index delta, mapped
+    flex = rec.flex
+    for r, f in enumerate(flex):
+        typ.append(4)
+        atm.append(r)
+        gmin_.append(0.0)
+        gmax_.append(float(f.n_rot - 1))
+        gdel.append(1.0)
+        gmap.append(1)
+        opt.append(0.0)
+    fx = {}
+    if flex:
+        bonded = []
+        for f in flex:
+            adj_r = [[] for _ in range(f.natm)]
+            for a, b in f.bonds:
+                adj_r[a].append(b)
+                adj_r[b].append(a)
+            bonded.append(bonded_matrix(adj_r, f.natm).reshape(-1))
+        fx = dict(flex_first=np.asarray([f.first for f in flex], np.int32),
+                  flex_natm=np.asarray([f.natm for f in flex], np.int32),
+                  flex_nrot=np.asarray([f.n_rot for f in flex], np.int32),
+                  flex_isbb=np.concatenate([f.isbb for f in flex]).astype(np.int8),
+                  flex_xyz=np.concatenate([f.rot_xyz.reshape(-1, 3) for f in flex]).astype(np.float32),
+                  flex_bonded=np.concatenate(bonded).astype(np.int8))
     base = ic2.copy()
     lrec4 = np.concatenate([lrec.astype(np.int32), rec3[:, None]], axis=1)
     w, off, ex, ey = inp.emat_tables()
-    return Descriptor(
+    return Descriptor(**fx,
         rec_xyz=rec.xyz.copy(), rec_radius=rec.radius.copy(), rec_type=rec.type.copy(), ori=ori,
         globalmin=gmin, globalmax=gmax, maxwidth=mw, grid_ic=grid, lig_radius=lig.radius.copy(),
         lig_type=lig.type.copy(), lig_rec=lrec4, lig_shift=shift, lig_ic=base,

@@ -13,6 +13,10 @@ The shapes follow the docking workloads this package is measured on:
 * energy matrix: symmetric ``ntypes x ntypes`` with N(0, 1) entries in fp32, single-valued
   (area-weighted) entries.
 * genes: uniform int32 in ``[0, 2**31 - 1]``.
+* flexible side chains: receptor atoms at the cleft wall replaced by residues of four backbone
+  atoms (N, CA, C, O) and a 4-6-atom branch (CB onwards) pointing into the cleft, with a set of
+  rotamers that re-sample the branch's dihedrals; receptor atoms within reach of any rotamer are
+  removed so that no rotamer clashes with the rigid atoms.
 
 Nothing here reads the reference; everything is reproducible from the seed.
 """
@@ -56,6 +60,25 @@ class Receptor:
     cleft_center: np.ndarray  # (3,) float32
     cleft_radius: float
     edge: float = 0.0         # cube edge used (A)
+    flex: list = field(default_factory=list)   # FlexResidue, in Calc order
+
+
+@dataclass
+class FlexResidue:
+    """A receptor residue with rotamers: its atoms are receptor atoms first .. first + natm - 1
+    (Calc order N, CA, C, O, CB, ...); rotamer 0 is the conformation in the receptor arrays."""
+    first: int
+    isbb: np.ndarray          # (natm,) int8, 1 = backbone atom (not scored)
+    rot_xyz: np.ndarray       # (n_rot, natm, 3) float32
+    bonds: list               # residue-local (i, j)
+
+    @property
+    def natm(self) -> int:
+        return int(self.isbb.shape[0])
+
+    @property
+    def n_rot(self) -> int:
+        return int(self.rot_xyz.shape[0])
 
 
 def poisson_disc_receptor(n_atoms: int, cleft_radius: float, seed: int,
@@ -177,6 +200,85 @@ def _place(a, b, c, bond, ang_deg, dih_deg):
     d2 = np.array([-bond * math.cos(ang), bond * math.sin(ang) * math.cos(dih),
                    bond * math.sin(ang) * math.sin(dih)])
     return a + d2[0] * bc + d2[1] * m + d2[2] * n
+
+
+def add_flexible_residues(rec: Receptor, n_res: int, n_rot: int, seed: int,
+                          branch=(4, 6), clearance: float = 3.0) -> Receptor:
+    """Receptor with ``n_res`` flexible residues of ``n_rot`` rotamers each (see module doc).
+
+    Anchors are receptor atoms 0.5-3.5 A outside the cleft sphere, at least 9 A apart; each
+    becomes the CA of a residue whose CB points at the cleft centre. Rigid atoms closer than
+    ``clearance`` to an atom of any rotamer are removed."""
+    rng = np.random.default_rng(seed)
+    c = np.asarray(rec.cleft_center, np.float64)
+    xyz = rec.xyz.astype(np.float64)
+    dist = np.linalg.norm(xyz - c, axis=1)
+    cand = np.flatnonzero((dist > rec.cleft_radius + 0.5) & (dist < rec.cleft_radius + 3.5))
+    rng.shuffle(cand)
+    anchors = []
+    for k in cand:
+        if all(np.linalg.norm(xyz[k] - xyz[a]) >= 9.0 for a in anchors):
+            anchors.append(int(k))
+        if len(anchors) == n_res:
+            break
+    if len(anchors) < n_res:
+        raise ValueError(f"only {len(anchors)} anchors for {n_res} flexible residues")
+    residues = {}
+    for a in anchors:
+        ca = xyz[a]
+        u = (c - ca) / np.linalg.norm(c - ca)
+        v = np.cross(u, [0.0, 0.0, 1.0] if abs(u[2]) < 0.9 else [1.0, 0.0, 0.0])
+        v /= np.linalg.norm(v)
+        w = np.cross(u, v)
+        n_at = ca + 1.46 * (-0.34 * u + 0.94 * v)
+        c_at = ca + 1.52 * (-0.34 * u - 0.47 * v + 0.82 * w)
+        o_at = c_at + 1.23 * (-0.6 * u + 0.8 * w)
+        cb = ca + 1.53 * u
+        nb = int(rng.integers(branch[0], branch[1] + 1))    # CB and the atoms after it
+        confs, chis = [], set()
+        while len(confs) < n_rot:
+            chi = tuple(int(rng.choice([-60, 60, 180])) for _ in range(nb - 1))
+            if chi in chis and len(chis) < 3 ** (nb - 1):
+                continue
+            chis.add(chi)
+            pts = [n_at, ca, c_at, o_at, cb]
+            prev = (cb, ca, n_at)
+            for x in chi:
+                p = _place(prev[0], prev[1], prev[2], 1.53, 109.5, x + rng.normal(0.0, 8.0))
+                pts.append(p)
+                prev = (p, prev[0], prev[1])
+            confs.append(np.asarray(pts))
+        natm = 4 + nb
+        types = rng.integers(1, NTYPES, size=natm).astype(np.int32)
+        bonds = [(0, 1), (1, 2), (2, 3), (1, 4)] + [(4 + i, 5 + i) for i in range(nb - 1)]
+        residues[a] = (np.asarray(confs, np.float32), types, bonds)
+    # rigid atoms within reach of any rotamer atom go (the anchors become the residues' CA)
+    every = np.concatenate([r[0].reshape(-1, 3) for r in residues.values()]).astype(np.float64)
+    keep = np.ones(len(xyz), bool)
+    for k in range(len(xyz)):
+        if k in residues:
+            continue
+        if np.min(np.linalg.norm(every - xyz[k], axis=1)) < clearance:
+            keep[k] = False
+    out_xyz, out_t, out_r, flex = [], [], [], []
+    for k in range(len(xyz)):
+        if k in residues:
+            confs, types, bonds = residues[k]
+            first = len(out_xyz)
+            natm = confs.shape[1]
+            flex.append(FlexResidue(first=first,
+                                    isbb=np.asarray([1, 1, 1, 1] + [0] * (natm - 4), np.int8),
+                                    rot_xyz=confs, bonds=bonds))
+            out_xyz.extend(confs[0])
+            out_t.extend(types)
+            out_r.extend(type_radius(t, 0) for t in types)
+        elif keep[k]:
+            out_xyz.append(rec.xyz[k])
+            out_t.append(rec.type[k])
+            out_r.append(rec.radius[k])
+    return Receptor(xyz=np.asarray(out_xyz, np.float32), type=np.asarray(out_t, np.int32),
+                    radius=np.asarray(out_r, np.float32), cleft_center=rec.cleft_center,
+                    cleft_radius=rec.cleft_radius, edge=rec.edge, flex=flex)
 
 
 def random_ligand(n_atoms: int, n_torsions: int, seed: int, bond: float = 1.53,

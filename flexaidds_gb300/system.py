@@ -104,7 +104,33 @@ class Descriptor:
     dee_clash: float = 0.5
     intramolecular: int = 1
     solventterm: float = 0.0
+    # flexible side chains (residues with rotamers), in Calc order; gene type 4 names the
+    # residue by its index here
+    flex_first: np.ndarray = None    # (R,) int32 receptor index of each residue's first atom
+    flex_natm: np.ndarray = None     # (R,) int32
+    flex_nrot: np.ndarray = None     # (R,) int32, rotamer 0 = the receptor's coordinates
+    flex_isbb: np.ndarray = None     # (sum natm,) int8, 1 = backbone (not scored)
+    flex_xyz: np.ndarray = None      # (sum nrot * natm, 3) float32
+    flex_bonded: np.ndarray = None   # (sum natm * natm,) int8, residue.bonded
     decode: list = field(default_factory=list)
+
+    def __post_init__(self):
+        if self.flex_first is None:
+            self.flex_first = np.zeros(0, np.int32)
+            self.flex_natm = np.zeros(0, np.int32)
+            self.flex_nrot = np.zeros(0, np.int32)
+            self.flex_isbb = np.zeros(0, np.int8)
+            self.flex_xyz = np.zeros((0, 3), np.float32)
+            self.flex_bonded = np.zeros(0, np.int8)
+
+    @property
+    def n_flex(self):
+        return int(self.flex_first.shape[0])
+
+    @property
+    def n_sc(self):
+        """Scored side-chain atoms (the non-backbone atoms of the flexible residues)."""
+        return int((self.flex_isbb == 0).sum())
 
     @property
     def n_rec(self):
@@ -130,16 +156,21 @@ class Descriptor:
                "gene_typ", "gene_atm", "gene_min", "gene_max", "gene_del", "gene_map", "opt_par",
                "emat_weight", "emat_off", "emat_x", "emat_y")
     _SCALARS = ("maxwidth", "ntypes", "permeability", "dee_clash", "intramolecular", "solventterm")
+    _FLEX = ("flex_first", "flex_natm", "flex_nrot", "flex_isbb", "flex_xyz", "flex_bonded")
 
     def to_arrays(self, prefix: str = "") -> dict:
         """Flat name -> array mapping (for np.savez)."""
         out = {prefix + k: np.asarray(getattr(self, k)) for k in self._ARRAYS}
         out.update({prefix + k: np.asarray(getattr(self, k)) for k in self._SCALARS})
+        if self.n_flex:
+            out.update({prefix + k: np.asarray(getattr(self, k)) for k in self._FLEX})
         return out
 
     @classmethod
     def from_arrays(cls, arrs, prefix: str = "") -> "Descriptor":
         kw = {k: np.asarray(arrs[prefix + k]).copy() for k in cls._ARRAYS}
+        if prefix + "flex_first" in arrs:
+            kw.update({k: np.asarray(arrs[prefix + k]).copy() for k in cls._FLEX})
         for k in cls._SCALARS:
             v = np.asarray(arrs[prefix + k]).item()
             kw[k] = int(v) if k in ("ntypes", "intramolecular") else float(v)
@@ -178,9 +209,13 @@ def gene_bins(gmin: float, gmax: float, gdel: float, gmap: int) -> np.ndarray:
 
 
 def make_inputs(n_rec: int, cleft_radius: float, n_lig: int, n_tor: int, seed: int,
-                spacing: float = 0.375, edge: float | None = None) -> SystemInputs:
-    """One seeded docking system of the given shape (``edge``: receptor cube edge to start from)."""
+                spacing: float = 0.375, edge: float | None = None, side_chains: int = 0,
+                rotamers: int = 8) -> SystemInputs:
+    """One seeded docking system of the given shape (``edge``: receptor cube edge to start from;
+    ``side_chains`` flexible residues of ``rotamers`` rotamers carved into the cleft wall)."""
     rec = synth.poisson_disc_receptor(n_rec, cleft_radius, seed=seed, edge=edge)
+    if side_chains:
+        rec = synth.add_flexible_residues(rec, side_chains, rotamers, seed=seed + 3)
     lig = synth.random_ligand(n_lig, n_tor, seed=seed + 1)
     grid = synth.cleft_grid(rec.cleft_center, cleft_radius, spacing)
     emat = synth.energy_matrix(seed + 2)

@@ -34,6 +34,22 @@ typedef enum fxe_status {
     FXE_ERR_INTERNAL = 8
 } fxe_status;
 
+/* A flexible side chain: a receptor residue with rotamers (LIB/build_rotamers.cpp). Its atoms
+ * are receptor atoms first .. first + n_atoms - 1 (Calc order). The residue's rotamer gene
+ * (gene type 4, gene_atom = the residue's index in fxe_receptor_desc.flex) selects rotamer
+ * r = (unsigned)(ic + 0.5) (LIB/ic2cf.cpp:90-94), whose coordinates the residue's atoms then
+ * take; rotamer 0 is the receptor's own conformation. Its non-backbone atoms are scored like
+ * ligand atoms (update_optres, LIB/update_optres.cpp:17-28), each residue with its own
+ * complementarity record summed after the ligand's (LIB/ic2cf.cpp:133-245). */
+typedef struct fxe_flex_residue {
+    int32_t first;
+    int32_t n_atoms;
+    int32_t n_rot;             /* rotamers, including rotamer 0 */
+    const int8_t* backbone;    /* n_atoms: 1 = backbone atom (keeps its place, not scored) */
+    const float* rot_xyz;      /* n_rot * n_atoms * 3 */
+    const int8_t* bonded;      /* n_atoms * n_atoms: residue.bonded (-1: not within bloops) */
+} fxe_flex_residue;
+
 /* Receptor, in the reference's Calc order (residue order, LIB/Vcontacts.cpp:1600-1630),
  * plus the state LIB/calc_center.cpp:8-61 leaves in FA and the cleft grid of
  * LIB/generate_grid.cpp / LIB/calc_cleftic.cpp. */
@@ -48,6 +64,8 @@ typedef struct fxe_receptor_desc {
     float maxwidth;            /* FA->maxwidth */
     int32_t n_grid;            /* cleft grid entries including entry 0 (initial anchor) */
     const float* grid_ic;      /* n_grid * 3: dis, ang, dih of each grid point */
+    int32_t n_flex;            /* flexible side chains (0..8; at most 32 scored atoms in all) */
+    const fxe_flex_residue* flex;
 } fxe_receptor_desc;
 
 /* Ligand build tree and genes (atoms/residue/FA->map_par after the reference set-up:
@@ -65,8 +83,8 @@ typedef struct fxe_ligand_desc {
     const int32_t* build_order;/* n_build: FA->mov[0] */
     const int8_t* bonded;      /* n_atoms * n_atoms: residue.bonded (-1: not within bloops) */
     int32_t n_genes;
-    const int32_t* gene_type;  /* optmap.typ: -1 grid index, 0 dis, 1 ang, 2 dih */
-    const int32_t* gene_atom;  /* optmap.atm, ligand-local */
+    const int32_t* gene_type;  /* optmap.typ: -1 grid index, 0 dis, 1 ang, 2 dih, 4 rotamer */
+    const int32_t* gene_atom;  /* optmap.atm, ligand-local; for a rotamer gene the residue */
     const double* gene_min;    /* genlim.min / max / del / map (LIB/gaboom.cpp:2491-2507) */
     const double* gene_max;
     const double* gene_del;
@@ -159,9 +177,11 @@ fxe_status fxe_eval_genes_device(fxe_context* ctx, int32_t n, const int32_t* d_g
                                  fxe_cf* d_out, void* stream);
 
 /* Contacts recorded for the last evaluated batch (the ca_rec lists vcfunction walks), for
- * inspection and parity checks: for pose p and ligand atom a, up to cap entries of
- * (partner Calc index, area). Returns the count through *n_out. */
-fxe_status fxe_last_contacts(fxe_context* ctx, int32_t pose, int32_t ligand_atom, int32_t cap,
+ * inspection and parity checks: for pose p and scored atom a, up to cap entries of
+ * (partner Calc index, area). Scored atoms are the flexible side chains' non-backbone atoms in
+ * Calc order, then the ligand atoms (without side chains: a is the ligand atom). Returns the
+ * count through *n_out. */
+fxe_status fxe_last_contacts(fxe_context* ctx, int32_t pose, int32_t atom, int32_t cap,
                              int32_t* partner, float* area, int32_t* n_out);
 
 /* Built ligand coordinates of pose `pose` of the last evaluated batch (n_atoms * 3). */

@@ -27,6 +27,7 @@
 #define O_MAX_POLY 2200           /* LIB/Vcontacts.h:54 */
 #define O_MAX_CONT 100            /* LIB/Vcontacts.h:52 */
 #define O_MAX_EDGES 200           /* LIB/Vcontacts.cpp:378 */
+#define O_MAX_FLEX 8              /* flexible side chains the descriptor may carry */
 
 static int g_compat = 0;
 
@@ -52,6 +53,14 @@ typedef struct { int numpts; int pt[O_MAX_CONT]; } PtOrder;
 
 typedef struct {
     int natoms, nrec, nlig;
+    /* per Calc slot: scored (ligand and side-chain atoms), residue (-1 a rigid one-atom residue,
+       r a flexible side chain, n_flex the ligand), index in the residue, scored-atom index */
+    char* score;
+    int* res_of;
+    int* loc;
+    int* mob;
+    int nflex;
+    const fxe_flex_residue* flex;
     float (*xyz)[3];
     const float* radius;      /* Calc-order radii (receptor then ligand) */
     const int* type;
@@ -774,6 +783,16 @@ static int save_areas(State* S, int NC, int az) {
     return 0;
 }
 
+/* residue.bonded of two Calc slots of one residue (ligand or flexible side chain); -1 when they
+ * belong to different residues or are more than bloops bonds apart. */
+static int residue_bonded(const State* S, const fxe_ligand_desc* lig, int a, int b) {
+    const int ra = S->res_of[a];
+    if (ra < 0 || ra != S->res_of[b]) return -1;
+    if (ra == S->nflex) return lig->bonded[S->loc[a] * lig->n_atoms + S->loc[b]];
+    const fxe_flex_residue* f = &S->flex[ra];
+    return f->bonded[S->loc[a] * f->n_atoms + S->loc[b]];
+}
+
 /* get_contlist4, LIB/Vcontacts.cpp:1725-1839: atoms of the 27 surrounding cells within
  * rado + r_j + Rw, skipping atoms already done unless they recorded a contact with this one.
  * With clash != NULL it also accumulates the wall term of the pre-filter. */
@@ -801,8 +820,7 @@ static int get_contlist(State* S, const fxe_ligand_desc* lig, int az, float rado
                 S->cand[NC].dist = sqrt(sq);
                 if (clash) {
                     if (S->cand[NC].dist < cd) {
-                        const int intra = (az >= S->nrec) && (j >= S->nrec);
-                        if (!intra || lig->bonded[(az - S->nrec) * lig->n_atoms + (j - S->nrec)] < 0)
+                        if (residue_bonded(S, lig, az, j) < 0)
                             *clash += O_KWALL * (pow(S->cand[NC].dist, -12.0) - pow(cd, -12.0));
                     }
                     S->done[az] = 'Y';
@@ -816,7 +834,8 @@ static int get_contlist(State* S, const fxe_ligand_desc* lig, int az, float rado
 }
 
 /* index_protein, LIB/Vcontacts.cpp:1570-1715, in the state after the first evaluation: the
- * receptor atoms keep their place while the scorable atoms are re-examined every call. */
+ * receptor atoms keep their place while the scorable atoms (ligand and side-chain atoms, whose
+ * Calc slots are refilled every call) are re-examined. */
 static int index_atoms(State* S, const fxe_receptor_desc* rec) {
     float gmin[3], gmax[3];
     int alter = 0;
@@ -825,8 +844,8 @@ static int index_atoms(State* S, const fxe_receptor_desc* rec) {
         gmax[j] = (int)rec->globalmax[j] + 1.0;
     }
     float mw = rec->maxwidth;
-    for (int i = S->nrec; i < S->natoms; ++i)
-        for (int j = 0; j < 3; ++j) {
+    for (int i = 0; i < S->natoms; ++i)
+        for (int j = 0; j < 3 && S->score[i]; ++j) {
             if (S->xyz[i][j] < gmin[j]) {
                 gmin[j] = S->xyz[i][j];
                 alter = 1;
@@ -892,7 +911,7 @@ static int vcontacts(State* S, const fxe_receptor_desc* rec, const fxe_ligand_de
     *clash = 0.0;
     for (int i = 0; i < S->natoms; ++i) {
         const int az = S->calclist[i];
-        if (az < S->nrec) continue;
+        if (!S->score[az]) continue;
         const float rado = S->rad_all[az] + O_RW;
         get_contlist(S, lig, az, rado, clash, permea);
     }
@@ -905,7 +924,7 @@ static int vcontacts(State* S, const fxe_receptor_desc* rec, const fxe_ligand_de
     S->ncarec = 0;
     for (int i = 0; i < S->natoms; ++i) {
         const int az = S->calclist[i];
-        if (az < S->nrec) continue;
+        if (!S->score[az]) continue;
         const float rado = S->rad_all[az] + O_RW;
         const int NC = get_contlist(S, lig, az, rado, NULL, 0.0);
         if (S->counts) {
@@ -1047,7 +1066,9 @@ static double get_yval(const fxe_emat_desc* em, int idx, double rel) {
 }
 
 /* vcfunction, LIB/vcfunction.cpp:14-574, after a successful Vcontacts: walks each scorable
- * atom's contact records in Calc order and accumulates com / wal / sas. */
+ * atom's contact records in Calc order (side-chain atoms, then the ligand) and accumulates
+ * com / wal / sas into its residue's record; ic2cf then adds the records up, the ligand's first
+ * and the side chains' in order (LIB/ic2cf.cpp:133-245). */
 static void score(State* S, const fxe_ligand_desc* lig, const fxe_emat_desc* em,
                   const fxe_params* prm, fxe_cf* cf, int pose, fxo_contact* cout, int64_t cap,
                   int64_t* ncout) {
@@ -1055,10 +1076,13 @@ static void score(State* S, const fxe_ligand_desc* lig, const fxe_emat_desc* em,
     const double permea = (double)prm->permeability;
     const double dee_clash = (double)prm->dee_clash;
     char* counted = (char*)calloc((size_t)S->natoms, 1);
-    double com = 0.0, wal = 0.0, sas = 0.0, totsas = 0.0;
+    double rcom[O_MAX_FLEX + 1] = {0}, rwal[O_MAX_FLEX + 1] = {0}, rsas[O_MAX_FLEX + 1] = {0};
+    double totsas = 0.0;
     int rclash = 0;
-    for (int i = S->nrec; i < S->natoms; ++i) {
-        const int li = i - S->nrec;
+    for (int i = 0; i < S->natoms; ++i) {
+        if (!S->score[i]) continue;
+        const int ri = S->res_of[i];
+        const int side = ri < S->nflex;
         const double radA = (double)S->rad_all[i];
         const double radoA = radA + O_RW;
         double SAS = 4.0 * O_PI * radoA * radoA;
@@ -1074,14 +1098,14 @@ static void score(State* S, const fxe_ligand_desc* lig, const fxe_emat_desc* em,
             if (cout && *ncout < cap) {
                 fxo_contact* c = &cout[*ncout];
                 c->pose = pose;
-                c->atom = li;
+                c->atom = S->mob[i];
                 c->partner = j;
                 c->area = (float)area;
                 c->dist = (float)S->carec[cur].dist;
             }
             if (ncout) ++*ncout;
-            const int intrares = j >= S->nrec;
-            if (intrares && lig->bonded[(j - S->nrec) * lig->n_atoms + li] >= 0) continue;
+            const int same = ri == S->res_of[j];
+            if (same && residue_bonded(S, lig, j, i) >= 0) continue;
             if (counted[j]) continue;
             const float clash_distance = permea * rAB;
             const double dd = S->carec[cur].dist;
@@ -1091,14 +1115,18 @@ static void score(State* S, const fxe_ligand_desc* lig, const fxe_emat_desc* em,
                 double cr = permea * rAB;
                 double cr2 = cr * cr, cr4 = cr2 * cr2, cr6 = cr4 * cr2;
                 double inv_cr12 = 1.0 / (cr6 * cr6);
-                wal += O_KWALL * (inv_d12 - inv_cr12);
+                rwal[ri] += O_KWALL * (inv_d12 - inv_cr12);
                 if (dd <= dee_clash * rAB) rclash = 1;
             }
-            double contribution = em->weight[eidx] ? yval * area : yval;
-            com += contribution;
+            /* intramolecular: one residue, or two protein residues (LIB/vcfunction.cpp:283-291) */
+            const int intra = same || (side && S->res_of[j] != S->nflex);
+            if (prm->intramolecular || !intra) {
+                double contribution = em->weight[eidx] ? yval * area : yval;
+                rcom[ri] += contribution;
+            }
         }
         if (SAS < 0.0) SAS = 0.0;
-        totsas += SAS;
+        if (!side) totsas += SAS;
         double contribution;
         if (prm->solventterm) {
             contribution = (double)prm->solventterm * SAS;
@@ -1107,14 +1135,19 @@ static void score(State* S, const fxe_ligand_desc* lig, const fxe_emat_desc* em,
             const double yval = get_yval(em, eidx, SAS / surfA);
             contribution = em->weight[eidx] ? yval * SAS : yval;
         }
-        sas += contribution;
+        rsas[ri] += contribution;
         counted[i] = 1;
     }
     free(counted);
     memset(cf, 0, sizeof(*cf));
-    cf->com = 0.0 + com;
-    cf->wal = 0.0 + wal;
-    cf->sas = 0.0 + sas;
+    cf->com = 0.0 + rcom[S->nflex];
+    cf->wal = 0.0 + rwal[S->nflex];
+    cf->sas = 0.0 + rsas[S->nflex];
+    for (int r = 0; r < S->nflex; ++r) {
+        cf->com += rcom[r];
+        cf->wal += rwal[r];
+        cf->sas += rsas[r];
+    }
     cf->con = 0.0;
     cf->totsas = totsas;
     /* ic2cf only reads the per-residue clash flag of flexible side chains; for the ligand the
@@ -1158,11 +1191,42 @@ int fxo_eval_ic(const fxe_receptor_desc* rec, const fxe_ligand_desc* lig,
     S.poly = (Vert*)malloc(O_MAX_POLY * sizeof(Vert));
     S.vedge = (Edge*)malloc(O_MAX_POLY * sizeof(Edge));
     S.lic = (float(*)[3])malloc((size_t)S.nlig * sizeof(*S.lic));
+    S.score = (char*)calloc((size_t)N, 1);
+    S.res_of = (int*)malloc((size_t)N * sizeof(int));
+    S.loc = (int*)malloc((size_t)N * sizeof(int));
+    S.mob = (int*)malloc((size_t)N * sizeof(int));
+    S.nflex = rec->n_flex;
+    S.flex = rec->flex;
     int rc = 0;
     if (!S.xyz || !S.rad_all || !S.type_all || !S.done || !S.boxnum || !S.calclist || !S.ca_index || !S.seed ||
-        !S.carec || !S.cand || !S.cont || !S.centerpt || !S.ptorder || !S.poly || !S.vedge || !S.lic) {
+        !S.carec || !S.cand || !S.cont || !S.centerpt || !S.ptorder || !S.poly || !S.vedge || !S.lic ||
+        !S.score || !S.res_of || !S.loc || !S.mob || S.nflex < 0 || S.nflex > O_MAX_FLEX) {
         rc = -1;
         goto cleanup;
+    }
+    for (int i = 0; i < N; ++i) {
+        S.res_of[i] = -1;
+        S.loc[i] = 0;
+        S.mob[i] = -1;
+    }
+    {
+        int m = 0;
+        for (int r = 0; r < S.nflex; ++r)
+            for (int k = 0; k < S.flex[r].n_atoms; ++k) {
+                const int i = S.flex[r].first + k;
+                S.res_of[i] = r;
+                S.loc[i] = k;
+                if (!S.flex[r].backbone[k]) {
+                    S.score[i] = 1;
+                    S.mob[i] = m++;
+                }
+            }
+        for (int l = 0; l < S.nlig; ++l) {
+            S.res_of[S.nrec + l] = S.nflex;
+            S.loc[S.nrec + l] = l;
+            S.score[S.nrec + l] = 1;
+            S.mob[S.nrec + l] = m++;
+        }
     }
     for (int i = 0; i < S.nrec; ++i) {
         for (int k = 0; k < 3; ++k) S.xyz[i][k] = rec->xyz[i * 3 + k];
@@ -1186,12 +1250,24 @@ int fxo_eval_ic(const fxe_receptor_desc* rec, const fxe_ligand_desc* lig,
         }
         assign_ic(&S, rec, lig, icv);
         buildcc(&S, rec, lig);
+        /* rotamer genes (LIB/ic2cf.cpp:90-94); index_protein refills the scored slots of the
+           side chains with the selected rotamer's atoms (LIB/Vcontacts.cpp:1600-1625) */
+        for (int g = 0; g < lig->n_genes; ++g) {
+            if (lig->gene_type[g] != 4) continue;
+            const fxe_flex_residue* f = &S.flex[lig->gene_atom[g]];
+            const unsigned rot = (unsigned)(icv[g] + 0.5f);
+            for (int k = 0; k < f->n_atoms; ++k) {
+                if (f->backbone[k]) continue;
+                for (int c = 0; c < 3; ++c) S.xyz[f->first + k][c] = f->rot_xyz[((size_t)rot * f->n_atoms + k) * 3 + c];
+            }
+        }
         if (xyz_out)
             for (int l = 0; l < S.nlig; ++l)
                 for (int k = 0; k < 3; ++k) xyz_out[((size_t)p * S.nlig + l) * 3 + k] = S.xyz[S.nrec + l][k];
         double clash = 0.0;
         int err = 0;
-        for (int l = 0; l < S.nlig; ++l) S.done[S.nrec + l] = 'N';
+        for (int i = 0; i < N; ++i)
+            if (S.score[i]) S.done[i] = 'N';
         if (g_compat) memset(S.ptorder, 0, (size_t)(N + 8) * sizeof(PtOrder));
         const int rv = vcontacts(&S, rec, lig, &clash, (double)prm->permeability, &err);
         fxe_cf* cf = &out[p];
@@ -1218,6 +1294,7 @@ cleanup:
     free(S.xyz); free(S.rad_all); free(S.type_all); free(S.done); free(S.boxnum); free(S.calclist);
     free(S.ca_index); free(S.seed); free(S.carec); free(S.cand); free(S.cont); free(S.centerpt);
     free(S.ptorder); free(S.poly); free(S.vedge); free(S.lic); free(S.box_n); free(S.box_f);
+    free(S.score); free(S.res_of); free(S.loc); free(S.mob);
     return rc;
 }
 

@@ -26,7 +26,9 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <array>
 #include <cstring>
+#include <utility>
 #include <vector>
 
 extern "C" {
@@ -57,6 +59,16 @@ struct ref_input {
     float dee_clash;
     int32_t intramolecular;
     float solventterm;
+    // flexible side chains: residues of receptor atoms first .. first + natm - 1 (receptor-local,
+    // ascending), with rotamer coordinates (rotamer 0 = the receptor's) and intra-residue bonds
+    int32_t n_flexres;
+    const int32_t* flex_first;
+    const int32_t* flex_natm;
+    const int32_t* flex_nrot;
+    const int8_t* flex_isbb;    // concatenated per residue
+    const float* flex_xyz;      // concatenated per residue: nrot * natm * 3
+    const int32_t* flex_nbonds;
+    const int32_t* flex_bonds;  // concatenated per residue: nbonds * 2, residue-local
 };
 
 struct ref_export_sizes {
@@ -78,6 +90,10 @@ struct Harness {
     resid* residue = nullptr;
     gridpoint* cleftgrid = nullptr;
     int n_rec = 0, n_lig = 0, lig_res = 0;
+    std::vector<int> sc_slot;   // Calc indices of the scored side-chain atoms
+    // every side-chain atom of every rotamer (atoms[] index, coordinates as given), so that the
+    // coordinates can be put back before each pose (see ref_eval)
+    std::vector<std::pair<int, std::array<float, 3>>> rotamer_atoms;
     std::vector<std::vector<int>> last_contacts;  // per ligand atom: partner Calc indices
     std::vector<std::vector<double>> last_areas;
     std::vector<std::vector<double>> last_dists;
@@ -176,39 +192,76 @@ int ref_setup(const ref_input* in) {
     h.n_rec = in->n_rec;
     h.n_lig = in->n_lig;
     const int N = in->n_rec, n = in->n_lig;
-    const int natoms_alloc = N + n + 2;
+    int n_copies = 0;
+    for (int r = 0; r < in->n_flexres; ++r) n_copies += (in->flex_nrot[r] - 1) * in->flex_natm[r];
+    const int natoms_alloc = N + n + n_copies + 2;
     h.atoms = (atom*)calloc(natoms_alloc, sizeof(atom));
     h.residue = (resid*)calloc(N + 3, sizeof(resid));
     atom* atoms = h.atoms;
     resid* residue = h.residue;
 
-    // receptor: one residue per atom, protein type
+    // receptor: one residue per atom (protein type), except the flexible side chains, whose
+    // atoms form one residue each (backbone flags, intra-residue bonds)
+    std::vector<int> flex_res(in->n_flexres, 0), isbb_off(in->n_flexres, 0), xyz_off(in->n_flexres, 0),
+        bond_off(in->n_flexres, 0);
+    for (int r = 1; r < in->n_flexres; ++r) {
+        isbb_off[r] = isbb_off[r - 1] + in->flex_natm[r - 1];
+        xyz_off[r] = xyz_off[r - 1] + in->flex_nrot[r - 1] * in->flex_natm[r - 1] * 3;
+        bond_off[r] = bond_off[r - 1] + in->flex_nbonds[r - 1] * 2;
+    }
+    int nres = 0, fr = 0;
     for (int k = 1; k <= N; ++k) {
         atom& a = atoms[k];
         for (int j = 0; j < 3; ++j) a.coor[j] = a.coor_ori[j] = in->rec_xyz[(k - 1) * 3 + j];
         a.number = k;
         a.radius = in->rec_radius[k - 1];
         a.type = in->rec_type[k - 1];
-        a.ofres = k;
         a.recs = 'r';
         a.acs = -1.0f;
         FA->num_atm[k] = k;
-        resid& r = residue[k];
-        r.fatm = (int*)malloc(sizeof(int));
-        r.latm = (int*)malloc(sizeof(int));
-        r.fatm[0] = r.latm[0] = k;
+        const bool starts = fr < in->n_flexres && in->flex_first[fr] == k - 1;
+        const bool inside = fr > 0 && k - 1 < in->flex_first[fr - 1] + in->flex_natm[fr - 1];
+        if (inside) {
+            a.ofres = nres;
+            a.isbb = in->flex_isbb[isbb_off[fr - 1] + (k - 1 - in->flex_first[fr - 1])];
+            continue;
+        }
+        resid& r = residue[++nres];
+        a.ofres = nres;
         r.type = 0;
-        r.number = k;
+        r.number = nres;
         r.chn = 'A';
         strcpy(r.name, "REC");
+        if (starts) {
+            const int nr = in->flex_nrot[fr], na = in->flex_natm[fr];
+            r.fatm = (int*)calloc(nr, sizeof(int));
+            r.latm = (int*)calloc(nr, sizeof(int));
+            r.fatm[0] = k;
+            r.latm[0] = k + na - 1;
+            strcpy(r.name, "FLX");
+            a.isbb = in->flex_isbb[isbb_off[fr]];
+            flex_res[fr] = nres;
+            ++fr;
+        } else {
+            r.fatm = (int*)malloc(sizeof(int));
+            r.latm = (int*)malloc(sizeof(int));
+            r.fatm[0] = r.latm[0] = k;
+        }
     }
-    FA->res_cnt = N;
+    for (int r = 0; r < in->n_flexres; ++r)
+        for (int b = 0; b < in->flex_nbonds[r]; ++b) {
+            const int x = in->flex_first[r] + 1 + in->flex_bonds[bond_off[r] + 2 * b];
+            const int y = in->flex_first[r] + 1 + in->flex_bonds[bond_off[r] + 2 * b + 1];
+            atoms[x].bond[++atoms[x].bond[0]] = y;
+            atoms[y].bond[++atoms[y].bond[0]] = x;
+        }
+    FA->res_cnt = nres;
     FA->atm_cnt = N;
     FA->atm_cnt_real = N;
     calc_center(FA, atoms, residue);
 
     // ligand residue
-    const int L = N + 1;
+    const int L = nres + 1;
     h.lig_res = L;
     FA->res_cnt = L;
     resid& lr = residue[L];
@@ -245,7 +298,7 @@ int ref_setup(const ref_input* in) {
     }
     for (int j = 0; j < 3; ++j) lr.gpa[j] = N + 1 + in->gpa[j];
     FA->atm_cnt = N + n;
-    FA->atm_cnt_real = N + n;
+    FA->atm_cnt_real = N + n;     // rotamer copies added below do not join Calc
     FA->num_het = 1;
     FA->num_het_atm = n;
 
@@ -283,6 +336,60 @@ int ref_setup(const ref_input* in) {
     for (int i = N + 1; i <= N + n; ++i)
         for (int j = 0; j < 3; ++j) atoms[i].coor_ori[j] = atoms[i].coor[j];
 
+    // flexible side chains as build_rotamers leaves them (LIB/build_rotamers.cpp:84-135,
+    // 300-350): each rotamer a copy of the residue's atoms appended after the last atom, with the
+    // rotamer's coordinates (given here instead of built from a rotamer library); an optimised
+    // residue of type 0 with its bonded matrix; the residue listed in FA->flex_res
+    FA->atm_cnt = N + n;
+    if (in->n_flexres > 0) {
+        FA->optres = (OptRes*)realloc(FA->optres, (size_t)(1 + in->n_flexres) * sizeof(OptRes));
+        memset(&FA->optres[1], 0, (size_t)in->n_flexres * sizeof(OptRes));
+        FA->flex_res = (flxsc*)calloc(in->n_flexres, sizeof(flxsc));
+        std::vector<int> bondlist(MAX_ATM_HET), neighbours(MAX_ATM_HET);
+        for (int r = 0; r < in->n_flexres; ++r) {
+            const int kres = flex_res[r], na = in->flex_natm[r], nr = in->flex_nrot[r];
+            resid& res = residue[kres];
+            for (int rot = 1; rot < nr; ++rot) {
+                const int delta = FA->atm_cnt - res.fatm[0] + 1;
+                res.fatm[rot] = res.fatm[0] + delta;
+                res.latm[rot] = res.latm[0] + delta;
+                for (int j = res.fatm[0]; j <= res.latm[0]; ++j) {
+                    atoms[j + delta] = atoms[j];
+                    for (int c = 0; c < 3; ++c)
+                        atoms[j + delta].coor[c] = atoms[j + delta].coor_ori[c] =
+                            in->flex_xyz[xyz_off[r] + ((rot * na) + (j - res.fatm[0])) * 3 + c];
+                }
+                FA->atm_cnt += na;
+            }
+            for (int rot = 0; rot < nr; ++rot)
+                for (int k = 0; k < na; ++k) {
+                    const int a = res.fatm[rot] + k;
+                    h.rotamer_atoms.push_back({a, {atoms[a].coor[0], atoms[a].coor[1], atoms[a].coor[2]}});
+                }
+            res.trot = nr - 1;
+            res.rot = 0;
+            FA->optres[1 + r].rnum = kres;
+            FA->optres[1 + r].type = 0;
+            FA->optres[1 + r].tot = na;
+            for (int i = 0; i < na; ++i) {
+                int nbonded = 0;
+                bondedlist(atoms, res.fatm[0] + i, FA->bloops, &nbonded, bondlist.data(), neighbours.data());
+                update_bonded(&res, na, nbonded, bondlist.data(), neighbours.data());
+            }
+            FA->flex_res[r].inum = kres;
+            FA->flex_res[r].num = res.number;
+            FA->flex_res[r].chn = res.chn;
+            FA->flex_res[r].prob = 1.0f;
+            FA->flex_res[r].cflag = 1;
+            strcpy(FA->flex_res[r].name, res.name);
+            for (int k = 0; k < na; ++k)
+                if (!in->flex_isbb[isbb_off[r] + k]) h.sc_slot.push_back(in->flex_first[r] + k);
+        }
+        FA->num_optres = 1 + in->n_flexres;
+        FA->nflxsc = in->n_flexres;
+        FA->nflxsc_real = in->n_flexres;
+    }
+
     // cleft grid: entry 0 is the initial ligand anchor (LIB/generate_grid.cpp:26-30)
     h.cleftgrid = (gridpoint*)calloc(in->n_grid + 1, sizeof(gridpoint));
     gridpoint* cg = h.cleftgrid;
@@ -310,6 +417,7 @@ int ref_setup(const ref_input* in) {
         opt[1] = j;
         add2_optimiz_vec(FA, atoms, residue, opt, ' ', "");
     }
+    if (in->n_flexres > 0) add2_optimiz_vec(FA, atoms, residue, opt, ' ', "SC");
     update_optres(atoms, residue, FA->atm_cnt, FA->optres, FA->num_optres);
 
     // energy matrix (LIB/read_emat.cpp:56-126 layout)
@@ -410,6 +518,9 @@ int ref_export(float* ori, float* gmin, float* gmax, float* maxwidth,
     for (int g = 0; g < FA->npar; ++g) {
         gene_typ[g] = FA->map_par[g].typ;
         gene_atm[g] = to_local(h, FA->map_par[g].atm);
+        if (FA->map_par[g].typ == 4)   // the flexible side chain, by its place in FA->flex_res
+            for (int r = 0; r < FA->nflxsc; ++r)
+                if (h.residue[FA->flex_res[r].inum].fatm[0] == FA->map_par[g].atm) gene_atm[g] = r;
         gene_min[g] = FA->min_opt_par[g];
         gene_max[g] = FA->max_opt_par[g];
         gene_del[g] = FA->del_opt_par[g];
@@ -417,6 +528,20 @@ int ref_export(float* ori, float* gmin, float* gmax, float* maxwidth,
         opt_par[g] = FA->opt_par[g];
     }
     return 0;
+}
+
+// The bonded matrices of the flexible side chains (natm * natm each, concatenated in order).
+int ref_export_flex_bonded(int8_t* out) {
+    if (!H) return -1;
+    Harness& h = *H;
+    size_t o = 0;
+    for (int r = 0; r < h.FA->nflxsc; ++r) {
+        const resid& res = h.residue[h.FA->flex_res[r].inum];
+        const int na = res.latm[0] - res.fatm[0] + 1;
+        for (int i = 0; i < na; ++i)
+            for (int j = 0; j < na; ++j) out[o++] = (int8_t)res.bonded[i][j];
+    }
+    return (int)o;
 }
 
 // Evaluates n chromosomes given as decoded ICs (n * n_genes doubles). cf_out holds, per pose,
@@ -441,6 +566,14 @@ int ref_eval(int32_t n, const double* ic, double* cf_out, int32_t* status_out,
         // code path writes before reading when a face has no vertex on its second plane; the
         // caller-owned workspace is zeroed before every pose so that such reads are defined.
         memset(h.VC->ptorder, 0, MAX_PT * sizeof(ptindex));
+        // voronoi_poly2 answers a hull walk of 200 edges by moving the atom by a random
+        // +-0.005 A and, on this path (VC->recalc = 0), does not move it back
+        // (LIB/Vcontacts.cpp:378-405, 480-487). Ligand atoms are rebuilt every pose; rotamer
+        // atoms are not, so the displacement would stay with every later pose. The rotamer
+        // coordinates are put back before each pose so that poses do not depend on the ones
+        // evaluated before them.
+        for (const auto& ra : h.rotamer_atoms)
+            for (int c = 0; c < 3; ++c) h.atoms[ra.first].coor[c] = ra.second[c];
         cfstr cf = ic2cf(FA, h.VC, h.atoms, h.residue, h.cleftgrid, ng, icv.data());
         double* o = cf_out + (size_t)p * 11;
         o[0] = cf.com; o[1] = cf.con; o[2] = cf.wal; o[3] = cf.sas; o[4] = cf.elec;
@@ -453,13 +586,15 @@ int ref_eval(int32_t n, const double* ic, double* cf_out, int32_t* status_out,
             for (int i = 0; i < h.n_lig; ++i)
                 for (int j = 0; j < 3; ++j)
                     lig_xyz_out[((size_t)p * h.n_lig + i) * 3 + j] = h.atoms[h.n_rec + 1 + i].coor[j];
-        // contact records of the scorable atoms (Calc indices of the ligand follow the receptor)
-        h.last_contacts.assign(h.n_lig, {});
-        h.last_areas.assign(h.n_lig, {});
-        h.last_dists.assign(h.n_lig, {});
+        // contact records of the scored atoms: side-chain atoms, then the ligand (whose Calc
+        // indices follow the receptor's)
+        const int nsc = (int)h.sc_slot.size(), ns = nsc + h.n_lig;
+        h.last_contacts.assign(ns, {});
+        h.last_areas.assign(ns, {});
+        h.last_dists.assign(ns, {});
         if (status_out[p] == 0) {
-            for (int i = 0; i < h.n_lig; ++i) {
-                int ci = h.VC->ca_index[h.n_rec + i];
+            for (int i = 0; i < ns; ++i) {
+                int ci = h.VC->ca_index[i < nsc ? h.sc_slot[i] : h.n_rec + (i - nsc)];
                 while (ci != -1) {
                     h.last_contacts[i].push_back(h.VC->ca_rec[ci].atom);
                     h.last_areas[i].push_back(h.VC->ca_rec[ci].area);
@@ -472,9 +607,10 @@ int ref_eval(int32_t n, const double* ic, double* cf_out, int32_t* status_out,
     return 0;
 }
 
-// Contact records of the last evaluated pose for ligand atom i (in record-walk order).
+// Contact records of the last evaluated pose for scored atom i (side-chain atoms first, then the
+// ligand), in record-walk order.
 int ref_last_contacts(int32_t i, int32_t cap, int32_t* partner, double* area, double* dist) {
-    if (!H || i < 0 || i >= H->n_lig) return -1;
+    if (!H || i < 0 || i >= (int)H->last_contacts.size()) return -1;
     const auto& c = H->last_contacts[i];
     const int m = (int)c.size();
     for (int k = 0; k < m && k < cap; ++k) {

@@ -32,6 +32,8 @@ class RefInput(C.Structure):
         ("ntypes", C.c_int32), ("emat_weight", _i), ("emat_off", _i), ("emat_x", _f),
         ("emat_y", _f), ("permeability", C.c_float), ("dee_clash", C.c_float),
         ("intramolecular", C.c_int32), ("solventterm", C.c_float),
+        ("n_flexres", C.c_int32), ("flex_first", _i), ("flex_natm", _i), ("flex_nrot", _i),
+        ("flex_isbb", _b), ("flex_xyz", _f), ("flex_nbonds", _i), ("flex_bonds", _i),
     ]
 
 
@@ -55,6 +57,7 @@ def _load():
         _lib.ref_export.argtypes = [_f, _f, _f, _f, _f, _f, _f, _i, _i, _b, _i, _i, _d, _d, _d, _i, _d]
         _lib.ref_eval.argtypes = [C.c_int32, _d, _d, _i, _f]
         _lib.ref_last_contacts.argtypes = [C.c_int32, C.c_int32, _i, _d, _d]
+        _lib.ref_export_flex_bonded.argtypes = [_b]
     return _lib
 
 
@@ -108,6 +111,17 @@ class RefHarness:
         r.dee_clash = inp.dee_clash
         r.intramolecular = inp.intramolecular
         r.solventterm = inp.solventterm
+        fl = rec.flex
+        r.n_flexres = len(fl)
+        if fl:
+            r.flex_first = _p(keep([f.first for f in fl], np.int32), _i)
+            r.flex_natm = _p(keep([f.natm for f in fl], np.int32), _i)
+            r.flex_nrot = _p(keep([f.n_rot for f in fl], np.int32), _i)
+            r.flex_isbb = _p(keep(np.concatenate([f.isbb for f in fl]), np.int8), _b)
+            r.flex_xyz = _p(keep(np.concatenate([f.rot_xyz.reshape(-1) for f in fl]), np.float32), _f)
+            r.flex_nbonds = _p(keep([len(f.bonds) for f in fl], np.int32), _i)
+            r.flex_bonds = _p(keep(np.asarray([b for f in fl for b in f.bonds], np.int32).reshape(-1),
+                                   np.int32), _i)
         self._r = r
         if lib.ref_setup(C.byref(r)) != 0:
             raise RuntimeError("reference set-up failed")
@@ -142,7 +156,17 @@ class RefHarness:
                        _p(gmp, _i), _p(opt, _d))
         w, off, ex, ey = self.inp.emat_tables()
         rec, lig = self.inp.receptor, self.inp.ligand
-        return Descriptor(
+        fx = {}
+        if rec.flex:
+            fb = np.zeros(sum(f.natm * f.natm for f in rec.flex), np.int8)
+            lib.ref_export_flex_bonded(_p(fb, _b))
+            fx = dict(flex_first=np.asarray([f.first for f in rec.flex], np.int32),
+                      flex_natm=np.asarray([f.natm for f in rec.flex], np.int32),
+                      flex_nrot=np.asarray([f.n_rot for f in rec.flex], np.int32),
+                      flex_isbb=np.concatenate([f.isbb for f in rec.flex]).astype(np.int8),
+                      flex_xyz=np.concatenate([f.rot_xyz.reshape(-1, 3) for f in rec.flex]).astype(np.float32),
+                      flex_bonded=fb)
+        return Descriptor(**fx,
             rec_xyz=rec.xyz.copy(), rec_radius=rec.radius.copy(), rec_type=rec.type.copy(),
             ori=ori, globalmin=gmin, globalmax=gmax, maxwidth=float(mw[0]), grid_ic=grid_ic,
             lig_radius=lig.radius.copy(), lig_type=lig.type.copy(), lig_rec=lrec,
@@ -164,11 +188,13 @@ class RefHarness:
         return cf, st, xyz
 
     def last_contacts(self):
-        """Per ligand atom: (partner Calc indices, areas, distances) of the last scored pose."""
+        """Per scored atom (side-chain atoms, then the ligand): (partner Calc indices, areas,
+        distances) of the last scored pose."""
         lib = _load()
         out = []
         cap = 4096
-        for i in range(self.sizes.n_lig):
+        n_sc = sum(int((f.isbb == 0).sum()) for f in self.inp.receptor.flex)
+        for i in range(n_sc + self.sizes.n_lig):
             p = np.zeros(cap, np.int32)
             a = np.zeros(cap, np.float64)
             d = np.zeros(cap, np.float64)

@@ -50,7 +50,8 @@ def tiny_system():
 
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-GOLDEN_NAMES = ("c0_2000_24", "curves_900_16", "outside_600_10", "scale_6000_48")
+GOLDEN_NAMES = ("c0_2000_24", "curves_900_16", "outside_600_10", "scale_6000_48", "flex_2000_24",
+                "flexcurves_900_16", "flexscale_6000_48")
 
 
 def load_golden(name):

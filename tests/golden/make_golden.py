@@ -13,7 +13,8 @@ For each system it writes ``tests/golden/<name>.npz`` holding
     LIB/gaboom.cpp, which does not compile without Eigen);
   * what the reference's ic2cf returns for every chromosome (the 11 cfstr terms and the status
     class), the ligand coordinates buildcc produced, and, for the first poses, the contact lists
-    (partner Calc index, area) Vcontacts recorded per ligand atom.
+    (partner Calc index, area) Vcontacts recorded per scored atom (side-chain atoms, then the
+    ligand).
 
 Chromosomes are drawn uniformly, then filtered with the C restatement so that the fixture holds
 mostly poses that get scored (uniform chromosomes clash about nine times in ten), some clashes
@@ -67,6 +68,17 @@ SYSTEMS = {
     # 12 torsions (receptor cube edge given, as the benchmark gives it)
     "scale_6000_48": dict(args=(6000, 12.0, 48, 12), seed=7, grid=768, pool=40000, scored=60,
                           clashed=10, contacts=3, tweak=None, edge=60.032427451306646),
+    # flexible side chains: three residues of eight rotamers carved into the cleft wall, their
+    # rotamer genes last
+    "flex_2000_24": dict(args=(2000, 8.0, 24, 6), seed=11, grid=1024, pool=8000, scored=120,
+                         clashed=30, contacts=8, tweak=None, side_chains=3),
+    # side chains with density curves, the other switches and intramolecular terms off
+    "flexcurves_900_16": dict(args=(900, 7.0, 16, 4), seed=23, grid=512, pool=6000, scored=80,
+                              clashed=20, contacts=6, tweak="curves", side_chains=2, intramolecular=0),
+    # the benchmark's shape with its three side chains
+    "flexscale_6000_48": dict(args=(6000, 12.0, 48, 12), seed=7, grid=768, pool=60000, scored=50,
+                              clashed=10, contacts=2, tweak=None, edge=60.032427451306646,
+                              side_chains=3),
 }
 
 
@@ -74,7 +86,9 @@ def inputs_for(name):
     """The generator inputs of fixture ``name`` (seeded; the cleft grid subsampled)."""
     cfg = SYSTEMS[name]
     n_rec, cleft, n_lig, n_tor = cfg["args"]
-    inp = system.make_inputs(n_rec, cleft, n_lig, n_tor, seed=cfg["seed"], edge=cfg.get("edge"))
+    inp = system.make_inputs(n_rec, cleft, n_lig, n_tor, seed=cfg["seed"], edge=cfg.get("edge"),
+                             side_chains=cfg.get("side_chains", 0))
+    inp.intramolecular = cfg.get("intramolecular", 1)
     rng = np.random.default_rng(cfg["seed"] + 100)
     keep = np.sort(rng.choice(inp.grid_xyz.shape[0], cfg["grid"], replace=False))
     inp.grid_xyz = np.ascontiguousarray(inp.grid_xyz[keep])

@@ -44,13 +44,15 @@ def test_ligand_generator_geometry():
 
 # --- set-up restatement against the reference's own set-up (golden descriptors) ---------------
 
-@pytest.mark.parametrize("name", ["c0_2000_24", "curves_900_16", "outside_600_10", "scale_6000_48"])
+@pytest.mark.parametrize("name", ["c0_2000_24", "curves_900_16", "outside_600_10", "scale_6000_48",
+                                  "flex_2000_24", "flexcurves_900_16"])
 def test_prepare_matches_reference_setup(name):
     from conftest import load_golden
     dref, _ = load_golden(name)
     d = prepare.prepare(_make_golden().inputs_for(name))
     for k in ("lig_rec", "build_order", "bonded", "gene_typ", "gene_atm", "gene_map", "rec_type",
-              "lig_type", "emat_weight", "emat_off"):
+              "lig_type", "emat_weight", "emat_off", "flex_first", "flex_natm", "flex_nrot",
+              "flex_isbb", "flex_xyz", "flex_bonded"):
         np.testing.assert_array_equal(getattr(d, k), getattr(dref, k), err_msg=k)
     for k in ("gene_min", "gene_max", "gene_del", "emat_x", "emat_y", "rec_xyz", "rec_radius",
               "lig_radius"):
