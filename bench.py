@@ -35,9 +35,10 @@ from flexaidds_gb300 import capi, prepare, synth, system  # noqa: E402
 
 METRIC = "poses scored/s on 1 GB300 (plain path, one population per launch)"
 WORKLOAD = dict(n_rec=6000, cleft=12.0, n_lig=48, n_tor=12, seed=7, edge=60.032427451306646,
-                population=2000)
-WORKLOAD_NAME = ("plain-scale: 6000-atom receptor, 12 A cleft (137060 grid points), 48-atom "
-                 "ligand, 12 torsions, populations of 2000 chromosomes that all pass the clash "
+                population=2000, side_chains=3, rotamers=8)
+WORKLOAD_NAME = ("plain-scale: 6000-atom receptor (before carving the side chains), 12 A cleft "
+                 "(137060 grid points), 48-atom ligand, 12 torsions, 3 flexible side chains of 8 "
+                 "rotamers (19 genes), populations of 2000 chromosomes that all pass the clash "
                  "pre-filter")
 N_POPULATIONS = 8           # distinct populations, cycled over the steps
 FLUSH_BYTES = 512 << 20     # L2 flush between timed steps (L2 is 129 MB)
@@ -54,7 +55,8 @@ NOMINAL_PEAK_TFLOPS = {"fast": 152 * 128 * 2 * 2.07e9 / 1e12, "reference": 1.25}
 
 def work_flops_per_pose(c: dict) -> float:
     """Algorithmic work of one pose from the oracle's per-pose mean counts:
-    sum over ligand atoms of 8 C + 14 NC + 12 NC E + 60 E_arc + 40 T + 30 V, plus 60 per built
+    sum over scored atoms (ligand and side-chain atoms) of 8 C + 14 NC + 12 NC E + 60 E_arc +
+    40 T + 30 V, plus 60 per built
     atom (C candidates scanned, NC contacts, E hull edges, E_arc arc edges, T spherical triangles
     and arc segments, V vertices)."""
     return (8 * c["candidates"] + 14 * c["contacts"] + 12 * c["plane_tests"] + 60 * c["arc_edges"]
@@ -68,7 +70,7 @@ def work_flops_per_pose(c: dict) -> float:
 def make_system():
     w = WORKLOAD
     inp = system.make_inputs(w["n_rec"], w["cleft"], w["n_lig"], w["n_tor"], seed=w["seed"],
-                             edge=w["edge"])
+                             edge=w["edge"], side_chains=w["side_chains"], rotamers=w["rotamers"])
     return prepare.prepare(inp)
 
 
@@ -364,7 +366,9 @@ def run_gpu(args):
         "data": "synthetic (seeded Poisson-disc receptor, seeded tree ligand, N(0,1) matrix)",
         "config": {"workload": WORKLOAD_NAME, "population": pop, "precision": prec,
                    "l2": f"flushed between timed steps ({FLUSH_BYTES >> 20} MB write)",
-                   "parallelism": f"replicas x{world}", "side_chains": "none (not modelled)"},
+                   "parallelism": f"replicas x{world}",
+                   "side_chains": f"{d.n_flex} residues x {int(d.flex_nrot[0]) if d.n_flex else 0} "
+                                  f"rotamers, {d.n_sc} scored side-chain atoms"},
         "e2e": {"value": world * pop * args.steps / e2e_s, "unit": "poses/s",
                 "h2d_bytes_per_step": pop * d.n_genes * 4, "d2h_bytes_per_step": pop * capi.CF_DTYPE.itemsize},
         "gpu_launches": launches,
