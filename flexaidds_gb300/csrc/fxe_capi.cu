@@ -1029,6 +1029,7 @@ extern "C" fxe_status fxe_batch_take_launches(fxe_batch* b, int64_t* launches) {
 namespace fxe {
 void launch_ga_init(const GaJob*, const int*, int, cudaStream_t);
 void launch_ga_breed(const GaJob*, const int*, int, cudaStream_t);
+void launch_ga_fitness(const GaJob*, const int*, int, bool, cudaStream_t);
 void launch_ga_select(GaJob*, const int*, int, bool, cudaStream_t);
 }  // namespace fxe
 
@@ -1119,7 +1120,8 @@ extern "C" fxe_status fxe_ga_job_bytes(const fxe_ga_job* job, int64_t* bytes) {
     if (!job || !job->ctx || !bytes) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
     const int64_t P = job->population, ng = job->ctx->S.n_genes, G = job->generations;
     *bytes = P * ng * 4 * 3 + P * 8 * 2 + P * (int64_t)sizeof(fxe_cf) + G * P * (ng * 4 + 8) + 16 +
-             2 * (P + 8) * (ng * 4 + 8) + (job->duplicates ? 0 : 8 * (int64_t)seen_slots(*job));
+             2 * (P + 8) * (ng * 4 + 8) + (job->duplicates ? 0 : 8 * (int64_t)seen_slots(*job)) +
+             P * ng * 8 + P * (8 * 3 + 4) + 32;
     return FXE_OK;
 }
 
@@ -1135,6 +1137,11 @@ extern "C" fxe_status fxe_ga_admit(fxe_ga* e, const fxe_ga_job* job, int32_t* sl
     const int nnew = job->n_new > 0 ? job->n_new : P;
     if (nnew > P || (job->steady && job->n_new <= 0))
         return fail(FXE_ERR_INVALID_ARGS, "n_new must be 1..population (STEADY needs it set)");
+    if (job->fitness != FXE_FITNESS_PSHARE && job->fitness != FXE_FITNESS_LINEAR && job->fitness != FXE_FITNESS_SMFREE)
+        return fail(FXE_ERR_INVALID_ARGS, "fitness must be PSHARE, LINEAR or SMFREE");
+    if (job->sharing_alpha < 0.0 || job->sharing_peaks < 0.0 || job->sharing_scale < 0.0 ||
+        !(job->entropy_weight >= 0.0 && job->entropy_weight <= 1.0))
+        return fail(FXE_ERR_INVALID_ARGS, "sharing parameters negative or entropy weight outside [0, 1]");
     if (ctx->device != e->device) return fail(FXE_ERR_INVALID_ARGS, "context on another device");
     for (const auto& s : e->slots)
         if (s.used && s.ctx == ctx) return fail(FXE_ERR_INVALID_ARGS, "the context already runs a job");
@@ -1180,6 +1187,28 @@ extern "C" fxe_status fxe_ga_admit(fxe_ga* e, const fxe_ga_job* job, int32_t* sl
         J.dec_tab = ctx->S.dec_tab;
         J.gene_min = ctx->S.gene_min;
         J.gene_del = ctx->S.gene_del;
+        J.gene_max = ctx->S.gene_max;
+        // fitness model; sig_share as LIB/gaboom.cpp:300-309 forms it from the gene limits
+        J.fitness = job->fitness;
+        const double alpha = job->sharing_alpha > 0.0 ? job->sharing_alpha : 1.0;
+        const double peaks = job->sharing_peaks > 0.0 ? job->sharing_peaks : 5.0;
+        const double scale = job->sharing_scale > 0.0 ? job->sharing_scale : 10.0;
+        double sig = 0.0;
+        for (int g = 0; g < ng; ++g) {
+            const double w = ctx->h_gmax[g] - ctx->h_gmin[g];
+            sig += w * w;
+        }
+        sig = std::sqrt(sig / (double)ng) / (2.0 * std::pow(peaks, 1.0 / (double)ng));
+        J.sig_share = sig / scale;
+        J.share_alpha = alpha;
+        J.ent_w = job->entropy_weight;
+        J.beta = job->temperature > 0.0 ? 1.0 / (0.001987206 * job->temperature) : 0.0;   // kB, LIB/statmech.h:26
+        FXE_TRY(get(sizeof(double) * P * ng, &q), "GA fitness"); J.pic = (double*)q;
+        FXE_TRY(get(sizeof(double) * P, &q), "GA fitness"); J.share = (double*)q;
+        FXE_TRY(get(sizeof(double) * P, &q), "GA fitness"); J.fit = (double*)q;
+        FXE_TRY(get(sizeof(double) * P, &q), "GA fitness"); J.fcum = (double*)q;
+        FXE_TRY(get(sizeof(int) * P, &q), "GA fitness"); J.ford = (int*)q;
+        FXE_TRY(get(sizeof(double) * 4, &q), "GA fitness"); J.fstat = (double*)q;
         J.seed = job->seed;
         J.cross_rate = job->cross_rate;
         J.mut_rate = job->mut_rate;
@@ -1202,9 +1231,10 @@ extern "C" fxe_status fxe_ga_admit(fxe_ga* e, const fxe_ga_job* job, int32_t* sl
         FXE_TRY(cudaMemcpyAsync((void*)J.child_cf, ctx->W.out, sizeof(fxe_cf) * P, cudaMemcpyDeviceToDevice, e->stream),
                 "GA records");
         fxe::launch_ga_select(e->d_all, e->d_ids + k, 1, true, e->stream);
+        fxe::launch_ga_fitness(e->d_all, e->d_ids + k, 1, true, e->stream);
         FXE_TRY(cudaGetLastError(), "GA launch");
         FXE_TRY(cudaStreamSynchronize(e->stream), "GA admission");   // gen0 and the host copy of J die here
-        e->launches += 6;
+        e->launches += 9;
         return FXE_OK;
     }();
     if (st != FXE_OK) {
@@ -1266,6 +1296,7 @@ extern "C" fxe_status fxe_ga_step(fxe_ga* e) {
         if (e->precision == FXE_PRECISION_FAST) fxe::f32::launch_poses_jobs(e->d_eval, n, total, e->stream);
         else fxe::f64::launch_poses_jobs(e->d_eval, n, total, e->stream);
         fxe::launch_ga_select(e->d_all, e->d_run, n, false, e->stream);
+        fxe::launch_ga_fitness(e->d_all, e->d_run, n, false, e->stream);
         cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
         if (ce != cudaSuccess) return cuda_fail(ce, "graph capture");
         ce = cudaGraphInstantiate(&e->exec, g, 0);
@@ -1274,7 +1305,7 @@ extern "C" fxe_status fxe_ga_step(fxe_ga* e) {
     }
     if (e->run.empty()) return FXE_OK;
     FXE_TRY(cudaGraphLaunch(e->exec, e->stream), "graph launch");
-    e->launches += 6;
+    e->launches += 9;
     e->graph_launches += 1;
     for (int i : e->run) {
         GaSlot& s = e->slots[i];
@@ -1308,7 +1339,9 @@ double host_genetoic(const fxe_context* ctx, int g, int32_t gene) {
     const double* lo = ctx->h_dtab.data() + ctx->h_doff[g];
     const double* hi = ctx->h_dtab.data() + ctx->h_doff[g + 1];
     const double* it = std::lower_bound(lo, hi, u);
-    return ctx->h_gmin[g] + ctx->h_gdel[g] * (double)(it - lo);
+    // the IC as eval_chromosome leaves it in the gene, clamped (LIB/gaboom.cpp:1851-1859)
+    const double v = ctx->h_gmin[g] + ctx->h_gdel[g] * (double)(it - lo);
+    return v > ctx->h_gmax[g] ? ctx->h_gmax[g] : (v < ctx->h_gmin[g] ? ctx->h_gmin[g] : v);
 }
 }  // namespace
 

@@ -237,7 +237,25 @@ struct GaJob {
     const double* dec_tab;
     const double* gene_min;
     const double* gene_del;
+    const double* gene_max;
+    // fitness (calculate_fitness, LIB/gaboom.cpp:1627-1760) and the order roulette walks the
+    // population in: energy order, or fitness order after a generation under PSHARE
+    int fitness;             // kFitPshare, kFitLinear, kFitSmfree
+    double sig_share;        // GB->sig_share (LIB/gaboom.cpp:300-309)
+    double share_alpha;      // GB->alpha
+    double ent_w;            // GB->entropy_weight
+    double beta;             // 1 / (kB T) of SMFREE's Boltzmann weights; <= 0: rank only
+    double* pic;             // [P * ng] ICs of the population, clamped as eval_chromosome leaves them
+    double* share;           // [P] niche counts
+    double* fit;             // [P] fitness at each roulette position
+    double* fcum;            // [P] running sums of fit
+    int* ford;               // [P] population index at each roulette position
+    double* fstat;           // [4] total, maximum and mean fitness (fitness_stats)
 };
+
+constexpr int kFitPshare = 0;
+constexpr int kFitLinear = 1;
+constexpr int kFitSmfree = 2;
 
 // one block's share of the ensemble reduction: running max of the log-weights and the sums
 // of exp(lw - m), E exp(lw - m), E^2 exp(lw - m)

@@ -2,8 +2,11 @@
 // mutation on the int32 genes) and replacement, one block per job, for populations kept in HBM.
 //
 // Semantics follow the reference's operators:
-//   * LINEAR fitness: after sorting by energy, rank i (0 = lowest energy) gets fitness P - i
-//     (LIB/gaboom.cpp:1627-1635);
+//   * fitness of the population sorted by energy (calculate_fitness, LIB/gaboom.cpp:1627-1760):
+//     LINEAR P - i; PSHARE (the reference's default) (P - i) / niche count, the niche count
+//     summing 1 - (rmsp / sig_share)^alpha over the chromosomes within sig_share; SMFREE the
+//     blend of rank and Boltzmann weight over the same niche count. Under PSHARE the population
+//     is walked in fitness order after a generation (LIB/gaboom.cpp:498-499);
 //   * roulette_wheel: r = u * sum(fitness), the first index whose running fitness sum exceeds r
 //     (LIB/gaboom.cpp:1158-1186);
 //   * the reproduce loop (LIB/gaboom.cpp:909-1000): pairs of parents, adaptive probabilities
@@ -66,16 +69,19 @@ __device__ void bitonic_sort(double* key, int* idx, int n) {
     }
 }
 
-// Roulette over LINEAR fitness: ranks 0..P-1 with fitness P - i; the first rank whose running
-// sum exceeds r = u * P (P + 1) / 2. The running sum of ranks 0..i is (i + 1) P - i (i + 1) / 2.
-__device__ __forceinline__ int roulette_linear(int P, double u) {
-    const double tot = (double)P * (double)(P + 1) * 0.5;
+// roulette_wheel (LIB/gaboom.cpp:1158-1186) over the fitness in roulette order: the first
+// position whose running sum exceeds r = u * total, the last position if none does, and a
+// uniform position when the total is not positive.
+__device__ __forceinline__ int roulette(const GaJob& J, double u) {
+    const int P = J.P;
+    const double tot = J.fstat[0];
+    if (!(tot > 0.0)) return (int)(u * (double)P) % P;
     const double r = u * tot;
-    int lo = 0, hi = P - 1;   // smallest i with cum(i) > r
+    int lo = 0, hi = P - 1;   // smallest k with fcum[k] > r
+    if (!(J.fcum[P - 1] > r)) return P - 1;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        const double cum = (double)(mid + 1) * P - 0.5 * (double)mid * (double)(mid + 1);
-        if (cum > r) hi = mid;
+        if (J.fcum[mid] > r) hi = mid;
         else lo = mid + 1;
     }
     return lo;
@@ -148,17 +154,18 @@ __global__ void __launch_bounds__(kGaThreads) ga_init_kernel(const GaJob* __rest
 // draws, optional adaptive probabilities, crossover with probability crossp, both children
 // mutated bit by bit.
 __device__ void breed_pair(const GaJob& J, int g, int k, int32_t* john, int32_t* mary) {
-    const int P = J.P, ng = J.ng;
+    const int ng = J.ng;
     const uint64_t sb = (uint64_t)(g + 1) << 32;   // streams of generation g + 1
-    // fitness statistics of the LINEAR fitness P - rank (fitness_stats, LIB/gaboom.cpp:818-840)
-    const double fit_max = (double)P, fit_avg = 0.5 * (double)(P + 1);
+    // fitness_stats (LIB/gaboom.cpp:818-840) of the population
+    const double fit_max = J.fstat[1], fit_avg = J.fstat[2];
     const uint64_t st = sb + (uint64_t)k;
     uint64_t d = 0;
-    const int a = roulette_linear(P, uniform(J.seed, st, d++));
-    const int b = roulette_linear(P, uniform(J.seed, st, d++));
+    const int pa = roulette(J, uniform(J.seed, st, d++));
+    const int pb = roulette(J, uniform(J.seed, st, d++));
+    const int a = J.ford[pa], b = J.ford[pb];
     double crossp = J.cross_rate, mutp = J.mut_rate;
     if (J.adaptive) {
-        const double f1 = (double)(P - a), f2 = (double)(P - b);
+        const double f1 = J.fit[pa], f2 = J.fit[pb];
         const double hi = f1 > f2 ? f1 : f2, lo = f1 > f2 ? f2 : f1;
         double denom = fit_max - fit_avg;
         if (denom < 1e-15) denom = 1e-15;   // GA_FITNESS_DENOM_FLOOR, LIB/ga_constants.h:38
@@ -366,6 +373,118 @@ __global__ void __launch_bounds__(kGaThreads) ga_select_kernel(GaJob* __restrict
         J.pop_e_next = pe;
         if (!kInitial) J.gen[0] = g + 1;
     }
+}
+
+// ICs of the (new) population, clamped into the gene limits as eval_chromosome leaves them in
+// the genes (LIB/gaboom.cpp:1845-1866), for the niche counts.
+__global__ void __launch_bounds__(kGaThreads) ga_decode_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
+    const GaJob& J = all[run[blockIdx.y]];
+    if (J.fitness == kFitLinear) return;
+    const int n = J.P * J.ng;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int q = t % J.ng;
+        double v = gene_ic(J, q, J.pop[t]);
+        if (v > J.gene_max[q]) v = J.gene_max[q];
+        else if (v < J.gene_min[q]) v = J.gene_min[q];
+        J.pic[t] = v;
+    }
+}
+
+constexpr int kNicheThreads = 64;
+constexpr int kNicheBlocks = (2048 + kNicheThreads - 1) / kNicheThreads;
+
+// Niche count of chromosome i: the sum over all j of 1 - (rmsp / sig_share)^alpha where rmsp
+// (calc_rmsp, LIB/gaboom.cpp:2874-2885: root mean square of the IC differences) is within
+// sig_share (LIB/gaboom.cpp:1652-1661). One thread per i, j in order.
+__global__ void __launch_bounds__(kNicheThreads) ga_niche_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
+    const GaJob& J = all[run[blockIdx.y]];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (J.fitness == kFitLinear || i >= J.P) return;
+    const int ng = J.ng;
+    const double* xi = J.pic + (size_t)i * ng;
+    const double sig = J.sig_share, alpha = J.share_alpha;
+    double s = 0.0;
+    for (int j = 0; j < J.P; ++j) {
+        const double* xj = J.pic + (size_t)j * ng;
+        double acc = 0.0;
+        for (int q = 0; q < ng; ++q) {
+            const double dq = xi[q] - xj[q];
+            acc += dq * dq;
+        }
+        const double r = sqrt(acc / (double)ng);
+        if (r <= sig) s += 1.0 - (alpha == 1.0 ? r / sig : pow(r / sig, alpha));
+    }
+    J.share[i] = s;
+}
+
+// Fitness of the population (sorted by energy), the roulette order, running sums and
+// fitness_stats. kInitial: the initial population, walked in energy order whatever the model.
+template <bool kInitial>
+__global__ void __launch_bounds__(kGaThreads) ga_fitness_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
+    __shared__ double key[kGaMaxSort];
+    __shared__ int idx[kGaMaxSort];
+    const GaJob& J = all[run[blockIdx.x]];
+    const int P = J.P, model = J.fitness;
+    const bool rank_only = model == kFitLinear || (model == kFitSmfree && !(J.beta > 0.0));
+    double e0 = J.pop_e[0];
+    if (!isfinite(e0)) e0 = 0.0;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        double f = (double)(P - i);
+        if (!rank_only) {
+            if (model == kFitPshare) {
+                f = f / J.share[i];
+            } else {
+                // SMFREE (LIB/gaboom.cpp:1666-1736): the Boltzmann weight over the largest one
+                // (that of the lowest energy)
+                const double e = J.pop_e[i];
+                const double bw = isfinite(e) && isfinite(J.pop_e[0]) ? exp(-J.beta * (e - e0)) : 0.0;
+                const double blended = (1.0 - J.ent_w) * (f / (double)P) + J.ent_w * bw;
+                f = blended * (double)P / J.share[i];
+            }
+        }
+        key[i] = f;
+        idx[i] = i;
+    }
+    __syncthreads();
+    if (!kInitial && model == kFitPshare) {
+        // QuickSort by fitness, descending (LIB/gaboom.cpp:499); equal fitness keeps energy order
+        int n = 1;
+        while (n < P) n <<= 1;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            if (i < P) key[i] = -key[i];
+            else {
+                key[i] = INFINITY;
+                idx[i] = i;
+            }
+        }
+        __syncthreads();
+        bitonic_sort(key, idx, n);
+        for (int i = threadIdx.x; i < P; i += blockDim.x) key[i] = -key[i];
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        J.fit[i] = key[i];
+        J.ford[i] = idx[i];
+    }
+    if (threadIdx.x == 0) {
+        double cum = 0.0, mx = key[0], sum = 0.0;
+        for (int i = 0; i < P; ++i) {
+            cum += key[i];
+            J.fcum[i] = cum;
+            if (key[i] > mx) mx = key[i];
+            sum += key[i];
+        }
+        J.fstat[0] = cum;
+        J.fstat[1] = mx;
+        J.fstat[2] = sum / (double)P;
+    }
+}
+
+void launch_ga_fitness(const GaJob* all, const int* run, int n_jobs, bool initial, cudaStream_t st) {
+    ga_decode_kernel<<<dim3(8, n_jobs), kGaThreads, 0, st>>>(all, run);
+    ga_niche_kernel<<<dim3(kNicheBlocks, n_jobs), kNicheThreads, 0, st>>>(all, run);
+    if (initial) ga_fitness_kernel<true><<<n_jobs, kGaThreads, 0, st>>>(all, run);
+    else ga_fitness_kernel<false><<<n_jobs, kGaThreads, 0, st>>>(all, run);
 }
 
 void launch_ga_init(const GaJob* all, const int* run, int n_jobs, cudaStream_t st) {

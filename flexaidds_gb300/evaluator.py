@@ -221,7 +221,13 @@ class GAJob(C.Structure):
     _fields_ = [("ctx", C.c_void_p), ("population", C.c_int32), ("generations", C.c_int32),
                 ("cross_rate", C.c_double), ("mut_rate", C.c_double), ("seed", C.c_uint64),
                 ("n_new", C.c_int32), ("steady", C.c_int32), ("intragenes", C.c_int32),
-                ("adaptive", C.c_int32), ("k", C.c_double * 4), ("duplicates", C.c_int32)]
+                ("adaptive", C.c_int32), ("k", C.c_double * 4), ("duplicates", C.c_int32),
+                ("fitness", C.c_int32), ("sharing_alpha", C.c_double), ("sharing_peaks", C.c_double),
+                ("sharing_scale", C.c_double), ("entropy_weight", C.c_double),
+                ("temperature", C.c_double)]
+
+
+FITNESS_MODELS = {"PSHARE": 0, "LINEAR": 1, "SMFREE": 2}
 
 
 class GAEngine:
@@ -238,14 +244,18 @@ class GAEngine:
     def job(ev: GPUEvaluator, population: int, generations: int, seed: int,
             cross_rate: float = 0.9, mut_rate: float = 0.01, n_new: int = 0, steady: bool = False,
             intragenes: bool = False, adaptive: bool = False, k=(1.0, 0.5, 1.0, 0.5),
-            duplicates: bool = False) -> GAJob:
-        """Defaults follow the reference's: BOOM with boom_fraction 1, crossover at gene
-        boundaries, fixed probabilities, duplicate chromosomes rejected
-        (LIB/config_parser.cpp:135-161)."""
+            duplicates: bool = False, fitness: str = "PSHARE", sharing_alpha: float = 1.0,
+            sharing_peaks: float = 5.0, sharing_scale: float = 10.0, entropy_weight: float = 0.5,
+            temperature: float = 300.0) -> GAJob:
+        """Defaults follow the reference's: PSHARE fitness, BOOM with boom_fraction 1, crossover
+        at gene boundaries, fixed probabilities, duplicate chromosomes rejected
+        (LIB/config_parser.cpp:108, 125-162)."""
         return GAJob(ev.handle.value, int(population), int(generations), float(cross_rate),
                      float(mut_rate), int(seed) & 0xFFFFFFFFFFFFFFFF, int(n_new), int(bool(steady)),
                      int(bool(intragenes)), int(bool(adaptive)), (C.c_double * 4)(*k),
-                     int(bool(duplicates)))
+                     int(bool(duplicates)), FITNESS_MODELS[fitness], float(sharing_alpha),
+                     float(sharing_peaks), float(sharing_scale), float(entropy_weight),
+                     float(temperature))
 
     def job_bytes(self, job: GAJob) -> int:
         b = C.c_int64(0)

@@ -281,11 +281,12 @@ fxe_status fxe_batch_take_launches(fxe_batch* batch, int64_t* launches);
 void fxe_batch_destroy(fxe_batch* batch);
 
 /* GA engine: docking jobs (one context each) run their genetic algorithm with the population in
- * HBM. A generation of every running job is one CUDA graph: breeding (LINEAR fitness, roulette
- * selection, the reference's bit crossover and mutation, LIB/gaboom.cpp:909-960), one batched
- * evaluation of all children, and BOOM replacement (parents and children merged, the best P
- * kept, LIB/gaboom.cpp:1023-1033). The graph is captured again only when the set of running
- * jobs changes, so jobs are admitted and retired between generations (continuous batching).
+ * HBM. A generation of every running job is one CUDA graph: breeding (roulette selection over
+ * the job's fitness model, the reference's bit crossover and mutation, LIB/gaboom.cpp:909-960),
+ * one batched evaluation of all children, BOOM or STEADY replacement (LIB/gaboom.cpp:1023-1033)
+ * and the fitness of the new population (niche counts on the device). The graph is captured
+ * again only when the set of running jobs changes, so jobs are admitted and retired between
+ * generations (continuous batching).
  * Random draws are counter-based hashes of (seed, generation, child, draw): a job's trajectory
  * depends on its seed only, whatever else runs. Chromosomes the job has produced before are
  * dropped unless the job allows duplicates (fxe_ga_job.duplicates). */
@@ -305,7 +306,16 @@ typedef struct fxe_ga_job {
     int32_t duplicates;      /* 0 (the reference's default): a chromosome whose hash_genes
                                 signature the job has produced before is dropped and another bred
                                 (LIB/gaboom.cpp:977-1018, 1040-1045); 1: duplicates allowed */
+    int32_t fitness;         /* FXE_FITNESS_PSHARE (0, the reference's default), _LINEAR, _SMFREE
+                                (calculate_fitness, LIB/gaboom.cpp:1627-1760) */
+    double sharing_alpha;    /* niche sharing: alpha, peaks, scale (0: the reference's defaults */
+    double sharing_peaks;    /* 1, 5 and 10; sig_share as LIB/gaboom.cpp:300-309 forms it) */
+    double sharing_scale;
+    double entropy_weight;   /* SMFREE: weight of the Boltzmann term (the reference's default 0.5) */
+    double temperature;      /* SMFREE: K (default 300); <= 0 ranks only, as the reference does */
 } fxe_ga_job;
+
+enum { FXE_FITNESS_PSHARE = 0, FXE_FITNESS_LINEAR = 1, FXE_FITNESS_SMFREE = 2 };
 
 fxe_status fxe_ga_create(int32_t max_jobs, int32_t precision, fxe_ga** out);
 /* Device bytes a job's GA state takes (populations, children, ensemble), for admission control. */

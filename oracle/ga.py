@@ -2,8 +2,9 @@
 
 TEST INFRASTRUCTURE ONLY: the checker for flexaidds_gb300/csrc/fxe_ga.cu, used by tests/.
 
-Operators as the reference defines them — LINEAR fitness (LIB/gaboom.cpp:1627-1635), roulette
-selection (:1158-1186), the reproduce loop's crossover-then-mutate of each pair (:918-960), the
+Operators as the reference defines them — LINEAR, PSHARE and SMFREE fitness
+(LIB/gaboom.cpp:1627-1760) with the roulette order PSHARE implies (:498-499), roulette selection
+(:1158-1186), the reproduce loop's crossover-then-mutate of each pair (:918-960), the
 bit crossover with intragenes (:2517-2614) and bit mutation (:2620-2641), duplicate rejection by
 hash_genes signature (:977-1018, 1040-1045, and the populate loop :1936-1978), BOOM replacement
 (:1023-1033) — driven by the counter-based draws the device uses (the reference's own draws come
@@ -13,6 +14,8 @@ Not restated: the device lets duplicates through after 16 batches of candidates 
 enough new ones (the reference loops on); the tests check that this never happened.
 """
 from __future__ import annotations
+
+import math
 
 import numpy as np
 
@@ -71,6 +74,90 @@ def initial_genes(seed: int, P: int, ng: int, rej: Rejector | None = None) -> np
     return np.asarray(out, np.int64).astype(np.int32).reshape(P, ng)
 
 
+KB = 0.001987206   # kcal/mol/K, LIB/statmech.h:26
+
+
+def sig_share(desc, peaks: float = 5.0, scale: float = 10.0) -> float:
+    """GB->sig_share from the gene limits (LIB/gaboom.cpp:300-309)."""
+    ng = desc.n_genes
+    s = 0.0
+    for g in range(ng):
+        w = float(desc.gene_max[g]) - float(desc.gene_min[g])
+        s += w * w
+    return math.sqrt(s / ng) / (2.0 * math.pow(peaks, 1.0 / ng)) / scale
+
+
+def clamped_ic(desc, genes) -> np.ndarray:
+    """to_ic of evaluated chromosomes: decoded, then clamped by eval_chromosome
+    (LIB/gaboom.cpp:1851-1859)."""
+    return np.clip(desc.genes_to_ic(genes), desc.gene_min, desc.gene_max)
+
+
+class Fitness:
+    """calculate_fitness (LIB/gaboom.cpp:1627-1760) of a population sorted by energy, the order
+    roulette_wheel walks it in (energy order; fitness order, descending, after a generation under
+    PSHARE, LIB/gaboom.cpp:498-499), its running sums and fitness_stats (:818-840). Niche counts
+    sum the reference's share term in order over j, the rmsp sum in order over the genes (the
+    reference's Eigen reduction may round its last bit otherwise); SMFREE's Boltzmann term is
+    exp(-beta (E_i - E_min)), the weight over the largest weight."""
+
+    def __init__(self, pop, pop_e, desc, model="PSHARE", initial=False, alpha=1.0, peaks=5.0,
+                 scale=10.0, entropy_weight=0.5, temperature=300.0):
+        P = len(pop)
+        fit = [float(P - i) for i in range(P)]
+        rank_only = model == "LINEAR" or (model == "SMFREE" and not temperature > 0)
+        if not rank_only:
+            ic = clamped_ic(desc, pop)
+            ng = ic.shape[1]
+            sig = sig_share(desc, peaks, scale)
+            share = []
+            for i in range(P):
+                s = 0.0
+                for j in range(P):
+                    acc = 0.0
+                    for q in range(ng):
+                        dq = ic[i, q] - ic[j, q]
+                        acc += dq * dq
+                    r = math.sqrt(acc / ng)
+                    if r <= sig:
+                        s += 1.0 - (r / sig if alpha == 1.0 else math.pow(r / sig, alpha))
+                share.append(s)
+            if model == "PSHARE":
+                fit = [fit[i] / share[i] for i in range(P)]
+            else:
+                beta = 1.0 / (KB * temperature)
+                e = [float(x) for x in pop_e]
+                e0 = e[0] if math.isfinite(e[0]) else 0.0
+                out = []
+                for i in range(P):
+                    bw = math.exp(-beta * (e[i] - e0)) if (math.isfinite(e[i]) and math.isfinite(e[0])) else 0.0
+                    blended = (1.0 - entropy_weight) * (fit[i] / P) + entropy_weight * bw
+                    out.append(blended * P / share[i])
+                fit = out
+        order = list(range(P))
+        if model == "PSHARE" and not initial:
+            order = sorted(range(P), key=lambda i: (-fit[i], i))
+        self.order = order
+        self.fit = [fit[i] for i in order]
+        cum, mx, tot = [], self.fit[0], 0.0
+        for f in self.fit:
+            tot += f
+            cum.append(tot)
+            mx = max(mx, f)
+        self.cum, self.total, self.max, self.avg = cum, tot, mx, tot / P
+
+    def roulette(self, u: float) -> int:
+        """roulette_wheel (LIB/gaboom.cpp:1158-1186): a roulette position."""
+        P = len(self.cum)
+        if not self.total > 0.0:
+            return int(u * P) % P
+        r = u * self.total
+        for k, c in enumerate(self.cum):
+            if c > r:
+                return k
+        return P - 1
+
+
 def roulette_linear(P: int, u: float) -> int:
     tot = float(P) * float(P + 1) * 0.5
     r = u * tot
@@ -91,15 +178,16 @@ def _mask(np_: int) -> int:
 
 def breed(pop: np.ndarray, gen: int, seed: int, cross_rate: float, mut_rate: float, nnew: int = 0,
           intragenes: bool = False, adaptive: bool = False, k=(1.0, 0.5, 1.0, 0.5),
-          rej: Rejector | None = None) -> np.ndarray:
-    """nnew children of generation gen + 1 from the sorted population `pop` (P, ng) int32: pair
-    kk's child 1, then its child 2, each kept unless `rej` has seen it, until there are nnew."""
+          rej: Rejector | None = None, fitness: Fitness | None = None) -> np.ndarray:
+    """nnew children of generation gen + 1 from the energy-sorted population `pop` (P, ng) int32
+    with its `fitness` (LINEAR when None): pair kk's child 1, then its child 2, each kept unless
+    `rej` has seen it, until there are nnew."""
     P, ng = pop.shape
     nnew = nnew or P
     out = []
     kk = 0
     while len(out) < nnew:
-        for ch in pair(pop, gen, seed, kk, cross_rate, mut_rate, intragenes, adaptive, k):
+        for ch in pair(pop, gen, seed, kk, cross_rate, mut_rate, intragenes, adaptive, k, fitness):
             if rej is None or rej.take(ch):
                 out.append(ch)
                 if len(out) == nnew:
@@ -109,12 +197,14 @@ def breed(pop: np.ndarray, gen: int, seed: int, cross_rate: float, mut_rate: flo
 
 
 def pair(pop: np.ndarray, gen: int, seed: int, kk: int, cross_rate: float, mut_rate: float,
-         intragenes: bool, adaptive: bool, k):
+         intragenes: bool, adaptive: bool, k, fitness: Fitness | None = None):
     """Pair kk of generation gen + 1's children (two lists of uint32 genes)."""
     P, ng = pop.shape
     u32 = pop.astype(np.int64) & 0xFFFFFFFF
     sb = (gen + 1) << 32
-    fit_max, fit_avg = float(P), 0.5 * float(P + 1)
+    if fitness is None:
+        fitness = Fitness(pop, np.zeros(P), None, "LINEAR")
+    fit_max, fit_avg = fitness.max, fitness.avg
     st = sb + kk
     d = 0
 
@@ -124,11 +214,12 @@ def pair(pop: np.ndarray, gen: int, seed: int, kk: int, cross_rate: float, mut_r
         d += 1
         return v
 
-    a = roulette_linear(P, draw())
-    b = roulette_linear(P, draw())
+    pa = fitness.roulette(draw())
+    pb = fitness.roulette(draw())
+    a, b = fitness.order[pa], fitness.order[pb]
     crossp, mutp = cross_rate, mut_rate
     if adaptive:
-        f1, f2 = float(P - a), float(P - b)
+        f1, f2 = fitness.fit[pa], fitness.fit[pb]
         hi, lo = max(f1, f2), min(f1, f2)
         denom = max(fit_max - fit_avg, 1e-15)
         crossp = k[0] * (fit_max - hi) / denom if hi > fit_avg else k[2]
@@ -206,7 +297,7 @@ def ensemble(snapshots, desc) -> np.ndarray:
     when every decoded gene is within 0.1 of the last one kept. Returns the kept energies."""
     g = np.concatenate([s[0] for s in snapshots])
     e = np.concatenate([s[1] for s in snapshots])
-    ic = desc.genes_to_ic(g)
+    ic = clamped_ic(desc, g)
     kept, last = [], None
     for i in np.argsort(e, kind="stable"):
         if last is None or not np.all(np.abs(ic[i] - last) < 0.1):

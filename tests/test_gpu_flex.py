@@ -158,7 +158,8 @@ def test_ga_generation_with_side_chains(flex):
     got = eng.read_population(slot, P)
     np.testing.assert_array_equal(got[0], pop)
     for gen in range(2):
-        child = ref_ga.breed(pop, gen, seed, pc, pm, rej=rej)
+        fz = ref_ga.Fitness(pop, pe, d, "PSHARE", initial=gen == 0)
+        child = ref_ga.breed(pop, gen, seed, pc, pm, rej=rej, fitness=fz)
         pop, pe = ref_ga.boom(pop, pe, child, check.eval_genes(child)["evalue"])
         eng.step()
         got = eng.read_population(slot, P)

@@ -28,9 +28,13 @@ GA_CASES = [
     (0, 0.02, dict()),
     (1, 0.02, dict(intragenes=True, adaptive=True, n_new=58)),
     (0, 0.02, dict(steady=True, n_new=20, adaptive=True, k=(0.8, 0.3, 0.9, 0.2))),
-    (0, 0.001, dict()),
-    (1, 0.001, dict(duplicates=True, n_new=31)),
+    (0, 0.001, dict(fitness="LINEAR")),
+    (1, 0.001, dict(duplicates=True, n_new=31, fitness="SMFREE", entropy_weight=0.3,
+                    temperature=500.0, adaptive=True)),
+    (0, 0.02, dict(sharing_alpha=2.0, sharing_peaks=3.0, sharing_scale=4.0, adaptive=True)),
+    (0, 0.02, dict(steady=True, n_new=40, fitness="SMFREE")),
 ]
+FITNESS_KEYS = ("sharing_alpha", "sharing_peaks", "sharing_scale", "entropy_weight", "temperature")
 
 
 @pytest.mark.parametrize("prec,pm,opts", GA_CASES)
@@ -51,9 +55,11 @@ def test_generation_matches_restated_operators(systems, prec, pm, opts):
     np.testing.assert_array_equal(pe, want_e)
     snaps = []
     bopts = {k: v for k, v in opts.items() if k in ("intragenes", "adaptive", "k")}
+    fopts = {k.replace("sharing_", ""): v for k, v in opts.items() if k in FITNESS_KEYS}
     nnew = opts.get("n_new", 0)
     for gen in range(3):
-        child = ref_ga.breed(pop, gen, seed, pc, pm, nnew=nnew, rej=rej, **bopts)
+        fz = ref_ga.Fitness(pop, pe, d, opts.get("fitness", "PSHARE"), initial=gen == 0, **fopts)
+        child = ref_ga.breed(pop, gen, seed, pc, pm, nnew=nnew, rej=rej, fitness=fz, **bopts)
         ce = check.eval_genes(child)["evalue"]
         if opts.get("steady"):
             want_g, want_e = ref_ga.steady(pop, pe, child, ce)
@@ -126,4 +132,4 @@ def test_best_energy_never_rises(systems):
     assert e == best[-1]
     assert np.isfinite(th["free_energy"])
     launches, graphs = eng.take_launches()
-    assert graphs == 12 and launches == 6 + 12 * 6
+    assert graphs == 12 and launches == 9 + 12 * 9

@@ -138,8 +138,10 @@ def test_struct_layouts_match_header():
 
 def test_ga_job_layout_matches_header():
     from flexaidds_gb300 import evaluator
-    assert C.sizeof(evaluator.GAJob) == 96
+    assert C.sizeof(evaluator.GAJob) == 136
     assert evaluator.GAJob.duplicates.offset == 88
+    assert evaluator.GAJob.fitness.offset == 92
+    assert evaluator.GAJob.temperature.offset == 128
 
 
 def test_hash_genes_signature_known_answers():
@@ -168,3 +170,28 @@ def test_ga_rejection_keeps_signatures_unique():
     # allowing duplicates takes the candidates in order
     free = ga.breed(pop, 5, 77, 0.9, 0.001, rej=ga.Rejector(d, allow=True))
     np.testing.assert_array_equal(free, ga.breed(pop, 5, 77, 0.9, 0.001))
+
+
+def test_fitness_models_restated():
+    """sig_share from the gene limits; PSHARE divides the rank by a niche count of at least one
+    and walks the population in fitness order after a generation; SMFREE with no temperature
+    ranks only."""
+    import math
+    from oracle import ga
+    d = prepare.prepare(system.make_inputs(600, 6.0, 10, 2, seed=4))
+    ng = d.n_genes
+    want = math.sqrt(sum((d.gene_max[g] - d.gene_min[g]) ** 2 for g in range(ng)) / ng)
+    want /= 2.0 * 5.0 ** (1.0 / ng)
+    assert abs(ga.sig_share(d) - want / 10.0) <= 1e-12 * want
+    pop = ga.initial_genes(9, 24, ng)
+    pe = np.sort(np.random.default_rng(1).normal(size=24))
+    lin = ga.Fitness(pop, pe, d, "LINEAR")
+    assert lin.fit == [float(24 - i) for i in range(24)] and lin.total == 300.0
+    first = ga.Fitness(pop, pe, d, "PSHARE", initial=True)
+    later = ga.Fitness(pop, pe, d, "PSHARE")
+    assert first.order == list(range(24))
+    assert all(f <= 24 - i for i, f in enumerate(first.fit))
+    assert sorted(first.fit, reverse=True) == later.fit
+    assert later.cum[-1] == later.total
+    flat = ga.Fitness(pop, pe, d, "SMFREE", temperature=0.0)
+    assert flat.fit == lin.fit
