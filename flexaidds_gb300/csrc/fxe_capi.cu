@@ -20,12 +20,13 @@
 namespace fxe {
 void launch_build(const DevSystem&, const DevWork&, int, const int32_t*, const double*, cudaStream_t);
 void launch_contacts(const DevSystem&, const DevWork&, int, cudaStream_t);
+void launch_order_poses(const DevSystem&, const DevWork&, int, cudaStream_t);
 namespace f32 {
-void launch_poses(const DevSystem&, const DevWork&, int, cudaStream_t);
+void launch_poses(const DevSystem&, const DevWork&, int, int*, cudaStream_t);
 cudaError_t configure_voronoi();
 }
 namespace f64 {
-void launch_poses(const DevSystem&, const DevWork&, int, cudaStream_t);
+void launch_poses(const DevSystem&, const DevWork&, int, int*, cudaStream_t);
 cudaError_t configure_voronoi();
 }
 int thermo_blocks(long, int);
@@ -490,7 +491,8 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
         FXE_TRY(ctx->alloc(&W.pose_seed, P * fxe::kMaxLig * 3), "workspace");
         FXE_TRY(ctx->alloc(&W.pose_rec, P * fxe::kMaxLig * fxe::kMaskWords), "workspace");
         FXE_TRY(ctx->alloc(&W.out, P), "workspace");
-        FXE_TRY(ctx->alloc(&W.counters, 4), "workspace");
+        FXE_TRY(ctx->alloc(&W.counters, 8), "workspace");   // [4]: the pose queue of pose_kernel
+        FXE_TRY(ctx->alloc(&W.pose_order, P), "workspace");
         FXE_TRY(ctx->alloc(&ctx->d_genes, P * (ng > 0 ? ng : 1)), "staging");
         FXE_TRY(ctx->alloc(&ctx->d_icin, P * (ng > 0 ? ng : 1)), "staging");
         FXE_TRY(cudaDeviceSynchronize(), "context set-up");
@@ -536,12 +538,13 @@ fxe_status run_chunk(fxe_context* ctx, int nb, const int32_t* d_genes, const dou
     if (t) cudaEventRecord(ctx->ev[1], s);
     fxe::launch_contacts(ctx->S, ctx->W, nb, s);
     if (t) cudaEventRecord(ctx->ev[2], s);
-    if (ctx->precision == FXE_PRECISION_FAST) fxe::f32::launch_poses(ctx->S, ctx->W, nb, s);
-    else fxe::f64::launch_poses(ctx->S, ctx->W, nb, s);
+    fxe::launch_order_poses(ctx->S, ctx->W, nb, s);
+    if (ctx->precision == FXE_PRECISION_FAST) fxe::f32::launch_poses(ctx->S, ctx->W, nb, ctx->W.counters + 4, s);
+    else fxe::f64::launch_poses(ctx->S, ctx->W, nb, ctx->W.counters + 4, s);
     if (t) cudaEventRecord(ctx->ev[3], s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
-    ctx->launches += 3;
+    ctx->launches += 4;
     if (t) {
         FXE_TRY(cudaEventSynchronize(ctx->ev[3]), "timing");
         for (int k = 0; k < 3; ++k) {
@@ -839,10 +842,10 @@ namespace fxe {
 void launch_build_jobs(const Job*, int, int, cudaStream_t);
 void launch_contacts_jobs(const Job*, int, long long, cudaStream_t);
 namespace f32 {
-void launch_poses_jobs(const Job*, int, int, cudaStream_t);
+void launch_poses_jobs(const Job*, int, int, int*, cudaStream_t);
 }
 namespace f64 {
-void launch_poses_jobs(const Job*, int, int, cudaStream_t);
+void launch_poses_jobs(const Job*, int, int, int*, cudaStream_t);
 }
 }  // namespace fxe
 
@@ -859,9 +862,11 @@ struct fxe_batch {
     int32_t* h_genes = nullptr;            // pinned
     fxe_cf* d_out = nullptr;
     fxe_cf* h_out = nullptr;               // pinned
+    int* d_next = nullptr;                 // pose queue of the polyhedron launch
     int64_t launches = 0;
     ~fxe_batch() {
         if (staged) cudaEventDestroy(staged);
+        if (d_next) cudaFree(d_next);
         if (d_jobs) cudaFree(d_jobs);
         if (h_jobs) cudaFreeHost(h_jobs);
         if (d_genes) cudaFree(d_genes);
@@ -888,6 +893,7 @@ extern "C" fxe_status fxe_batch_create(int32_t max_jobs, int64_t max_poses, int3
         FXE_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         FXE_TRY(cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming), "cudaEventCreate");
         FXE_TRY(cudaMalloc(&b->d_jobs, sizeof(fxe::Job) * max_jobs), "batch job table");
+        FXE_TRY(cudaMalloc(&b->d_next, sizeof(int)), "batch pose queue");
         FXE_TRY(cudaMallocHost(&b->h_jobs, sizeof(fxe::Job) * max_jobs), "batch job table");
         FXE_TRY(cudaMalloc(&b->d_genes, sizeof(int32_t) * max_poses * max_genes), "batch staging");
         FXE_TRY(cudaMallocHost(&b->h_genes, sizeof(int32_t) * max_poses * max_genes), "batch staging");
@@ -937,8 +943,8 @@ fxe_status batch_launch(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, cudaS
     FXE_TRY(cudaEventRecord(b->staged, s), "cudaEventRecord");
     fxe::launch_build_jobs(b->d_jobs, k, total, s);
     fxe::launch_contacts_jobs(b->d_jobs, k, items, s);
-    if (prec == FXE_PRECISION_FAST) fxe::f32::launch_poses_jobs(b->d_jobs, k, total, s);
-    else fxe::f64::launch_poses_jobs(b->d_jobs, k, total, s);
+    if (prec == FXE_PRECISION_FAST) fxe::f32::launch_poses_jobs(b->d_jobs, k, total, b->d_next, s);
+    else fxe::f64::launch_poses_jobs(b->d_jobs, k, total, b->d_next, s);
     FXE_TRY(cudaGetLastError(), "batched kernel launch");
     b->launches += 3;
     return FXE_OK;
@@ -1054,6 +1060,7 @@ struct fxe_ga {
     int* d_ids = nullptr;               // [max_jobs] 0..max_jobs-1
     int* d_run = nullptr;               // [max_jobs] running slots of the captured graph
     fxe::Job* d_eval = nullptr;         // [max_jobs] batched-evaluation table of the running slots
+    int* d_next = nullptr;              // pose queue of the polyhedron launch
     std::vector<int> run;               // running slots of the captured graph
     cudaGraphExec_t exec = nullptr;
     bool dirty = true;
@@ -1067,6 +1074,7 @@ struct fxe_ga {
         if (d_ids) cudaFree(d_ids);
         if (d_run) cudaFree(d_run);
         if (d_eval) cudaFree(d_eval);
+        if (d_next) cudaFree(d_next);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -1089,6 +1097,7 @@ extern "C" fxe_status fxe_ga_create(int32_t max_jobs, int32_t precision, fxe_ga*
         FXE_TRY(cudaMalloc(&e->d_ids, sizeof(int) * max_jobs), "GA state");
         FXE_TRY(cudaMalloc(&e->d_run, sizeof(int) * max_jobs), "GA state");
         FXE_TRY(cudaMalloc(&e->d_eval, sizeof(fxe::Job) * max_jobs), "GA state");
+        FXE_TRY(cudaMalloc(&e->d_next, sizeof(int)), "GA state");
         std::vector<int> ids(max_jobs);
         for (int i = 0; i < max_jobs; ++i) ids[i] = i;
         FXE_TRY(cudaMemcpy(e->d_ids, ids.data(), sizeof(int) * max_jobs, cudaMemcpyHostToDevice), "GA state");
@@ -1293,8 +1302,8 @@ extern "C" fxe_status fxe_ga_step(fxe_ga* e) {
         fxe::launch_ga_breed(e->d_all, e->d_run, n, e->stream);
         fxe::launch_build_jobs(e->d_eval, n, total, e->stream);
         fxe::launch_contacts_jobs(e->d_eval, n, items, e->stream);
-        if (e->precision == FXE_PRECISION_FAST) fxe::f32::launch_poses_jobs(e->d_eval, n, total, e->stream);
-        else fxe::f64::launch_poses_jobs(e->d_eval, n, total, e->stream);
+        if (e->precision == FXE_PRECISION_FAST) fxe::f32::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->stream);
+        else fxe::f64::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->stream);
         fxe::launch_ga_select(e->d_all, e->d_run, n, false, e->stream);
         fxe::launch_ga_fitness(e->d_all, e->d_run, n, false, e->stream);
         cudaError_t ce = cudaStreamEndCapture(e->stream, &g);

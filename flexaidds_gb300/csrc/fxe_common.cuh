@@ -140,6 +140,7 @@ struct DevWork {
     uint32_t* pose_rec;    // [P * kMaxLig * kMaskWords] mobile partners each processed atom kept
     fxe_cf* out;           // [P]
     int* counters;         // [4]: unused, hull failures, capacity, no-partner faces
+    int* pose_order;       // [P] poses in the order pose_kernel takes them (costliest first)
 };
 
 // One job of a batched launch: a context's system and workspace (W.out pointing at the job's

@@ -184,6 +184,61 @@ contacts_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, long long total) 
     contacts_atom(job.S, job.W, (int)(r / nm), (int)(r % nm), lane);
 }
 
+// The order pose_kernel takes the poses in: costliest first (sum over the pose's atoms of the
+// squared candidate count, which the hull walk's plane tests grow with), so that the slowest
+// poses start early and the launch does not end on one of them while the SMs run dry. Sorted in
+// segments of kOrderSeg poses, one block each.
+constexpr int kOrderSeg = 4096;
+
+__global__ void __launch_bounds__(1024) order_poses_kernel(const int* __restrict__ cand_n, int nm, int n,
+                                                           int* __restrict__ order) {
+    __shared__ long long key[kOrderSeg];
+    __shared__ int idx[kOrderSeg];
+    const int base = blockIdx.x * kOrderSeg;
+    const int m = min(kOrderSeg, n - base);
+    int len = 1;
+    while (len < m) len <<= 1;
+    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+        long long c = 0x7FFFFFFFFFFFFFFFll;   // padding sorts last
+        if (i < m) {
+            const int* cn = cand_n + (size_t)(base + i) * nm;
+            long long cost = 0;
+            for (int a = 0; a < nm; ++a) {
+                const int k = cn[a];
+                if (k > 0) cost += (long long)k * k;
+            }
+            c = -cost;
+        }
+        key[i] = c;
+        idx[i] = i;
+    }
+    __syncthreads();
+    for (int k = 2; k <= len; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < len; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const bool up = (i & k) == 0;
+                    const long long a = key[i], b = key[l];
+                    const bool gt = a > b || (a == b && idx[i] > idx[l]);
+                    if (gt == up) {
+                        key[i] = b;
+                        key[l] = a;
+                        const int t = idx[i];
+                        idx[i] = idx[l];
+                        idx[l] = t;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < m; i += blockDim.x) order[base + i] = base + idx[i];
+}
+
+void launch_order_poses(const DevSystem& S, const DevWork& W, int n, cudaStream_t st) {
+    order_poses_kernel<<<(n + kOrderSeg - 1) / kOrderSeg, 1024, 0, st>>>(W.cand_n, S.n_sc + S.n_lig, n, W.pose_order);
+}
+
 void launch_contacts(const DevSystem& S, const DevWork& W, int n, cudaStream_t st) {
     const long warps = (long)n * (S.n_sc + S.n_lig);
     contacts_kernel<<<(unsigned)((warps + 3) / 4), 128, 0, st>>>(S, W, n);

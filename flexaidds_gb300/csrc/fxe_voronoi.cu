@@ -1332,44 +1332,73 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
     if (lane == 0) W.out[p] = cf;
 }
 
+// Poses are handed out from a queue (`next`, zeroed before the launch): the launch keeps only as
+// many blocks as the SMs hold at once, and each warp takes the next pose when it finishes one.
+// Pose times vary several-fold, so this fills the SMs to the end of the launch where a grid of
+// one block per pose pair left a partial last wave and idle SMs behind the slowest poses.
+__device__ __forceinline__ int next_pose(int* next, int lane) {
+    int p = 0;
+    if (lane == 0) p = atomicAdd(next, 1);
+    return __shfl_sync(kFull, p, 0);
+}
+
 __global__ void __launch_bounds__(kVorWarps * 32)
-pose_kernel(DevSystem S, DevWork W, int n) {
+pose_kernel(DevSystem S, DevWork W, int n, int* next) {
     extern __shared__ __align__(16) unsigned char smem[];
     PoseShared& ps = reinterpret_cast<PoseShared*>(smem)[threadIdx.x >> 5];
-    const int p = blockIdx.x * kVorWarps + (threadIdx.x >> 5);
-    if (p >= n) return;
-    score_pose(S, W, p, threadIdx.x & 31, ps);
+    const int lane = threadIdx.x & 31;
+    for (int q = next_pose(next, lane); q < n; q = next_pose(next, lane)) {
+        score_pose(S, W, W.pose_order[q], lane, ps);
+        __syncwarp();
+    }
 }
 
 // The same over the poses of several jobs; the job's system and workspace descriptors are read
 // from the job table (they stay in L1), keeping shared memory for the polyhedron workspace.
 __global__ void __launch_bounds__(kVorWarps * 32)
-pose_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, int total) {
+pose_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, int total, int* next) {
     extern __shared__ __align__(16) unsigned char smem[];
     PoseShared& ps = reinterpret_cast<PoseShared*>(smem)[threadIdx.x >> 5];
-    const int gp = blockIdx.x * kVorWarps + (threadIdx.x >> 5);
-    if (gp >= total) return;
-    const Job& job = jobs[find_job(jobs, n_jobs, gp, false)];
-    score_pose(job.S, job.W, gp - job.pose0, threadIdx.x & 31, ps);
+    const int lane = threadIdx.x & 31;
+    for (int gp = next_pose(next, lane); gp < total; gp = next_pose(next, lane)) {
+        const Job& job = jobs[find_job(jobs, n_jobs, gp, false)];
+        score_pose(job.S, job.W, gp - job.pose0, lane, ps);
+        __syncwarp();
+    }
 }
 
 size_t pose_smem_bytes() { return sizeof(PoseShared) * kVorWarps; }
 size_t pose_jobs_smem_bytes() { return sizeof(PoseShared) * kVorWarps; }
 
-void launch_poses(const DevSystem& S, const DevWork& W, int n, cudaStream_t st) {
-    pose_kernel<<<(unsigned)((n + kVorWarps - 1) / kVorWarps), kVorWarps * 32, pose_smem_bytes(), st>>>(S, W, n);
+static int g_resident_blocks = 0;   // blocks of pose_kernel the device holds at once
+
+static unsigned pose_blocks(int n) {
+    const int want = (n + kVorWarps - 1) / kVorWarps;
+    return (unsigned)(g_resident_blocks > 0 && g_resident_blocks < want ? g_resident_blocks : want);
 }
 
-void launch_poses_jobs(const Job* jobs, int n_jobs, int total, cudaStream_t st) {
-    pose_kernel_jobs<<<(unsigned)((total + kVorWarps - 1) / kVorWarps), kVorWarps * 32, pose_jobs_smem_bytes(),
-                       st>>>(jobs, n_jobs, total);
+void launch_poses(const DevSystem& S, const DevWork& W, int n, int* next, cudaStream_t st) {
+    cudaMemsetAsync(next, 0, sizeof(int), st);
+    pose_kernel<<<pose_blocks(n), kVorWarps * 32, pose_smem_bytes(), st>>>(S, W, n, next);
+}
+
+void launch_poses_jobs(const Job* jobs, int n_jobs, int total, int* next, cudaStream_t st) {
+    cudaMemsetAsync(next, 0, sizeof(int), st);
+    pose_kernel_jobs<<<pose_blocks(total), kVorWarps * 32, pose_jobs_smem_bytes(), st>>>(jobs, n_jobs, total, next);
 }
 
 cudaError_t configure_voronoi() {
     cudaError_t e = cudaFuncSetAttribute(pose_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pose_smem_bytes());
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(pose_kernel_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)pose_jobs_smem_bytes());
+    e = cudaFuncSetAttribute(pose_kernel_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pose_jobs_smem_bytes());
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pose_kernel, kVorWarps * 32, pose_smem_bytes())) != cudaSuccess)
+        return e;
+    g_resident_blocks = sms * (per_sm > 0 ? per_sm : 1);
+    return cudaSuccess;
 }
 
 }  // namespace FXE_VARIANT
