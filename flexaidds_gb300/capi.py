@@ -22,7 +22,7 @@ POSE_SCORED, POSE_POLYHEDRON_FAILED, POSE_CLASHED, POSE_CAPACITY = 0, 1, 2, 3
 
 class FlexResidue(C.Structure):
     _fields_ = [("first", C.c_int32), ("n_atoms", C.c_int32), ("n_rot", C.c_int32),
-                ("backbone", _b), ("rot_xyz", _f), ("bonded", _b)]
+                ("backbone", _b), ("rot_xyz", _f), ("bonded", _b), ("prob", C.c_float)]
 
 
 class ReceptorDesc(C.Structure):
@@ -105,6 +105,7 @@ class Packed:
                 fr[i].backbone = ptr(k(d.flex_isbb[a0:a0 + na], np.int8), _b)
                 fr[i].rot_xyz = ptr(k(d.flex_xyz[r0:r0 + nr * na], np.float32), _f)
                 fr[i].bonded = ptr(k(d.flex_bonded[b0:b0 + na * na], np.int8), _b)
+                fr[i].prob = float(d.flex_prob[i])
                 a0, r0, b0 = a0 + na, r0 + nr * na, b0 + na * na
             self.keep.append(fr)
             r.flex = fr

@@ -56,6 +56,7 @@ struct DevBlock {
     std::vector<void*> ptrs;
     std::vector<float4> grid_ic;   // host copy of the cleft-grid ICs
     std::vector<int> flex_nrot;    // rotamers of each flexible side chain
+    std::vector<float> flex_prob;  // their flxsc.prob (GA engine)
     ~DevBlock() {
         for (void* p : ptrs) cudaFree(p);
     }
@@ -162,9 +163,9 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
         for (int r = 0; r < rec->n_flex; ++r) {
             const fxe_flex_residue& f = rec->flex[r];
             if (f.first < next || f.n_atoms < 1 || f.n_atoms > 255 || f.first + f.n_atoms > rec->n_atoms ||
-                f.n_rot < 2 || !f.backbone || !f.rot_xyz || !f.bonded)
+                f.n_rot < 2 || !f.backbone || !f.rot_xyz || !f.bonded || !(f.prob >= 0.0f && f.prob <= 1.0f))
                 return fail(FXE_ERR_INVALID_ARGS, "flexible side chain " + std::to_string(r) +
-                                                      ": atoms out of order or range, or fewer than two rotamers");
+                                                      ": atoms out of order or range, fewer than two rotamers, or prob outside [0, 1]");
             next = f.first + f.n_atoms;
             int ns = 0;
             for (int k = 0; k < f.n_atoms; ++k) ns += f.backbone[k] ? 0 : 1;
@@ -296,6 +297,7 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
         S.n_flex = rec->n_flex;
         S.n_sc = (int)sc_slot.size();
         ctx->receptor->flex_nrot = flex_nrot;
+        for (int r = 0; r < rec->n_flex; ++r) ctx->receptor->flex_prob.push_back(rec->flex[r].prob);
         if (S.n_flex) {
             FXE_TRY(ctx->upload_receptor(&S.sc_slot, sc_slot.data(), sc_slot.size()), "side-chain upload");
             FXE_TRY(ctx->upload_receptor(&S.sc_res, sc_res.data(), sc_res.size()), "side-chain upload");
@@ -1130,7 +1132,7 @@ extern "C" fxe_status fxe_ga_job_bytes(const fxe_ga_job* job, int64_t* bytes) {
     const int64_t P = job->population, ng = job->ctx->S.n_genes, G = job->generations;
     *bytes = P * ng * 4 * 3 + P * 8 * 2 + P * (int64_t)sizeof(fxe_cf) + G * P * (ng * 4 + 8) + 16 +
              2 * (P + 8) * (ng * 4 + 8) + (job->duplicates ? 0 : 8 * (int64_t)seen_slots(*job)) +
-             P * ng * 8 + P * (8 * 3 + 4) + 32;
+             P * ng * 8 + P * (8 * 3 + 4) + 32 + ng * 4;
     return FXE_OK;
 }
 
@@ -1197,6 +1199,27 @@ extern "C" fxe_status fxe_ga_admit(fxe_ga* e, const fxe_ga_job* job, int32_t* sl
         J.gene_min = ctx->S.gene_min;
         J.gene_del = ctx->S.gene_del;
         J.gene_max = ctx->S.gene_max;
+        {
+            // rotamer genes and their side chains' probabilities; like the reference's mutation
+            // (genes before num_genes - nflxsc_real, then each rotamer gene) they come last
+            std::vector<float> gp(ng, -1.0f);
+            std::vector<int> gt(ng), ga(ng);
+            FXE_TRY(cudaMemcpy(gt.data(), ctx->S.gene_type, sizeof(int) * ng, cudaMemcpyDeviceToHost), "GA genes");
+            FXE_TRY(cudaMemcpy(ga.data(), ctx->S.gene_atom, sizeof(int) * ng, cudaMemcpyDeviceToHost), "GA genes");
+            bool seen_rot = false;
+            for (int g = 0; g < ng; ++g) {
+                if (gt[g] == 4) {
+                    gp[g] = ctx->receptor->flex_prob[ga[g]];
+                    seen_rot = true;
+                } else if (seen_rot) {
+                    return fail(FXE_ERR_INVALID_ARGS, "rotamer genes must come after the other genes");
+                }
+            }
+            FXE_TRY(get(sizeof(float) * ng, &q), "GA genes");
+            J.gene_prob = (const float*)q;
+            FXE_TRY(cudaMemcpyAsync(q, gp.data(), sizeof(float) * ng, cudaMemcpyHostToDevice, e->stream), "GA genes");
+            FXE_TRY(cudaStreamSynchronize(e->stream), "GA genes");
+        }
         // fitness model; sig_share as LIB/gaboom.cpp:300-309 forms it from the gene limits
         J.fitness = job->fitness;
         const double alpha = job->sharing_alpha > 0.0 ? job->sharing_alpha : 1.0;

@@ -239,6 +239,7 @@ struct GaJob {
     const double* gene_min;
     const double* gene_del;
     const double* gene_max;
+    const float* gene_prob;  // [ng] a rotamer gene's side-chain probability (flxsc.prob), -1 otherwise
     // fitness (calculate_fitness, LIB/gaboom.cpp:1627-1760) and the order roulette walks the
     // population in: energy order, or fitness order after a generation under PSHARE
     int fitness;             // kFitPshare, kFitLinear, kFitSmfree

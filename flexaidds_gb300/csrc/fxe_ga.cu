@@ -135,12 +135,21 @@ __device__ __forceinline__ int32_t uniform_gene(const GaJob& J, uint64_t i) {
 }
 
 // Initial candidates c0 .. c0 + 2 npairs - 1: uniform genes in [0, 2^31) like the reference's
-// RandomInt over MAX_RANDOM_VALUE; candidate c's gene q is draw c * ng + q.
+// RandomInt over MAX_RANDOM_VALUE; candidate c's gene q is draw c * ng + q. A rotamer gene is
+// drawn only with its side chain's probability, else 0 (rotamer 0, the input conformation;
+// generate_random_individual, LIB/gaboom.cpp:1875-1895), that chance being draw c * ng + q of
+// stream kInitRotStream.
+constexpr uint64_t kInitRotStream = 0xFFFFFFFEull;
+
 __device__ void initial_candidates(const GaJob& J, long long c0, int npairs) {
     const int ng = J.ng;
     for (int c = threadIdx.x; c < 2 * npairs; c += blockDim.x) {
         int32_t* g = J.cand + (size_t)c * ng;
-        for (int q = 0; q < ng; ++q) g[q] = uniform_gene(J, (uint64_t)(c0 + c) * ng + q);
+        for (int q = 0; q < ng; ++q) {
+            const uint64_t i = (uint64_t)(c0 + c) * ng + q;
+            const float pr = J.gene_prob[q];
+            g[q] = pr < 0.0f || uniform(J.seed, kInitRotStream, i) < (double)pr ? uniform_gene(J, i) : 0;
+        }
         J.cand_sig[c] = signature(J, g);
     }
 }
@@ -228,10 +237,13 @@ __device__ void breed_pair(const GaJob& J, int g, int k, int32_t* john, int32_t*
             m[gen_b] = (int32_t)((uj & optr) | (um & ~optr));
         }
     }
-    // mutate both children (LIB/gaboom.cpp:2620-2641)
+    // mutate both children (LIB/gaboom.cpp:2620-2641): the genes before the rotamer genes, then
+    // each rotamer gene with its side chain's probability (LIB/gaboom.cpp:944-966)
     for (int c = 0; c < 2; ++c) {
         int32_t* ch = c == 0 ? john : m;
         for (int q = 0; q < ng; ++q) {
+            const float pr = J.gene_prob[q];
+            if (pr >= 0.0f && !(uniform(J.seed, st, d++) < (double)pr)) continue;
             uint32_t optr = 0u;
             for (int bit = 0; bit < 32; ++bit)
                 if (uniform(J.seed, st, d++) < mutp) optr |= 1u << bit;

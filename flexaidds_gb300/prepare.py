@@ -328,7 +328,8 @@ def prepare(inp: SystemInputs) -> Descriptor:
                   flex_nrot=np.asarray([f.n_rot for f in flex], np.int32),
                   flex_isbb=np.concatenate([f.isbb for f in flex]).astype(np.int8),
                   flex_xyz=np.concatenate([f.rot_xyz.reshape(-1, 3) for f in flex]).astype(np.float32),
-                  flex_bonded=np.concatenate(bonded).astype(np.int8))
+                  flex_bonded=np.concatenate(bonded).astype(np.int8),
+                  flex_prob=np.asarray([f.prob for f in flex], np.float32))
     base = ic2.copy()
     lrec4 = np.concatenate([lrec.astype(np.int32), rec3[:, None]], axis=1)
     w, off, ex, ey = inp.emat_tables()

@@ -71,6 +71,7 @@ class FlexResidue:
     isbb: np.ndarray          # (natm,) int8, 1 = backbone atom (not scored)
     rot_xyz: np.ndarray       # (n_rot, natm, 3) float32
     bonds: list               # residue-local (i, j)
+    prob: float = 1.0         # GA: chance a child's rotamer gene mutates / an initial one is drawn
 
     @property
     def natm(self) -> int:
@@ -252,6 +253,9 @@ def add_flexible_residues(rec: Receptor, n_res: int, n_rot: int, seed: int,
         types = rng.integers(1, NTYPES, size=natm).astype(np.int32)
         bonds = [(0, 1), (1, 2), (2, 3), (1, 4)] + [(4 + i, 5 + i) for i in range(nb - 1)]
         residues[a] = (np.asarray(confs, np.float32), types, bonds)
+    # per-residue probabilities of the GA's rotamer moves, in the range of the reference's
+    # internal per-residue-type values (0.05-0.55)
+    probs = {a: float(np.float32(rng.uniform(0.05, 0.55))) for a in anchors}
     # rigid atoms within reach of any rotamer atom go (the anchors become the residues' CA)
     every = np.concatenate([r[0].reshape(-1, 3) for r in residues.values()]).astype(np.float64)
     keep = np.ones(len(xyz), bool)
@@ -268,7 +272,7 @@ def add_flexible_residues(rec: Receptor, n_res: int, n_rot: int, seed: int,
             natm = confs.shape[1]
             flex.append(FlexResidue(first=first,
                                     isbb=np.asarray([1, 1, 1, 1] + [0] * (natm - 4), np.int8),
-                                    rot_xyz=confs, bonds=bonds))
+                                    rot_xyz=confs, bonds=bonds, prob=probs[k]))
             out_xyz.extend(confs[0])
             out_t.extend(types)
             out_r.extend(type_radius(t, 0) for t in types)

@@ -112,6 +112,7 @@ class Descriptor:
     flex_isbb: np.ndarray = None     # (sum natm,) int8, 1 = backbone (not scored)
     flex_xyz: np.ndarray = None      # (sum nrot * natm, 3) float32
     flex_bonded: np.ndarray = None   # (sum natm * natm,) int8, residue.bonded
+    flex_prob: np.ndarray = None     # (R,) float32, flxsc.prob (GA rotamer moves)
     decode: list = field(default_factory=list)
 
     def __post_init__(self):
@@ -122,6 +123,8 @@ class Descriptor:
             self.flex_isbb = np.zeros(0, np.int8)
             self.flex_xyz = np.zeros((0, 3), np.float32)
             self.flex_bonded = np.zeros(0, np.int8)
+        if self.flex_prob is None:
+            self.flex_prob = np.ones(self.flex_first.shape[0], np.float32)
 
     @property
     def n_flex(self):
@@ -163,7 +166,7 @@ class Descriptor:
         out = {prefix + k: np.asarray(getattr(self, k)) for k in self._ARRAYS}
         out.update({prefix + k: np.asarray(getattr(self, k)) for k in self._SCALARS})
         if self.n_flex:
-            out.update({prefix + k: np.asarray(getattr(self, k)) for k in self._FLEX})
+            out.update({prefix + k: np.asarray(getattr(self, k)) for k in self._FLEX + ("flex_prob",)})
         return out
 
     @classmethod
@@ -171,6 +174,8 @@ class Descriptor:
         kw = {k: np.asarray(arrs[prefix + k]).copy() for k in cls._ARRAYS}
         if prefix + "flex_first" in arrs:
             kw.update({k: np.asarray(arrs[prefix + k]).copy() for k in cls._FLEX})
+            if prefix + "flex_prob" in arrs:
+                kw["flex_prob"] = np.asarray(arrs[prefix + "flex_prob"]).copy()
         for k in cls._SCALARS:
             v = np.asarray(arrs[prefix + k]).item()
             kw[k] = int(v) if k in ("ntypes", "intramolecular") else float(v)

@@ -48,6 +48,10 @@ typedef struct fxe_flex_residue {
     const int8_t* backbone;    /* n_atoms: 1 = backbone atom (keeps its place, not scored) */
     const float* rot_xyz;      /* n_rot * n_atoms * 3 */
     const int8_t* bonded;      /* n_atoms * n_atoms: residue.bonded (-1: not within bloops) */
+    float prob;                /* flxsc.prob, for the GA engine: the chance that a child's rotamer
+                                  gene mutates and that an initial chromosome draws one (else
+                                  rotamer 0) (LIB/gaboom.cpp:944-966, 1875-1895; the reference's
+                                  per-residue defaults are set_intprob's, LIB/set_intprob.cpp) */
 } fxe_flex_residue;
 
 /* Receptor, in the reference's Calc order (residue order, LIB/Vcontacts.cpp:1600-1630),

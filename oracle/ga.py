@@ -62,12 +62,28 @@ class Rejector:
         return True
 
 
-def initial_genes(seed: int, P: int, ng: int, rej: Rejector | None = None) -> np.ndarray:
-    """Uniform chromosomes; candidate c's gene q is draw c * ng + q. With `rej`, candidates whose
-    signature was seen are skipped (the populate loop)."""
+def gene_probs(desc) -> list:
+    """Per gene: the side chain's probability for a rotamer gene (flxsc.prob), else -1."""
+    return [float(np.float32(desc.flex_prob[int(desc.gene_atm[g])])) if int(desc.gene_typ[g]) == 4 else -1.0
+            for g in range(desc.n_genes)]
+
+
+INIT_ROT_STREAM = 0xFFFFFFFE
+
+
+def initial_genes(seed: int, P: int, ng: int, rej: Rejector | None = None, prob=None) -> np.ndarray:
+    """Uniform chromosomes; candidate c's gene q is draw c * ng + q. A rotamer gene (prob[q] >= 0)
+    is drawn only with its side chain's probability, else 0 (generate_random_individual,
+    LIB/gaboom.cpp:1875-1895). With `rej`, candidates whose signature was seen are skipped (the
+    populate loop)."""
+    prob = prob or [-1.0] * ng
     out, c = [], 0
     while len(out) < P:
-        g = [mix64(seed ^ mix64((0xFFFFFFFF * 977 + c * ng + q) & M64)) >> 33 for q in range(ng)]
+        g = []
+        for q in range(ng):
+            i = c * ng + q
+            take = prob[q] < 0 or uniform(seed, INIT_ROT_STREAM, i) < prob[q]
+            g.append(mix64(seed ^ mix64((0xFFFFFFFF * 977 + i) & M64)) >> 33 if take else 0)
         c += 1
         if rej is None or rej.take(g):
             out.append(g)
@@ -178,7 +194,7 @@ def _mask(np_: int) -> int:
 
 def breed(pop: np.ndarray, gen: int, seed: int, cross_rate: float, mut_rate: float, nnew: int = 0,
           intragenes: bool = False, adaptive: bool = False, k=(1.0, 0.5, 1.0, 0.5),
-          rej: Rejector | None = None, fitness: Fitness | None = None) -> np.ndarray:
+          rej: Rejector | None = None, fitness: Fitness | None = None, prob=None) -> np.ndarray:
     """nnew children of generation gen + 1 from the energy-sorted population `pop` (P, ng) int32
     with its `fitness` (LINEAR when None): pair kk's child 1, then its child 2, each kept unless
     `rej` has seen it, until there are nnew."""
@@ -187,7 +203,7 @@ def breed(pop: np.ndarray, gen: int, seed: int, cross_rate: float, mut_rate: flo
     out = []
     kk = 0
     while len(out) < nnew:
-        for ch in pair(pop, gen, seed, kk, cross_rate, mut_rate, intragenes, adaptive, k, fitness):
+        for ch in pair(pop, gen, seed, kk, cross_rate, mut_rate, intragenes, adaptive, k, fitness, prob):
             if rej is None or rej.take(ch):
                 out.append(ch)
                 if len(out) == nnew:
@@ -197,9 +213,10 @@ def breed(pop: np.ndarray, gen: int, seed: int, cross_rate: float, mut_rate: flo
 
 
 def pair(pop: np.ndarray, gen: int, seed: int, kk: int, cross_rate: float, mut_rate: float,
-         intragenes: bool, adaptive: bool, k, fitness: Fitness | None = None):
+         intragenes: bool, adaptive: bool, k, fitness: Fitness | None = None, prob=None):
     """Pair kk of generation gen + 1's children (two lists of uint32 genes)."""
     P, ng = pop.shape
+    prob = prob or [-1.0] * ng
     u32 = pop.astype(np.int64) & 0xFFFFFFFF
     sb = (gen + 1) << 32
     if fitness is None:
@@ -258,6 +275,9 @@ def pair(pop: np.ndarray, gen: int, seed: int, kk: int, cross_rate: float, mut_r
             mary[gen_b] = (uj & m) | (um & ~m & 0xFFFFFFFF)
     for ch in (john, mary):
         for q in range(ng):
+            # rotamer genes mutate with their side chain's probability (LIB/gaboom.cpp:944-966)
+            if prob[q] >= 0 and not draw() < prob[q]:
+                continue
             m = 0
             for bit in range(32):
                 if draw() < mutp:

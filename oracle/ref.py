@@ -165,7 +165,7 @@ class RefHarness:
                       flex_nrot=np.asarray([f.n_rot for f in rec.flex], np.int32),
                       flex_isbb=np.concatenate([f.isbb for f in rec.flex]).astype(np.int8),
                       flex_xyz=np.concatenate([f.rot_xyz.reshape(-1, 3) for f in rec.flex]).astype(np.float32),
-                      flex_bonded=fb)
+                      flex_bonded=fb, flex_prob=np.asarray([f.prob for f in rec.flex], np.float32))
         return Descriptor(**fx,
             rec_xyz=rec.xyz.copy(), rec_radius=rec.radius.copy(), rec_type=rec.type.copy(),
             ori=ori, globalmin=gmin, globalmax=gmax, maxwidth=float(mw[0]), grid_ic=grid_ic,

@@ -152,14 +152,17 @@ def test_ga_generation_with_side_chains(flex):
     eng = evaluator.GAEngine(max_jobs=1)
     slot = eng.admit(eng.job(ev, P, 2, seed, pc, pm), ev)
     rej = ref_ga.Rejector(d)
-    init = ref_ga.initial_genes(seed, P, d.n_genes, rej)
+    prob = ref_ga.gene_probs(d)
+    assert sum(p >= 0 for p in prob) == 3
+    init = ref_ga.initial_genes(seed, P, d.n_genes, rej, prob)
+    assert (init[:, -3:] == 0).any()          # rotamer genes left at rotamer 0 by their chance
     e0 = check.eval_genes(init)["evalue"]
     pop, pe = ref_ga.boom(init[:0], e0[:0], init, e0)
     got = eng.read_population(slot, P)
     np.testing.assert_array_equal(got[0], pop)
     for gen in range(2):
         fz = ref_ga.Fitness(pop, pe, d, "PSHARE", initial=gen == 0)
-        child = ref_ga.breed(pop, gen, seed, pc, pm, rej=rej, fitness=fz)
+        child = ref_ga.breed(pop, gen, seed, pc, pm, rej=rej, fitness=fz, prob=prob)
         pop, pe = ref_ga.boom(pop, pe, child, check.eval_genes(child)["evalue"])
         eng.step()
         got = eng.read_population(slot, P)
