@@ -333,7 +333,8 @@ def run_gpu(args):
         from flexaidds_gb300.system import SystemInputs  # noqa: F401
         w, b = WORKLOAD, BATCH
         served = run_served(prec, {
-            "6000": system.make_inputs(w["n_rec"], w["cleft"], 12, 3, seed=w["seed"], edge=w["edge"]),
+            "6000": system.make_inputs(w["n_rec"], w["cleft"], 12, 3, seed=w["seed"], edge=w["edge"],
+                                       side_chains=w["side_chains"], rotamers=w["rotamers"]),
             "4000": system.make_inputs(b["n_rec"], b["cleft"], 12, 3, seed=b["seed"], edge=b["edge"])})
 
     if rank != 0:
@@ -484,8 +485,10 @@ def run_batched(args, prec, flush, stream):
 SERVE = dict(rates=(10.0, 50.0, 200.0), jobs=48, population=500, generations=20, budget=150e9,
              atoms_median=30, atoms=(10, 70), torsions=(0, 15), seed=77)
 SERVE_NAME = ("served: Poisson arrivals at 10, 50 and 200 jobs/s, 48 jobs per rate, receptors from a "
-              "cache of two (6000 and 4000 atoms), ligands lognormal median 30 heavy atoms (10-70) "
-              "with U[0,15] torsions, population 500 for 20 generations, 150 GB admission budget")
+              "cache of two (6000 atoms with three flexible side chains of 8 rotamers, and 4000 "
+              "atoms), ligands lognormal median 30 heavy atoms (10-70) with U[0,15] torsions, "
+              "population 500 for 20 generations, the reference's GA defaults (PSHARE fitness, "
+              "BOOM, duplicates rejected), 150 GB admission budget")
 
 
 def run_served(prec, receptors):

@@ -242,14 +242,14 @@ class GAEngine:
 
     @staticmethod
     def job(ev: GPUEvaluator, population: int, generations: int, seed: int,
-            cross_rate: float = 0.9, mut_rate: float = 0.01, n_new: int = 0, steady: bool = False,
+            cross_rate: float = 0.8, mut_rate: float = 0.03, n_new: int = 0, steady: bool = False,
             intragenes: bool = False, adaptive: bool = False, k=(1.0, 0.5, 1.0, 0.5),
             duplicates: bool = False, fitness: str = "PSHARE", sharing_alpha: float = 1.0,
             sharing_peaks: float = 5.0, sharing_scale: float = 10.0, entropy_weight: float = 0.5,
             temperature: float = 300.0) -> GAJob:
-        """Defaults follow the reference's: PSHARE fitness, BOOM with boom_fraction 1, crossover
-        at gene boundaries, fixed probabilities, duplicate chromosomes rejected
-        (LIB/config_parser.cpp:108, 125-162)."""
+        """Defaults follow the reference's: crossover 0.8, mutation 0.03, PSHARE fitness, BOOM
+        with boom_fraction 1, crossover at gene boundaries, fixed probabilities, duplicate
+        chromosomes rejected (LIB/config_parser.cpp:108, 125-162)."""
         return GAJob(ev.handle.value, int(population), int(generations), float(cross_rate),
                      float(mut_rate), int(seed) & 0xFFFFFFFFFFFFFFFF, int(n_new), int(bool(steady)),
                      int(bool(intragenes)), int(bool(adaptive)), (C.c_double * 4)(*k),

@@ -32,8 +32,8 @@ class JobRequest:
     population: int = 500
     generations: int = 100
     seed: int = 0
-    cross_rate: float = 0.9
-    mut_rate: float = 0.01
+    cross_rate: float = 0.8     # the reference's defaults (LIB/config_parser.cpp:128-129)
+    mut_rate: float = 0.03
 
 
 @dataclass
