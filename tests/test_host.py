@@ -195,3 +195,42 @@ def test_fitness_models_restated():
     assert later.cum[-1] == later.total
     flat = ga.Fitness(pop, pe, d, "SMFREE", temperature=0.0)
     assert flat.fit == lin.fit
+
+
+def test_side_chain_descriptors_are_validated(libfxe):
+    """The ABI rejects inconsistent side-chain descriptors before it looks for a device."""
+    import copy
+    from flexaidds_gb300 import capi as ca
+    libfxe.fxe_last_error.restype = C.c_char_p
+    libfxe.fxe_context_create.argtypes = [C.c_void_p] * 4 + [C.c_int32, C.c_void_p]
+    d = prepare.prepare(system.make_inputs(600, 6.0, 10, 2, seed=4, side_chains=2))
+
+    def create(dd):
+        pk = ca.Packed(dd)
+        out = C.c_void_p()
+        rc = libfxe.fxe_context_create(C.byref(pk.rec), C.byref(pk.lig), C.byref(pk.emat),
+                                       C.byref(pk.params), 16, C.byref(out))
+        return rc, libfxe.fxe_last_error().decode()
+
+    bad = copy.deepcopy(d)
+    bad.flex_xyz = bad.flex_xyz.copy()
+    bad.flex_xyz[0, 0] += 0.5                       # rotamer 0 differs from the receptor
+    rc, msg = create(bad)
+    assert rc == 1 and "rotamer 0" in msg
+    bad = copy.deepcopy(d)
+    bad.gene_max = bad.gene_max.copy()
+    bad.gene_max[-1] = float(bad.flex_nrot[-1])      # one past the last rotamer
+    rc, msg = create(bad)
+    assert rc == 1 and "rotamer gene limits" in msg
+    bad = copy.deepcopy(d)
+    bad.gene_atm = bad.gene_atm.copy()
+    bad.gene_atm[-1] = 5                             # no such side chain
+    rc, msg = create(bad)
+    assert rc == 1 and "names no flexible side chain" in msg
+    bad = copy.deepcopy(d)
+    bad.flex_prob = np.asarray([1.5, 0.2], np.float32)
+    rc, msg = create(bad)
+    assert rc == 1 and "prob" in msg
+    # the valid descriptor gets past validation (and stops at the missing device here)
+    rc, msg = create(d)
+    assert rc in (0, 7)
