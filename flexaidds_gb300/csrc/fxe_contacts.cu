@@ -2,8 +2,9 @@
 //
 // contacts_kernel, one warp per (pose, mobile atom): the 27-cell scan of get_contlist4
 // (LIB/Vcontacts.cpp:1725-1839) over the receptor's cell list of rigid atoms and the pose's
-// mobile atoms (side-chain atoms at their Calc places among the rigid atoms, then the ligand),
-// in the reference's candidate order (cells in scan order, atoms in Calc order within a cell),
+// mobile atoms (side-chain and ligand atoms). The 27 cells' rigid entries are scanned as one
+// flat list, 32 at a time, the mobile atoms once; the passing candidates are then sorted into
+// the reference's candidate order (cells in scan order, atoms in Calc order within a cell),
 // with the reference's single-precision squared distance and its double-precision cut-off test,
 // plus the atom's share of the clash pre-filter (LIB/Vcontacts.cpp:36-51): rigid partners and
 // the mobile partners processed after it in Calclist order, pairs of one residue within bloops
@@ -23,7 +24,18 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 // ------------------------------------------------------------------------------------------
 // contacts_kernel
 // ------------------------------------------------------------------------------------------
-__device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork& W, int p, int a, int lane) {
+// Per-warp staging of an atom's passing candidates, sorted into the reference's order after the
+// scan: by (cell in scan order, Calc index), packed into one key.
+struct ContactStage {
+    int key[128];
+    int idx[128];
+    float d2[128];
+    int coff[28];   // running candidate counts of the 27 cells
+    int cst[27];    // their first entries in the cell list
+};
+
+__device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork& W, int p, int a, int lane,
+                                              ContactStage& cs) {
     const int nsc = S.n_sc, nm = nsc + S.n_lig;
     const size_t lb = (size_t)p * nm;
     const int4 pg = W.pose_grid[p];
@@ -40,30 +52,19 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
     const int my_rank = W.mob_rank[lb + a];
     const int dim = pg.y, dim2 = dim * dim, dim3 = dim2 * dim;
     const int box0 = W.mob_cell[lb + a];
-    // mobile atoms held by this lane (atom lane + 32 * slot): cell offset key 0..26 or -1; the
-    // side-chain atoms (fewer than 33) are the lanes of slot 0
-    int key[kMaxLig / 32];
-    float4 lpos[kMaxLig / 32];
-#pragma unroll
-    for (int s = 0; s < kMaxLig / 32; ++s) {
-        const int m = lane + 32 * s;
-        key[s] = -1;
-        lpos[s] = make_float4(0, 0, 0, 0);
-        if (m < nm) {
-            lpos[s] = W.mob_pos[lb + m];
-            const int o = W.mob_cell[lb + m] - box0 + dim2 + dim + 1;
-            if (o >= 0) {
-                const int di = o / dim2, rem = o - di * dim2, dj = rem / dim, dk = rem - dj * dim;
-                if (di <= 2 && dj <= 2 && dk <= 2) key[s] = di * 9 + dj * 3 + dk;
-            }
-        }
-    }
-    const int my_slot = lane < nsc ? S.sc_slot[lane] : 0;
-    const float4 gm = W.pose_gmin[p];
+    const int n_calc = S.n_rec + S.n_lig;   // keys: cell * n_calc + Calc index
+    // scan position 0..26 of linear cell c around box0 (the reference's 27 offsets, which wrap
+    // around the rows of the linear index at the grid's faces), or -1
+    auto scan_pos = [&](int c) -> int {
+        const int o = c - box0 + dim2 + dim + 1;
+        if (o < 0) return -1;
+        const int di = o / dim2, rem = o - di * dim2, dj = rem / dim, dk = rem - dj * dim;
+        return (di <= 2 && dj <= 2 && dk <= 2) ? di * 9 + dj * 3 + dk : -1;
+    };
     int nc = 0;
     double clash = 0.0;
     const double permea = (double)S.permeability;
-    auto consider = [&](bool in, int j, float4 pj) {
+    auto consider = [&](bool in, int pos, int j, float4 pj) {
         bool pass = false;
         float sq = 0.0f;
         if (in) {
@@ -76,8 +77,9 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
         if (pass) {
             const int w = nc + __popc(m & lanemask_lt());
             if (w < kMaxCand) {
-                W.cand_idx[cb + w] = j;
-                W.cand_d2[cb + w] = sq;
+                cs.key[w] = pos * n_calc + j;
+                cs.idx[w] = j;
+                cs.d2[w] = sq;
             }
             // clash pre-filter share: rigid partners, and mobile partners processed later
             const int mj = mobile_of(S, j);
@@ -92,69 +94,112 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
         }
         nc += __popc(m);
     };
-    // rigid atoms of one cell in Calc order, entries [k0, k1) of the cell list (or, on a grid
-    // re-derived for this pose, Calc indices [k0, k1) that fall into cell bi)
-    auto scan_rigid = [&](int k0, int k1, int bi) {
-        for (int kb = k0; kb < k1; kb += 32) {
-            const int k = kb + lane;
-            bool in = k < k1;
-            int j = 0;
-            float4 pj = make_float4(0, 0, 0, 0);
-            if (!pg.x) {
-                if (in) {
-                    j = S.cell_atom[k];
-                    pj = S.cell_pos[k];
-                }
-            } else if (in) {
-                j = k;
-                pj = S.rec_pos[k];
-                const int cb2 = (int)((pj.x - gm.x) / kCell) * dim2 + (int)((pj.y - gm.y) / kCell) * dim +
-                                (int)((pj.z - gm.z) / kCell);
-                in = cb2 == bi && (nsc == 0 || S.rec_mob[k] < 0);
+    if (!pg.x) {
+        // the rigid atoms of the 27 cells as one list: lane i < 27 counts cell i's entries
+        int cnt = 0, st = 0;
+        if (lane < 27) {
+            const int bi = box0 + dim2 * ((lane / 9) - 1) + dim * (((lane / 3) % 3) - 1) + (lane % 3) - 1;
+            if (bi >= 0 && bi < dim3) {
+                st = S.cell_start[bi];
+                cnt = S.cell_start[bi + 1] - st;
             }
-            consider(in, j, pj);
         }
-    };
-    for (int i = 0; i < 27; ++i) {
-        const int bi = box0 + dim2 * ((i / 9) - 1) + dim * (((i / 3) % 3) - 1) + (i % 3) - 1;
-        if (bi < 0 || bi >= dim3) continue;
-        int k0, k1;
-        if (!pg.x) {
-            k0 = S.cell_start[bi];
-            k1 = S.cell_start[bi + 1];
-        } else {
-            k0 = 0;
-            k1 = S.n_rec;
-        }
-        // side-chain atoms in this cell take their Calc places among the rigid atoms
-        unsigned scm = __ballot_sync(kFull, lane < nsc && key[0] == i);
-        while (scm) {
-            const int q = __ffs(scm) - 1;
-            scm &= scm - 1;
-            const int qs = __shfl_sync(kFull, my_slot, q);
-            int split = qs;
-            if (!pg.x) {   // rigid entries of the cell before Calc index qs
-                split = k0;
-                for (int kb = k0; kb < k1; kb += 32) {
-                    const int k = kb + lane;
-                    const unsigned lt = __ballot_sync(kFull, k < k1 && S.cell_atom[k] < qs);
-                    split += __popc(lt);
-                    if (lt != kFull) break;
-                }
-            }
-            scan_rigid(k0, split, bi);
-            consider(lane == q, qs, lpos[0]);
-            k0 = split;
-        }
-        scan_rigid(k0, k1, bi);
+        int inc = cnt;
 #pragma unroll
-        for (int s = 0; s < kMaxLig / 32; ++s) {
-            if (32 * s >= nm) break;
-            const int m = lane + 32 * s;
-            consider(key[s] == i && m >= nsc, S.n_rec + (m - nsc), lpos[s]);
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(kFull, inc, o);
+            if (lane >= o) inc += v;
+        }
+        const int total = __shfl_sync(kFull, inc, 31);
+        if (lane < 27) {
+            cs.coff[lane + 1] = inc;
+            cs.cst[lane] = st;
+        }
+        if (lane == 0) cs.coff[0] = 0;
+        __syncwarp();
+        for (int t0 = 0; t0 < total; t0 += 32) {
+            const int t = t0 + lane;
+            const bool in = t < total;
+            int pos = 0, j = 0;
+            float4 pj = make_float4(0, 0, 0, 0);
+            if (in) {
+                int lo = 0, hi = 26;   // the last cell whose first item is at or before t
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (cs.coff[mid] <= t) lo = mid;
+                    else hi = mid - 1;
+                }
+                pos = lo;
+                const int k = cs.cst[lo] + (t - cs.coff[lo]);
+                j = S.cell_atom[k];
+                pj = S.cell_pos[k];
+            }
+            consider(in, pos, j, pj);
+        }
+    } else {
+        // a grid re-derived for this pose: every rigid atom, binned on that grid
+        const float4 gm = W.pose_gmin[p];
+        for (int k0 = 0; k0 < S.n_rec; k0 += 32) {
+            const int k = k0 + lane;
+            bool in = false;
+            int pos = -1;
+            float4 pj = make_float4(0, 0, 0, 0);
+            if (k < S.n_rec && (nsc == 0 || S.rec_mob[k] < 0)) {
+                pj = S.rec_pos[k];
+                const int c = (int)((pj.x - gm.x) / kCell) * dim2 + (int)((pj.y - gm.y) / kCell) * dim +
+                              (int)((pj.z - gm.z) / kCell);
+                pos = scan_pos(c);
+                in = pos >= 0;
+            }
+            consider(in, pos, k, pj);
         }
     }
+    // the mobile atoms (side-chain atoms and the ligand) in the 27 cells
+#pragma unroll
+    for (int s = 0; s < kMaxLig / 32; ++s) {
+        if (32 * s >= nm) break;
+        const int m = lane + 32 * s;
+        int pos = -1;
+        float4 pj = make_float4(0, 0, 0, 0);
+        if (m < nm) {
+            pj = W.mob_pos[lb + m];
+            pos = scan_pos(W.mob_cell[lb + m]);
+        }
+        consider(pos >= 0, pos, m < nm ? slot_of(S, m) : 0, pj);
+    }
     clash = warp_sum_d(clash);
+    // into the reference's order: bitonic sort of the staged keys
+    if (nc <= kMaxCand) {
+        int len = 32;
+        while (len < nc) len <<= 1;
+        for (int i = nc + lane; i < len; i += 32) cs.key[i] = 0x7FFFFFFF;
+        __syncwarp();
+        for (int k = 2; k <= len; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = lane; i < len; i += 32) {
+                    const int l = i ^ j;
+                    if (l > i) {
+                        const bool up = (i & k) == 0;
+                        const int ka = cs.key[i], kb = cs.key[l];
+                        if ((ka > kb) == up) {
+                            cs.key[i] = kb;
+                            cs.key[l] = ka;
+                            const int ti = cs.idx[i];
+                            cs.idx[i] = cs.idx[l];
+                            cs.idx[l] = ti;
+                            const float td = cs.d2[i];
+                            cs.d2[i] = cs.d2[l];
+                            cs.d2[l] = td;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        for (int i = lane; i < nc; i += 32) {
+            W.cand_idx[cb + i] = cs.idx[i];
+            W.cand_d2[cb + i] = cs.d2[i];
+        }
+    }
     if (lane == 0) {
         W.cand_n[lb + a] = nc > kMaxCand ? -nc : nc;
         W.clash_part[lb + a] = clash;
@@ -163,16 +208,18 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
 
 __global__ void __launch_bounds__(128)
 contacts_kernel(DevSystem S, DevWork W, int n) {
+    __shared__ ContactStage stage[4];
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nm = n_mobile(S);
     if (gw >= n * nm) return;
-    contacts_atom(S, W, gw / nm, gw % nm, threadIdx.x & 31);
+    contacts_atom(S, W, gw / nm, gw % nm, threadIdx.x & 31, stage[threadIdx.x >> 5]);
 }
 
 // The same over the (pose, mobile atom) items of several jobs.
 __global__ void __launch_bounds__(128)
 contacts_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, long long total) {
     __shared__ Job job_all[4];
+    __shared__ ContactStage stage[4];
     const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (gw >= total) return;
@@ -181,7 +228,7 @@ contacts_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, long long total) 
     copy_job(&job, &jobs[j], lane);
     const int nm = n_mobile(job.S);
     const long long r = gw - job.warp0;
-    contacts_atom(job.S, job.W, (int)(r / nm), (int)(r % nm), lane);
+    contacts_atom(job.S, job.W, (int)(r / nm), (int)(r % nm), lane, stage[wib]);
 }
 
 // The order pose_kernel takes the poses in: costliest first (sum over the pose's atoms of the
