@@ -169,3 +169,24 @@ def test_ga_generation_with_side_chains(flex):
         np.testing.assert_array_equal(got[0], pop)
         np.testing.assert_array_equal(got[1], pe)
     eng.collect(slot, 300.0)
+
+
+def test_side_chains_through_the_receptor_cache(flex):
+    """A context sharing a receptor with side chains (fxe_context_create_shared) scores another
+    ligand exactly as a context with its own copy of the receptor."""
+    d, _ = flex
+    lig = synth.random_ligand(18, 5, seed=501)
+    inp = system.make_inputs(2000, 8.0, 24, 6, seed=43, side_chains=3)
+    d2 = prepare.prepare(system.SystemInputs(receptor=inp.receptor, ligand=lig, grid_xyz=inp.grid_xyz,
+                                             emat=inp.emat))
+    assert d2.n_flex == 3
+    genes = enriched(d2, 8000, 502, 150, 50)
+    base = evaluator.GPUEvaluator(d, max_poses=8)
+    shared = evaluator.GPUEvaluator(d2, max_poses=256, share_receptor_with=base)
+    own = evaluator.GPUEvaluator(d2, max_poses=256)
+    a, b = shared.eval_genes(genes), own.eval_genes(genes)
+    np.testing.assert_array_equal(a["status"], b["status"])
+    np.testing.assert_array_equal(a["evalue"], b["evalue"])
+    assert (a["status"] == 0).sum() >= 100
+    for ev in (shared, own, base):
+        ev.close()
