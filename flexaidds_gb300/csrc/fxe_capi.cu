@@ -843,11 +843,12 @@ extern "C" fxe_status fxe_thermo_compute_device_fixed(const double* d_energies, 
 namespace fxe {
 void launch_build_jobs(const Job*, int, int, cudaStream_t);
 void launch_contacts_jobs(const Job*, int, long long, cudaStream_t);
+void launch_order_poses_jobs(const Job*, int, int, int*, cudaStream_t);
 namespace f32 {
-void launch_poses_jobs(const Job*, int, int, int*, cudaStream_t);
+void launch_poses_jobs(const Job*, int, int, int*, const int*, cudaStream_t);
 }
 namespace f64 {
-void launch_poses_jobs(const Job*, int, int, int*, cudaStream_t);
+void launch_poses_jobs(const Job*, int, int, int*, const int*, cudaStream_t);
 }
 }  // namespace fxe
 
@@ -865,10 +866,12 @@ struct fxe_batch {
     fxe_cf* d_out = nullptr;
     fxe_cf* h_out = nullptr;               // pinned
     int* d_next = nullptr;                 // pose queue of the polyhedron launch
+    int* d_order = nullptr;                // [max_poses] its order, costliest first
     int64_t launches = 0;
     ~fxe_batch() {
         if (staged) cudaEventDestroy(staged);
         if (d_next) cudaFree(d_next);
+        if (d_order) cudaFree(d_order);
         if (d_jobs) cudaFree(d_jobs);
         if (h_jobs) cudaFreeHost(h_jobs);
         if (d_genes) cudaFree(d_genes);
@@ -896,6 +899,7 @@ extern "C" fxe_status fxe_batch_create(int32_t max_jobs, int64_t max_poses, int3
         FXE_TRY(cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming), "cudaEventCreate");
         FXE_TRY(cudaMalloc(&b->d_jobs, sizeof(fxe::Job) * max_jobs), "batch job table");
         FXE_TRY(cudaMalloc(&b->d_next, sizeof(int)), "batch pose queue");
+        FXE_TRY(cudaMalloc(&b->d_order, sizeof(int) * max_poses), "batch pose queue");
         FXE_TRY(cudaMallocHost(&b->h_jobs, sizeof(fxe::Job) * max_jobs), "batch job table");
         FXE_TRY(cudaMalloc(&b->d_genes, sizeof(int32_t) * max_poses * max_genes), "batch staging");
         FXE_TRY(cudaMallocHost(&b->h_genes, sizeof(int32_t) * max_poses * max_genes), "batch staging");
@@ -945,10 +949,11 @@ fxe_status batch_launch(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, cudaS
     FXE_TRY(cudaEventRecord(b->staged, s), "cudaEventRecord");
     fxe::launch_build_jobs(b->d_jobs, k, total, s);
     fxe::launch_contacts_jobs(b->d_jobs, k, items, s);
-    if (prec == FXE_PRECISION_FAST) fxe::f32::launch_poses_jobs(b->d_jobs, k, total, b->d_next, s);
-    else fxe::f64::launch_poses_jobs(b->d_jobs, k, total, b->d_next, s);
+    fxe::launch_order_poses_jobs(b->d_jobs, k, total, b->d_order, s);
+    if (prec == FXE_PRECISION_FAST) fxe::f32::launch_poses_jobs(b->d_jobs, k, total, b->d_next, b->d_order, s);
+    else fxe::f64::launch_poses_jobs(b->d_jobs, k, total, b->d_next, b->d_order, s);
     FXE_TRY(cudaGetLastError(), "batched kernel launch");
-    b->launches += 3;
+    b->launches += 4;
     return FXE_OK;
 }
 
@@ -1063,6 +1068,8 @@ struct fxe_ga {
     int* d_run = nullptr;               // [max_jobs] running slots of the captured graph
     fxe::Job* d_eval = nullptr;         // [max_jobs] batched-evaluation table of the running slots
     int* d_next = nullptr;              // pose queue of the polyhedron launch
+    int* d_order = nullptr;             // its order, costliest first
+    int order_cap = 0;
     std::vector<int> run;               // running slots of the captured graph
     cudaGraphExec_t exec = nullptr;
     bool dirty = true;
@@ -1077,6 +1084,7 @@ struct fxe_ga {
         if (d_run) cudaFree(d_run);
         if (d_eval) cudaFree(d_eval);
         if (d_next) cudaFree(d_next);
+        if (d_order) cudaFree(d_order);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -1266,7 +1274,7 @@ extern "C" fxe_status fxe_ga_admit(fxe_ga* e, const fxe_ga_job* job, int32_t* sl
         fxe::launch_ga_fitness(e->d_all, e->d_ids + k, 1, true, e->stream);
         FXE_TRY(cudaGetLastError(), "GA launch");
         FXE_TRY(cudaStreamSynchronize(e->stream), "GA admission");   // gen0 and the host copy of J die here
-        e->launches += 9;
+        e->launches += 10;
         return FXE_OK;
     }();
     if (st != FXE_OK) {
@@ -1317,6 +1325,14 @@ extern "C" fxe_status fxe_ga_step(fxe_ga* e) {
             total += J.n;
             items += (long long)J.n * (s.ctx->S.n_sc + s.ctx->S.n_lig);
         }
+        if (total > e->order_cap) {   // the pose order of the polyhedron launch, sized for the running jobs
+            FXE_TRY(cudaStreamSynchronize(e->stream), "GA table");
+            if (e->d_order) cudaFree(e->d_order);
+            e->d_order = nullptr;
+            e->order_cap = 0;
+            FXE_TRY(cudaMalloc(&e->d_order, sizeof(int) * total), "GA pose order");
+            e->order_cap = total;
+        }
         FXE_TRY(cudaMemcpyAsync(e->d_run, e->run.data(), sizeof(int) * n, cudaMemcpyHostToDevice, e->stream), "GA table");
         FXE_TRY(cudaMemcpyAsync(e->d_eval, ev.data(), sizeof(fxe::Job) * n, cudaMemcpyHostToDevice, e->stream), "GA table");
         FXE_TRY(cudaStreamSynchronize(e->stream), "GA table");
@@ -1325,8 +1341,9 @@ extern "C" fxe_status fxe_ga_step(fxe_ga* e) {
         fxe::launch_ga_breed(e->d_all, e->d_run, n, e->stream);
         fxe::launch_build_jobs(e->d_eval, n, total, e->stream);
         fxe::launch_contacts_jobs(e->d_eval, n, items, e->stream);
-        if (e->precision == FXE_PRECISION_FAST) fxe::f32::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->stream);
-        else fxe::f64::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->stream);
+        fxe::launch_order_poses_jobs(e->d_eval, n, total, e->d_order, e->stream);
+        if (e->precision == FXE_PRECISION_FAST) fxe::f32::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->d_order, e->stream);
+        else fxe::f64::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->d_order, e->stream);
         fxe::launch_ga_select(e->d_all, e->d_run, n, false, e->stream);
         fxe::launch_ga_fitness(e->d_all, e->d_run, n, false, e->stream);
         cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
@@ -1337,7 +1354,7 @@ extern "C" fxe_status fxe_ga_step(fxe_ga* e) {
     }
     if (e->run.empty()) return FXE_OK;
     FXE_TRY(cudaGraphLaunch(e->exec, e->stream), "graph launch");
-    e->launches += 9;
+    e->launches += 10;
     e->graph_launches += 1;
     for (int i : e->run) {
         GaSlot& s = e->slots[i];

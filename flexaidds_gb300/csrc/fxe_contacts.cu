@@ -282,6 +282,59 @@ __global__ void __launch_bounds__(1024) order_poses_kernel(const int* __restrict
     for (int i = threadIdx.x; i < m; i += blockDim.x) order[base + i] = base + idx[i];
 }
 
+// The same over the poses of several jobs (global pose index gp of the launch).
+__global__ void __launch_bounds__(1024) order_poses_jobs_kernel(const Job* __restrict__ jobs, int n_jobs, int n,
+                                                                int* __restrict__ order) {
+    __shared__ long long key[kOrderSeg];
+    __shared__ int idx[kOrderSeg];
+    const int base = blockIdx.x * kOrderSeg;
+    const int m = min(kOrderSeg, n - base);
+    int len = 1;
+    while (len < m) len <<= 1;
+    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+        long long c = 0x7FFFFFFFFFFFFFFFll;
+        if (i < m) {
+            const int gp = base + i;
+            const Job& J = jobs[find_job(jobs, n_jobs, gp, false)];
+            const int nm = J.S.n_sc + J.S.n_lig;
+            const int* cn = J.W.cand_n + (size_t)(gp - J.pose0) * nm;
+            long long cost = 0;
+            for (int a = 0; a < nm; ++a) {
+                const int k = cn[a];
+                if (k > 0) cost += (long long)k * k;
+            }
+            c = -cost;
+        }
+        key[i] = c;
+        idx[i] = i;
+    }
+    __syncthreads();
+    for (int k = 2; k <= len; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < len; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const bool up = (i & k) == 0;
+                    const long long a = key[i], b = key[l];
+                    const bool gt = a > b || (a == b && idx[i] > idx[l]);
+                    if (gt == up) {
+                        key[i] = b;
+                        key[l] = a;
+                        const int t = idx[i];
+                        idx[i] = idx[l];
+                        idx[l] = t;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < m; i += blockDim.x) order[base + i] = base + idx[i];
+}
+
+void launch_order_poses_jobs(const Job* jobs, int n_jobs, int total, int* order, cudaStream_t st) {
+    order_poses_jobs_kernel<<<(total + kOrderSeg - 1) / kOrderSeg, 1024, 0, st>>>(jobs, n_jobs, total, order);
+}
+
 void launch_order_poses(const DevSystem& S, const DevWork& W, int n, cudaStream_t st) {
     order_poses_kernel<<<(n + kOrderSeg - 1) / kOrderSeg, 1024, 0, st>>>(W.cand_n, S.n_sc + S.n_lig, n, W.pose_order);
 }

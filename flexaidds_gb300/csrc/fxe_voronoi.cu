@@ -1356,11 +1356,12 @@ pose_kernel(DevSystem S, DevWork W, int n, int* next) {
 // The same over the poses of several jobs; the job's system and workspace descriptors are read
 // from the job table (they stay in L1), keeping shared memory for the polyhedron workspace.
 __global__ void __launch_bounds__(kVorWarps * 32)
-pose_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, int total, int* next) {
+pose_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, int total, int* next, const int* __restrict__ order) {
     extern __shared__ __align__(16) unsigned char smem[];
     PoseShared& ps = reinterpret_cast<PoseShared*>(smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
-    for (int gp = next_pose(next, lane); gp < total; gp = next_pose(next, lane)) {
+    for (int q = next_pose(next, lane); q < total; q = next_pose(next, lane)) {
+        const int gp = order[q];
         const Job& job = jobs[find_job(jobs, n_jobs, gp, false)];
         score_pose(job.S, job.W, gp - job.pose0, lane, ps);
         __syncwarp();
@@ -1382,9 +1383,10 @@ void launch_poses(const DevSystem& S, const DevWork& W, int n, int* next, cudaSt
     pose_kernel<<<pose_blocks(n), kVorWarps * 32, pose_smem_bytes(), st>>>(S, W, n, next);
 }
 
-void launch_poses_jobs(const Job* jobs, int n_jobs, int total, int* next, cudaStream_t st) {
+void launch_poses_jobs(const Job* jobs, int n_jobs, int total, int* next, const int* order, cudaStream_t st) {
     cudaMemsetAsync(next, 0, sizeof(int), st);
-    pose_kernel_jobs<<<pose_blocks(total), kVorWarps * 32, pose_jobs_smem_bytes(), st>>>(jobs, n_jobs, total, next);
+    pose_kernel_jobs<<<pose_blocks(total), kVorWarps * 32, pose_jobs_smem_bytes(), st>>>(jobs, n_jobs, total, next,
+                                                                                         order);
 }
 
 cudaError_t configure_voronoi() {

@@ -36,7 +36,7 @@ def test_batch_equals_single_contexts(jobs_on_one_receptor, prec):
         outs = batch.eval_genes(list(zip(evs, genes)))
         for a, b in zip(outs, alone):
             np.testing.assert_array_equal(a, b)
-    assert batch.take_launches() == 6
+    assert batch.take_launches() == 8   # build, contacts, order, polyhedra; twice
     assert sum(int((o["status"] == 0).sum()) for o in outs) > 20
 
 

@@ -132,4 +132,4 @@ def test_best_energy_never_rises(systems):
     assert e == best[-1]
     assert np.isfinite(th["free_energy"])
     launches, graphs = eng.take_launches()
-    assert graphs == 12 and launches == 9 + 12 * 9
+    assert graphs == 12 and launches == 10 + 12 * 10
