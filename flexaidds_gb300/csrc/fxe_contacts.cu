@@ -64,6 +64,7 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
     int nc = 0;
     double clash = 0.0;
     const double permea = (double)S.permeability;
+    const float permea_f = S.permeability;
     auto consider = [&](bool in, int pos, int j, float4 pj) {
         bool pass = false;
         float sq = 0.0f;
@@ -71,7 +72,9 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
             const float dx = __fsub_rn(me.x, pj.x), dy = __fsub_rn(me.y, pj.y), dz = __fsub_rn(me.z, pj.z);
             sq = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
             const float nd = __fadd_rn(__fadd_rn(rado, pj.w), kRw);
-            pass = ((double)sq < (double)nd * (double)nd) && sq != 0.0f;
+            // the reference's test sq < nd * nd in double, where the product is exact: the sign of
+            // sq - nd * nd rounded once (a fused multiply-add) is the sign of the exact difference
+            pass = __fmaf_rn(-nd, nd, sq) < 0.0f && sq != 0.0f;
         }
         const unsigned m = __ballot_sync(kFull, pass);
         if (pass) {
@@ -84,8 +87,12 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
             // clash pre-filter share: rigid partners, and mobile partners processed later
             const int mj = mobile_of(S, j);
             const bool later = mj < 0 || W.mob_rank[lb + mj] > my_rank;
-            if (later) {
-                const double rAB = (double)__fadd_rn(me.w, pj.w);
+            const float rABf = __fadd_rn(me.w, pj.w);
+            const float cdf = permea_f * rABf;
+            // surely beyond the clash distance (single-precision bound well outside rounding)
+            const bool far = sq > cdf * cdf * 1.0001f;
+            if (later && !far) {
+                const double rAB = (double)rABf;
                 const double cd = permea * rAB;
                 const double dist = sqrt((double)sq);
                 if (dist < cd && residue_pair(S, a, j) != 1)
