@@ -1,13 +1,15 @@
 // fxe_common.cuh — device-side layout shared by the evaluation kernels.
 //
 // Layout in HBM (one evaluation context, resident for the context's lifetime):
-//   receptor atoms as float4 (x, y, z, radius) in Calc order, and a second copy sorted by cell
-//   of the receptor's steady cell grid (the 6.5 A grid index_protein builds once the receptor
-//   atoms are indexed, LIB/Vcontacts.cpp:1570-1715) with CSR offsets per cell;
+//   receptor atoms as float4 (x, y, z, radius) in Calc order, and a copy of its rigid atoms
+//   sorted by cell of the receptor's steady cell grid (the 6.5 A grid index_protein builds once
+//   the receptor atoms are indexed, LIB/Vcontacts.cpp:1570-1715) with CSR offsets per cell;
+//   flexible side chains (rotamer coordinates, residue bonded matrices, Calc places);
 //   ligand build tree, genes and decode tables; energy matrix; cleft-grid ICs as float4.
 // Per batch of poses (workspace sized at context creation for max_poses):
-//   ligand coordinates, cells and processing ranks per pose; candidate lists (Calc index,
-//   squared distance) and Voronoi results (area, flags) per (pose, ligand atom, slot).
+//   mobile-atom (side-chain and ligand) coordinates, cells and processing ranks per pose;
+//   candidate lists (Calc index, squared distance) and Voronoi results (area, flags) per
+//   (pose, mobile atom, slot).
 #pragma once
 
 #include <cstdint>

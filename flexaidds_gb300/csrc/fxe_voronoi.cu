@@ -1,15 +1,13 @@
-// fxe_voronoi.cu — contact candidates, Voronoi contact surfaces and complementarity scoring.
+// fxe_voronoi.cu — Voronoi contact surfaces and complementarity scoring (the candidate lists
+// come from contacts_kernel, fxe_contacts.cu).
 //
-// contacts_kernel  one warp per (pose, ligand atom): the 27-cell scan of get_contlist4
-//                  (LIB/Vcontacts.cpp:1725-1839) over the receptor's cell list and the pose's
-//                  ligand atoms, in the reference's candidate order, and the atom's share of the
-//                  clash pre-filter (LIB/Vcontacts.cpp:36-51).
 // pose_kernel      one warp per pose: calc_region's loop over the scorable atoms in Calclist
 //                  order (LIB/Vcontacts.cpp:74-139) — each atom's list without the saved atoms
 //                  that kept no contact with it, its extended-radical-plane polyhedron started
 //                  from the seed an earlier atom left (voronoi_poly2, :147-490), faces
-//                  (order_faces, :699-831) and spherical areas (calc_areas, :838-1044) in FP32,
-//                  the contacts it keeps (save_areas) and the seeds it leaves (save_seeds) —
+//                  (order_faces, :699-831) and spherical areas (calc_areas, :838-1044) in FP64
+//                  (reference precision) or FP32 (fast precision), the contacts it keeps
+//                  (save_areas) and the seeds it leaves (save_seeds) —
 //                  then vcfunction's walk over the kept contacts (LIB/vcfunction.cpp:14-574).
 //
 // The atoms of one pose stay in order because the reference's results depend on it: which
@@ -1006,7 +1004,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     return kAtomOk;
 }
 
-// Planes of the candidates of one ligand atom (LIB/Vcontacts.cpp:186-221). Slots set in
+// Planes of the candidates of one scored atom (LIB/Vcontacts.cpp:186-221). Slots set in
 // `excl` (a candidate the reference's list does not hold) get a plane that never binds, which
 // leaves the order of the remaining planes, and so every tie-break, as in the shorter list.
 __device__ void load_planes(VorShared& sh, const DevSystem& S, const DevWork& W, int p, int a,
