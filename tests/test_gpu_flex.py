@@ -190,3 +190,29 @@ def test_side_chains_through_the_receptor_cache(flex):
     assert (a["status"] == 0).sum() >= 100
     for ev in (shared, own, base):
         ev.close()
+
+
+def test_side_chains_with_poses_outside_the_box():
+    """Anchors beyond the receptor's box: index_protein re-derives the cell grid for those poses,
+    and the contact scan bins every rigid atom on it with the side-chain atoms set apart."""
+    inp = system.make_inputs(600, 6.0, 10, 2, seed=37, side_chains=2)
+    rng = np.random.default_rng(38)
+    lo, hi = inp.receptor.xyz.min(axis=0), inp.receptor.xyz.max(axis=0)
+    m = 256
+    pts = rng.uniform(lo, hi, size=(m, 3))
+    axis = rng.integers(0, 3, size=m)
+    off = rng.uniform(0.5, 4.0, size=m)
+    for k in range(m):
+        pts[k, axis[k]] = hi[axis[k]] + off[k] if k % 2 else lo[axis[k]] - off[k]
+    inp.grid_xyz = np.ascontiguousarray(np.concatenate([inp.grid_xyz[:256], pts]).astype(np.float32))
+    d = prepare.prepare(inp)
+    genes = synth.random_genes(3000, d.n_genes, seed=39)
+    r = oracle_eval(d, d.genes_to_ic(genes))["cf"]
+    ev = evaluator.GPUEvaluator(d, max_poses=3000, precision=REF)
+    g = ev.eval_genes(genes)
+    np.testing.assert_array_equal(g["status"], r["status"])
+    ok = g["status"] == 0
+    assert ok.sum() >= 100
+    assert rel_err(g["evalue"], r["evalue"]).max() <= 1e-6
+    assert rel_err(g["evalue"][ok], r["evalue"][ok]).max() <= 1e-9
+    ev.close()
