@@ -213,6 +213,43 @@ def gene_bins(gmin: float, gmax: float, gdel: float, gmap: int) -> np.ndarray:
     return t
 
 
+def read_emat(path: str):
+    """An energy-matrix file in the reference's format (read_emat, LIB/read_emat.cpp:8-148): the
+    upper triangle of ntypes x ntypes, one line per type pair (i, j >= i) in order, the values
+    after the "=" (or the whole line): one number is a single value (weight 1), an even count
+    are the (x, y) points of a density curve (weight 0). ntypes follows from the line count.
+    Returns (emat, emat_weight, emat_curves) as SystemInputs takes them."""
+    with open(path) as f:
+        lines = [ln for ln in f.read().split("\n")]
+    if lines and lines[-1] == "":
+        lines.pop()
+    n = len(lines)
+    t = int(round((-1.0 + (1.0 + 8.0 * n) ** 0.5) / 2.0))
+    if t * (t + 1) // 2 != n:
+        raise ValueError(f"{path}: {n} lines is not the upper triangle of a square matrix")
+    emat = np.zeros((t, t), np.float32)
+    weight = np.zeros((t, t), np.int32)
+    curves = {}
+    k = 0
+    for i in range(t):
+        for j in range(i, t):
+            line = lines[k]
+            k += 1
+            if "=" in line:
+                line = line[line.index("=") + 1:]
+            vals = line.split()
+            if len(vals) == 1:
+                emat[i, j] = emat[j, i] = np.float32(float(vals[0]))
+                weight[i, j] = weight[j, i] = 1
+            elif vals and len(vals) % 2 == 0:
+                pts = [(float(np.float32(float(vals[q]))), float(np.float32(float(vals[q + 1]))))
+                       for q in range(0, len(vals), 2)]
+                curves[(i, j)] = pts
+            else:
+                raise ValueError(f"{path}: line {k}: {len(vals)} values for pair {i + 1}-{j + 1}")
+    return emat, weight, curves
+
+
 def make_inputs(n_rec: int, cleft_radius: float, n_lig: int, n_tor: int, seed: int,
                 spacing: float = 0.375, edge: float | None = None, side_chains: int = 0,
                 rotamers: int = 8) -> SystemInputs:

@@ -234,3 +234,32 @@ def test_side_chain_descriptors_are_validated(libfxe):
     # the valid descriptor gets past validation (and stops at the missing device here)
     rc, msg = create(d)
     assert rc in (0, 7)
+
+
+def test_energy_matrix_file_format(tmp_path):
+    """read_emat takes the reference's upper-triangle lines: single values and density curves."""
+    lines = []
+    t = 3
+    for i in range(t):
+        for j in range(i, t):
+            if (i, j) == (0, 2):
+                lines.append(f"{i + 1:7d}-{j + 1:2d} =   0.0 -1.5  0.4 2.25  1.0 0.5")
+            else:
+                lines.append(f"{i + 1:7d}-{j + 1:2d} = {10.0 * i - j:8.1f}")
+    p = tmp_path / "emat.dat"
+    p.write_text("\n".join(lines) + "\n")
+    emat, w, curves = system.read_emat(str(p))
+    assert emat.shape == (3, 3) and w[0, 2] == 0 and w[2, 0] == 0 and w.sum() == 7
+    assert emat[1, 2] == emat[2, 1] == np.float32(8.0)
+    assert curves[(0, 2)] == [(0.0, -1.5), (0.4000000059604645, 2.25), (1.0, 0.5)]
+    bad = tmp_path / "bad.dat"
+    bad.write_text("\n".join(lines[:5]) + "\n")
+    with pytest.raises(ValueError):
+        system.read_emat(str(bad))
+
+
+@pytest.mark.skipif(not os.path.exists("/root/reference/WRK/MC_st0r5.2_6.dat"),
+                    reason="the reference checkout is not present")
+def test_reference_energy_matrix_file_reads():
+    emat, w, curves = system.read_emat("/root/reference/WRK/MC_st0r5.2_6.dat")
+    assert emat.shape == (40, 40) and int(w.sum()) + 2 * len(curves) - sum(1 for (i, j) in curves if i == j) == 1600
