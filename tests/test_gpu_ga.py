@@ -133,3 +133,24 @@ def test_best_energy_never_rises(systems):
     assert np.isfinite(th["free_energy"])
     launches, graphs = eng.take_launches()
     assert graphs == 12 and launches == 10 + 12 * 10
+
+
+def test_duplicates_let_through_when_no_new_chromosome_exists(systems):
+    """With crossover and mutation off every child repeats a parent: the reference would loop
+    for new chromosomes forever; the engine takes them as they come after 16 batches, counts
+    them, and the run completes with the population unchanged."""
+    d = systems[2]
+    P = 8
+    ev = evaluator.GPUEvaluator(d, max_poses=P)
+    eng = evaluator.GAEngine(max_jobs=1)
+    slot = eng.admit(eng.job(ev, P, 2, 99, cross_rate=0.0, mut_rate=0.0, fitness="LINEAR"), ev)
+    g0, e0 = eng.read_population(slot, P)
+    for _ in range(2):
+        eng.step()
+    assert eng.finished() == [slot]
+    rejected, forced = eng.duplicates(slot)
+    assert forced == 2 * P and rejected > 0
+    g2, e2 = eng.read_population(slot, P)
+    assert set(map(tuple, g2.tolist())) <= set(map(tuple, g0.tolist()))
+    assert e2[0] == e0[0]
+    eng.collect(slot, 300.0)
