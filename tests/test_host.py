@@ -263,3 +263,15 @@ def test_energy_matrix_file_format(tmp_path):
 def test_reference_energy_matrix_file_reads():
     emat, w, curves = system.read_emat("/root/reference/WRK/MC_st0r5.2_6.dat")
     assert emat.shape == (40, 40) and int(w.sum()) + 2 * len(curves) - sum(1 for (i, j) in curves if i == j) == 1600
+
+
+def test_roulette_restatement_edges():
+    """roulette_wheel: the first running sum above u * total, the last position when rounding
+    leaves none above it, a uniform position when the total is not positive
+    (LIB/gaboom.cpp:1158-1186)."""
+    from oracle import ga
+    f = ga.Fitness(np.zeros((4, 2), np.int32), np.zeros(4), None, "LINEAR")
+    assert f.fit == [4.0, 3.0, 2.0, 1.0] and f.cum == [4.0, 7.0, 9.0, 10.0]
+    assert [f.roulette(u) for u in (0.0, 0.39, 0.4, 0.69, 0.7, 0.89, 0.9, 0.999)] == [0, 0, 1, 1, 2, 2, 3, 3]
+    f.cum, f.total = [0.0, 0.0, 0.0, 0.0], 0.0
+    assert [f.roulette(u) for u in (0.0, 0.3, 0.6, 0.99)] == [0, 1, 2, 3]
