@@ -327,6 +327,7 @@ def run_gpu(args):
         sm_ms.append(a.elapsed_time(b))
     sm_best = min(sm_ms)
 
+    clustered = run_cluster(ev, d) if args.cluster else None
     batched = run_batched(args, prec, flush, stream) if args.batched else None
     served = None
     if args.served:
@@ -388,9 +389,55 @@ def run_gpu(args):
                                   "frac": (sm_gbs / hbm) if hbm else None, "traffic": None}},
         "batched": batched,
         "served": served,
+        "cluster": clustered,
     }
     print(json.dumps(out), flush=True)
     ranks.close()
+
+
+# ---------------------------------------------------------------------------------------------
+# clustering of a run's ensemble (cluster, LIB/cluster.cpp): 1e6 chromosomes, the reference's
+# default options (cluster_rmsd 2.0, max_results 10, temperature 0)
+# ---------------------------------------------------------------------------------------------
+
+CLUSTER = dict(centres=2000, per_centre=500, seed=17, rmsd=2.0, max_results=10, temperature=0,
+               cpu_sample=20_000)
+
+
+def run_cluster(ev, d):
+    """Device time of fxe_cluster's kernels (CUDA events inside the call), its end-to-end time
+    (host ICs and energies in, results out), and the C restatement on a bounded sample."""
+    c = CLUSTER
+    ic, e = synth.clustered_ensemble(d, c["centres"], c["per_centre"], seed=c["seed"])
+    n = ic.shape[0]
+    args = (ic, e, c["temperature"], c["rmsd"], c["max_results"])
+    ev.cluster(*args)                                       # warm-up
+    dev, e2e = [], []
+    for _ in range(3):
+        t = time.perf_counter()
+        r = ev.cluster(*args)
+        e2e.append(time.perf_counter() - t)
+        dev.append(ev.cluster_time())
+    out = {"workload": f"{n} chromosomes of the plain-scale system ({c['centres']} centres x "
+                       f"{c['per_centre']} variants a few bins apart, sorted by energy), "
+                       f"cluster_rmsd {c['rmsd']}, max_results {c['max_results']}, "
+                       f"temperature {c['temperature']}",
+           "clusters": int(r["n_clusters"]), "clustered": int(r["freq"].sum()),
+           "device_ms": min(dev), "e2e_ms": 1e3 * min(e2e),
+           "chromosomes_per_s": n / (min(dev) / 1e3), "e2e_chromosomes_per_s": n / min(e2e),
+           "kernels_per_call": 2 + c["max_results"] + (1 if c["temperature"] else 0)}
+    try:
+        from oracle import port
+        m = c["cpu_sample"]
+        o = port.Oracle(d)
+        t = time.perf_counter()
+        o.cluster(ic[:m], e[:m], c["temperature"], c["rmsd"], c["max_results"])
+        cs = time.perf_counter() - t
+        out["cpu_baseline"] = {"value": m / cs, "unit": "chromosomes/s", "cores": 1, "kind": "port",
+                               "sample": f"first {m} chromosomes of the same ensemble"}
+    except Exception as ex:   # the oracle library could not be built or loaded
+        out["cpu_baseline"] = {"value": None, "sample": f"unavailable: {ex}"}
+    return out
 
 
 # ---------------------------------------------------------------------------------------------
@@ -602,6 +649,8 @@ def main():
                     help="also serve Poisson streams of docking jobs and report latency percentiles")
     ap.add_argument("--batched", type=int, default=1,
                     help="also time the batched many-ligand workload against one launch per job")
+    ap.add_argument("--cluster", type=int, default=1,
+                    help="also time the clustering of a 1e6-chromosome ensemble")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

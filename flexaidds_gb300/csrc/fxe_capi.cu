@@ -29,6 +29,8 @@ namespace f64 {
 void launch_poses(const DevSystem&, const DevWork&, int, int*, cudaStream_t);
 cudaError_t configure_voronoi();
 }
+int cluster_blocks(int);
+void launch_cluster(const DevSystem&, const ClusterWork&, cudaStream_t);
 int thermo_blocks(long, int);
 void launch_thermo_partial(const double*, const int32_t*, long, double, LsePart*, int, cudaStream_t);
 void launch_thermo_weights(const double*, const int32_t*, long, double, double, double*, int, cudaStream_t);
@@ -84,6 +86,7 @@ struct fxe_context {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     double stage_ms[3] = {0.0, 0.0, 0.0};
     int64_t launches = 0;
+    double cluster_ms = 0.0;          // device time of the last fxe_cluster call
 
     template <typename T>
     cudaError_t alloc(T** p, size_t count) {
@@ -794,6 +797,195 @@ extern "C" fxe_status fxe_thermo_compute_device(const double* d_energies, const 
     if (!d_energies || n <= 0 || !(temperature > 0.0) || !out)
         return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
     return thermo_run(d_energies, d_multiplicity, n, temperature, out, nullptr, (cudaStream_t)stream);
+}
+
+// ------------------------------------------------------------------------------------------
+// fxe_cluster: CF-based clustering of a docking result (LIB/cluster.cpp:9-182).
+// ------------------------------------------------------------------------------------------
+namespace {
+
+// QuickSort_Clusters (LIB/cluster.cpp:323-363): the reference's quicksort of the cluster entries
+// beg..end by ACF, ascending (QS_ASC, LIB/gaboom.h:40), with its pivots and swaps, so that equal
+// ACFs end where the reference puts them. perm follows the entries (each one's index before the
+// sort).
+void quicksort_clusters(int* top, int* fre, double* tcf, double* acf, int* perm, int beg, int end) {
+    auto swap_at = [&](int x, int y) {
+        std::swap(top[x], top[y]);
+        std::swap(fre[x], fre[y]);
+        std::swap(tcf[x], tcf[y]);
+        std::swap(acf[x], acf[y]);
+        std::swap(perm[x], perm[y]);
+    };
+    while (beg < end) {
+        int l = beg, p = beg + (end - beg) / 2, r = end;
+        const double piv = acf[p];
+        while (true) {
+            while (l <= r && (acf[l] - piv) <= 0) ++l;
+            while (l <= r && (acf[r] - piv) > 0) --r;
+            if (l > r) break;
+            swap_at(l, r);
+            if (p == r) p = l;
+            ++l;
+            --r;
+        }
+        swap_at(p, r);
+        --r;
+        if ((r - beg) < (end - l)) {
+            quicksort_clusters(top, fre, tcf, acf, perm, beg, r);
+            beg = l;
+        } else {
+            quicksort_clusters(top, fre, tcf, acf, perm, l, end);
+            end = r;
+        }
+    }
+}
+
+struct DevScratch {
+    std::vector<void*> p;
+    template <typename T>
+    cudaError_t get(T** out, size_t count) {
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, count * sizeof(T) + 16);
+        if (e == cudaSuccess) p.push_back(q);
+        *out = reinterpret_cast<T*>(q);
+        return e;
+    }
+    ~DevScratch() {
+        for (void* q : p) cudaFree(q);
+    }
+};
+
+}  // namespace
+
+extern "C" fxe_status fxe_cluster(fxe_context* ctx, int64_t n, const double* ic, const double* app_evalue,
+                                  int32_t temperature, float rmsd_threshold, int32_t max_results,
+                                  int32_t* top, int32_t* freq, double* tcf, double* acf, int32_t* member_of,
+                                  float* rmsd, float* top_rmsd, int32_t* n_clusters) {
+    g_err.clear();
+    if (!ctx || !ic || !app_evalue || !top || !freq || !tcf || !acf || !n_clusters)
+        return fail(FXE_ERR_INVALID_ARGS, "NULL argument");
+    if (n < 1 || n > FXE_CLUSTER_MAX_N) return fail(FXE_ERR_INVALID_ARGS, "n out of range");
+    if (temperature < 0 || !(rmsd_threshold >= 0.0f) || max_results < 1 || max_results > FXE_CLUSTER_MAX_RESULTS)
+        return fail(FXE_ERR_INVALID_ARGS, "temperature < 0, rmsd_threshold < 0 or max_results out of range");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
+    const int N = (int)n, R = max_results, ng = ctx->S.n_genes, nl = ctx->S.n_lig;
+    const int nb = fxe::cluster_blocks(N);
+    cudaStream_t st = ctx->stream;
+    DevScratch m;
+    fxe::ClusterWork C{};
+    C.n = N;
+    C.temperature = temperature;
+    C.beta = temperature > 0 ? (double)(1.0 / temperature) : 0.0;   // read_input's FA->beta
+    C.thr = rmsd_threshold;
+    // a float sum above thr^2 * n_atoms * (1 + 1e-5) gives sqrtf(sum / n_atoms) > thr whatever
+    // the rounding of the division and the root
+    {
+        const double lim = (double)rmsd_threshold * rmsd_threshold * nl * (1.0 + 1e-5);
+        float f = (float)lim;
+        if ((double)f < lim) f = std::nextafter(f, INFINITY);
+        C.exit_sum = f;
+    }
+    C.max_results = R;
+    double* d_ic = nullptr;
+    double* d_e = nullptr;
+    FXE_TRY(m.get(&d_ic, (size_t)N * ng), "cluster ICs");
+    FXE_TRY(m.get(&d_e, (size_t)N), "cluster energies");
+    C.ic = d_ic;
+    C.e = d_e;
+    FXE_TRY(m.get(&C.xyz, (size_t)3 * nl * N), "cluster coordinates");
+    FXE_TRY(m.get(&C.status, 1), "cluster status");
+    FXE_TRY(m.get(&C.part_z, (size_t)nb), "cluster partials");
+    FXE_TRY(m.get(&C.member, (size_t)N), "cluster members");
+    FXE_TRY(m.get(&C.rmsd, (size_t)N), "cluster rmsd");
+    FXE_TRY(m.get(&C.next, (size_t)R + 1), "cluster heads");
+    FXE_TRY(m.get(&C.part_acf, (size_t)R * nb), "cluster partials");
+    FXE_TRY(m.get(&C.part_cnt, (size_t)R * nb), "cluster partials");
+    FXE_TRY(m.get(&C.top, (size_t)R), "cluster results");
+    FXE_TRY(m.get(&C.freq, (size_t)R), "cluster results");
+    FXE_TRY(m.get(&C.tcf, (size_t)R), "cluster results");
+    FXE_TRY(m.get(&C.acf, (size_t)R), "cluster results");
+    FXE_TRY(m.get(&C.head_rmsd, (size_t)R * R), "cluster results");
+    FXE_TRY(m.get(&C.z, 1), "cluster results");
+    std::vector<int> h_next(R + 1, N);
+    h_next[0] = 0;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    FXE_TRY(cudaEventCreate(&ev[0]), "cluster events");
+    if (cudaEventCreate(&ev[1]) != cudaSuccess) {
+        cudaEventDestroy(ev[0]);
+        return fail(FXE_ERR_LAUNCH, "cluster events");
+    }
+    struct EvGuard {
+        cudaEvent_t* e;
+        ~EvGuard() {
+            cudaEventDestroy(e[0]);
+            cudaEventDestroy(e[1]);
+        }
+    } ev_guard{ev};
+    FXE_TRY(cudaMemcpyAsync(d_ic, ic, sizeof(double) * N * ng, cudaMemcpyHostToDevice, st), "cluster ICs");
+    FXE_TRY(cudaMemcpyAsync(d_e, app_evalue, sizeof(double) * N, cudaMemcpyHostToDevice, st), "cluster energies");
+    FXE_TRY(cudaMemcpyAsync(C.next, h_next.data(), sizeof(int) * (R + 1), cudaMemcpyHostToDevice, st), "cluster heads");
+    FXE_TRY(cudaMemsetAsync(C.member, 0xff, sizeof(int) * N, st), "cluster members");
+    FXE_TRY(cudaMemsetAsync(C.rmsd, 0, sizeof(float) * N, st), "cluster rmsd");
+    FXE_TRY(cudaMemsetAsync(C.status, 0, sizeof(int), st), "cluster status");
+    FXE_TRY(cudaEventRecord(ev[0], st), "cluster events");
+    fxe::launch_cluster(ctx->S, C, st);
+    FXE_TRY(cudaGetLastError(), "cluster launch");
+    FXE_TRY(cudaEventRecord(ev[1], st), "cluster events");
+    ctx->launches += 2 + (temperature > 0 ? 1 : 0) + R;
+    std::vector<int> h_top(R), h_freq(R);
+    std::vector<double> h_tcf(R), h_acf(R);
+    std::vector<float> h_hr((size_t)R * R);
+    int status = 0;
+    double z = 0.0;
+    FXE_TRY(cudaMemcpyAsync(h_next.data(), C.next, sizeof(int) * (R + 1), cudaMemcpyDeviceToHost, st), "cluster results");
+    FXE_TRY(cudaMemcpyAsync(h_top.data(), C.top, sizeof(int) * R, cudaMemcpyDeviceToHost, st), "cluster results");
+    FXE_TRY(cudaMemcpyAsync(h_freq.data(), C.freq, sizeof(int) * R, cudaMemcpyDeviceToHost, st), "cluster results");
+    FXE_TRY(cudaMemcpyAsync(h_tcf.data(), C.tcf, sizeof(double) * R, cudaMemcpyDeviceToHost, st), "cluster results");
+    FXE_TRY(cudaMemcpyAsync(h_acf.data(), C.acf, sizeof(double) * R, cudaMemcpyDeviceToHost, st), "cluster results");
+    FXE_TRY(cudaMemcpyAsync(h_hr.data(), C.head_rmsd, sizeof(float) * R * R, cudaMemcpyDeviceToHost, st), "cluster results");
+    FXE_TRY(cudaMemcpyAsync(&status, C.status, sizeof(int), cudaMemcpyDeviceToHost, st), "cluster results");
+    FXE_TRY(cudaMemcpyAsync(&z, C.z, sizeof(double), cudaMemcpyDeviceToHost, st), "cluster results");
+    if (member_of)
+        FXE_TRY(cudaMemcpyAsync(member_of, C.member, sizeof(int) * N, cudaMemcpyDeviceToHost, st), "cluster members");
+    if (rmsd) FXE_TRY(cudaMemcpyAsync(rmsd, C.rmsd, sizeof(float) * N, cudaMemcpyDeviceToHost, st), "cluster rmsd");
+    FXE_TRY(cudaStreamSynchronize(st), "cluster");
+    float ms = 0.0f;
+    FXE_TRY(cudaEventElapsedTime(&ms, ev[0], ev[1]), "cluster events");
+    ctx->cluster_ms = ms;
+    if (status & 2) return fail(FXE_ERR_INVALID_ARGS, "an IC lies outside its gene limits");
+    if (status & 1) return fail(FXE_ERR_INVALID_ARGS, "a grid gene names no cleft point");
+    if (temperature > 0 && z == 0.0)
+        return fail(FXE_ERR_INVALID_ARGS, "the partition function of the clustering step is zero");
+    int nc = 0;
+    while (nc < R && h_next[nc] < N) ++nc;
+    std::vector<int> perm(R);
+    for (int k = 0; k < R; ++k) perm[k] = k;
+    // the reference sorts its first max_results entries (LIB/cluster.cpp:177-181); its arrays
+    // hold num_chrom entries, so at most n of them here
+    if (temperature > 0) quicksort_clusters(h_top.data(), h_freq.data(), h_tcf.data(), h_acf.data(), perm.data(), 0,
+                                            (R < N ? R : N) - 1);
+    for (int k = 0; k < R; ++k) {
+        top[k] = h_top[k];
+        freq[k] = h_freq[k];
+        tcf[k] = h_tcf[k];
+        acf[k] = h_acf[k];
+    }
+    if (top_rmsd)
+        for (int a = 0; a < R; ++a)
+            for (int b = 0; b < R; ++b) {
+                // entries past the clusters formed name chromosome 0, the first cluster's head
+                const int ca = perm[a] < nc ? perm[a] : 0, cb = perm[b] < nc ? perm[b] : 0;
+                top_rmsd[(size_t)a * R + b] = h_hr[(size_t)ca * nc + cb];
+            }
+    *n_clusters = nc;
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_last_cluster_time(fxe_context* ctx, double* device_ms) {
+    g_err.clear();
+    if (!ctx || !device_ms) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    *device_ms = ctx->cluster_ms;
+    return FXE_OK;
 }
 
 // ------------------------------------------------------------------------------------------

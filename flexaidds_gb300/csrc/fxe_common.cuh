@@ -267,6 +267,33 @@ struct LsePart {
     double m, s, e1, e2;
 };
 
+// Device buffers and parameters of one clustering call (fxe_cluster). nb = cluster_blocks(n)
+// blocks run each pass; R = max_results.
+struct ClusterWork {
+    int n;
+    const double* ic;        // [n * n_genes]
+    const double* e;         // [n] app_evalue
+    float* xyz;              // [3 * n_lig * n] ligand coordinates by coordinate, then chromosome
+    int* status;             // [1] set when a grid gene is out of range
+    int temperature;         // K; 0: no Boltzmann terms
+    double beta;             // 1 / temperature (read_input's FA->beta)
+    float thr;               // RMSD threshold
+    float exit_sum;          // a sum of squares past which the RMSD is above thr
+    int max_results;
+    double* part_z;          // [nb]
+    int* member;             // [n] head of the chromosome's cluster, -1 none
+    float* rmsd;             // [n]
+    int* next;               // [R + 1] head of each cluster (n: none)
+    double* part_acf;        // [R * nb]
+    int* part_cnt;           // [R * nb]
+    int* top;                // [R]
+    int* freq;               // [R]
+    double* tcf;             // [R]
+    double* acf;             // [R]
+    float* head_rmsd;        // [R * R] (the first n_clusters^2 entries are written)
+    double* z;               // [1] partition function
+};
+
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

@@ -69,6 +69,9 @@ def load_library():
         lib.fxe_ga_duplicates.argtypes = [vp, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         lib.fxe_ga_destroy.argtypes = [vp]
         lib.fxe_ga_destroy.restype = None
+        lib.fxe_cluster.argtypes = [vp, C.c_int64, _d, _d, C.c_int32, C.c_float, C.c_int32, _i, _i, _d, _d,
+                                    _i, _f, _f, _i]
+        lib.fxe_last_cluster_time.argtypes = [vp, _d]
         lib.fxe_context_destroy.argtypes = [vp]
         lib.fxe_context_destroy.restype = None
         lib.fxe_last_error.restype = C.c_char_p
@@ -159,6 +162,37 @@ class GPUEvaluator:
         out = np.zeros((self.desc.n_lig, 3), np.float32)
         _check(self.lib.fxe_last_ligand_xyz(self.handle, pose, ptr(out, _f)))
         return out
+
+    def cluster(self, ic: np.ndarray, app_evalue: np.ndarray, temperature: int = 0, rmsd: float = 2.0,
+                max_results: int = 10) -> dict:
+        """CF-based clustering of a docking result (cluster, LIB/cluster.cpp:9-182) on the device:
+        ic (n, n_genes) decoded ICs within their gene limits, best first (the GA's ensemble),
+        app_evalue (n,). temperature (K, integer; 0 = the reference's default), rmsd
+        (FA->cluster_rmsd) and max_results (FA->max_results) as the reference's options.
+        Returns n_clusters and, per cluster entry in the reference's final order, top (head
+        chromosome), freq, tcf, acf; per chromosome member_of (head, -1 = unclustered) and rmsd;
+        top_rmsd (entries x entries), the RMSD between entry heads listed in the .cad file."""
+        ic = np.ascontiguousarray(ic, np.float64)
+        e = np.ascontiguousarray(app_evalue, np.float64)
+        if ic.ndim != 2 or ic.shape[1] != self.desc.n_genes or e.shape != (ic.shape[0],):
+            raise FxeError("cluster: ic must be (n, n_genes) and app_evalue (n,)")
+        n, R = ic.shape[0], int(max_results)
+        top, freq = np.zeros(R, np.int32), np.zeros(R, np.int32)
+        tcf, acf = np.zeros(R, np.float64), np.zeros(R, np.float64)
+        member, rms = np.zeros(n, np.int32), np.zeros(n, np.float32)
+        top_rmsd = np.zeros((R, R), np.float32)
+        nc = C.c_int32(0)
+        _check(self.lib.fxe_cluster(self.handle, n, ptr(ic, _d), ptr(e, _d), int(temperature), float(rmsd), R,
+                                    ptr(top, _i), ptr(freq, _i), ptr(tcf, _d), ptr(acf, _d), ptr(member, _i),
+                                    ptr(rms, _f), ptr(top_rmsd, _f), C.byref(nc)))
+        return {"n_clusters": nc.value, "top": top, "freq": freq, "tcf": tcf, "acf": acf,
+                "member_of": member, "rmsd": rms, "top_rmsd": top_rmsd}
+
+    def cluster_time(self) -> float:
+        """Device milliseconds of the last cluster call's kernels."""
+        ms = np.zeros(1, np.float64)
+        _check(self.lib.fxe_last_cluster_time(self.handle, ptr(ms, _d)))
+        return float(ms[0])
 
     def stats(self) -> dict:
         o = np.zeros(4, np.int32)

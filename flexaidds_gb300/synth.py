@@ -469,3 +469,27 @@ def energy_matrix(seed: int, ntypes: int = NTYPES) -> np.ndarray:
 def random_genes(n_chrom: int, n_genes: int, seed: int) -> np.ndarray:
     rng = np.random.default_rng(seed)
     return rng.integers(0, 2 ** 31, size=(n_chrom, n_genes), dtype=np.int64).astype(np.int32)
+
+
+def clustered_ensemble(desc, n_centres: int, per_centre: int, seed: int, spread: int = 2):
+    """A seeded stand-in for a GA ensemble with structure to cluster: n_centres chromosomes drawn
+    at random, each with per_centre variants whose genes move a few bins from the centre's
+    (the grid index by up to 3 * spread points, each angle by up to spread bins), the values
+    kept on their bins (min + del * i, as genetoic gives them) and within the gene limits.
+    Energies are drawn around a per-centre mean; the rows come sorted by energy, best first.
+    Returns (ic (n, n_genes), app_evalue (n,))."""
+    rng = np.random.default_rng(seed)
+    ng = desc.n_genes
+    base = desc.genes_to_ic(random_genes(n_centres, ng, seed + 1))
+    lo = np.zeros(ng, np.int64)
+    hi = np.floor((desc.gene_max - desc.gene_min) / desc.gene_del + 1e-9).astype(np.int64)
+    idx = np.rint((base - desc.gene_min) / desc.gene_del).astype(np.int64)           # (C, ng)
+    mean = rng.normal(-25.0, 6.0, size=n_centres)
+    step = rng.integers(-spread, spread + 1, size=(n_centres, per_centre, ng))
+    step[:, :, desc.gene_typ == -1] *= 3
+    step[:, :, desc.gene_typ == 4] = 0
+    k = np.clip(idx[:, None, :] + step, lo, hi).reshape(-1, ng)
+    ic = desc.gene_min + desc.gene_del * k.astype(np.float64)
+    e = (mean[:, None] + rng.normal(0.0, 1.5, size=(n_centres, per_centre))).reshape(-1)
+    order = np.argsort(e, kind="stable")
+    return np.ascontiguousarray(ic[order]), np.ascontiguousarray(e[order])

@@ -239,6 +239,45 @@ fxe_status fxe_thermo_compute_device_fixed(const double* d_energies, const int32
 fxe_status fxe_thermo_weights(const double* energies, const int32_t* multiplicity, int64_t n,
                               double temperature, double* weights);
 
+/* CF-based clustering of a docking result: cluster (LIB/cluster.cpp:9-182), the reference's
+ * default clustering of the GA's ensemble (LIB/top.cpp:1351-1354; its file outputs come from
+ * these results, see the Python writers).
+ *
+ * Input: n chromosomes as decoded ICs (n * n_genes, each within its gene limits, as the GA's
+ * ensemble holds them: best first) and their apparent energies (app_evalue). The ligand of each
+ * is built as calc_rmsd_chrom builds it (LIB/calc_rmsd_chrom.cpp:7-145). While chromosomes are
+ * left and fewer than max_results (FA->max_results, default 10) clusters exist, the first
+ * chromosome no cluster holds heads a new cluster, which takes in every later chromosome not yet
+ * clustered whose ligand RMSD to the head (single precision over the ligand atoms in order) is
+ * at most rmsd_threshold (FA->cluster_rmsd, default 2.0).
+ * temperature (FA->temperature, K, an integer; 0, the reference's default, turns it off): with
+ * beta = 1 / temperature (FA->beta as read_input sets it) and Z the sum of exp(-beta E) over all
+ * n, a cluster's TCF is P E - T P ln P of its head and its ACF that plus P E + T P ln P of each
+ * member (P = exp(-beta E) / Z), and the first min(max_results, n) entries are then reordered by
+ * ACF with the reference's quicksort (QuickSort_Clusters); at temperature 0 the TCF is the
+ * head's energy and the ACF the sum of the energies in the cluster.
+ *
+ * Outputs (host arrays, caller-owned): top, freq, tcf, acf [max_results]: the cluster entries in
+ * the reference's final order (head chromosome, members counting the head, TCF, ACF; entries
+ * past *n_clusters hold zeros, which the ACF sort can move forward, as in the reference);
+ * member_of [n] (or NULL): the head of each chromosome's cluster, -1 for chromosomes left
+ * unclustered after max_results clusters (the reference's Clus_GAPOP before its sort, which
+ * also swaps the first entries of that per-chromosome array); rmsd [n] (or NULL): the RMSD of
+ * each clustered chromosome to its head; top_rmsd [max_results^2] (or NULL): the RMSD between
+ * the heads of entries a and b (row a), as calc_rmsd_chrom computes it for the .cad file.
+ * FXE_ERR_INVALID_ARGS when an IC lies outside its gene limits or Z is zero (the reference stops
+ * there, LIB/cluster.cpp:83-88). */
+#define FXE_CLUSTER_MAX_N ((int64_t)1 << 30)
+#define FXE_CLUSTER_MAX_RESULTS 1024
+fxe_status fxe_cluster(fxe_context* ctx, int64_t n, const double* ic, const double* app_evalue,
+                       int32_t temperature, float rmsd_threshold, int32_t max_results, int32_t* top,
+                       int32_t* freq, double* tcf, double* acf, int32_t* member_of, float* rmsd,
+                       float* top_rmsd, int32_t* n_clusters);
+
+/* Device time (ms, CUDA events on the context's stream) of the kernels of the last fxe_cluster
+ * call. No reference counterpart. */
+fxe_status fxe_last_cluster_time(fxe_context* ctx, double* device_ms);
+
 /* Per-stage device time of the evaluation calls. When enabled, every batch records CUDA events
  * around its three kernels (pose build, contact candidates, polyhedra and scoring) on the
  * batch's stream and waits for the last one, so fxe_eval_genes_device returns only after its

@@ -1369,3 +1369,192 @@ int fxo_thermo_weights(const double* e, const int32_t* mult, int64_t n, double T
     for (int64_t i = 0; i < n; ++i) w[i] /= z;
     return 0;
 }
+
+/* ----------------------------------------------------------------------------------------
+ * CF-based clustering (cluster, LIB/cluster.cpp:9-182)
+ * -------------------------------------------------------------------------------------- */
+
+/* Ligand coordinates of n chromosomes as calc_rmsd_chrom builds them
+ * (LIB/calc_rmsd_chrom.cpp:7-145): the ICs as given (no clamp), assigned as ic2cf does, then
+ * buildcc; xyz_out holds n * n_lig * 3 floats, atoms in ligand order. */
+int fxo_build_ic(const fxe_receptor_desc* rec, const fxe_ligand_desc* lig, int32_t n, const double* ic,
+                 float* xyz_out) {
+    if (!rec || !lig || n < 0 || (n > 0 && (!ic || !xyz_out))) return -1;
+    State S;
+    memset(&S, 0, sizeof(S));
+    S.nrec = 0;
+    S.nlig = lig->n_atoms;
+    S.xyz = (float(*)[3])calloc((size_t)(S.nlig > 0 ? S.nlig : 1), sizeof(*S.xyz));
+    S.lic = (float(*)[3])calloc((size_t)(S.nlig > 0 ? S.nlig : 1), sizeof(*S.lic));
+    if (!S.xyz || !S.lic) {
+        free(S.xyz);
+        free(S.lic);
+        return -1;
+    }
+    for (int p = 0; p < n; ++p) {
+        const double* icv = ic + (size_t)p * lig->n_genes;
+        for (int g = 0; g < lig->n_genes; ++g)
+            if (lig->gene_type[g] == -1 && !(icv[g] >= 0.0 && icv[g] < (double)rec->n_grid)) {
+                free(S.xyz);
+                free(S.lic);
+                return -1;
+            }
+        assign_ic(&S, rec, lig, icv);
+        buildcc(&S, rec, lig);
+        for (int l = 0; l < S.nlig; ++l)
+            for (int k = 0; k < 3; ++k) xyz_out[((size_t)p * S.nlig + l) * 3 + k] = S.xyz[l][k];
+    }
+    free(S.xyz);
+    free(S.lic);
+    return 0;
+}
+
+/* QuickSort_Clusters and swap_clusters, LIB/cluster.cpp:323-374 (QS_ASC(a,b) = a - b,
+ * LIB/gaboom.h:40). The reference swaps its per-chromosome Clus_GAPOP entries along with the
+ * cluster entries; that array is returned here as it was before the sort. */
+static void qs_clusters(int* top, int* fre, double* tcf, double* acf, int beg, int end) {
+    while (beg < end) {
+        int l = beg, p = beg + (end - beg) / 2, r = end;
+        const double piv = acf[p];
+        for (;;) {
+            while (l <= r && (acf[l] - piv) <= 0) ++l;
+            while (l <= r && (acf[r] - piv) > 0) --r;
+            if (l > r) break;
+            { int t = top[l]; top[l] = top[r]; top[r] = t; t = fre[l]; fre[l] = fre[r]; fre[r] = t; }
+            { double t = tcf[l]; tcf[l] = tcf[r]; tcf[r] = t; t = acf[l]; acf[l] = acf[r]; acf[r] = t; }
+            if (p == r) p = l;
+            ++l;
+            --r;
+        }
+        { int t = top[p]; top[p] = top[r]; top[r] = t; t = fre[p]; fre[p] = fre[r]; fre[r] = t; }
+        { double t = tcf[p]; tcf[p] = tcf[r]; tcf[r] = t; t = acf[p]; acf[p] = acf[r]; acf[r] = t; }
+        --r;
+        if ((r - beg) < (end - l)) {
+            qs_clusters(top, fre, tcf, acf, beg, r);
+            beg = l;
+        } else {
+            qs_clusters(top, fre, tcf, acf, l, end);
+            end = r;
+        }
+    }
+}
+
+/* cluster, LIB/cluster.cpp:9-218: the coordinate cache, the partition function, the clusters
+ * formed head by head, the ACF sort, and the RMSD between cluster heads of the .cad file
+ * (calc_rmsd_chrom with calc_rmsd = true: sqrdist summed atom by atom, LIB/geometry.cpp:96-102).
+ * Outputs as fxe_cluster (include/fxe.h). Returns 0, -1 on invalid input, -2 when the partition
+ * function is zero (the reference stops, LIB/cluster.cpp:83-88). */
+int fxo_cluster(const fxe_receptor_desc* rec, const fxe_ligand_desc* lig, int32_t n, const double* ic,
+                const double* app_evalue, int32_t temperature, float rmsd_threshold, int32_t max_results,
+                int32_t* top, int32_t* freq, double* tcf, double* acf, int32_t* member_of, float* rmsd,
+                float* top_rmsd, int32_t* n_clusters) {
+    if (!rec || !lig || n < 1 || !ic || !app_evalue || temperature < 0 || max_results < 1 || !top || !freq ||
+        !tcf || !acf || !n_clusters)
+        return -1;
+    const int nl = lig->n_atoms, stride = 3 * nl;
+    const int m = n > max_results ? n : max_results;
+    float* xyz = (float*)malloc((size_t)n * stride * sizeof(float));
+    int* gap = (int*)malloc((size_t)n * sizeof(int));
+    float* rt = (float*)calloc((size_t)n, sizeof(float));
+    double* cacf = (double*)calloc((size_t)m, sizeof(double));
+    double* ctcf = (double*)calloc((size_t)m, sizeof(double));
+    int* ctop = (int*)calloc((size_t)m, sizeof(int));
+    int* cfre = (int*)calloc((size_t)m, sizeof(int));
+    int rc = 0;
+    if (!xyz || !gap || !rt || !cacf || !ctcf || !ctop || !cfre || fxo_build_ic(rec, lig, n, ic, xyz) != 0) {
+        rc = -1;
+        goto done;
+    }
+    {
+        const unsigned T = (unsigned)temperature;
+        const double beta = T ? (double)(1.0 / T) : 0.0;
+        double pf = 0.0;
+        for (int j = 0; j < n; ++j) {
+            gap[j] = -1;
+            if (T) pf += exp((-1.0) * beta * app_evalue[j]);
+        }
+        if (T && pf == 0.0) {
+            rc = -2;
+            goto done;
+        }
+        int nunc = n, nc = 0;
+        while (nunc > 0) {
+            int j;
+            for (j = 0; j < n; ++j)
+                if (gap[j] == -1) break;
+            if (j >= n) break;
+            gap[j] = j;
+            rt[j] = 0.0f;
+            nunc--;
+            if (T > 0) {
+                const double Pj = exp((-1.0) * beta * app_evalue[j]) / pf;
+                cacf[nc] = (double)((Pj * app_evalue[j]) - (T * Pj * log(Pj)));
+                ctcf[nc] = (double)((Pj * app_evalue[j]) - (T * Pj * log(Pj)));
+            } else {
+                ctcf[nc] = app_evalue[j];
+                cacf[nc] = app_evalue[j];
+            }
+            ctop[nc] = j;
+            cfre[nc]++;
+            const float* cj = xyz + (size_t)j * stride;
+            for (int i = j + 1; i < n; ++i) {
+                if (gap[i] != -1) continue;
+                const float* ci = xyz + (size_t)i * stride;
+                /* flexaids::sum_sq_distances_f, scalar form (LIB/simd_distance.h:712-713) */
+                float d = 0.0f;
+                for (int k = 0; k < stride; ++k) {
+                    const float t = ci[k] - cj[k];
+                    d += t * t;
+                }
+                const float loc = sqrtf(d / (float)nl);
+                if (loc <= rmsd_threshold) {
+                    gap[i] = j;
+                    rt[i] = loc;
+                    nunc--;
+                    if (T) {
+                        const double Pi = exp((-1.0) * beta * app_evalue[i]) / pf;
+                        cacf[nc] += (double)((Pi * app_evalue[i]) + (T * Pi * log(Pi)));
+                    } else {
+                        cacf[nc] += app_evalue[i];
+                    }
+                    cfre[nc]++;
+                }
+            }
+            nc++;
+            if (nc == max_results) break;
+        }
+        if (T) qs_clusters(ctop, cfre, ctcf, cacf, 0, (max_results < n ? max_results : n) - 1);
+        for (int k = 0; k < max_results; ++k) {
+            top[k] = ctop[k];
+            freq[k] = cfre[k];
+            tcf[k] = ctcf[k];
+            acf[k] = cacf[k];
+        }
+        if (top_rmsd)
+            for (int a = 0; a < max_results; ++a)
+                for (int b = 0; b < max_results; ++b) {
+                    const float* pa = xyz + (size_t)ctop[a] * stride;
+                    const float* pb = xyz + (size_t)ctop[b] * stride;
+                    float s = 0.0f;
+                    for (int l = 0; l < nl; ++l) {
+                        const float d0 = pa[3 * l] - pb[3 * l];
+                        const float d1 = pa[3 * l + 1] - pb[3 * l + 1];
+                        const float d2 = pa[3 * l + 2] - pb[3 * l + 2];
+                        s += d0 * d0 + d1 * d1 + d2 * d2;
+                    }
+                    top_rmsd[(size_t)a * max_results + b] = (float)sqrt(s / ((float)nl));
+                }
+        if (member_of) memcpy(member_of, gap, (size_t)n * sizeof(int));
+        if (rmsd) memcpy(rmsd, rt, (size_t)n * sizeof(float));
+        *n_clusters = nc;
+    }
+done:
+    free(xyz);
+    free(gap);
+    free(rt);
+    free(cacf);
+    free(ctcf);
+    free(ctop);
+    free(cfre);
+    return rc;
+}

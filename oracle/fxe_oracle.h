@@ -61,6 +61,19 @@ int fxo_thermo(const double* e, const int32_t* mult, int64_t n, double temperatu
 int fxo_thermo_weights(const double* e, const int32_t* mult, int64_t n, double temperature,
                        double* w);
 
+/* Ligand coordinates of n chromosomes given as ICs, as calc_rmsd_chrom builds them (no clamp);
+ * xyz_out n * n_lig * 3. */
+int fxo_build_ic(const fxe_receptor_desc* rec, const fxe_ligand_desc* lig, int32_t n, const double* ic,
+                 float* xyz_out);
+
+/* CF-based clustering (cluster, LIB/cluster.cpp:9-218), serial, with the reference's order of
+ * sums; arguments and outputs as fxe_cluster. Returns 0, -1 (invalid input) or -2 (zero
+ * partition function). */
+int fxo_cluster(const fxe_receptor_desc* rec, const fxe_ligand_desc* lig, int32_t n, const double* ic,
+                const double* app_evalue, int32_t temperature, float rmsd_threshold, int32_t max_results,
+                int32_t* top, int32_t* freq, double* tcf, double* acf, int32_t* member_of, float* rmsd,
+                float* top_rmsd, int32_t* n_clusters);
+
 /* Geometry helpers restated from LIB/Vcontacts.cpp, exported for known-answer tests. */
 int fxo_solve_3x3(const double* eq0, const double* eq1, const double* eq2, double* pt);
 int fxo_solve_2xS(const double* p0, const double* p1, float rado, double* pt0, double* pt1);

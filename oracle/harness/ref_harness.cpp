@@ -21,6 +21,7 @@
 // clamp each IC into its gene limits, then ic2cf).
 
 #include "flexaid.h"
+#include "gaboom.h"
 #include "Vcontacts.h"
 
 #include <cstdint>
@@ -619,6 +620,53 @@ int ref_last_contacts(int32_t i, int32_t cap, int32_t* partner, double* area, do
         dist[k] = H->last_dists[i][k];
     }
     return m;
+}
+
+// Runs the reference's CF-based clustering (cluster, LIB/cluster.cpp:9-182) over n chromosomes
+// given as ICs (n * n_genes, within their gene limits) and their app_evalue, with
+// FA->temperature, FA->beta (1 / temperature, as read_input sets it), FA->cluster_rmsd and
+// FA->max_results as given. The reference writes <prefix>.cad (cluster table and the RMSD between
+// cluster heads) and <prefix>_<k>.pdb per result, which the tests read.
+int ref_cluster(int32_t n, const double* ic, const double* app_evalue, int32_t temperature, float rmsd,
+                int32_t max_results, const char* prefix) {
+    if (!H || n < 1 || !prefix || strlen(prefix) + 16 >= MAX_PATH__) return -1;
+    Harness& h = *H;
+    FA_Global* FA = h.FA;
+    const int ng = FA->npar;
+    GB_Global GB{};
+    GB.num_genes = ng;
+    std::vector<chromosome> chrom(n);
+    std::vector<gene> genes((size_t)n * ng);
+    for (int p = 0; p < n; ++p) {
+        chrom[p] = chromosome{};
+        chrom[p].genes = &genes[(size_t)p * ng];
+        for (int g = 0; g < ng; ++g) genes[(size_t)p * ng + g].to_ic = ic[(size_t)p * ng + g];
+        chrom[p].evalue = chrom[p].app_evalue = app_evalue[p];
+    }
+    std::vector<genlim> lim(ng > 0 ? ng : 1);
+    for (int g = 0; g < ng; ++g) {
+        lim[g].min = FA->min_opt_par[g];
+        lim[g].max = FA->max_opt_par[g];
+        lim[g].del = FA->del_opt_par[g];
+        lim[g].map = FA->map_opt_par[g];
+    }
+    FA->temperature = (uint)temperature;
+    FA->beta = temperature > 0 ? (double)(1.0 / FA->temperature) : 0.0;
+    FA->cluster_rmsd = rmsd;
+    FA->max_results = max_results;
+    FA->htpmode = false;
+    FA->refstructure = 0;
+    FA->het_res[1] = h.lig_res;   // the ligand residue (write_pdb's CONECT records)
+    char end_strfile[MAX_PATH__], tmp_end_strfile[MAX_PATH__], dockinp[] = "dock.inp", gainp[] = "ga.inp";
+    snprintf(end_strfile, sizeof(end_strfile), "%s", prefix);
+    for (const auto& ra : h.rotamer_atoms)
+        for (int c = 0; c < 3; ++c) h.atoms[ra.first].coor[c] = ra.second[c];
+    cluster(FA, &GB, h.VC, chrom.data(), lim.data(), h.atoms, h.residue, h.cleftgrid, n, end_strfile,
+            tmp_end_strfile, dockinp, gainp);
+    FA->htpmode = true;
+    FA->temperature = 0;
+    FA->beta = 0.0;
+    return 0;
 }
 
 }  // extern "C"

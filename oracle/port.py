@@ -58,6 +58,9 @@ def _load():
         _lib.fxo_cosPQR.restype = C.c_double
         _lib.fxo_spherical_arc.argtypes = [_d, C.c_double, _d, C.c_double, _d, C.c_double, C.c_float]
         _lib.fxo_spherical_arc.restype = C.c_double
+        _lib.fxo_build_ic.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, _d, _f]
+        _lib.fxo_cluster.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, _d, _d, C.c_int32, C.c_float,
+                                     C.c_int32, _i, _i, _d, _d, _i, _f, _f, _i]
     return _lib
 
 
@@ -98,6 +101,36 @@ class Oracle:
         if counts:
             res["counts"] = {k: getattr(cnt, k) for k, _ in Counts._fields_}
         return res
+
+    def build_ic(self, ic: np.ndarray) -> np.ndarray:
+        """Ligand coordinates (n, n_lig, 3) as calc_rmsd_chrom builds them."""
+        lib = _load()
+        ic = np.ascontiguousarray(ic, np.float64)
+        xyz = np.zeros((ic.shape[0], self.d.n_lig, 3), np.float32)
+        if lib.fxo_build_ic(C.byref(self.packed.rec), C.byref(self.packed.lig), ic.shape[0], ptr(ic, _d),
+                            ptr(xyz, _f)) != 0:
+            raise RuntimeError("fxo_build_ic failed")
+        return xyz
+
+    def cluster(self, ic: np.ndarray, app_evalue: np.ndarray, temperature: int = 0, rmsd: float = 2.0,
+                max_results: int = 10) -> dict:
+        """CF-based clustering, serial restatement of cluster (LIB/cluster.cpp)."""
+        lib = _load()
+        ic = np.ascontiguousarray(ic, np.float64)
+        e = np.ascontiguousarray(app_evalue, np.float64)
+        n, R = ic.shape[0], int(max_results)
+        top, freq = np.zeros(R, np.int32), np.zeros(R, np.int32)
+        tcf, acf = np.zeros(R, np.float64), np.zeros(R, np.float64)
+        member, rms = np.zeros(n, np.int32), np.zeros(n, np.float32)
+        top_rmsd = np.zeros((R, R), np.float32)
+        nc = C.c_int32(0)
+        rc = lib.fxo_cluster(C.byref(self.packed.rec), C.byref(self.packed.lig), n, ptr(ic, _d), ptr(e, _d),
+                             int(temperature), float(rmsd), R, ptr(top, _i), ptr(freq, _i), ptr(tcf, _d),
+                             ptr(acf, _d), ptr(member, _i), ptr(rms, _f), ptr(top_rmsd, _f), C.byref(nc))
+        if rc != 0:
+            raise RuntimeError(f"fxo_cluster failed ({rc})")
+        return {"n_clusters": nc.value, "top": top, "freq": freq, "tcf": tcf, "acf": acf,
+                "member_of": member, "rmsd": rms, "top_rmsd": top_rmsd}
 
     def genes_to_ic(self, genes: np.ndarray) -> np.ndarray:
         lib = _load()

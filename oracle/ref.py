@@ -58,6 +58,7 @@ def _load():
         _lib.ref_eval.argtypes = [C.c_int32, _d, _d, _i, _f]
         _lib.ref_last_contacts.argtypes = [C.c_int32, C.c_int32, _i, _d, _d]
         _lib.ref_export_flex_bonded.argtypes = [_b]
+        _lib.ref_cluster.argtypes = [C.c_int32, _d, _d, C.c_int32, C.c_float, C.c_int32, C.c_char_p]
     return _lib
 
 
@@ -201,3 +202,18 @@ class RefHarness:
             m = lib.ref_last_contacts(i, cap, _p(p, _i), _p(a, _d), _p(d, _d))
             out.append((p[:m].copy(), a[:m].copy(), d[:m].copy()))
         return out
+
+    def cluster(self, ic: np.ndarray, app_evalue: np.ndarray, temperature: int, rmsd: float,
+                max_results: int, prefix: str) -> str:
+        """Runs the reference's CF-based clustering (cluster, LIB/cluster.cpp) and returns the
+        text of the .cad file it writes at <prefix>.cad (its <prefix>_<k>.pdb files stay beside
+        it)."""
+        lib = _load()
+        ic = np.ascontiguousarray(ic, np.float64)
+        e = np.ascontiguousarray(app_evalue, np.float64)
+        rc = lib.ref_cluster(ic.shape[0], _p(ic, _d), _p(e, _d), int(temperature), float(rmsd),
+                             int(max_results), prefix.encode())
+        if rc != 0:
+            raise RuntimeError(f"ref_cluster failed ({rc})")
+        with open(prefix + ".cad") as f:
+            return f.read()

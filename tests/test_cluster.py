@@ -1,0 +1,214 @@
+"""CF-based clustering (cluster, LIB/cluster.cpp:9-218) and the result files.
+
+CPU: the C restatement against the golden fixtures made by the reference's own cluster()
+(tests/golden/make_golden_cluster.py: the .cad text it wrote, byte for byte), its invariants, and
+the writers' formats (.cad, _par.res). GPU: fxe_cluster through the C ABI against the
+restatement on the fixtures and on larger seeded ensembles: heads, frequencies, members and
+RMSDs bit for bit, the FP64 TCF/ACF sums within 1e-12 (the device adds them in another order),
+and the .cad text identical to the reference's.
+"""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from flexaidds_gb300 import results, synth
+from flexaidds_gb300.system import Descriptor
+from oracle import port
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CLUSTER_FIXTURES = ("cluster_flex_900_16", "cluster_lig_2000_24")
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    d = Descriptor.from_arrays(z, "d_")
+    cases = [(int(t), float(r), int(m)) for t, r, m in z["cases"]]
+    cads = [bytes(z[f"cad_{k}"]).decode() for k in range(len(cases))]
+    return d, z["ic"], z["app_evalue"], cases, cads
+
+
+@pytest.fixture(scope="module", params=CLUSTER_FIXTURES)
+def fixture(request):
+    return load(request.param)
+
+
+def oracle_cluster(d, ic, e, T, thr, R):
+    port.set_trig_rounding(False)
+    return port.Oracle(d).cluster(ic, e, T, thr, R)
+
+
+def test_oracle_against_reference_cad(fixture):
+    d, ic, e, cases, cads = fixture
+    for (T, thr, R), cad in zip(cases, cads):
+        r = oracle_cluster(d, ic, e, T, thr, R)
+        assert results.cad_text(r) == cad, (T, thr, R)
+
+
+def test_oracle_cluster_invariants(fixture):
+    d, ic, e, cases, _ = fixture
+    n = ic.shape[0]
+    xyz = port.Oracle(d).build_ic(ic).reshape(n, -1)
+    for T, thr, R in cases:
+        r = oracle_cluster(d, ic, e, T, thr, R)
+        nc, mem = r["n_clusters"], r["member_of"]
+        heads = np.unique(mem[mem >= 0])
+        assert len(heads) == nc <= R
+        assert np.all(mem[heads] == heads)
+        # a head is the first chromosome of its cluster, and heads come in chromosome order
+        for h in heads:
+            assert np.nonzero(mem == h)[0][0] == h
+        # members are within the threshold of their head (the RMSD recomputed here in float64
+        # agrees with the single-precision one to rounding)
+        k = np.nonzero(mem >= 0)[0]
+        ref = np.sqrt(((xyz[k] - xyz[mem[k]]).astype(np.float64) ** 2).sum(1) / d.n_lig)
+        np.testing.assert_allclose(r["rmsd"][k], ref, rtol=1e-5, atol=1e-5)
+        assert np.all(r["rmsd"][k] <= thr)
+        # frequencies and (at temperature 0) ACF = the cluster's energy sum, in entry order
+        real = r["freq"] > 0
+        assert r["freq"].sum() == len(k)
+        if T == 0:
+            for c in range(nc):
+                sel = mem == r["top"][c]
+                assert r["freq"][c] == sel.sum()
+                assert abs(r["acf"][c] - e[sel].sum()) <= 1e-9 * max(1.0, abs(r["acf"][c]))
+                assert r["tcf"][c] == e[r["top"][c]]
+        else:
+            assert np.all(np.diff(r["acf"][: min(R, n)]) >= 0)   # sorted by ACF
+            assert real.sum() == nc
+
+
+def test_unclustered_after_max_results(fixture):
+    d, ic, e, _, _ = fixture
+    r = oracle_cluster(d, ic, e, 0, 0.5, 3)
+    assert r["n_clusters"] == 3
+    mem = r["member_of"]
+    assert (mem == -1).any()
+    assert np.all(r["rmsd"][mem == -1] == 0.0)
+
+
+def test_cad_text_format():
+    res = {"n_clusters": 2, "top": np.array([3, 0, 0]), "freq": np.array([4, 1, 0]),
+           "tcf": np.array([-12.5, -3.25, 0.0]), "acf": np.array([-40.0, -3.25, 0.0]),
+           "top_rmsd": np.array([[0, 1.5, 0], [1.5, 0, 0], [0, 0, 0]], np.float32)}
+    assert results.cad_text(res) == (
+        "Cluster 0: TOP=3 TCF=-12.500000 ACF=-40.000000 freq=4\n"
+        "Cluster 1: TOP=0 TCF=-3.250000 ACF=-3.250000 freq=1\n"
+        "RMSD between clusters\n"
+        "rmsd(0,1)=1.500000\n")
+    res["n_clusters"] = 1
+    assert results.cad_text(res) == "Cluster 0: TOP=3 TCF=-12.500000 ACF=-40.000000 freq=4\n"
+
+
+def test_par_file_layout(tiny_system):
+    """write_par (LIB/gaboom.cpp:2771-2803): "genes", one 48-byte genlim per gene, "chrom", the
+    int32 genes chromosome by chromosome."""
+    _, d = tiny_system
+    genes = synth.random_genes(7, d.n_genes, seed=3)
+    data = results.par_bytes(d, genes)
+    ng = d.n_genes
+    assert len(data) == 5 + 48 * ng + 5 + 4 * 7 * ng
+    assert data[:5] == b"genes" and data[5 + 48 * ng:10 + 48 * ng] == b"chrom"
+    lim, back = results.read_par(data, ng)
+    np.testing.assert_array_equal(back, genes)
+    for g in range(ng):
+        mx, mn, de, b, nbin, mp = lim[g]
+        assert (mx, mn, de, mp) == (d.gene_max[g], d.gene_min[g], d.gene_del[g], d.gene_map[g])
+        assert b == 1.0 / nbin
+    # set_bins by hand: a dihedral gene of -180..180 by 10 has 36 bins; the grid gene of 1..N-1
+    # by 1, mapped, has N - 2 + 1
+    assert results.set_bins(-180.0, 180.0, 10.0, 0) == (1.0 / 36.0, 36.0)
+    assert results.set_bins(1.0, 1000.0, 1.0, 1) == (1.0 / 1000.0, 1000.0)
+    # a fractional count gets one more bin added, not rounded: 360 / 7 + 1
+    assert results.set_bins(-180.0, 180.0, 7.0, 0)[1] == 360.0 / 7.0 + 1.0
+    assert data[5:5 + 48] == struct.pack("<5di4x", *lim[0])
+
+
+# ---------------------------------------------------------------------------------------------
+# GPU: fxe_cluster through the C ABI
+# ---------------------------------------------------------------------------------------------
+
+def assert_same(g, r, R):
+    nc = r["n_clusters"]
+    assert g["n_clusters"] == nc
+    for k in ("top", "freq", "member_of"):
+        np.testing.assert_array_equal(g[k], r[k], err_msg=k)
+    np.testing.assert_array_equal(g["rmsd"].view(np.int32), r["rmsd"].view(np.int32))
+    for k in ("tcf", "acf"):
+        scale = np.maximum(1.0, np.abs(r[k]))
+        assert (np.abs(g[k] - r[k]) / scale).max() <= 1e-12, k
+    np.testing.assert_array_equal(g["top_rmsd"][:nc, :nc], r["top_rmsd"][:nc, :nc])
+
+
+@pytest.mark.gpu
+def test_gpu_cluster_golden(fixture):
+    from flexaidds_gb300 import evaluator
+    d, ic, e, cases, cads = fixture
+    ev = evaluator.GPUEvaluator(d, max_poses=64)
+    for (T, thr, R), cad in zip(cases, cads):
+        g = ev.cluster(ic, e, T, thr, R)
+        assert results.cad_text(g) == cad, (T, thr, R)
+        assert_same(g, oracle_cluster(d, ic, e, T, thr, R), R)
+    ev.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("T,thr,R", [(0, 2.0, 10), (300, 2.0, 10), (0, 1.5, 300), (298, 2.5, 64)])
+def test_gpu_cluster_large(small_system, T, thr, R):
+    from flexaidds_gb300 import evaluator
+    _, d = small_system
+    ic, e = synth.clustered_ensemble(d, 150, 120, seed=91, spread=3)
+    ev = evaluator.GPUEvaluator(d, max_poses=64)
+    g = ev.cluster(ic, e, T, thr, R)
+    r = oracle_cluster(d, ic, e, T, thr, R)
+    assert r["n_clusters"] == min(R, r["n_clusters"]) and r["freq"].sum() > R
+    assert_same(g, r, R)
+    assert ev.cluster_time() > 0.0
+    ev.close()
+
+
+@pytest.mark.gpu
+def test_gpu_cluster_with_side_chains():
+    """Rotamer genes select side chains only; the ligand's coordinates, and so the clusters, do not
+    depend on them."""
+    from flexaidds_gb300 import evaluator, prepare, system
+    d = prepare.prepare(system.make_inputs(2000, 8.0, 24, 6, seed=43, side_chains=3))
+    ic, e = synth.clustered_ensemble(d, 40, 50, seed=92)
+    ev = evaluator.GPUEvaluator(d, max_poses=64)
+    g = ev.cluster(ic, e, 300, 2.0, 20)
+    assert_same(g, oracle_cluster(d, ic, e, 300, 2.0, 20), 20)
+    ic2 = ic.copy()
+    rot = np.nonzero(d.gene_typ == 4)[0]
+    ic2[:, rot] = d.gene_max[rot]
+    g2 = ev.cluster(ic2, e, 300, 2.0, 20)
+    for k in ("top", "freq", "member_of", "rmsd", "acf"):
+        np.testing.assert_array_equal(g2[k], g[k])
+    ev.close()
+
+
+@pytest.mark.gpu
+def test_gpu_cluster_edges(small_system):
+    from flexaidds_gb300 import evaluator
+    _, d = small_system
+    ic, e = synth.clustered_ensemble(d, 5, 20, seed=93)
+    ev = evaluator.GPUEvaluator(d, max_poses=64)
+    one = ev.cluster(ic[:1], e[:1], 0, 2.0, 10)
+    assert one["n_clusters"] == 1 and one["top"][0] == 0 and one["freq"][0] == 1
+    assert one["member_of"][0] == 0 and one["acf"][0] == e[0]
+    for T, thr, R in [(0, 0.0, 1), (0, 1e9, 5), (300, 1e9, 4), (0, 0.0, 1000)]:
+        assert_same(ev.cluster(ic, e, T, thr, R), oracle_cluster(d, ic, e, T, thr, R), R)
+    # an IC outside its gene limits, a zero partition function, bad arguments
+    bad = ic.copy()
+    bad[3, 1] = d.gene_max[1] + 1.0
+    with pytest.raises(evaluator.FxeError):
+        ev.cluster(bad, e, 0, 2.0, 10)
+    with pytest.raises(evaluator.FxeError):
+        ev.cluster(ic, np.full_like(e, 1.0e6), 1, 2.0, 10)
+    with pytest.raises(evaluator.FxeError):
+        ev.cluster(ic, e, 0, -1.0, 10)
+    with pytest.raises(evaluator.FxeError):
+        ev.cluster(ic, e, 0, 2.0, 0)
+    # the context still answers after the rejected calls
+    assert_same(ev.cluster(ic, e, 0, 2.0, 10), oracle_cluster(d, ic, e, 0, 2.0, 10), 10)
+    ev.close()
