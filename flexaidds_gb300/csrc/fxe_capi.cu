@@ -347,8 +347,8 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
         std::vector<float4> ta(rec->n_grid), td(rec->n_grid);
         for (int g = 0; g < rec->n_grid; ++g) {
             const float a = build_angle(gic[g].y), d = build_angle(gic[g].z);
-            ta[g] = make_float4(a, cosf(a), sinf(a), 0.0f);
-            td[g] = make_float4(d, cosf(d), sinf(d), 0.0f);
+            ta[g] = make_float4(a, cosf(a), sinf(a), gic[g].y);
+            td[g] = make_float4(d, cosf(d), sinf(d), gic[g].z);
         }
         FXE_TRY(ctx->upload_receptor(&S.grid_trig_a, ta.data(), rec->n_grid), "grid upload");
         FXE_TRY(ctx->upload_receptor(&S.grid_trig_d, td.data(), rec->n_grid), "grid upload");
@@ -449,10 +449,10 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
                     cnt[k] = (int)vals.size();
                     for (float a : vals) {
                         const float x = build_angle(a);
-                        tab.push_back(make_float4(x, cosf(x), sinf(x), 0.0f));
+                        tab.push_back(make_float4(x, cosf(x), sinf(x), a));
                     }
                 }
-            if (tab.empty()) tab.push_back(make_float4(0.0f, 1.0f, 0.0f, 0.0f));
+            if (tab.empty()) tab.push_back(make_float4(0.0f, 1.0f, 0.0f, 0.0f));   // never matched: cnt is 0
             FXE_TRY(ctx->upload(&S.trig_tab, tab.data(), tab.size()), "trig upload");
             FXE_TRY(ctx->upload(&S.trig_src, src.data(), 2 * n), "trig upload");
             FXE_TRY(ctx->upload(&S.trig_off, off.data(), 2 * n), "trig upload");
@@ -1584,6 +1584,42 @@ double host_genetoic(const fxe_context* ctx, int g, int32_t gene) {
     const double v = ctx->h_gmin[g] + ctx->h_gdel[g] * (double)(it - lo);
     return v > ctx->h_gmax[g] ? ctx->h_gmax[g] : (v < ctx->h_gmin[g] ? ctx->h_gmin[g] : v);
 }
+
+// The ensemble of a job as the reference's GA assembles it (LIB/gaboom.cpp:520-540): every
+// generation's population, sorted by energy, chromosomes within 0.1 of the last one kept on every
+// decoded gene dropped (remove_dups, :2728-2747); ties in energy in snapshot order. The kept
+// chromosomes' decoded ICs (clamped as eval_chromosome leaves them) go to *ic when set.
+fxe_status ga_ensemble(const GaSlot& s, const fxe::GaJob& J, std::vector<double>* ic, std::vector<double>* kept_e) {
+    const int P = s.job.population, ng = s.ctx->S.n_genes, G = s.job.generations;
+    const size_t N = (size_t)G * P;
+    std::vector<int32_t> sg(N * ng);
+    std::vector<double> se(N);
+    if (N) {
+        FXE_TRY(cudaMemcpy(sg.data(), J.snap, sizeof(int32_t) * N * ng, cudaMemcpyDeviceToHost), "GA snapshots");
+        FXE_TRY(cudaMemcpy(se.data(), J.snap_e, sizeof(double) * N, cudaMemcpyDeviceToHost), "GA snapshots");
+    }
+    std::vector<size_t> ord(N);
+    for (size_t i = 0; i < N; ++i) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return se[a] < se[b]; });
+    std::vector<double> last(ng), cur(ng);
+    bool have = false;
+    kept_e->clear();
+    if (ic) ic->clear();
+    for (size_t i : ord) {
+        for (int g = 0; g < ng; ++g) cur[g] = host_genetoic(s.ctx, g, sg[i * ng + g]);
+        int same = 0;
+        if (have)
+            for (int g = 0; g < ng; ++g) same += std::fabs(cur[g] - last[g]) < 0.1;
+        if (!have || same != ng) {
+            kept_e->push_back(se[i]);
+            if (ic) ic->insert(ic->end(), cur.begin(), cur.end());
+            last = cur;
+            have = true;
+        }
+    }
+    return FXE_OK;
+}
+
 }  // namespace
 
 extern "C" fxe_status fxe_ga_collect(fxe_ga* e, int32_t slot, double temperature, int32_t* best_genes,
@@ -1600,42 +1636,39 @@ extern "C" fxe_status fxe_ga_collect(fxe_ga* e, int32_t slot, double temperature
     if (best_genes) FXE_TRY(cudaMemcpy(best_genes, J.pop, sizeof(int32_t) * ng, cudaMemcpyDeviceToHost), "GA result");
     if (best_energy) FXE_TRY(cudaMemcpy(best_energy, J.pop_e, sizeof(double), cudaMemcpyDeviceToHost), "GA result");
     if (thermo || n_ensemble) {
-        // the ensemble of the reference's GA (LIB/gaboom.cpp:520-540): every generation's
-        // population, sorted by energy, chromosomes within 0.1 of the last one kept on every
-        // decoded gene dropped (remove_dups, :2728-2747); ties in energy in snapshot order
-        const int G = s.job.generations;
-        const size_t N = (size_t)G * P;
-        std::vector<int32_t> sg(N * ng);
-        std::vector<double> se(N);
-        if (N) {
-            FXE_TRY(cudaMemcpy(sg.data(), J.snap, sizeof(int32_t) * N * ng, cudaMemcpyDeviceToHost), "GA snapshots");
-            FXE_TRY(cudaMemcpy(se.data(), J.snap_e, sizeof(double) * N, cudaMemcpyDeviceToHost), "GA snapshots");
-        }
-        std::vector<size_t> ord(N);
-        for (size_t i = 0; i < N; ++i) ord[i] = i;
-        std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return se[a] < se[b]; });
-        std::vector<double> kept_e, last(ng), cur(ng);
-        bool have = false;
-        for (size_t i : ord) {
-            for (int g = 0; g < ng; ++g) cur[g] = host_genetoic(s.ctx, g, sg[i * ng + g]);
-            int same = 0;
-            if (have)
-                for (int g = 0; g < ng; ++g) same += std::fabs(cur[g] - last[g]) < 0.1;
-            if (!have || same != ng) {
-                kept_e.push_back(se[i]);
-                last = cur;
-                have = true;
-            }
-        }
+        std::vector<double> kept_e;
+        fxe_status st = ga_ensemble(s, J, nullptr, &kept_e);
+        if (st != FXE_OK) return st;
         if (n_ensemble) *n_ensemble = (int64_t)kept_e.size();
         if (thermo) {
             if (kept_e.empty()) return fail(FXE_ERR_INVALID_ARGS, "the job ran no generation: empty ensemble");
-            fxe_status st = thermo_host(kept_e.data(), nullptr, (int64_t)kept_e.size(), temperature, thermo, nullptr);
+            st = thermo_host(kept_e.data(), nullptr, (int64_t)kept_e.size(), temperature, thermo, nullptr);
             if (st != FXE_OK) return st;
         }
     }
     for (void* p : s.mem) cudaFree(p);
     s = GaSlot();
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_ga_ensemble(fxe_ga* e, int32_t slot, int64_t cap, double* ic, double* energies,
+                                      int64_t* n) {
+    g_err.clear();
+    if (!e || !n || slot < 0 || slot >= e->max_jobs || !e->slots[slot].used || !e->slots[slot].finished)
+        return fail(FXE_ERR_INVALID_ARGS, "slot does not hold a finished job");
+    GaSlot& s = e->slots[slot];
+    if (cudaSetDevice(e->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
+    FXE_TRY(cudaStreamSynchronize(e->stream), "GA step");
+    fxe::GaJob J;
+    FXE_TRY(cudaMemcpy(&J, e->d_all + slot, sizeof(J), cudaMemcpyDeviceToHost), "GA state");
+    std::vector<double> kic, ke;
+    fxe_status st = ga_ensemble(s, J, ic ? &kic : nullptr, &ke);
+    if (st != FXE_OK) return st;
+    *n = (int64_t)ke.size();
+    if (!ic && !energies) return FXE_OK;
+    if (cap < *n) return fail(FXE_ERR_CAPACITY, "the ensemble holds more chromosomes than cap");
+    if (ic) std::copy(kic.begin(), kic.end(), ic);
+    if (energies) std::copy(ke.begin(), ke.end(), energies);
     return FXE_OK;
 }
 

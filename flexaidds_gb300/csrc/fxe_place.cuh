@@ -21,10 +21,14 @@ struct BuildShared {
     int bad;
 };
 
-// cos and sin of a build angle: the C library's values tabulated by the host for the angles the
-// genes produce (so that coordinates match the reference built on the same host bit for bit),
-// else the correctly rounded values.
-__device__ __forceinline__ void build_trig(const DevSystem& S, const BuildShared& sh, int l, int c, float x,
+// cos and sin of the build angle x = (float)(deg * PI / 180) that buildcc forms from an IC in
+// degrees (LIB/buildcc.cpp:80-100). The host tabulates, for the values the genes (or the grid, or
+// the base ICs) give each atom, the degrees, x and the C library's cosf/sinf of x, so that
+// coordinates match the reference built on the same host bit for bit. A table entry whose degrees
+// equal deg gives the pair with no double-precision arithmetic at all; otherwise x is formed in
+// double precision as buildcc forms it and the entry is used if its x equals x; else the
+// correctly rounded values.
+__device__ __forceinline__ void build_trig(const DevSystem& S, const BuildShared& sh, int l, int c, float deg,
                                            float* cs, float* sn) {
     const int k = 2 * l + c, src = S.trig_src[k];
     float4 e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -41,6 +45,12 @@ __device__ __forceinline__ void build_trig(const DevSystem& S, const BuildShared
             have = true;
         }
     }
+    if (have && __float_as_int(e.w) == __float_as_int(deg)) {
+        *cs = e.y;
+        *sn = e.z;
+        return;
+    }
+    const float x = (float)(deg * kPi / 180.0f);
     if (have && __float_as_int(e.x) == __float_as_int(x)) {
         *cs = e.y;
         *sn = e.z;
@@ -171,16 +181,14 @@ __device__ __forceinline__ void place_ligand(const DevSystem& S, BuildShared& sh
         a = cx * cx;
         b = cy * cy;
         c = cz * cz;
-        const float angPI = (float)(sh.ic[l][1] * kPi / 180.0f);
         float ct, st;
-        build_trig(S, sh, l, 0, angPI, &ct, &st);
+        build_trig(S, sh, l, 0, sh.ic[l][1], &ct, &st);
         st = -st;
         op = 1.0f - ct;
         const float xk = (cx * cz * op - cy * st) * zn + ((1.0f - a) * ct + a) * xn + (cx * cy * op + cz * st) * yn;
         const float yk = (cy * cx * op - cz * st) * xn + ((1.0f - b) * ct + b) * yn + (cy * cz * op + cx * st) * zn;
         const float zk = (cz * cy * op - cx * st) * yn + ((1.0f - c) * ct + c) * zn + (cz * cx * op + cy * st) * xn;
-        const float dihPI = (float)(sh.ic[l][2] * kPi / 180.0f);
-        build_trig(S, sh, l, 1, dihPI, &ct, &st);
+        build_trig(S, sh, l, 1, sh.ic[l][2], &ct, &st);
         op = 1.0f - ct;
         cx = (x[2] - x[1]) * d;
         cy = (y[2] - y[1]) * d;

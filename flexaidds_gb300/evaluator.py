@@ -65,6 +65,7 @@ def load_library():
         lib.fxe_ga_collect.argtypes = [vp, C.c_int32, C.c_double, _i, C.POINTER(C.c_double), vp,
                                        C.POINTER(C.c_int64)]
         lib.fxe_ga_population.argtypes = [vp, C.c_int32, _i, _d]
+        lib.fxe_ga_ensemble.argtypes = [vp, C.c_int32, C.c_int64, _d, _d, C.POINTER(C.c_int64)]
         lib.fxe_ga_take_launches.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         lib.fxe_ga_duplicates.argtypes = [vp, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         lib.fxe_ga_destroy.argtypes = [vp]
@@ -324,6 +325,18 @@ class GAEngine:
         e = np.zeros(population, np.float64)
         _check(self.lib.fxe_ga_population(self.handle, slot, ptr(g, _i), ptr(e, _d)))
         return g, e
+
+    def ensemble(self, slot: int):
+        """A finished job's ensemble, best first (the input of GPUEvaluator.cluster as the
+        reference's cluster() receives chrom_snapshot): (ic (n, n_genes), energies (n,)). Call
+        before collect."""
+        ng = self.jobs[slot].desc.n_genes
+        n = C.c_int64(0)
+        _check(self.lib.fxe_ga_ensemble(self.handle, slot, 0, None, None, C.byref(n)))
+        ic = np.zeros((n.value, ng), np.float64)
+        e = np.zeros(n.value, np.float64)
+        _check(self.lib.fxe_ga_ensemble(self.handle, slot, n.value, ptr(ic, _d), ptr(e, _d), C.byref(n)))
+        return ic, e
 
     def collect(self, slot: int, temperature: float = 300.0):
         ev = self.jobs.pop(slot)

@@ -376,6 +376,14 @@ fxe_status fxe_ga_finished(fxe_ga* ga, int32_t* slots, int32_t cap, int32_t* n);
  * *n_ensemble; frees the slot. */
 fxe_status fxe_ga_collect(fxe_ga* ga, int32_t slot, double temperature, int32_t* best_genes,
                           double* best_energy, fxe_thermo* thermo, int64_t* n_ensemble);
+/* A finished job's ensemble as fxe_ga_collect assembles it (best first, near-duplicates
+ * removed): *n chromosomes as decoded ICs (n * n_genes, clamped as eval_chromosome leaves them)
+ * and their energies, the input of fxe_cluster as the reference's cluster() receives
+ * chrom_snapshot (LIB/top.cpp:1351-1354). With ic and energies NULL only *n is set; else cap
+ * must be at least *n (FXE_ERR_CAPACITY otherwise). Call before fxe_ga_collect, which frees
+ * the slot. */
+fxe_status fxe_ga_ensemble(fxe_ga* ga, int32_t slot, int64_t cap, double* ic, double* energies,
+                           int64_t* n);
 /* The current population of a job (sorted by energy): P * n_genes genes and P energies. */
 fxe_status fxe_ga_population(fxe_ga* ga, int32_t slot, int32_t* genes, double* energies);
 /* Candidates a job has dropped as duplicates so far, and those taken although seen before

@@ -212,3 +212,39 @@ def test_gpu_cluster_edges(small_system):
     # the context still answers after the rejected calls
     assert_same(ev.cluster(ic, e, 0, 2.0, 10), oracle_cluster(d, ic, e, 0, 2.0, 10), 10)
     ev.close()
+
+
+@pytest.mark.gpu
+def test_gpu_cluster_of_a_ga_ensemble(small_system):
+    """A GA job's ensemble (fxe_ga_ensemble: every generation's population, sorted, near-duplicates
+    removed) clustered on the device, as the reference clusters chrom_snapshot after its GA."""
+    from flexaidds_gb300 import evaluator
+    from oracle import ga as ref_ga
+    _, d = small_system
+    P, G = 128, 4
+    ev = evaluator.GPUEvaluator(d, max_poses=P)
+    eng = evaluator.GAEngine(max_jobs=1)
+    slot = eng.admit(eng.job(ev, P, G, 4242, 0.9, 0.02), ev)
+    snaps = []
+    for _ in range(G):
+        eng.step()
+        snaps.append(eng.read_population(slot, P))
+    assert eng.finished() == [slot]
+    ic, e = eng.ensemble(slot)
+    # the restated assembly: snapshots sorted by energy (ties in snapshot order), a chromosome
+    # dropped when every decoded gene is within 0.1 of the last one kept
+    g_all = np.concatenate([s[0] for s in snaps])
+    e_all = np.concatenate([s[1] for s in snaps])
+    ic_all = ref_ga.clamped_ic(d, g_all)
+    keep, last = [], None
+    for i in np.argsort(e_all, kind="stable"):
+        if last is None or not np.all(np.abs(ic_all[i] - last) < 0.1):
+            keep.append(i)
+            last = ic_all[i]
+    np.testing.assert_array_equal(e, e_all[keep])
+    np.testing.assert_array_equal(ic, ic_all[keep])
+    _, best, th = eng.collect(slot, 300.0)
+    assert th["n_ensemble"] == len(e) and best == e[0]
+    for T in (0, 300):
+        assert_same(ev.cluster(ic, e, T, 2.0, 10), oracle_cluster(d, ic, e, T, 2.0, 10), 10)
+    ev.close()
