@@ -34,8 +34,9 @@ __device__ __forceinline__ void build_pose(const DevSystem& S, const DevWork& W,
     __syncwarp();
 
     // 2-3. IC assignment, genes in order, and buildcc over the rebuild list
-    if (lane == 0) place_ligand(S, sh, ic_row);
+    if (lane == 0) assign_ics(S, sh, ic_row);
     __syncwarp();
+    build_atoms(S, sh, lane);
 
     // 4. side-chain atoms of the selected rotamers
     const int nsc = S.n_sc, nm = nsc + nl;

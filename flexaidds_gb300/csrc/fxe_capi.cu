@@ -369,6 +369,42 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
         FXE_TRY(ctx->upload(&S.lig_ic, lic.data(), n), "ligand upload");
         S.n_build = lig->n_build;
         FXE_TRY(ctx->upload(&S.build_order, lig->build_order, lig->n_build), "ligand upload");
+        {
+            // dependency levels of the rebuild list: an atom's level is one more than its latest
+            // build reference's; references outside the list or later in it, or an atom listed
+            // twice, keep the list order
+            std::vector<int> at(n, -1), level(n, 0);
+            bool ok = true;
+            for (int i = 0; i < lig->n_build; ++i) {
+                if (at[lig->build_order[i]] >= 0) ok = false;   // an atom listed twice: list order
+                at[lig->build_order[i]] = i;
+            }
+            int top = 0;
+            for (int i = 0; i < lig->n_build && ok; ++i) {
+                const int l = lig->build_order[i];
+                int lv = 0;
+                for (int r = 0; r < 3; ++r) {
+                    const int j = lig->rec[4 * l + r];
+                    if (j < 0) continue;
+                    if (at[j] < 0 || at[j] >= i) ok = false;
+                    else lv = std::max(lv, level[j] + 1);
+                }
+                level[l] = lv;
+                top = std::max(top, lv);
+            }
+            S.n_levels = 0;
+            if (ok) {
+                std::vector<int> off(top + 2, 0), atoms;
+                for (int i = 0; i < lig->n_build; ++i) ++off[level[lig->build_order[i]] + 1];
+                for (int v = 0; v <= top; ++v) off[v + 1] += off[v];
+                atoms.resize(lig->n_build);
+                std::vector<int> fill(off.begin(), off.end() - 1);
+                for (int i = 0; i < lig->n_build; ++i) atoms[fill[level[lig->build_order[i]]]++] = lig->build_order[i];
+                S.n_levels = top + 1;
+                FXE_TRY(ctx->upload(&S.level_off, off.data(), off.size()), "ligand upload");
+                FXE_TRY(ctx->upload(&S.level_atom, atoms.data(), atoms.size()), "ligand upload");
+            }
+        }
         FXE_TRY(ctx->upload(&S.bonded, lig->bonded, (size_t)n * n), "ligand upload");
         // genes and genetoic decode tables (running bin totals, LIB/gaboom.cpp:2295-2308, 2887-2906)
         const int ng = lig->n_genes;

@@ -42,10 +42,11 @@ cluster_build_kernel(DevSystem S, int n, const double* __restrict__ ic, float* _
     reset_pose(S, sh, lane);
     __syncwarp();
     if (lane == 0) {
-        place_ligand(S, sh, ic + (size_t)p * S.n_genes);
+        assign_ics(S, sh, ic + (size_t)p * S.n_genes);
         if (sh.bad) atomicOr(bad, 1);
     }
     __syncwarp();
+    build_atoms(S, sh, lane);
     for (int k = lane; k < 3 * S.n_lig; k += 32) xyz[(size_t)k * n + p] = sh.pos[k / 3][k % 3];
 }
 

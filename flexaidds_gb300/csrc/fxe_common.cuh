@@ -75,6 +75,11 @@ struct DevSystem {
     const float4* lig_ic;        // base dis, ang, dih
     int n_build;
     const int* build_order;
+    // the rebuild list by dependency level: the atoms of one level have their build references in
+    // earlier levels only, so a warp's lanes build them at once (n_levels 0: build in list order)
+    int n_levels;
+    const int* level_off;        // [n_levels + 1] into level_atom
+    const int* level_atom;       // [n_build]
     const int8_t* bonded;        // [n_lig * n_lig]
     int n_genes;
     const int* gene_type;
@@ -85,7 +90,7 @@ struct DevSystem {
     const int* dec_off;          // [n_genes + 1] offsets into dec_tab
     const double* dec_tab;       // running bin totals per gene
     // cosf/sinf of the host's C library for every single-precision angle the pose build can
-    // meet, as (angle, cos, sin, 0): per grid point (the anchor atom's angle and dihedral), and
+    // meet, as (angle, cos, sin, the angle in degrees): per grid point (the anchor atom's angle and dihedral), and
     // per (ligand atom, angle|dihedral) over the bins of the gene that sets it last (trig_src:
     // -1 no gene, -2 the grid gene, else the gene's index; trig_off/trig_cnt locate its entries)
     const float4* grid_trig_a;   // [n_grid]

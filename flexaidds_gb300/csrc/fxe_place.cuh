@@ -95,11 +95,11 @@ __device__ __forceinline__ void decode_ics(const DevSystem& S, int p, const int3
     }
 }
 
-// Steps 2-3, by lane 0 after decode_ics and a __syncwarp: the IC assignment of ic2cf
-// (LIB/ic2cf.cpp:53-105: grid index, angle, dihedral with the rec[3] cascade, rotamer index) and
-// buildcc over the rebuild list. sh.ic must hold the ligand's base ICs; genes >= 64 are read from
-// ic_row. Sets sh.gi, sh.rot and sh.bad (1: grid index out of range).
-__device__ __forceinline__ void place_ligand(const DevSystem& S, BuildShared& sh, const double* ic_row) {
+// Step 2, by lane 0 after decode_ics and a __syncwarp: the IC assignment of ic2cf
+// (LIB/ic2cf.cpp:53-105: grid index, angle, dihedral with the rec[3] cascade, rotamer index).
+// sh.ic must hold the ligand's base ICs; genes >= 64 are read from ic_row. Sets sh.gi, sh.rot and
+// sh.bad (1: grid index out of range).
+__device__ __forceinline__ void assign_ics(const DevSystem& S, BuildShared& sh, const double* ic_row) {
     const int ng = S.n_genes, nl = S.n_lig;
     for (int g = 0; g < ng; ++g) {
         const double v = g < 64 ? sh.icv[g] : ic_row[g];
@@ -137,72 +137,90 @@ __device__ __forceinline__ void place_ligand(const DevSystem& S, BuildShared& sh
         default: break;
         }
     }
-    // buildcc over the rebuild list
+}
+
+// buildcc (LIB/buildcc.cpp:6-134) of ligand atom l from its three build references (or the
+// frame points around FA->ori), which must already be placed.
+__device__ __forceinline__ void build_atom(const DevSystem& S, BuildShared& sh, int l) {
     const float* ori = S.ori;
-    for (int an = 0; an < S.n_build; ++an) {
-        const int l = S.build_order[an];
-        const int4 r = S.lig_rec[l];
-        const int ref[3] = {r.x, r.y, r.z};
-        float x[4], y[4], z[4];
-        for (int i = 1; i <= 3; ++i) {
-            const int j = ref[i - 1];
-            if (j >= 0) {
-                x[i] = sh.pos[j][0];
-                y[i] = sh.pos[j][1];
-                z[i] = sh.pos[j][2];
-            } else if (i == 1) {
-                x[i] = 1.0f + ori[0];
-                y[i] = 0.0f + ori[1];
-                z[i] = 0.0f + ori[2];
-            } else if (i == 3) {
-                x[i] = 0.0f + ori[0];
-                y[i] = 1.0f + ori[1];
-                z[i] = 0.0f + ori[2];
-            } else {
-                x[i] = 0.0f + ori[0];
-                y[i] = 0.0f + ori[1];
-                z[i] = 0.0f + ori[2];
-            }
-            x[i] += 1e-10f;
-            y[i] += 1e-10f;
-            z[i] += 1e-10f;
+    const int4 r = S.lig_rec[l];
+    const int ref[3] = {r.x, r.y, r.z};
+    float x[4], y[4], z[4];
+    for (int i = 1; i <= 3; ++i) {
+        const int j = ref[i - 1];
+        if (j >= 0) {
+            x[i] = sh.pos[j][0];
+            y[i] = sh.pos[j][1];
+            z[i] = sh.pos[j][2];
+        } else if (i == 1) {
+            x[i] = 1.0f + ori[0];
+            y[i] = 0.0f + ori[1];
+            z[i] = 0.0f + ori[2];
+        } else if (i == 3) {
+            x[i] = 0.0f + ori[0];
+            y[i] = 1.0f + ori[1];
+            z[i] = 0.0f + ori[2];
+        } else {
+            x[i] = 0.0f + ori[0];
+            y[i] = 0.0f + ori[1];
+            z[i] = 0.0f + ori[2];
         }
-        float a = y[1] * (z[2] - z[3]) + y[2] * (z[3] - z[1]) + y[3] * (z[1] - z[2]);
-        float b = z[1] * (x[2] - x[3]) + z[2] * (x[3] - x[1]) + z[3] * (x[1] - x[2]);
-        float c = x[1] * (y[2] - y[3]) + x[2] * (y[3] - y[1]) + x[3] * (y[1] - y[2]);
-        float op = sqrtf(a * a + b * b + c * c);
-        float cx = a / op, cy = b / op, cz = c / op;
-        a = x[2] - x[1];
-        b = y[2] - y[1];
-        c = z[2] - z[1];
-        const float d = 1.0f / sqrtf(a * a + b * b + c * c);
-        op = sh.ic[l][0] * d;
-        const float xn = a * op, yn = b * op, zn = c * op;
-        a = cx * cx;
-        b = cy * cy;
-        c = cz * cz;
-        float ct, st;
-        build_trig(S, sh, l, 0, sh.ic[l][1], &ct, &st);
-        st = -st;
-        op = 1.0f - ct;
-        const float xk = (cx * cz * op - cy * st) * zn + ((1.0f - a) * ct + a) * xn + (cx * cy * op + cz * st) * yn;
-        const float yk = (cy * cx * op - cz * st) * xn + ((1.0f - b) * ct + b) * yn + (cy * cz * op + cx * st) * zn;
-        const float zk = (cz * cy * op - cx * st) * yn + ((1.0f - c) * ct + c) * zn + (cz * cx * op + cy * st) * xn;
-        build_trig(S, sh, l, 1, sh.ic[l][2], &ct, &st);
-        op = 1.0f - ct;
-        cx = (x[2] - x[1]) * d;
-        cy = (y[2] - y[1]) * d;
-        cz = (z[2] - z[1]) * d;
-        a = cx * cx;
-        b = cy * cy;
-        c = cz * cz;
-        sh.pos[l][0] = (cx * cz * op - cy * st) * zk + ((1.0f - a) * ct + a) * xk + (cx * cy * op + cz * st) * yk + x[1];
-        sh.pos[l][1] = (cy * cx * op - cz * st) * xk + ((1.0f - b) * ct + b) * yk + (cy * cz * op + cx * st) * zk + y[1];
-        sh.pos[l][2] = (cz * cy * op - cx * st) * yk + ((1.0f - c) * ct + c) * zk + (cz * cx * op + cy * st) * xk + z[1];
+        x[i] += 1e-10f;
+        y[i] += 1e-10f;
+        z[i] += 1e-10f;
+    }
+    float a = y[1] * (z[2] - z[3]) + y[2] * (z[3] - z[1]) + y[3] * (z[1] - z[2]);
+    float b = z[1] * (x[2] - x[3]) + z[2] * (x[3] - x[1]) + z[3] * (x[1] - x[2]);
+    float c = x[1] * (y[2] - y[3]) + x[2] * (y[3] - y[1]) + x[3] * (y[1] - y[2]);
+    float op = sqrtf(a * a + b * b + c * c);
+    float cx = a / op, cy = b / op, cz = c / op;
+    a = x[2] - x[1];
+    b = y[2] - y[1];
+    c = z[2] - z[1];
+    const float d = 1.0f / sqrtf(a * a + b * b + c * c);
+    op = sh.ic[l][0] * d;
+    const float xn = a * op, yn = b * op, zn = c * op;
+    a = cx * cx;
+    b = cy * cy;
+    c = cz * cz;
+    float ct, st;
+    build_trig(S, sh, l, 0, sh.ic[l][1], &ct, &st);
+    st = -st;
+    op = 1.0f - ct;
+    const float xk = (cx * cz * op - cy * st) * zn + ((1.0f - a) * ct + a) * xn + (cx * cy * op + cz * st) * yn;
+    const float yk = (cy * cx * op - cz * st) * xn + ((1.0f - b) * ct + b) * yn + (cy * cz * op + cx * st) * zn;
+    const float zk = (cz * cy * op - cx * st) * yn + ((1.0f - c) * ct + c) * zn + (cz * cx * op + cy * st) * xn;
+    build_trig(S, sh, l, 1, sh.ic[l][2], &ct, &st);
+    op = 1.0f - ct;
+    cx = (x[2] - x[1]) * d;
+    cy = (y[2] - y[1]) * d;
+    cz = (z[2] - z[1]) * d;
+    a = cx * cx;
+    b = cy * cy;
+    c = cz * cz;
+    sh.pos[l][0] = (cx * cz * op - cy * st) * zk + ((1.0f - a) * ct + a) * xk + (cx * cy * op + cz * st) * yk + x[1];
+    sh.pos[l][1] = (cy * cx * op - cz * st) * xk + ((1.0f - b) * ct + b) * yk + (cy * cz * op + cx * st) * zk + y[1];
+    sh.pos[l][2] = (cz * cy * op - cx * st) * yk + ((1.0f - c) * ct + c) * zk + (cz * cx * op + cy * st) * xk + z[1];
+}
+
+// Step 3, by every lane after assign_ics and a __syncwarp: buildcc over the rebuild list. The
+// atoms of one dependency level are built by the warp's lanes at once (each atom's arithmetic is
+// the same as in list order: its references are placed in earlier levels); without levels, lane 0
+// follows the list.
+__device__ __forceinline__ void build_atoms(const DevSystem& S, BuildShared& sh, int lane) {
+    if (S.n_levels > 0) {
+        for (int v = 0; v < S.n_levels; ++v) {
+            for (int i = S.level_off[v] + lane; i < S.level_off[v + 1]; i += 32) build_atom(S, sh, S.level_atom[i]);
+            __syncwarp();
+        }
+    } else {
+        if (lane == 0)
+            for (int an = 0; an < S.n_build; ++an) build_atom(S, sh, S.build_order[an]);
+        __syncwarp();
     }
 }
 
-// The ligand's base ICs into sh.ic and the per-pose state reset, before decode_ics/place_ligand.
+// The ligand's base ICs into sh.ic and the per-pose state reset, before assign_ics.
 __device__ __forceinline__ void reset_pose(const DevSystem& S, BuildShared& sh, int lane) {
     for (int l = lane; l < S.n_lig; l += 32) {
         const float4 b = S.lig_ic[l];
