@@ -19,12 +19,12 @@
 
 namespace fxe {
 
-constexpr int kClusterBuildWarps = 8;   // 8 chromosomes per block: 32-byte runs of each coordinate
+constexpr int kClusterBuildWarps = 4;   // 4 chromosomes per block: 16-byte runs of each coordinate
 constexpr int kPassThreads = 256;
 
 // Ligand of chromosome p from its ICs: the IC assignment of calc_rmsd_chrom (the same as ic2cf's)
 // and buildcc, the ligand atoms in order; xyz[(3 * l + c) * n + p].
-__global__ void __launch_bounds__(kClusterBuildWarps * 32)
+__global__ void __launch_bounds__(kClusterBuildWarps * 32, 8)   // 8 blocks (32 warps) per SM
 cluster_build_kernel(DevSystem S, int n, const double* __restrict__ ic, float* __restrict__ xyz,
                      int* __restrict__ bad) {
     __shared__ BuildShared sh_all[kClusterBuildWarps];

@@ -13,6 +13,7 @@ struct BuildShared {
     float ic[kMaxLig][3];
     float pos[kMaxLig][3];
     int cell[kMaxLig];          // per mobile atom
+    float trig[kMaxLig][4];     // per ligand atom: cos, sin of its build angle, then of its dihedral
     float sc[kMaxSc][4];        // side-chain atoms: x, y, z, radius
     int rot[kMaxFlex];          // rotamer of each flexible residue
     double icv[64];
@@ -183,14 +184,13 @@ __device__ __forceinline__ void build_atom(const DevSystem& S, BuildShared& sh, 
     a = cx * cx;
     b = cy * cy;
     c = cz * cz;
-    float ct, st;
-    build_trig(S, sh, l, 0, sh.ic[l][1], &ct, &st);
-    st = -st;
+    float ct = sh.trig[l][0], st = -sh.trig[l][1];
     op = 1.0f - ct;
     const float xk = (cx * cz * op - cy * st) * zn + ((1.0f - a) * ct + a) * xn + (cx * cy * op + cz * st) * yn;
     const float yk = (cy * cx * op - cz * st) * xn + ((1.0f - b) * ct + b) * yn + (cy * cz * op + cx * st) * zn;
     const float zk = (cz * cy * op - cx * st) * yn + ((1.0f - c) * ct + c) * zn + (cz * cx * op + cy * st) * xn;
-    build_trig(S, sh, l, 1, sh.ic[l][2], &ct, &st);
+    ct = sh.trig[l][2];
+    st = sh.trig[l][3];
     op = 1.0f - ct;
     cx = (x[2] - x[1]) * d;
     cy = (y[2] - y[1]) * d;
@@ -203,11 +203,22 @@ __device__ __forceinline__ void build_atom(const DevSystem& S, BuildShared& sh, 
     sh.pos[l][2] = (cz * cy * op - cx * st) * yk + ((1.0f - c) * ct + c) * zk + (cz * cx * op + cy * st) * xk + z[1];
 }
 
-// Step 3, by every lane after assign_ics and a __syncwarp: buildcc over the rebuild list. The
-// atoms of one dependency level are built by the warp's lanes at once (each atom's arithmetic is
-// the same as in list order: its references are placed in earlier levels); without levels, lane 0
-// follows the list.
+// Step 3, by every lane after assign_ics and a __syncwarp: buildcc over the rebuild list. First
+// the cos/sin pairs of every atom's angle and dihedral, which depend on its ICs only, one atom per
+// lane; then the atoms of one dependency level are built by the warp's lanes at once (each atom's
+// arithmetic is the same as in list order: its references are placed in earlier levels); without
+// levels, lane 0 follows the list.
 __device__ __forceinline__ void build_atoms(const DevSystem& S, BuildShared& sh, int lane) {
+    for (int l = lane; l < S.n_lig; l += 32) {
+        float c, s;
+        build_trig(S, sh, l, 0, sh.ic[l][1], &c, &s);
+        sh.trig[l][0] = c;
+        sh.trig[l][1] = s;
+        build_trig(S, sh, l, 1, sh.ic[l][2], &c, &s);
+        sh.trig[l][2] = c;
+        sh.trig[l][3] = s;
+    }
+    __syncwarp();
     if (S.n_levels > 0) {
         for (int v = 0; v < S.n_levels; ++v) {
             for (int i = S.level_off[v] + lane; i < S.level_off[v + 1]; i += 32) build_atom(S, sh, S.level_atom[i]);
