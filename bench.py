@@ -404,10 +404,12 @@ CLUSTER = dict(centres=2000, per_centre=500, seed=17, rmsd=2.0, max_results=10, 
                cpu_sample=20_000)
 
 
-def run_cluster(ev, d):
+def run_cluster(ev, d, centres=None):
     """Device time of fxe_cluster's kernels (CUDA events inside the call), its end-to-end time
     (host ICs and energies in, results out), and the C restatement on a bounded sample."""
-    c = CLUSTER
+    c = dict(CLUSTER)
+    if centres:
+        c["centres"] = centres
     ic, e = synth.clustered_ensemble(d, c["centres"], c["per_centre"], seed=c["seed"])
     n = ic.shape[0]
     args = (ic, e, c["temperature"], c["rmsd"], c["max_results"])
@@ -651,7 +653,17 @@ def main():
                     help="also time the batched many-ligand workload against one launch per job")
     ap.add_argument("--cluster", type=int, default=1,
                     help="also time the clustering of a 1e6-chromosome ensemble")
+    ap.add_argument("--cluster-only", type=int, default=0, metavar="CENTRES",
+                    help="time only the clustering, of CENTRES x 500 chromosomes (a small case "
+                         "for a profiler: few launches before the clustering kernels)")
     args = ap.parse_args()
+    if args.cluster_only:
+        from flexaidds_gb300 import evaluator
+        d = make_system()
+        ev = evaluator.GPUEvaluator(d, max_poses=64)
+        print(json.dumps({"cluster": run_cluster(ev, d, centres=args.cluster_only)}), flush=True)
+        ev.close()
+        return
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     if args.impl == "reference":
