@@ -434,12 +434,15 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
         {
             // which gene sets each atom's angle and dihedral last, and through which cascade
             // (the IC assignment of ic2cf, LIB/ic2cf.cpp:53-105, replayed symbolically)
-            std::vector<int> src(2 * n, -1), pos(2 * n, 0);
+            std::vector<int> src(2 * n, -1), pos(2 * n, 0), dsrc(n, -1);
             std::vector<std::vector<int>> chain(ng);
             for (int g = 0; g < ng; ++g) {
                 const int atm = lig->gene_atom[g], t = lig->gene_type[g];
                 if (t == -1) {
                     src[2 * atm] = src[2 * atm + 1] = -2;
+                    dsrc[atm] = -2;
+                } else if (t == 0) {
+                    dsrc[atm] = g;
                 } else if (t == 1) {
                     src[2 * atm] = g;
                     pos[2 * atm] = 0;
@@ -493,6 +496,20 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
             FXE_TRY(ctx->upload(&S.trig_src, src.data(), 2 * n), "trig upload");
             FXE_TRY(ctx->upload(&S.trig_off, off.data(), 2 * n), "trig upload");
             FXE_TRY(ctx->upload(&S.trig_cnt, cnt.data(), 2 * n), "trig upload");
+            // for a build that forms each atom's ICs without replaying the assignment: the gene
+            // (or grid, -2; base, -1) that sets each distance last, and per atom whose dihedral a
+            // gene's cascade sets, the atoms whose shifts are added after the gene's value
+            std::vector<int> coff(n + 1, 0), catoms;
+            for (int l = 0; l < n; ++l) {
+                const int g = src[2 * l + 1];
+                if (g >= 0)
+                    for (int q = 1; q <= pos[2 * l + 1]; ++q) catoms.push_back(chain[g][q]);
+                coff[l + 1] = (int)catoms.size();
+            }
+            if (catoms.empty()) catoms.push_back(0);
+            FXE_TRY(ctx->upload(&S.dis_src, dsrc.data(), n), "trig upload");
+            FXE_TRY(ctx->upload(&S.cas_off, coff.data(), n + 1), "trig upload");
+            FXE_TRY(ctx->upload(&S.cas_atom, catoms.data(), catoms.size()), "trig upload");
         }
         if (!flex_gene.empty()) FXE_TRY(ctx->upload(&S.flex_gene, flex_gene.data(), flex_gene.size()), "gene upload");
         FXE_TRY(ctx->upload(&S.gene_type, lig->gene_type, ng), "gene upload");

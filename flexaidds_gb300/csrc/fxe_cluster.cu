@@ -50,6 +50,73 @@ cluster_build_kernel(DevSystem S, int n, const double* __restrict__ ic, float* _
     for (int k = lane; k < 3 * S.n_lig; k += 32) xyz[(size_t)k * n + p] = sh.pos[k / 3][k % 3];
 }
 
+// The same with one thread per chromosome, kThreadBuild chromosomes per block: a warp builds 32
+// ligands in step, so the serial chain of each atom costs one instruction stream for 32
+// chromosomes instead of one. Each thread forms its atoms' ICs without replaying the assignment:
+// the host's replay names the gene (or grid point, or base IC) that sets each distance, angle and
+// dihedral last, and the atoms whose shifts a dihedral cascade adds (dis_src, trig_src, cas_*).
+// Shared memory, per block: the placed atoms [3 * n_lig][kThreadBuild], and per gene its value as
+// a float and its bin [n_genes][kThreadBuild] each.
+constexpr int kThreadBuild = 64;
+constexpr size_t kThreadBuildMaxSmem = 200 * 1024;
+
+size_t thread_build_smem(const DevSystem& S) {
+    return sizeof(float) * kThreadBuild * (3 * (size_t)S.n_lig + 2 * (size_t)S.n_genes);
+}
+
+__global__ void __launch_bounds__(kThreadBuild)
+cluster_build_thread_kernel(DevSystem S, int n, const double* __restrict__ ic, float* __restrict__ xyz,
+                            int* __restrict__ bad) {
+    extern __shared__ __align__(16) float tsm[];
+    const int t = threadIdx.x, ng = S.n_genes, nl = S.n_lig;
+    float* pos = tsm;                                    // [(3 l + k) * kThreadBuild + t]
+    float* fv = pos + (size_t)3 * nl * kThreadBuild;     // [g * kThreadBuild + t]
+    int* gb = reinterpret_cast<int*>(fv + (size_t)ng * kThreadBuild);
+    const int p = blockIdx.x * kThreadBuild + t;
+    if (p >= n) return;   // no block-wide barrier follows
+    const double* row = ic + (size_t)p * ng;
+    int gi = -1, st = 0;
+    for (int g = 0; g < ng; ++g) {
+        const double v = row[g];
+        if (!(v >= S.gene_min[g] && v <= S.gene_max[g])) st |= 2;
+        // the bin this value would come from; a table entry is used only if its angle matches
+        const double b = (v - S.gene_min[g]) / S.gene_del[g];
+        gb[g * kThreadBuild + t] = (b >= 0.0 && b < 2147483647.0) ? (int)rint(b) : -1;
+        fv[g * kThreadBuild + t] = (float)v;
+        if (S.gene_type[g] == -1) {
+            // the grid gene (LIB/ic2cf.cpp:60-67); an index past the grid is an error and leaves
+            // the anchor's base ICs
+            const unsigned u = (unsigned)v;
+            if (u >= (unsigned)S.n_grid) st |= 1;
+            else gi = (int)u;
+        }
+    }
+    if (st) atomicOr(bad, st);
+    for (int k = 0; k < 3 * nl; ++k) pos[k * kThreadBuild + t] = 0.0f;
+    const float4 grid = gi >= 0 ? S.grid_ic[gi] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int an = 0; an < S.n_build; ++an) {
+        const int l = S.build_order[an];
+        const float4 base = S.lig_ic[l];
+        // distance, angle and dihedral as the IC assignment leaves them
+        const int sd = S.dis_src[l], sa = S.trig_src[2 * l], sx = S.trig_src[2 * l + 1];
+        const float dis = sd == -2 ? (gi >= 0 ? grid.x : base.x) : (sd >= 0 ? fv[sd * kThreadBuild + t] : base.x);
+        const float ang = sa == -2 ? (gi >= 0 ? grid.y : base.y) : (sa >= 0 ? fv[sa * kThreadBuild + t] : base.y);
+        float dih = sx == -2 ? (gi >= 0 ? grid.z : base.z) : (sx >= 0 ? fv[sx * kThreadBuild + t] : base.z);
+        if (sx >= 0)
+            for (int q = S.cas_off[l]; q < S.cas_off[l + 1]; ++q) dih = dih + S.lig_shift[S.cas_atom[q]];
+        float ca, sn_a, cd, sn_d;
+        trig_of(S, l, 0, gi, sa >= 0 ? gb[sa * kThreadBuild + t] : -1, ang, &ca, &sn_a);
+        trig_of(S, l, 1, gi, sx >= 0 ? gb[sx * kThreadBuild + t] : -1, dih, &cd, &sn_d);
+        float x[4], y[4], z[4], out[3];
+        buildcc_refs(S, S.lig_rec[l], [&](int j, int k) { return pos[(3 * j + k) * kThreadBuild + t]; }, x, y, z);
+        buildcc_place(x, y, z, dis, ca, sn_a, cd, sn_d, out);
+        pos[(3 * l) * kThreadBuild + t] = out[0];
+        pos[(3 * l + 1) * kThreadBuild + t] = out[1];
+        pos[(3 * l + 2) * kThreadBuild + t] = out[2];
+    }
+    for (int k = 0; k < 3 * nl; ++k) xyz[(size_t)k * n + p] = pos[k * kThreadBuild + t];
+}
+
 // Partition function of the clustering step: sum of exp(-beta * app_evalue)
 // (LIB/cluster.cpp:68-80), one partial per block.
 __global__ void __launch_bounds__(kPassThreads)
@@ -233,8 +300,18 @@ int cluster_blocks(int n) {
 
 void launch_cluster(const DevSystem& S, const ClusterWork& C, cudaStream_t st) {
     const int n = C.n, nl = S.n_lig, nb = cluster_blocks(n);
-    cluster_build_kernel<<<(n + kClusterBuildWarps - 1) / kClusterBuildWarps, kClusterBuildWarps * 32, 0, st>>>(
-        S, n, C.ic, C.xyz, C.status);
+    // one thread per chromosome when its shared memory fits (ligands up to about 200 atoms),
+    // else one warp per chromosome
+    const size_t tsmem = thread_build_smem(S);
+    if (tsmem <= kThreadBuildMaxSmem &&
+        cudaFuncSetAttribute(cluster_build_thread_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tsmem) == cudaSuccess) {
+        cluster_build_thread_kernel<<<(n + kThreadBuild - 1) / kThreadBuild, kThreadBuild, tsmem, st>>>(
+            S, n, C.ic, C.xyz, C.status);
+    } else {
+        cluster_build_kernel<<<(n + kClusterBuildWarps - 1) / kClusterBuildWarps, kClusterBuildWarps * 32, 0,
+                               st>>>(S, n, C.ic, C.xyz, C.status);
+    }
     if (C.temperature > 0) cluster_z_kernel<<<nb, kPassThreads, 0, st>>>(n, C.e, C.beta, C.part_z);
     for (int c = 0; c < C.max_results; ++c)
         cluster_pass_kernel<<<nb, kPassThreads, 0, st>>>(n, nl, c, C.xyz, C.thr, C.exit_sum, C.e, C.temperature,

@@ -99,6 +99,11 @@ struct DevSystem {
     const int* trig_src;         // [n_lig * 2]
     const int* trig_off;         // [n_lig * 2]
     const int* trig_cnt;         // [n_lig * 2]
+    // the same replay for the distances (dis_src: -1 base, -2 grid, else the gene), and for each
+    // dihedral a gene's cascade sets, the atoms whose shifts follow the gene's value in it
+    const int* dis_src;          // [n_lig]
+    const int* cas_off;          // [n_lig + 1] into cas_atom
+    const int* cas_atom;
     // flexible side chains. Their non-backbone atoms ("side-chain atoms") are scored: with the
     // ligand atoms they form the pose's mobile atoms, side-chain atoms first (Calc order), then
     // the ligand (mobile index n_sc + l). Mobile atoms are re-placed every pose; the other

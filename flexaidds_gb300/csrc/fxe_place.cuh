@@ -28,19 +28,20 @@ struct BuildShared {
 // coordinates match the reference built on the same host bit for bit. A table entry whose degrees
 // equal deg gives the pair with no double-precision arithmetic at all; otherwise x is formed in
 // double precision as buildcc forms it and the entry is used if its x equals x; else the
-// correctly rounded values.
-__device__ __forceinline__ void build_trig(const DevSystem& S, const BuildShared& sh, int l, int c, float deg,
-                                           float* cs, float* sn) {
+// correctly rounded values. gi is the pose's grid point, bin the bin of the gene that sets the
+// angle (-1: none known).
+__device__ __forceinline__ void trig_of(const DevSystem& S, int l, int c, int gi, int bin, float deg, float* cs,
+                                        float* sn) {
     const int k = 2 * l + c, src = S.trig_src[k];
     float4 e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     bool have = false;
     if (src == -2) {
-        if ((unsigned)sh.gi < (unsigned)S.n_grid) {
-            e = c == 0 ? S.grid_trig_a[sh.gi] : S.grid_trig_d[sh.gi];
+        if ((unsigned)gi < (unsigned)S.n_grid) {
+            e = c == 0 ? S.grid_trig_a[gi] : S.grid_trig_d[gi];
             have = true;
         }
     } else {
-        const int idx = src < 0 ? 0 : (src < 64 ? sh.gbin[src] : -1);
+        const int idx = src < 0 ? 0 : bin;
         if (idx >= 0 && idx < S.trig_cnt[k]) {
             e = S.trig_tab[S.trig_off[k] + idx];
             have = true;
@@ -59,6 +60,13 @@ __device__ __forceinline__ void build_trig(const DevSystem& S, const BuildShared
         *cs = (float)cos((double)x);
         *sn = (float)sin((double)x);
     }
+}
+
+// The same for a warp's pose: its grid point and gene bins from the pose's shared state.
+__device__ __forceinline__ void build_trig(const DevSystem& S, const BuildShared& sh, int l, int c, float deg,
+                                           float* cs, float* sn) {
+    const int src = S.trig_src[2 * l + c];
+    trig_of(S, l, c, sh.gi, (src >= 0 && src < 64) ? sh.gbin[src] : -1, deg, cs, sn);
 }
 
 // Step 1: genes -> ICs (genetoic, LIB/gaboom.cpp:2887-2906, as a binary search in the running bin
@@ -140,19 +148,20 @@ __device__ __forceinline__ void assign_ics(const DevSystem& S, BuildShared& sh, 
     }
 }
 
-// buildcc (LIB/buildcc.cpp:6-134) of ligand atom l from its three build references (or the
-// frame points around FA->ori), which must already be placed.
-__device__ __forceinline__ void build_atom(const DevSystem& S, BuildShared& sh, int l) {
+// The reference points of buildcc (LIB/buildcc.cpp:20-60) for an atom with build references ref:
+// the placed reference atoms (pos_of(j, k)) or, for a missing one, the frame points around
+// FA->ori; each offset by 1e-10f.
+template <typename PosOf>
+__device__ __forceinline__ void buildcc_refs(const DevSystem& S, const int4& r, PosOf pos_of, float x[4], float y[4],
+                                             float z[4]) {
     const float* ori = S.ori;
-    const int4 r = S.lig_rec[l];
     const int ref[3] = {r.x, r.y, r.z};
-    float x[4], y[4], z[4];
     for (int i = 1; i <= 3; ++i) {
         const int j = ref[i - 1];
         if (j >= 0) {
-            x[i] = sh.pos[j][0];
-            y[i] = sh.pos[j][1];
-            z[i] = sh.pos[j][2];
+            x[i] = pos_of(j, 0);
+            y[i] = pos_of(j, 1);
+            z[i] = pos_of(j, 2);
         } else if (i == 1) {
             x[i] = 1.0f + ori[0];
             y[i] = 0.0f + ori[1];
@@ -170,6 +179,13 @@ __device__ __forceinline__ void build_atom(const DevSystem& S, BuildShared& sh, 
         y[i] += 1e-10f;
         z[i] += 1e-10f;
     }
+}
+
+// buildcc's placement of one atom (LIB/buildcc.cpp:60-130) from its reference points, its
+// distance and the cos/sin of its angle (ca, sa) and dihedral (cd, sd), single precision in the
+// reference's order of operations.
+__device__ __forceinline__ void buildcc_place(const float x[4], const float y[4], const float z[4], float dis,
+                                              float ca, float sa, float cd, float sd, float out[3]) {
     float a = y[1] * (z[2] - z[3]) + y[2] * (z[3] - z[1]) + y[3] * (z[1] - z[2]);
     float b = z[1] * (x[2] - x[3]) + z[2] * (x[3] - x[1]) + z[3] * (x[1] - x[2]);
     float c = x[1] * (y[2] - y[3]) + x[2] * (y[3] - y[1]) + x[3] * (y[1] - y[2]);
@@ -179,18 +195,18 @@ __device__ __forceinline__ void build_atom(const DevSystem& S, BuildShared& sh, 
     b = y[2] - y[1];
     c = z[2] - z[1];
     const float d = 1.0f / sqrtf(a * a + b * b + c * c);
-    op = sh.ic[l][0] * d;
+    op = dis * d;
     const float xn = a * op, yn = b * op, zn = c * op;
     a = cx * cx;
     b = cy * cy;
     c = cz * cz;
-    float ct = sh.trig[l][0], st = -sh.trig[l][1];
+    float ct = ca, st = -sa;
     op = 1.0f - ct;
     const float xk = (cx * cz * op - cy * st) * zn + ((1.0f - a) * ct + a) * xn + (cx * cy * op + cz * st) * yn;
     const float yk = (cy * cx * op - cz * st) * xn + ((1.0f - b) * ct + b) * yn + (cy * cz * op + cx * st) * zn;
     const float zk = (cz * cy * op - cx * st) * yn + ((1.0f - c) * ct + c) * zn + (cz * cx * op + cy * st) * xn;
-    ct = sh.trig[l][2];
-    st = sh.trig[l][3];
+    ct = cd;
+    st = sd;
     op = 1.0f - ct;
     cx = (x[2] - x[1]) * d;
     cy = (y[2] - y[1]) * d;
@@ -198,9 +214,20 @@ __device__ __forceinline__ void build_atom(const DevSystem& S, BuildShared& sh, 
     a = cx * cx;
     b = cy * cy;
     c = cz * cz;
-    sh.pos[l][0] = (cx * cz * op - cy * st) * zk + ((1.0f - a) * ct + a) * xk + (cx * cy * op + cz * st) * yk + x[1];
-    sh.pos[l][1] = (cy * cx * op - cz * st) * xk + ((1.0f - b) * ct + b) * yk + (cy * cz * op + cx * st) * zk + y[1];
-    sh.pos[l][2] = (cz * cy * op - cx * st) * yk + ((1.0f - c) * ct + c) * zk + (cz * cx * op + cy * st) * xk + z[1];
+    out[0] = (cx * cz * op - cy * st) * zk + ((1.0f - a) * ct + a) * xk + (cx * cy * op + cz * st) * yk + x[1];
+    out[1] = (cy * cx * op - cz * st) * xk + ((1.0f - b) * ct + b) * yk + (cy * cz * op + cx * st) * zk + y[1];
+    out[2] = (cz * cy * op - cx * st) * yk + ((1.0f - c) * ct + c) * zk + (cz * cx * op + cy * st) * xk + z[1];
+}
+
+// buildcc (LIB/buildcc.cpp:6-134) of ligand atom l from its three build references (or the
+// frame points around FA->ori), which must already be placed.
+__device__ __forceinline__ void build_atom(const DevSystem& S, BuildShared& sh, int l) {
+    float x[4], y[4], z[4], out[3];
+    buildcc_refs(S, S.lig_rec[l], [&](int j, int k) { return sh.pos[j][k]; }, x, y, z);
+    buildcc_place(x, y, z, sh.ic[l][0], sh.trig[l][0], sh.trig[l][1], sh.trig[l][2], sh.trig[l][3], out);
+    sh.pos[l][0] = out[0];
+    sh.pos[l][1] = out[1];
+    sh.pos[l][2] = out[2];
 }
 
 // Step 3, by every lane after assign_ics and a __syncwarp: buildcc over the rebuild list. First
