@@ -517,6 +517,15 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
         FXE_TRY(ctx->upload(&S.gene_min, lig->gene_min, ng), "gene upload");
         FXE_TRY(ctx->upload(&S.gene_max, lig->gene_max, ng), "gene upload");
         FXE_TRY(ctx->upload(&S.gene_del, lig->gene_del, ng), "gene upload");
+        {
+            std::vector<float> fmin(ng), fidel(ng);
+            for (int g = 0; g < ng; ++g) {
+                fmin[g] = (float)lig->gene_min[g];
+                fidel[g] = (float)(1.0 / lig->gene_del[g]);
+            }
+            FXE_TRY(ctx->upload(&S.gene_minf, fmin.data(), ng), "gene upload");
+            FXE_TRY(ctx->upload(&S.gene_idelf, fidel.data(), ng), "gene upload");
+        }
         FXE_TRY(ctx->upload(&S.dec_off, doff.data(), ng + 1), "gene upload");
         FXE_TRY(ctx->upload(&S.dec_tab, dtab.data(), dtab.size()), "gene upload");
         // energy matrix

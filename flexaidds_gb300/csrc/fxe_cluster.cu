@@ -79,10 +79,12 @@ cluster_build_thread_kernel(DevSystem S, int n, const double* __restrict__ ic, f
     for (int g = 0; g < ng; ++g) {
         const double v = row[g];
         if (!(v >= S.gene_min[g] && v <= S.gene_max[g])) st |= 2;
-        // the bin this value would come from; a table entry is used only if its angle matches
-        const double b = (v - S.gene_min[g]) / S.gene_del[g];
-        gb[g * kThreadBuild + t] = (b >= 0.0 && b < 2147483647.0) ? (int)rint(b) : -1;
-        fv[g * kThreadBuild + t] = (float)v;
+        // a guess, in single precision, of the bin this value comes from; a table entry is used
+        // only if its angle matches, and a miss retries with the bin formed in double precision
+        const float f = (float)v;
+        const float b = (f - S.gene_minf[g]) * S.gene_idelf[g];
+        gb[g * kThreadBuild + t] = (b >= 0.0f && b < 2.0e9f) ? (int)rintf(b) : -1;
+        fv[g * kThreadBuild + t] = f;
         if (S.gene_type[g] == -1) {
             // the grid gene (LIB/ic2cf.cpp:60-67); an index past the grid is an error and leaves
             // the anchor's base ICs
@@ -105,8 +107,17 @@ cluster_build_thread_kernel(DevSystem S, int n, const double* __restrict__ ic, f
         if (sx >= 0)
             for (int q = S.cas_off[l]; q < S.cas_off[l + 1]; ++q) dih = dih + S.lig_shift[S.cas_atom[q]];
         float ca, sn_a, cd, sn_d;
-        trig_of(S, l, 0, gi, sa >= 0 ? gb[sa * kThreadBuild + t] : -1, ang, &ca, &sn_a);
-        trig_of(S, l, 1, gi, sx >= 0 ? gb[sx * kThreadBuild + t] : -1, dih, &cd, &sn_d);
+        auto trig = [&](int c, int src, float deg, float* cs, float* sn) {
+            if (trig_table(S, l, c, gi, src >= 0 ? gb[src * kThreadBuild + t] : -1, deg, cs, sn)) return;
+            if (src >= 0) {
+                const double b = (row[src] - S.gene_min[src]) / S.gene_del[src];
+                const int exact = (b >= 0.0 && b < 2147483647.0) ? (int)rint(b) : -1;
+                if (exact != gb[src * kThreadBuild + t] && trig_table(S, l, c, gi, exact, deg, cs, sn)) return;
+            }
+            trig_exact(deg, cs, sn);
+        };
+        trig(0, sa, ang, &ca, &sn_a);
+        trig(1, sx, dih, &cd, &sn_d);
         float x[4], y[4], z[4], out[3];
         buildcc_refs(S, S.lig_rec[l], [&](int j, int k) { return pos[(3 * j + k) * kThreadBuild + t]; }, x, y, z);
         buildcc_place(x, y, z, dis, ca, sn_a, cd, sn_d, out);

@@ -87,6 +87,8 @@ struct DevSystem {
     const double* gene_min;
     const double* gene_max;
     const double* gene_del;
+    const float* gene_minf;      // gene_min and 1 / gene_del in single precision (bin guesses)
+    const float* gene_idelf;
     const int* dec_off;          // [n_genes + 1] offsets into dec_tab
     const double* dec_tab;       // running bin totals per gene
     // cosf/sinf of the host's C library for every single-precision angle the pose build can

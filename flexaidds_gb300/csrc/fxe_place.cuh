@@ -29,9 +29,9 @@ struct BuildShared {
 // equal deg gives the pair with no double-precision arithmetic at all; otherwise x is formed in
 // double precision as buildcc forms it and the entry is used if its x equals x; else the
 // correctly rounded values. gi is the pose's grid point, bin the bin of the gene that sets the
-// angle (-1: none known).
-__device__ __forceinline__ void trig_of(const DevSystem& S, int l, int c, int gi, int bin, float deg, float* cs,
-                                        float* sn) {
+// angle (-1: none known); trig_table answers whether a table entry gave the pair.
+__device__ __forceinline__ bool trig_table(const DevSystem& S, int l, int c, int gi, int bin, float deg, float* cs,
+                                           float* sn) {
     const int k = 2 * l + c, src = S.trig_src[k];
     float4 e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     bool have = false;
@@ -47,19 +47,25 @@ __device__ __forceinline__ void trig_of(const DevSystem& S, int l, int c, int gi
             have = true;
         }
     }
-    if (have && __float_as_int(e.w) == __float_as_int(deg)) {
+    if (!have) return false;
+    if (__float_as_int(e.w) == __float_as_int(deg) || __float_as_int(e.x) == __float_as_int((float)(deg * kPi / 180.0f))) {
         *cs = e.y;
         *sn = e.z;
-        return;
+        return true;
     }
+    return false;
+}
+
+// Correctly rounded cos and sin of the build angle, for angles no table entry holds.
+__device__ __forceinline__ void trig_exact(float deg, float* cs, float* sn) {
     const float x = (float)(deg * kPi / 180.0f);
-    if (have && __float_as_int(e.x) == __float_as_int(x)) {
-        *cs = e.y;
-        *sn = e.z;
-    } else {
-        *cs = (float)cos((double)x);
-        *sn = (float)sin((double)x);
-    }
+    *cs = (float)cos((double)x);
+    *sn = (float)sin((double)x);
+}
+
+__device__ __forceinline__ void trig_of(const DevSystem& S, int l, int c, int gi, int bin, float deg, float* cs,
+                                        float* sn) {
+    if (!trig_table(S, l, c, gi, bin, deg, cs, sn)) trig_exact(deg, cs, sn);
 }
 
 // The same for a warp's pose: its grid point and gene bins from the pose's shared state.
