@@ -30,7 +30,7 @@ void launch_poses(const DevSystem&, const DevWork&, int, int*, cudaStream_t);
 cudaError_t configure_voronoi();
 }
 int cluster_blocks(int);
-void launch_cluster(const DevSystem&, const ClusterWork&, cudaStream_t);
+cudaError_t launch_cluster(const DevSystem&, const ClusterWork&, cudaStream_t);
 int thermo_blocks(long, int);
 void launch_thermo_partial(const double*, const int32_t*, long, double, LsePart*, int, cudaStream_t);
 void launch_thermo_weights(const double*, const int32_t*, long, double, double, double*, int, cudaStream_t);
@@ -929,6 +929,9 @@ extern "C" fxe_status fxe_cluster(fxe_context* ctx, int64_t n, const double* ic,
     if (n < 1 || n > FXE_CLUSTER_MAX_N) return fail(FXE_ERR_INVALID_ARGS, "n out of range");
     if (temperature < 0 || !(rmsd_threshold >= 0.0f) || max_results < 1 || max_results > FXE_CLUSTER_MAX_RESULTS)
         return fail(FXE_ERR_INVALID_ARGS, "temperature < 0, rmsd_threshold < 0 or max_results out of range");
+    if (ctx->S.n_genes > FXE_CLUSTER_MAX_GENES)
+        return fail(FXE_ERR_INVALID_ARGS, "clustering takes ligands of at most " +
+                                              std::to_string(FXE_CLUSTER_MAX_GENES) + " genes");
     if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
     const int N = (int)n, R = max_results, ng = ctx->S.n_genes, nl = ctx->S.n_lig;
     const int nb = fxe::cluster_blocks(N);
@@ -990,8 +993,7 @@ extern "C" fxe_status fxe_cluster(fxe_context* ctx, int64_t n, const double* ic,
     FXE_TRY(cudaMemsetAsync(C.rmsd, 0, sizeof(float) * N, st), "cluster rmsd");
     FXE_TRY(cudaMemsetAsync(C.status, 0, sizeof(int), st), "cluster status");
     FXE_TRY(cudaEventRecord(ev[0], st), "cluster events");
-    fxe::launch_cluster(ctx->S, C, st);
-    FXE_TRY(cudaGetLastError(), "cluster launch");
+    FXE_TRY(fxe::launch_cluster(ctx->S, C, st), "cluster launch");
     FXE_TRY(cudaEventRecord(ev[1], st), "cluster events");
     ctx->launches += 2 + (temperature > 0 ? 1 : 0) + R;
     std::vector<int> h_top(R), h_freq(R);

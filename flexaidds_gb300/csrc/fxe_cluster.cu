@@ -8,7 +8,7 @@
 // every later unclustered chromosome whose ligand RMSD to it is at most FA->cluster_rmsd
 // (LIB/cluster.cpp:116-175), until every chromosome is clustered or max_results clusters exist.
 //
-// Here: one kernel builds every ligand (the pose build's placement code), stored by coordinate
+// Here: one kernel builds every ligand (the pose build's placement arithmetic), stored by coordinate
 // (x of atom 0 for all chromosomes, then y, ...) so that each pass reads whole sectors; one
 // launch per cluster compares the unclustered chromosomes with the head and leaves the next
 // head (the first chromosome it did not take) for the next launch, so the passes run back to back
@@ -19,46 +19,18 @@
 
 namespace fxe {
 
-constexpr int kClusterBuildWarps = 4;   // 4 chromosomes per block: 16-byte runs of each coordinate
-constexpr int kPassThreads = 256;
-
-// Ligand of chromosome p from its ICs: the IC assignment of calc_rmsd_chrom (the same as ic2cf's)
-// and buildcc, the ligand atoms in order; xyz[(3 * l + c) * n + p].
-__global__ void __launch_bounds__(kClusterBuildWarps * 32, 8)   // 8 blocks (32 warps) per SM
-cluster_build_kernel(DevSystem S, int n, const double* __restrict__ ic, float* __restrict__ xyz,
-                     int* __restrict__ bad) {
-    __shared__ BuildShared sh_all[kClusterBuildWarps];
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int p = blockIdx.x * kClusterBuildWarps + wib;
-    if (p >= n) return;
-    BuildShared& sh = sh_all[wib];
-    // calc_rmsd_chrom uses to_ic as stored, without eval_chromosome's clamp (the host admits
-    // only ICs within their gene limits, so the two agree)
-    decode_ics(S, p, nullptr, ic, false, nullptr, sh, lane);
-    for (int g = lane; g < S.n_genes; g += 32) {
-        const double v = ic[(size_t)p * S.n_genes + g];
-        if (!(v >= S.gene_min[g] && v <= S.gene_max[g])) atomicOr(bad, 2);
-    }
-    reset_pose(S, sh, lane);
-    __syncwarp();
-    if (lane == 0) {
-        assign_ics(S, sh, ic + (size_t)p * S.n_genes);
-        if (sh.bad) atomicOr(bad, 1);
-    }
-    __syncwarp();
-    build_atoms(S, sh, lane);
-    for (int k = lane; k < 3 * S.n_lig; k += 32) xyz[(size_t)k * n + p] = sh.pos[k / 3][k % 3];
-}
-
-// The same with one thread per chromosome, kThreadBuild chromosomes per block: a warp builds 32
-// ligands in step, so the serial chain of each atom costs one instruction stream for 32
-// chromosomes instead of one. Each thread forms its atoms' ICs without replaying the assignment:
+// Ligand of each chromosome from its ICs, one thread per chromosome and kThreadBuild chromosomes
+// per block: the IC assignment of calc_rmsd_chrom (the same as ic2cf's) and buildcc, the ligand
+// atoms in order, stored as xyz[(3 * l + c) * n + p]. A warp builds 32 ligands in step, so the
+// serial chain of each atom costs one instruction stream for 32 chromosomes. calc_rmsd_chrom uses
+// to_ic as stored, without eval_chromosome's clamp (the host admits only ICs within their gene
+// limits, so the two agree). Each thread forms its atoms' ICs without replaying the assignment:
 // the host's replay names the gene (or grid point, or base IC) that sets each distance, angle and
 // dihedral last, and the atoms whose shifts a dihedral cascade adds (dis_src, trig_src, cas_*).
 // Shared memory, per block: the placed atoms [3 * n_lig][kThreadBuild], and per gene its value as
 // a float and its bin [n_genes][kThreadBuild] each.
 constexpr int kThreadBuild = 64;
-constexpr size_t kThreadBuildMaxSmem = 200 * 1024;
+constexpr int kPassThreads = 256;
 
 size_t thread_build_smem(const DevSystem& S) {
     return sizeof(float) * kThreadBuild * (3 * (size_t)S.n_lig + 2 * (size_t)S.n_genes);
@@ -309,20 +281,15 @@ int cluster_blocks(int n) {
     return want < 4 * 152 ? (want < 1 ? 1 : want) : 4 * 152;
 }
 
-void launch_cluster(const DevSystem& S, const ClusterWork& C, cudaStream_t st) {
+cudaError_t launch_cluster(const DevSystem& S, const ClusterWork& C, cudaStream_t st) {
     const int n = C.n, nl = S.n_lig, nb = cluster_blocks(n);
-    // one thread per chromosome when its shared memory fits (ligands up to about 200 atoms),
-    // else one warp per chromosome
+    // at most 128 atoms and 100 genes (checked by the caller): 146 KB for 64 chromosomes
     const size_t tsmem = thread_build_smem(S);
-    if (tsmem <= kThreadBuildMaxSmem &&
-        cudaFuncSetAttribute(cluster_build_thread_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)tsmem) == cudaSuccess) {
-        cluster_build_thread_kernel<<<(n + kThreadBuild - 1) / kThreadBuild, kThreadBuild, tsmem, st>>>(
-            S, n, C.ic, C.xyz, C.status);
-    } else {
-        cluster_build_kernel<<<(n + kClusterBuildWarps - 1) / kClusterBuildWarps, kClusterBuildWarps * 32, 0,
-                               st>>>(S, n, C.ic, C.xyz, C.status);
-    }
+    cudaError_t e = cudaFuncSetAttribute(cluster_build_thread_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)tsmem);
+    if (e != cudaSuccess) return e;
+    cluster_build_thread_kernel<<<(n + kThreadBuild - 1) / kThreadBuild, kThreadBuild, tsmem, st>>>(S, n, C.ic,
+                                                                                                  C.xyz, C.status);
     if (C.temperature > 0) cluster_z_kernel<<<nb, kPassThreads, 0, st>>>(n, C.e, C.beta, C.part_z);
     for (int c = 0; c < C.max_results; ++c)
         cluster_pass_kernel<<<nb, kPassThreads, 0, st>>>(n, nl, c, C.xyz, C.thr, C.exit_sum, C.e, C.temperature,
@@ -331,6 +298,7 @@ void launch_cluster(const DevSystem& S, const ClusterWork& C, cudaStream_t st) {
     cluster_finish_kernel<<<1, kPassThreads, 0, st>>>(n, nl, C.max_results, nb, C.xyz, C.e, C.temperature, C.beta,
                                                       C.part_z, nb, C.next, C.part_acf, C.part_cnt, C.top, C.freq,
                                                       C.tcf, C.acf, C.head_rmsd, C.z);
+    return cudaGetLastError();
 }
 
 }  // namespace fxe

@@ -269,6 +269,7 @@ fxe_status fxe_thermo_weights(const double* energies, const int32_t* multiplicit
  * there, LIB/cluster.cpp:83-88). */
 #define FXE_CLUSTER_MAX_N ((int64_t)1 << 30)
 #define FXE_CLUSTER_MAX_RESULTS 1024
+#define FXE_CLUSTER_MAX_GENES 100   /* the reference's MAX_NUM_GENES (LIB/gaboom.h:33) */
 fxe_status fxe_cluster(fxe_context* ctx, int64_t n, const double* ic, const double* app_evalue,
                        int32_t temperature, float rmsd_threshold, int32_t max_results, int32_t* top,
                        int32_t* freq, double* tcf, double* acf, int32_t* member_of, float* rmsd,
