@@ -90,3 +90,60 @@ def read_par(data: bytes, n_genes: int):
     off += 5
     genes = np.frombuffer(data[off:], dtype="<i4").reshape(-1, n_genes).astype(np.int32)
     return lim, genes
+
+
+# ------------------------------------------------------------------------------------------
+# Pose PDB files (write_pdb, LIB/write_pdb.cpp:91-170)
+# ------------------------------------------------------------------------------------------
+
+def element_of(atom_type: int) -> str:
+    """The two-character element write_pdb prints for an atom type (get_element,
+    LIB/write_pdb.cpp:218-300: the FlexAID type ranges of C, N, O and S, then one type per
+    element; other types print blank)."""
+    t = int(atom_type)
+    for lo, hi, sym in ((1, 5, " C"), (6, 12, " N"), (13, 16, " O"), (17, 21, " S")):
+        if lo <= t <= hi:
+            return sym
+    single = {22: " P", 23: " F", 24: "Cl", 25: "Br", 26: " I", 27: "Se", 28: "Mg", 29: "Sr", 30: "Cu",
+              31: "Mn", 32: "Hg", 33: "Cd", 34: "Ni", 35: "Zn", 36: "Ca", 37: "Fe", 38: "Co", 39: "Du"}
+    return single.get(t, "  ")
+
+
+class PdbAtom:
+    """One atom's record fields as the reference's atoms/residue arrays hold them: serial number,
+    atom name (the PDB's four columns, spaces kept), residue name, chain, residue number,
+    HETATM (ligand residue) or ATOM, FlexAID type."""
+    __slots__ = ("number", "name", "resname", "chain", "resnum", "hetatm", "type")
+
+    def __init__(self, number, name, resname, chain, resnum, hetatm, atom_type):
+        self.number, self.name, self.resname = int(number), str(name), str(resname)
+        self.chain, self.resnum, self.hetatm, self.type = str(chain), int(resnum), bool(hetatm), int(atom_type)
+
+
+def pdb_atom_line(a: PdbAtom, xyz) -> str:
+    """One coordinate record in write_pdb's format (LIB/write_pdb.cpp:130-141)."""
+    return "%s%5d %s %s %c%4d    %8.3f%8.3f%8.3f  1.00  0.00          %2s  \n" % (
+        "HETATM" if a.hetatm else "ATOM  ", a.number, a.name, a.resname, a.chain, a.resnum,
+        float(xyz[0]), float(xyz[1]), float(xyz[2]), element_of(a.type))
+
+
+def pose_pdb_text(remark: str, atoms, xyz, ligand_bonds=None, ligand_atoms=None) -> str:
+    """A pose file laid out as write_pdb writes it: the generator line, the caller's remark
+    block, one record per atom (receptor residues, with the rotamer each flexible side chain
+    takes, then the ligand: coordinates in xyz, float32 as the reference keeps them), the CONECT
+    records of the ligand atoms (ligand_atoms: their indices in atoms; ligand_bonds: per ligand
+    atom the indices in atoms of its bonded atoms, in the order the reference stores them) and
+    END. The reference's optional block of per-type contribution remarks (write_contributions)
+    is not written."""
+    out = ["REMARK coordinate file generated by FlexAID\n", remark + "\n"]
+    xyz = np.asarray(xyz, np.float32)
+    for k, a in enumerate(atoms):
+        out.append(pdb_atom_line(a, xyz[k]))
+    if ligand_atoms is not None:
+        for k, j in enumerate(ligand_atoms):
+            line = "CONECT%5d" % atoms[j].number
+            for b in (ligand_bonds[k] if ligand_bonds is not None else []):
+                line += "%5d" % atoms[b].number
+            out.append(line + "\n")
+    out.append("END\n")
+    return "".join(out)

@@ -10,7 +10,8 @@ For each system it writes ``tests/golden/cluster_<name>.npz`` holding the descri
 the reference's own set-up (cleft grid cut to its first points so the fixture stays small), a
 seeded ensemble with structure to cluster (``synth.clustered_ensemble``: chromosomes a few bins
 around random centres, sorted by energy), and, for each clustering case (temperature,
-cluster_rmsd, max_results), the text of the .cad file the reference's cluster() wrote.
+cluster_rmsd, max_results), the text of the .cad file the reference's cluster() wrote, and for the
+first case the PDB file of its first result (write_pdb) with the ligand's bond list.
 """
 import os
 import sys
@@ -47,10 +48,15 @@ def make(name):
     ic, e = synth.clustered_ensemble(d, centres, per, seed=seed + 7)
     arrs = d.to_arrays("d_")
     arrs.update(ic=ic, app_evalue=e, cases=np.asarray(CASES, np.float64))
+    arrs["lig_bonds"] = np.asarray(inp.ligand.bonds, np.int32).reshape(-1, 2)
     with tempfile.TemporaryDirectory() as tmp:
         for k, (T, thr, R) in enumerate(CASES):
             txt = h.cluster(ic, e, int(T), float(thr), int(R), os.path.join(tmp, f"case{k}"))
             arrs[f"cad_{k}"] = np.frombuffer(txt.encode(), np.uint8)
+            if k == 0:
+                # the pose file of the first result (write_pdb after ic2cf of its head)
+                with open(os.path.join(tmp, "case0_0.pdb"), "rb") as f:
+                    arrs["pdb_0"] = np.frombuffer(f.read(), np.uint8)
     path = os.path.join(OUT, f"cluster_{name}.npz")
     np.savez_compressed(path, **arrs)
     print(f"{path}: {ic.shape[0]} chromosomes, {len(CASES)} cases, {os.path.getsize(path) / 1024:.0f} KB")

@@ -248,3 +248,89 @@ def test_gpu_cluster_of_a_ga_ensemble(small_system):
     for T in (0, 300):
         assert_same(ev.cluster(ic, e, T, 2.0, 10), oracle_cluster(d, ic, e, T, 2.0, 10), 10)
     ev.close()
+
+
+# ---------------------------------------------------------------------------------------------
+# Pose PDB files: the records of the reference's first result file (write_pdb after ic2cf of
+# the head of cluster 0), rebuilt with the naming the pinning harness gives its atoms
+# ---------------------------------------------------------------------------------------------
+
+def harness_records(d, lig_bonds):
+    """The atoms as the harness names them: receptor atom k (1-based) numbered k in residue "REC"
+    of chain A, one residue per atom except the flexible side chains ("FLX", one residue each);
+    ligand atoms 90001.. in residue "LIG" 1; names empty. Returns (receptor records of the
+    rigid residues with their receptor indices, ligand records, ligand bond lists)."""
+    first = {int(f): int(n) for f, n in zip(getattr(d, "flex_first", []), getattr(d, "flex_natm", []))}
+    rec, nres, k = [], 0, 0
+    while k < d.rec_type.shape[0]:
+        nres += 1
+        if k in first:
+            k += first[k]
+            continue
+        rec.append((k, results.PdbAtom(k + 1, "", "REC", "A", nres, False, d.rec_type[k])))
+        k += 1
+    lig = [results.PdbAtom(90001 + i, "", "LIG", " ", 1, True, d.lig_type[i]) for i in range(d.n_lig)]
+    adj = [[] for _ in range(d.n_lig)]
+    for a, b in lig_bonds:
+        adj[a].append(b)
+        adj[b].append(a)
+    return rec, lig, adj
+
+
+def records_of(text):
+    keep = []
+    for line in text.splitlines():
+        if line.startswith("HETATM") or line.startswith("CONECT") or line == "END":
+            keep.append(line)
+        elif line.startswith("ATOM  ") and line[17:20] == "REC":
+            keep.append(line)
+    return keep
+
+
+def pose_text(d, z, lig_xyz):
+    rec, lig, adj = harness_records(d, z["lig_bonds"])
+    atoms = [a for _, a in rec] + lig
+    xyz = np.concatenate([np.asarray(d.rec_xyz, np.float32).reshape(-1, 3)[[k for k, _ in rec]],
+                          np.asarray(lig_xyz, np.float32).reshape(-1, 3)])
+    nr = len(rec)
+    return results.pose_pdb_text("REMARK optimized structure", atoms, xyz,
+                                 ligand_bonds=[[nr + b for b in adj[i]] for i in range(d.n_lig)],
+                                 ligand_atoms=list(range(nr, nr + d.n_lig)))
+
+
+@pytest.mark.parametrize("name", CLUSTER_FIXTURES)
+def test_pose_pdb_against_reference(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    d, ic, e, cases, _ = load(name)
+    T, thr, R = cases[0]
+    top0 = int(oracle_cluster(d, ic, e, T, thr, R)["top"][0])
+    xyz = port.Oracle(d).build_ic(ic[top0:top0 + 1])[0]
+    ref = records_of(bytes(z["pdb_0"]).decode())
+    mine = records_of(pose_text(d, z, xyz))
+    assert len(ref) > d.n_lig * 2
+    assert mine == ref
+
+
+def test_element_table():
+    """get_element's ranges (LIB/write_pdb.cpp:218-300)."""
+    assert [results.element_of(t) for t in (1, 5, 6, 12, 13, 16, 17, 21)] == \
+        [" C", " C", " N", " N", " O", " O", " S", " S"]
+    assert results.element_of(24) == "Cl" and results.element_of(39) == "Du"
+    assert results.element_of(40) == "  " and results.element_of(0) == "  "
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CLUSTER_FIXTURES)
+def test_gpu_pose_pdb_against_reference(name):
+    """The head of the first cluster, built by the device (fxe_eval_ic), written as a pose file:
+    its records equal the reference's."""
+    from flexaidds_gb300 import evaluator
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    d, ic, e, cases, _ = load(name)
+    T, thr, R = cases[0]
+    ev = evaluator.GPUEvaluator(d, max_poses=64)
+    top0 = int(ev.cluster(ic, e, T, thr, R)["top"][0])
+    ev.eval_ic(ic[top0:top0 + 1])
+    mine = records_of(pose_text(d, z, ev.ligand_xyz(0)))
+    assert mine == records_of(bytes(z["pdb_0"]).decode())
+    ev.close()
