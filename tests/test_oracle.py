@@ -232,3 +232,23 @@ def test_genes_decode_matches_fixture(golden):
     name, d, g = golden
     np.testing.assert_array_equal(port.Oracle(d).genes_to_ic(g["genes"]), g["ic"])
     np.testing.assert_array_equal(d.genes_to_ic(g["genes"]), g["ic"])
+
+
+def test_build_only_matches_reference_coordinates(golden):
+    """fxo_build_ic (the clustering's coordinate cache, calc_rmsd_chrom's build) gives the
+    ligand coordinates the reference's ic2cf left for every scored and every clashed pose of the
+    fixture (the ICs clamped first, as eval_chromosome leaves them). After a polyhedron failure
+    the reference's coordinates carry the random displacement of its 200-edge abort, so those
+    poses are left out."""
+    name, d, g = golden
+    ic = np.clip(g["ic"], d.gene_min, d.gene_max)
+    port.set_trig_rounding(False)
+    xyz = port.Oracle(d).build_ic(ic)
+    keep = g["status"] != 1
+    assert keep.sum() >= 50
+    if platform.machine() in ("x86_64", "AMD64"):   # the fixtures were made with this C library
+        np.testing.assert_array_equal(xyz[keep], g["xyz"][keep])
+    else:
+        np.testing.assert_allclose(xyz[keep], g["xyz"][keep], atol=1e-4)
+    # and the same as the scoring restatement's build for every pose
+    np.testing.assert_array_equal(xyz, port.Oracle(d).eval_ic(ic, want_xyz=True)["xyz"])
