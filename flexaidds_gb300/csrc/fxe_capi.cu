@@ -1696,7 +1696,7 @@ extern "C" fxe_status fxe_ga_collect(fxe_ga* e, int32_t slot, double temperature
     FXE_TRY(cudaStreamSynchronize(e->stream), "GA step");
     fxe::GaJob J;
     FXE_TRY(cudaMemcpy(&J, e->d_all + slot, sizeof(J), cudaMemcpyDeviceToHost), "GA state");
-    const int P = s.job.population, ng = s.ctx->S.n_genes;
+    const int ng = s.ctx->S.n_genes;
     if (best_genes) FXE_TRY(cudaMemcpy(best_genes, J.pop, sizeof(int32_t) * ng, cudaMemcpyDeviceToHost), "GA result");
     if (best_energy) FXE_TRY(cudaMemcpy(best_energy, J.pop_e, sizeof(double), cudaMemcpyDeviceToHost), "GA result");
     if (thermo || n_ensemble) {
