@@ -11,6 +11,11 @@ clash about 99 times in 100 on this system and cost far less).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision reference|fast]
   python bench.py --impl reference ...   the same workload on the host cores (CPU restatement)
+  python bench.py --cluster-only C       only the clustering of C x 500 chromosomes (profiling)
+
+Beside the headline, the JSON line carries the statmech reduction of 1e6 energies, the batched
+many-ligand workload, the served Poisson streams and the clustering of a 1e6-chromosome ensemble
+(each leg can be switched off: --batched 0, --served 0, --cluster 0).
 
 Several GPUs run independent replicas (the path has no exchange step); value counts all ranks.
 """
