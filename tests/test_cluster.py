@@ -334,3 +334,18 @@ def test_gpu_pose_pdb_against_reference(name):
     mine = records_of(pose_text(d, z, ev.ligand_xyz(0)))
     assert mine == records_of(bytes(z["pdb_0"]).decode())
     ev.close()
+
+
+def test_clustered_ensemble_generator(tiny_system):
+    """The seeded stand-in ensemble: sorted by energy, every IC on a bin and within its limits,
+    rotamer genes untouched, the same for the same seed."""
+    _, d = tiny_system
+    ic, e = synth.clustered_ensemble(d, 7, 11, seed=3)
+    assert ic.shape == (77, d.n_genes) and e.shape == (77,)
+    assert np.all(np.diff(e) >= 0)
+    assert np.all(ic >= d.gene_min) and np.all(ic <= d.gene_max)
+    k = (ic - d.gene_min) / d.gene_del
+    np.testing.assert_array_equal(ic, d.gene_min + d.gene_del * np.rint(k))
+    ic2, e2 = synth.clustered_ensemble(d, 7, 11, seed=3)
+    np.testing.assert_array_equal(ic, ic2)
+    np.testing.assert_array_equal(e, e2)
