@@ -349,3 +349,19 @@ def test_clustered_ensemble_generator(tiny_system):
     ic2, e2 = synth.clustered_ensemble(d, 7, 11, seed=3)
     np.testing.assert_array_equal(ic, ic2)
     np.testing.assert_array_equal(e, e2)
+
+
+def test_result_file_edges(tiny_system):
+    _, d = tiny_system
+    assert results.cad_text({"n_clusters": 0, "top": [], "freq": [], "tcf": [], "acf": [], "top_rmsd": []}) == ""
+    with pytest.raises(ValueError):
+        results.read_par(b"chrom" + bytes(10), d.n_genes)
+    data = results.par_bytes(d, np.zeros((0, d.n_genes), np.int32))
+    lim, genes = results.read_par(data, d.n_genes)
+    assert len(lim) == d.n_genes and genes.shape == (0, d.n_genes)
+    with pytest.raises(ValueError):
+        results.par_bytes(d, np.zeros((3, d.n_genes + 1), np.int32))
+    text = results.pose_pdb_text("REMARK x", [results.PdbAtom(1, " CA ", "ALA", "A", 7, False, 2)],
+                                 [[1.0, -2.0, 3.5]])
+    assert text == ("REMARK coordinate file generated by FlexAID\nREMARK x\n"
+                    "ATOM      1  CA  ALA A   7       1.000  -2.000   3.500  1.00  0.00           C  \nEND\n")
