@@ -22,12 +22,20 @@ void launch_build(const DevSystem&, const DevWork&, int, const int32_t*, const d
 void launch_contacts(const DevSystem&, const DevWork&, int, cudaStream_t);
 void launch_order_poses(const DevSystem&, const DevWork&, int, cudaStream_t);
 namespace f32 {
-void launch_poses(const DevSystem&, const DevWork&, int, int*, cudaStream_t);
+void launch_poses(const DevSystem&, const DevWork&, int, int*, uint8_t*, size_t, cudaStream_t);
 cudaError_t configure_voronoi();
+size_t pose_hist_bytes();
 }
 namespace f64 {
-void launch_poses(const DevSystem&, const DevWork&, int, int*, cudaStream_t);
+void launch_poses(const DevSystem&, const DevWork&, int, int*, uint8_t*, size_t, cudaStream_t);
 cudaError_t configure_voronoi();
+size_t pose_hist_bytes();
+}
+// Face history of a polyhedron launch, large enough for either precision's launch: the warps the
+// device holds at once, kHistStride bytes each (configure_voronoi first).
+inline size_t pose_hist_bytes() {
+    const size_t a = f32::pose_hist_bytes(), b = f64::pose_hist_bytes();
+    return a > b ? a : b;
 }
 int cluster_blocks(int);
 cudaError_t launch_cluster(const DevSystem&, const ClusterWork&, cudaStream_t);
@@ -81,6 +89,9 @@ struct fxe_context {
     int last_n = 0;
     int counters[4] = {0, 0, 0, 0};
     int precision = FXE_PRECISION_REFERENCE;
+    int face_order = FXE_FACE_ORDER_REFERENCE;
+    uint8_t* d_hist = nullptr;        // face history of the polyhedron launch
+    size_t hist_bytes = 0;
     // per-stage timing (fxe_context_enable_timing) and the count of kernels launched
     bool timing = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -562,6 +573,8 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
         FXE_TRY(ctx->alloc(&W.pose_order, P), "workspace");
         FXE_TRY(ctx->alloc(&ctx->d_genes, P * (ng > 0 ? ng : 1)), "staging");
         FXE_TRY(ctx->alloc(&ctx->d_icin, P * (ng > 0 ? ng : 1)), "staging");
+        ctx->hist_bytes = fxe::pose_hist_bytes();
+        FXE_TRY(ctx->alloc(&ctx->d_hist, ctx->hist_bytes), "face history");
         FXE_TRY(cudaDeviceSynchronize(), "context set-up");
         return FXE_OK;
     }();
@@ -606,8 +619,10 @@ fxe_status run_chunk(fxe_context* ctx, int nb, const int32_t* d_genes, const dou
     fxe::launch_contacts(ctx->S, ctx->W, nb, s);
     if (t) cudaEventRecord(ctx->ev[2], s);
     fxe::launch_order_poses(ctx->S, ctx->W, nb, s);
-    if (ctx->precision == FXE_PRECISION_FAST) fxe::f32::launch_poses(ctx->S, ctx->W, nb, ctx->W.counters + 4, s);
-    else fxe::f64::launch_poses(ctx->S, ctx->W, nb, ctx->W.counters + 4, s);
+    uint8_t* hist = ctx->face_order == FXE_FACE_ORDER_REFERENCE ? ctx->d_hist : nullptr;
+    if (ctx->precision == FXE_PRECISION_FAST)
+        fxe::f32::launch_poses(ctx->S, ctx->W, nb, ctx->W.counters + 4, hist, ctx->hist_bytes, s);
+    else fxe::f64::launch_poses(ctx->S, ctx->W, nb, ctx->W.counters + 4, hist, ctx->hist_bytes, s);
     if (t) cudaEventRecord(ctx->ev[3], s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
@@ -758,6 +773,14 @@ extern "C" fxe_status fxe_context_set_precision(fxe_context* ctx, int32_t precis
     if (!ctx || (precision != FXE_PRECISION_REFERENCE && precision != FXE_PRECISION_FAST))
         return fail(FXE_ERR_INVALID_ARGS, "invalid precision mode");
     ctx->precision = precision;
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_context_set_face_order(fxe_context* ctx, int32_t mode) {
+    g_err.clear();
+    if (!ctx || (mode != FXE_FACE_ORDER_REFERENCE && mode != FXE_FACE_ORDER_GEOMETRIC))
+        return fail(FXE_ERR_INVALID_ARGS, "invalid face order mode");
+    ctx->face_order = mode;
     return FXE_OK;
 }
 
@@ -1101,10 +1124,10 @@ void launch_build_jobs(const Job*, int, int, cudaStream_t);
 void launch_contacts_jobs(const Job*, int, long long, cudaStream_t);
 void launch_order_poses_jobs(const Job*, int, int, int*, cudaStream_t);
 namespace f32 {
-void launch_poses_jobs(const Job*, int, int, int*, const int*, cudaStream_t);
+void launch_poses_jobs(const Job*, int, int, int*, const int*, uint8_t*, size_t, cudaStream_t);
 }
 namespace f64 {
-void launch_poses_jobs(const Job*, int, int, int*, const int*, cudaStream_t);
+void launch_poses_jobs(const Job*, int, int, int*, const int*, uint8_t*, size_t, cudaStream_t);
 }
 }  // namespace fxe
 
@@ -1123,9 +1146,12 @@ struct fxe_batch {
     fxe_cf* h_out = nullptr;               // pinned
     int* d_next = nullptr;                 // pose queue of the polyhedron launch
     int* d_order = nullptr;                // [max_poses] its order, costliest first
+    uint8_t* d_hist = nullptr;             // face history of the polyhedron launch
+    size_t hist_bytes = 0;
     int64_t launches = 0;
     ~fxe_batch() {
         if (staged) cudaEventDestroy(staged);
+        if (d_hist) cudaFree(d_hist);
         if (d_next) cudaFree(d_next);
         if (d_order) cudaFree(d_order);
         if (d_jobs) cudaFree(d_jobs);
@@ -1156,6 +1182,10 @@ extern "C" fxe_status fxe_batch_create(int32_t max_jobs, int64_t max_poses, int3
         FXE_TRY(cudaMalloc(&b->d_jobs, sizeof(fxe::Job) * max_jobs), "batch job table");
         FXE_TRY(cudaMalloc(&b->d_next, sizeof(int)), "batch pose queue");
         FXE_TRY(cudaMalloc(&b->d_order, sizeof(int) * max_poses), "batch pose queue");
+        FXE_TRY(fxe::f32::configure_voronoi(), "cudaFuncSetAttribute");
+        FXE_TRY(fxe::f64::configure_voronoi(), "cudaFuncSetAttribute");
+        b->hist_bytes = fxe::pose_hist_bytes();
+        FXE_TRY(cudaMalloc(&b->d_hist, b->hist_bytes + 16), "face history");
         FXE_TRY(cudaMallocHost(&b->h_jobs, sizeof(fxe::Job) * max_jobs), "batch job table");
         FXE_TRY(cudaMalloc(&b->d_genes, sizeof(int32_t) * max_poses * max_genes), "batch staging");
         FXE_TRY(cudaMallocHost(&b->h_genes, sizeof(int32_t) * max_poses * max_genes), "batch staging");
@@ -1180,7 +1210,7 @@ namespace {
 // genes_of / out_of give each job's device chromosomes and records.
 template <typename G, typename O>
 fxe_status batch_launch(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, cudaStream_t s, G genes_of, O out_of) {
-    int prec = -1, total = 0;
+    int prec = -1, order = FXE_FACE_ORDER_REFERENCE, total = 0;
     long long items = 0;
     FXE_TRY(cudaEventSynchronize(b->staged), "batch staging");
     int k = 0;
@@ -1199,6 +1229,7 @@ fxe_status batch_launch(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, cudaS
         items += (long long)jobs[i].n * (ctx->S.n_sc + ctx->S.n_lig);
         ctx->last_n = jobs[i].n;
         prec = ctx->precision;
+        order = ctx->face_order;
     }
     if (k == 0) return FXE_OK;
     FXE_TRY(cudaMemcpyAsync(b->d_jobs, b->h_jobs, sizeof(fxe::Job) * k, cudaMemcpyHostToDevice, s), "job table");
@@ -1206,8 +1237,10 @@ fxe_status batch_launch(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, cudaS
     fxe::launch_build_jobs(b->d_jobs, k, total, s);
     fxe::launch_contacts_jobs(b->d_jobs, k, items, s);
     fxe::launch_order_poses_jobs(b->d_jobs, k, total, b->d_order, s);
-    if (prec == FXE_PRECISION_FAST) fxe::f32::launch_poses_jobs(b->d_jobs, k, total, b->d_next, b->d_order, s);
-    else fxe::f64::launch_poses_jobs(b->d_jobs, k, total, b->d_next, b->d_order, s);
+    uint8_t* hist = order == FXE_FACE_ORDER_REFERENCE ? b->d_hist : nullptr;
+    if (prec == FXE_PRECISION_FAST)
+        fxe::f32::launch_poses_jobs(b->d_jobs, k, total, b->d_next, b->d_order, hist, b->hist_bytes, s);
+    else fxe::f64::launch_poses_jobs(b->d_jobs, k, total, b->d_next, b->d_order, hist, b->hist_bytes, s);
     FXE_TRY(cudaGetLastError(), "batched kernel launch");
     b->launches += 4;
     return FXE_OK;
@@ -1326,6 +1359,8 @@ struct fxe_ga {
     int* d_next = nullptr;              // pose queue of the polyhedron launch
     int* d_order = nullptr;             // its order, costliest first
     int order_cap = 0;
+    uint8_t* d_hist = nullptr;          // face history of the polyhedron launch
+    size_t hist_bytes = 0;
     std::vector<int> run;               // running slots of the captured graph
     cudaGraphExec_t exec = nullptr;
     bool dirty = true;
@@ -1341,6 +1376,7 @@ struct fxe_ga {
         if (d_eval) cudaFree(d_eval);
         if (d_next) cudaFree(d_next);
         if (d_order) cudaFree(d_order);
+        if (d_hist) cudaFree(d_hist);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -1364,6 +1400,10 @@ extern "C" fxe_status fxe_ga_create(int32_t max_jobs, int32_t precision, fxe_ga*
         FXE_TRY(cudaMalloc(&e->d_run, sizeof(int) * max_jobs), "GA state");
         FXE_TRY(cudaMalloc(&e->d_eval, sizeof(fxe::Job) * max_jobs), "GA state");
         FXE_TRY(cudaMalloc(&e->d_next, sizeof(int)), "GA state");
+        FXE_TRY(fxe::f32::configure_voronoi(), "cudaFuncSetAttribute");
+        FXE_TRY(fxe::f64::configure_voronoi(), "cudaFuncSetAttribute");
+        e->hist_bytes = fxe::pose_hist_bytes();
+        FXE_TRY(cudaMalloc(&e->d_hist, e->hist_bytes + 16), "face history");
         std::vector<int> ids(max_jobs);
         for (int i = 0; i < max_jobs; ++i) ids[i] = i;
         FXE_TRY(cudaMemcpy(e->d_ids, ids.data(), sizeof(int) * max_jobs, cudaMemcpyHostToDevice), "GA state");
@@ -1598,8 +1638,13 @@ extern "C" fxe_status fxe_ga_step(fxe_ga* e) {
         fxe::launch_build_jobs(e->d_eval, n, total, e->stream);
         fxe::launch_contacts_jobs(e->d_eval, n, items, e->stream);
         fxe::launch_order_poses_jobs(e->d_eval, n, total, e->d_order, e->stream);
-        if (e->precision == FXE_PRECISION_FAST) fxe::f32::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->d_order, e->stream);
-        else fxe::f64::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->d_order, e->stream);
+        // the GA engine keeps the reference's face order unless a running job's context asks otherwise
+        bool ref_order = true;
+        for (int sl : e->run) ref_order = ref_order && e->slots[sl].ctx->face_order == FXE_FACE_ORDER_REFERENCE;
+        uint8_t* hist = ref_order ? e->d_hist : nullptr;
+        if (e->precision == FXE_PRECISION_FAST)
+            fxe::f32::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->d_order, hist, e->hist_bytes, e->stream);
+        else fxe::f64::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->d_order, hist, e->hist_bytes, e->stream);
         fxe::launch_ga_select(e->d_all, e->d_run, n, false, e->stream);
         fxe::launch_ga_fitness(e->d_all, e->d_run, n, false, e->stream);
         cudaError_t ce = cudaStreamEndCapture(e->stream, &g);

@@ -159,18 +159,16 @@ __global__ void __launch_bounds__(kGaThreads) ga_init_kernel(const GaJob* __rest
     initial_candidates(J, 0, min(J.ncand, J.gen[1]));
 }
 
-// One pair of children of generation g + 1 (pair k of the generation's draw stream): two roulette
-// draws, optional adaptive probabilities, crossover with probability crossp, both children
-// mutated bit by bit.
-__device__ void breed_pair(const GaJob& J, int g, int k, int32_t* john, int32_t* mary) {
+// One pair of children: two roulette draws, optional adaptive probabilities, crossover with
+// probability crossp, both children mutated bit by bit. draw() gives the next uniform in [0, 1)
+// of the pair's stream, in the order the reference makes its draws.
+template <typename Draw>
+__device__ __forceinline__ void breed_pair_with(const GaJob& J, Draw&& draw, int32_t* john, int32_t* mary) {
     const int ng = J.ng;
-    const uint64_t sb = (uint64_t)(g + 1) << 32;   // streams of generation g + 1
     // fitness_stats (LIB/gaboom.cpp:818-840) of the population
     const double fit_max = J.fstat[1], fit_avg = J.fstat[2];
-    const uint64_t st = sb + (uint64_t)k;
-    uint64_t d = 0;
-    const int pa = roulette(J, uniform(J.seed, st, d++));
-    const int pb = roulette(J, uniform(J.seed, st, d++));
+    const int pa = roulette(J, draw());
+    const int pb = roulette(J, draw());
     const int a = J.ford[pa], b = J.ford[pb];
     double crossp = J.cross_rate, mutp = J.mut_rate;
     if (J.adaptive) {
@@ -186,16 +184,16 @@ __device__ void breed_pair(const GaJob& J, int g, int k, int32_t* john, int32_t*
         john[q] = J.pop[(size_t)a * ng + q];
         m[q] = J.pop[(size_t)b * ng + q];
     }
-    if (uniform(J.seed, st, d++) < crossp) {
+    if (draw() < crossp) {
         // LIB/gaboom.cpp:2527-2598
-        int gen_a = (int)(uniform(J.seed, st, d++) * (double)ng);
-        int gen_b = (int)(uniform(J.seed, st, d++) * (double)ng);
+        int gen_a = (int)(draw() * (double)ng);
+        int gen_b = (int)(draw() * (double)ng);
         if (gen_a >= ng) gen_a = ng - 1;
         if (gen_b >= ng) gen_b = ng - 1;
         int pnt_a, pnt_b;
         if (J.intragenes) {
-            pnt_a = (int)(uniform(J.seed, st, d++) * 32.0);
-            pnt_b = (int)(uniform(J.seed, st, d++) * 32.0);
+            pnt_a = (int)(draw() * 32.0);
+            pnt_b = (int)(draw() * 32.0);
             if (gen_a > gen_b) {
                 const int tg = gen_a, tp = pnt_a;
                 gen_a = gen_b; pnt_a = pnt_b;
@@ -213,8 +211,8 @@ __device__ void breed_pair(const GaJob& J, int g, int k, int32_t* john, int32_t*
                 gen_b = tg;
             }
             if (gen_a != gen_b) {
-                pnt_a = uniform(J.seed, st, d++) < 0.5 ? 32 : 0;
-                pnt_b = uniform(J.seed, st, d++) < 0.5 ? 32 : 0;
+                pnt_a = draw() < 0.5 ? 32 : 0;
+                pnt_b = draw() < 0.5 ? 32 : 0;
                 if (gen_b - gen_a == 1 && pnt_a == 0 && pnt_b == 32) pnt_b = pnt_a;
             } else {
                 pnt_a = 32;
@@ -243,13 +241,20 @@ __device__ void breed_pair(const GaJob& J, int g, int k, int32_t* john, int32_t*
         int32_t* ch = c == 0 ? john : m;
         for (int q = 0; q < ng; ++q) {
             const float pr = J.gene_prob[q];
-            if (pr >= 0.0f && !(uniform(J.seed, st, d++) < (double)pr)) continue;
+            if (pr >= 0.0f && !(draw() < (double)pr)) continue;
             uint32_t optr = 0u;
             for (int bit = 0; bit < 32; ++bit)
-                if (uniform(J.seed, st, d++) < mutp) optr |= 1u << bit;
+                if (draw() < mutp) optr |= 1u << bit;
             ch[q] ^= (int32_t)optr;
         }
     }
+}
+
+// Pair k of the children of generation g + 1, from the generation's counter-based stream.
+__device__ void breed_pair(const GaJob& J, int g, int k, int32_t* john, int32_t* mary) {
+    const uint64_t st = ((uint64_t)(g + 1) << 32) + (uint64_t)k;   // streams of generation g + 1
+    uint64_t d = 0;
+    breed_pair_with(J, [&]() { return uniform(J.seed, st, d++); }, john, mary);
 }
 
 // Pairs k0 .. k0 + npairs - 1 of the running generation's children as candidates, with their
@@ -429,6 +434,21 @@ __global__ void __launch_bounds__(kNicheThreads) ga_niche_kernel(const GaJob* __
     J.share[i] = s;
 }
 
+// Running sums of the fitness in roulette order (roullete_wheel's walk, LIB/gaboom.cpp:1158-1186)
+// and fitness_stats' total, maximum and mean (LIB/gaboom.cpp:818-840), in order.
+__device__ void fitness_sums(const GaJob& J, const double* fit, int P) {
+    double cum = 0.0, mx = fit[0], sum = 0.0;
+    for (int i = 0; i < P; ++i) {
+        cum += fit[i];
+        J.fcum[i] = cum;
+        if (fit[i] > mx) mx = fit[i];
+        sum += fit[i];
+    }
+    J.fstat[0] = cum;
+    J.fstat[1] = mx;
+    J.fstat[2] = sum / (double)P;
+}
+
 // Fitness of the population (sorted by energy), the roulette order, running sums and
 // fitness_stats. kInitial: the initial population, walked in energy order whatever the model.
 template <bool kInitial>
@@ -478,18 +498,7 @@ __global__ void __launch_bounds__(kGaThreads) ga_fitness_kernel(const GaJob* __r
         J.fit[i] = key[i];
         J.ford[i] = idx[i];
     }
-    if (threadIdx.x == 0) {
-        double cum = 0.0, mx = key[0], sum = 0.0;
-        for (int i = 0; i < P; ++i) {
-            cum += key[i];
-            J.fcum[i] = cum;
-            if (key[i] > mx) mx = key[i];
-            sum += key[i];
-        }
-        J.fstat[0] = cum;
-        J.fstat[1] = mx;
-        J.fstat[2] = sum / (double)P;
-    }
+    if (threadIdx.x == 0) fitness_sums(J, key, P);
 }
 
 void launch_ga_fitness(const GaJob* all, const int* run, int n_jobs, bool initial, cudaStream_t st) {
@@ -507,6 +516,40 @@ void launch_ga_breed(const GaJob* all, const int* run, int n_jobs, cudaStream_t 
     ga_breed_kernel<<<n_jobs, kGaThreads, 0, st>>>(all, run);
     ga_accept_kernel<false><<<n_jobs, kGaThreads, 0, st>>>(all, run);
 }
+// Breeding with the caller's draws (fxe_ga_breed_draws): J.fit and J.ford given, one block forms
+// the running sums and fitness_stats, then one thread per pair breeds from its row of draws.
+__global__ void ga_draws_stats_kernel(const GaJob* __restrict__ J) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) fitness_sums(*J, J->fit, J->P);
+}
+
+__global__ void __launch_bounds__(kGaThreads) ga_breed_draws_kernel(const GaJob* __restrict__ Jp, const double* __restrict__ draws,
+                                                                    long long stride, int n_pairs, int* __restrict__ used) {
+    const GaJob& J = *Jp;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_pairs) return;
+    const double* row = draws + (size_t)k * stride;
+    long long d = 0;
+    bool over = false;
+    int32_t* john = J.child + (size_t)(2 * k) * J.ng;
+    breed_pair_with(J, [&]() {
+        if (d >= stride) { over = true; return 0.0; }
+        return row[d++];
+    }, john, john + J.ng);
+    used[k] = over ? -1 : (int)d;
+}
+
+void launch_ga_breed_draws(const GaJob* J, const double* draws, long long stride, int n_pairs, int* used,
+                           cudaStream_t st) {
+    ga_draws_stats_kernel<<<1, 32, 0, st>>>(J);
+    ga_breed_draws_kernel<<<(n_pairs + kGaThreads - 1) / kGaThreads, kGaThreads, 0, st>>>(J, draws, stride, n_pairs, used);
+}
+
+// Niche counts of a population whose ICs are given (fxe_ga_niche_counts): the generation's kernel
+// on one job.
+void launch_ga_niche(const GaJob* all, const int* run, cudaStream_t st) {
+    ga_niche_kernel<<<dim3(kNicheBlocks, 1), kNicheThreads, 0, st>>>(all, run);
+}
+
 void launch_ga_select(GaJob* all, const int* run, int n_jobs, bool initial, cudaStream_t st) {
     if (initial) ga_select_kernel<true><<<n_jobs, kGaThreads, 0, st>>>(all, run);
     else ga_select_kernel<false><<<n_jobs, kGaThreads, 0, st>>>(all, run);

@@ -109,7 +109,8 @@ __device__ __forceinline__ int warp_excl_scan(int v, int lane, int* total) {
 struct VorShared {
     real4 pl[kMaxPlanes];          // plane A.x + D = 0 (A unit normal, D = -plane distance)
     real area[kMaxCand];
-    int cidx[kMaxCand];             // Calc index of each candidate
+    int cidx[kMaxCand];             // Calc index of each contact
+    uint8_t cslot[kMaxCand];        // the contact's slot in the atom's candidate list
     real4 vx[kMaxVerts];           // vertex x, y, z, distance to the atom centre
     uchar4 vp[kMaxVerts];           // the vertex's planes (kNone = sphere)
     union {
@@ -548,11 +549,31 @@ __device__ FXE_COLD void engulf_corrections(VorShared& sh, int NC, real rado, re
     }
 }
 
+// Face history of one pose (reference face order): order_faces leaves each contact's point list
+// in ptorder[X].pt[] (LIB/Vcontacts.cpp:726-831), a workspace that outlives the atom, and reads
+// ptorder[X].pt[numpts] — a slot past the face's own list — when no point shares the first
+// point's second plane (:800-812). That slot holds what an earlier atom of the pose left there
+// (zero at the start of the pose). The history keeps those lists per contact index X, rows of
+// kHistPts entries, followed by the pre-extra contents of the vertex slots the antipodal points
+// take (the reference appends them one face at a time, so a face's read of a later face's slot
+// still sees the old vertex there).
+constexpr int kHistPts = 64;
+constexpr int kHistBytes = kMaxCand * kHistPts;
+constexpr size_t kHistStride = kHistBytes + kMaxCand * (sizeof(real4) + sizeof(uchar4));
+static_assert(kHistBytes % 32 == 0 && kHistStride % 32 == 0, "history rows keep 32-byte alignment");
+
+__device__ __forceinline__ real4* hist_vx(uint8_t* h) { return reinterpret_cast<real4*>(h + kHistBytes); }
+__device__ __forceinline__ uchar4* hist_vp(uint8_t* h) {
+    return reinterpret_cast<uchar4*>(h + kHistBytes + kMaxCand * sizeof(real4));
+}
+
 // One extended-radical-plane polyhedron and its contact areas. sh.pl/flag/cidx hold the
-// planes of the NC candidates (excluded slots carry a plane that never binds). Returns
-// kAtomOk, kAtomHullFail (the walk reached 200 edges) or kAtomCapacity.
-__device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_partner,
-                            int seedA, int seedB, int seedC) {
+// planes of the NC contacts in the order of the reference's contact list. hist: the pose's face
+// history (reference face order), or null (a face whose first point has no neighbour on its
+// second plane is then ordered from the point's other plane). Returns kAtomOk, kAtomHullFail
+// (the walk reached 200 edges) or kAtomCapacity.
+__device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_partner, int* unreplayed,
+                            int seedA, int seedB, int seedC, uint8_t* hist) {
     // rado * rado in single precision, as the reference squares its float radius
     const real rr = (real)((float)rado * (float)rado);
     // bounding planes
@@ -823,6 +844,10 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         if (NV + n_extra + t > kMaxVerts - 1) return kAtomCapacity;
         if (extra) {
             const int w = NV + n_extra + off;
+            if (hist) {
+                hist_vx(hist)[w - NV] = sh.vx[w];
+                hist_vp(hist)[w - NV] = sh.vp[w];
+            }
             sh.vx[w] = make_real4(ex[0], ex[1], ex[2], rado);
             sh.vp[w] = make_uchar4((uint8_t)X, kNone, kNone, 0);
             sh.u.f.pt[sh.foff[X] + sh.fnp[X]] = (uint8_t)w;
@@ -832,50 +857,77 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     }
     __syncwarp();
     // ordering around each face (pt[0], a neighbour of it, then decreasing cosine)
-    int np_miss = 0;
+    int np_miss = 0, np_lost = 0;
     for (int X = lane; X < NC; X += 32) {
         if (sh.flag[X] == 0) continue;
         const int np = sh.fnp[X];
-        if (np <= 3) continue;
         uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
-        real* cs = &sh.u.f.cosv[sh.foff[X]];
-        const uchar4 P0 = sh.vp[pt[0]];
-        const int pY = (P0.x == X) ? P0.y : P0.x;
-        int vi = 1;
-        for (; vi < np; ++vi) {
-            const uchar4 q = sh.vp[pt[vi]];
-            if (q.x == pY || q.y == pY || q.z == pY) break;
-        }
-        if (vi == np) {
-            ++np_miss;
-            const int pZ = (P0.x == X || P0.y == X) ? P0.z : P0.y;
-            vi = 1;
-            if (pZ != kNone) {
-                int w = 1;
-                for (; w < np; ++w) {
-                    const uchar4 q = sh.vp[pt[w]];
-                    if (q.x == pZ || q.y == pZ || q.z == pZ) break;
-                }
-                if (w < np) vi = w;
+        int stale_prev = -1;   // point 1 of the face before a replayed read of the slot past its end
+        if (np > 3) {
+            real* cs = &sh.u.f.cosv[sh.foff[X]];
+            const uchar4 P0 = sh.vp[pt[0]];
+            const int pY = (P0.x == X) ? P0.y : P0.x;
+            int vi = 1;
+            for (; vi < np; ++vi) {
+                const uchar4 q = sh.vp[pt[vi]];
+                if (q.x == pY || q.y == pY || q.z == pY) break;
             }
-        }
-        const uint8_t tmp = pt[vi];
-        pt[vi] = pt[1];
-        pt[1] = tmp;
-        const real4 v0 = sh.vx[pt[0]], v1 = sh.vx[pt[1]];
-        for (int k = 2; k < np; ++k) cs[k] = cos_pqr(v1, v0, sh.vx[pt[k]]);
-        for (int a = 2; a < np - 1; ++a)
-            for (int b = a + 1; b < np; ++b)
-                if (cs[a] < cs[b]) {
-                    const uint8_t t = pt[a];
-                    pt[a] = pt[b];
-                    pt[b] = t;
-                    const real tc = cs[a];
-                    cs[a] = cs[b];
-                    cs[b] = tc;
+            real4 v1;
+            bool replayed = false;
+            if (vi == np) {
+                ++np_miss;
+                const int s = (hist && np < kHistPts) ? (int)hist[X * kHistPts + np] : -1;
+                if (s >= 0 && s < kMaxVerts - 1) {
+                    // the reference swaps pt[1] with the stale slot: the slot's vertex becomes
+                    // point 1, the old point 1 stays behind in the slot. The vertex is read as it
+                    // stood when this face was ordered: an antipodal point a later face appends
+                    // had not yet replaced the slot's old contents.
+                    replayed = true;
+                    stale_prev = pt[1];
+                    pt[1] = (uint8_t)s;
+                    v1 = (s >= NV && s < NV + n_extra && sh.vp[s].x > X) ? hist_vx(hist)[s - NV] : sh.vx[s];
+                } else {
+                    if (hist) ++np_lost;
+                    const int pZ = (P0.x == X || P0.y == X) ? P0.z : P0.y;
+                    vi = 1;
+                    if (pZ != kNone) {
+                        int w = 1;
+                        for (; w < np; ++w) {
+                            const uchar4 q = sh.vp[pt[w]];
+                            if (q.x == pZ || q.y == pZ || q.z == pZ) break;
+                        }
+                        if (w < np) vi = w;
+                    }
                 }
+            }
+            if (!replayed) {
+                const uint8_t tmp = pt[vi];
+                pt[vi] = pt[1];
+                pt[1] = tmp;
+                v1 = sh.vx[pt[1]];
+            }
+            const real4 v0 = sh.vx[pt[0]];
+            for (int k = 2; k < np; ++k) cs[k] = cos_pqr(v1, v0, sh.vx[pt[k]]);
+            for (int a = 2; a < np - 1; ++a)
+                for (int b = a + 1; b < np; ++b)
+                    if (cs[a] < cs[b]) {
+                        const uint8_t t = pt[a];
+                        pt[a] = pt[b];
+                        pt[b] = t;
+                        const real tc = cs[a];
+                        cs[a] = cs[b];
+                        cs[b] = tc;
+                    }
+        }
+        if (hist) {
+            uint8_t* h = hist + X * kHistPts;
+            const int nw = np < kHistPts ? np : kHistPts;
+            for (int k = 0; k < nw; ++k) h[k] = pt[k];
+            if (stale_prev >= 0) h[np] = (uint8_t)stale_prev;
+        }
     }
     *no_partner += warp_sum(np_miss);
+    *unreplayed += warp_sum(np_lost);
     __syncwarp();
 
     // ---- areas (LIB/Vcontacts.cpp:838-1044) ----
@@ -1004,48 +1056,50 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     return kAtomOk;
 }
 
-// Planes of the candidates of one scored atom (LIB/Vcontacts.cpp:186-221). Slots set in
-// `excl` (a candidate the reference's list does not hold) get a plane that never binds, which
-// leaves the order of the remaining planes, and so every tie-break, as in the shorter list.
-__device__ void load_planes(VorShared& sh, const DevSystem& S, const DevWork& W, int p, int a,
-                            int NC, float4 me, float rado, const uint32_t* excl, int lane) {
+// Planes of the contacts of one scored atom (LIB/Vcontacts.cpp:186-221): the candidates whose
+// bit in `excl` is clear (the list get_contlist4 gives; an excluded candidate is a saved atom that
+// kept no contact with this one, or one at distance zero), packed in candidate order, so that
+// each plane's index, and every tie-break on it, is the reference's contact index. Returns NC.
+__device__ int load_planes(VorShared& sh, const DevSystem& S, const DevWork& W, int p, int a,
+                           int n_cand, float4 me, float rado, const uint32_t* excl, int lane) {
     const int nm = n_mobile(S);
     const size_t cb = ((size_t)p * nm + a) * kMaxCand;
     const float rr = rado * rado;          // single-precision products, as in the reference
-    for (int c = lane; c < NC; c += 32) {
-        const int j = W.cand_idx[cb + c];
-        const float d2 = W.cand_d2[cb + c];
-        sh.cidx[c] = j;
-        const int mj = mobile_of(S, j);
-        const float4 pj = mj < 0 ? S.rec_pos[j] : W.mob_pos[(size_t)p * nm + mj];
-        const bool ex = ((excl[c >> 5] >> (c & 31)) & 1u) || d2 < 1e-20f;
-        if (ex) {
-            sh.pl[c] = make_real4(real(0.0), real(0.0), real(0.0), -real(1e30));
+    int NC = 0;
+    for (int c0 = 0; c0 < n_cand; c0 += 32) {
+        const int c = c0 + lane;
+        const bool keep = c < n_cand && !((excl[c >> 5] >> (c & 31)) & 1u);
+        const unsigned m = __ballot_sync(kFull, keep);
+        if (keep) {
+            const int r = NC + __popc(m & lanemask_lt());
+            const int j = W.cand_idx[cb + c];
+            const float d2 = W.cand_d2[cb + c];
+            sh.cidx[r] = j;
+            sh.cslot[r] = (uint8_t)c;
+            const int mj = mobile_of(S, j);
+            const float4 pj = mj < 0 ? S.rec_pos[j] : W.mob_pos[(size_t)p * nm + mj];
+            const real d = sqrt((real)d2);
+            const float q = kRw + pj.w;
+            const float qq = q * q;
+            // the reference squares the double distance; in single precision d2 itself is closer
+            const real dd = sizeof(real) == 8 ? d * d : (real)d2;
+            const real num = (dd + (real)rr) - (real)qq;
+            bool eng = num < real(0.0);
+            if (sizeof(real) < 8 && fabs(num) < real(1e-3)) eng = ((double)d2 + (double)rr) - (double)qq < 0.0;
+            const real4 P = make_real4((real)(pj.x - me.x) / d, (real)(pj.y - me.y) / d, (real)(pj.z - me.z) / d,
+                                       -(num / (real(2.0) * d)));
+            sh.pl[r] = P;
 #if FXE_FILTER
-            sh.plf[c] = make_float4(0.0f, 0.0f, 0.0f, -1e30f);
+            sh.plf[r] = make_float4((float)P.x, (float)P.y, (float)P.z, (float)P.w);
 #endif
-            sh.flag[c] = 0;
-            continue;
+            sh.flag[r] = eng ? kEngulf : 0;
         }
-        const real d = sqrt((real)d2);
-        const float q = kRw + pj.w;
-        const float qq = q * q;
-        // the reference squares the double distance; in single precision d2 itself is closer
-        const real dd = sizeof(real) == 8 ? d * d : (real)d2;
-        const real num = (dd + (real)rr) - (real)qq;
-        bool eng = num < real(0.0);
-        if (sizeof(real) < 8 && fabs(num) < real(1e-3)) eng = ((double)d2 + (double)rr) - (double)qq < 0.0;
-        const real4 P = make_real4((real)(pj.x - me.x) / d, (real)(pj.y - me.y) / d, (real)(pj.z - me.z) / d,
-                                   -(num / (real(2.0) * d)));
-        sh.pl[c] = P;
-#if FXE_FILTER
-        sh.plf[c] = make_float4((float)P.x, (float)P.y, (float)P.z, (float)P.w);
-#endif
-        sh.flag[c] = eng ? kEngulf : 0;
+        NC += __popc(m);
     }
     // project_points' fallback centre for two engulfing planes: the atom's own coordinates + rado
     if (lane == 0) sh.vx[kMaxVerts - 1] = make_real4((real)(me.x + rado), (real)me.y, (real)me.z, real(0.0));
     __syncwarp();
+    return NC;
 }
 
 __device__ double pose_clash_sum(const DevSystem& S, const DevWork& W, int p, int lane) {
@@ -1100,7 +1154,7 @@ __device__ void finish_failed(const DevWork& W, int p, int lane, int status, dou
 }
 
 __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W, int p, int lane,
-                                           PoseShared& ps) {
+                                           PoseShared& ps, uint8_t* hist) {
     VorShared& sh = ps.v;
     const int nl = n_mobile(S);      // the scored atoms: side-chain atoms, then the ligand
     // polyhedron seeds (Calc indices, -1 = none) and the mobile partners each processed atom kept
@@ -1129,33 +1183,41 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         for (int w = 0; w < kMaskWords; ++w) rec[l][w] = 0;
     }
     if (lane < kMaskWords) ps.done[lane] = 0;
+    // the face history starts the pose at zero, as the reference's ptorder does on a workspace
+    // cleared before the pose
+    if (hist) {
+        uint4* h4 = reinterpret_cast<uint4*>(hist);
+        for (int k = lane; k < kHistBytes / 16; k += 32) h4[k] = make_uint4(0u, 0u, 0u, 0u);
+    }
     __syncwarp();
     // calc_region: atoms in Calclist order (LIB/Vcontacts.cpp:74-139)
     for (int r = 0; r < nl; ++r) {
         const int a = ps.order[r];
-        const int NC = W.cand_n[lb + a];
-        if (NC < 0) {
+        const int n_cand = W.cand_n[lb + a];
+        if (n_cand < 0) {
             if (lane == 0) atomicAdd(&W.counters[2], 1);
             finish_failed(W, p, lane, FXE_POSE_CAPACITY, 0.0);
             return;
         }
         const size_t cb = (lb + a) * kMaxCand;
-        // get_contlist4's list: saved atoms drop out unless they kept a contact with this one
+        // get_contlist4's list: saved atoms drop out unless they kept a contact with this one, and
+        // so does an atom at distance zero
         uint32_t excl[kMaxCand / 32];
         int kept_n = 0;
 #pragma unroll
         for (int w = 0; w < kMaxCand / 32; ++w) {
             const int c = w * 32 + lane;
             bool ex = false;
-            if (c < NC) {
+            if (c < n_cand) {
                 const int l = mobile_of(S, W.cand_idx[cb + c]);
                 if (l >= 0) ex = bit(ps.done, l) && !bit(rec[l], a);
+                if (W.cand_d2[cb + c] < 1e-20f) ex = true;
             }
             excl[w] = __ballot_sync(kFull, ex);
-            kept_n += __popc(__ballot_sync(kFull, c < NC && !ex));
+            kept_n += __popc(__ballot_sync(kFull, c < n_cand && !ex));
         }
         if (kept_n == 0) {   // no contacts: SAS -1, nothing saved, the atom is not marked done
-            for (int c = lane; c < NC; c += 32) {
+            for (int c = lane; c < n_cand; c += 32) {
                 W.cand_area[cb + c] = 0.0;
                 W.cand_flag[cb + c] = 0;
             }
@@ -1163,15 +1225,14 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         }
         const float4 me = W.mob_pos[lb + a];
         const float rado = me.w + kRw;
-        load_planes(sh, S, W, p, a, NC, me, rado, excl, lane);
+        const int NC = load_planes(sh, S, W, p, a, n_cand, me, rado, excl, lane);
         // seed vertex left by an earlier atom, if all three of its planes are in the list
         int sA = -1, sB = -1, sC = -1;
         if (seed[a][0] != -1) {
             const int s0 = seed[a][0], s1 = seed[a][1], s2 = seed[a][2];
             for (int c0 = 0; c0 < NC; c0 += 32) {
                 const int c = c0 + lane;
-                int j = -2;
-                if (c < NC && !((excl[c >> 5] >> (c & 31)) & 1u)) j = sh.cidx[c];
+                const int j = c < NC ? sh.cidx[c] : -2;
                 const unsigned m0 = __ballot_sync(kFull, j == s0);
                 const unsigned m1 = __ballot_sync(kFull, j == s1 && j != s0);
                 const unsigned m2 = __ballot_sync(kFull, j == s2 && j != s0 && j != s1);
@@ -1180,9 +1241,10 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
                 if (m2) sC = c0 + 31 - __clz(m2);
             }
         }
-        int np_miss = 0;
-        const int st = voronoi_warp(sh, NC, rado, lane, &np_miss, sA, sB, sC);
+        int np_miss = 0, np_lost = 0;
+        const int st = voronoi_warp(sh, NC, rado, lane, &np_miss, &np_lost, sA, sB, sC, hist);
         if (lane == 0 && np_miss) atomicAdd(&W.counters[3], np_miss);
+        if (lane == 0 && np_lost) atomicAdd(&W.counters[0], np_lost);
         if (st == kAtomCapacity) {
             if (lane == 0) atomicAdd(&W.counters[2], 1);
             finish_failed(W, p, lane, FXE_POSE_CAPACITY, 0.0);
@@ -1193,16 +1255,23 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
             finish_failed(W, p, lane, FXE_POSE_POLYHEDRON_FAILED, (double)kPolyPenalty);
             return;
         }
-        // save_areas (LIB/Vcontacts.cpp:1149-1220): contacts with area > 0 on a contact plane
+        // save_areas (LIB/Vcontacts.cpp:1149-1220): contacts with area > 0 on a contact plane;
+        // candidates outside the contact list record nothing
         uint32_t keep_lig[kMaskWords] = {0, 0, 0, 0};
-        for (int c = lane; c < NC; c += 32) {
-            const bool ex = (excl[c >> 5] >> (c & 31)) & 1u;
-            const real ar = ex ? real(0.0) : sh.area[c];
-            const uint8_t f = ex ? 0 : sh.flag[c];
+        for (int c = lane; c < n_cand; c += 32) {
+            if ((excl[c >> 5] >> (c & 31)) & 1u) {
+                W.cand_area[cb + c] = 0.0;
+                W.cand_flag[cb + c] = 0;
+            }
+        }
+        for (int k = lane; k < NC; k += 32) {
+            const real ar = sh.area[k];
+            const uint8_t f = sh.flag[k];
             const bool kept = ar > real(0.0) && (f & (kOnHull | kEngulf));
+            const int c = sh.cslot[k];
             W.cand_area[cb + c] = (double)ar;
             W.cand_flag[cb + c] = (uint8_t)(f | (kept ? kRecorded : 0));
-            const int l = kept ? mobile_of(S, sh.cidx[c]) : -1;
+            const int l = kept ? mobile_of(S, sh.cidx[k]) : -1;
             if (l >= 0) keep_lig[l >> 5] |= 1u << (l & 31);
         }
 #pragma unroll
@@ -1340,13 +1409,19 @@ __device__ __forceinline__ int next_pose(int* next, int lane) {
     return __shfl_sync(kFull, p, 0);
 }
 
+// The warp's face history (hist_all: kHistStride bytes per warp of the launch), or null.
+__device__ __forceinline__ uint8_t* warp_hist(uint8_t* hist_all) {
+    return hist_all ? hist_all + (size_t)(blockIdx.x * kVorWarps + (threadIdx.x >> 5)) * kHistStride : nullptr;
+}
+
 __global__ void __launch_bounds__(kVorWarps * 32)
-pose_kernel(DevSystem S, DevWork W, int n, int* next) {
+pose_kernel(DevSystem S, DevWork W, int n, int* next, uint8_t* hist_all) {
     extern __shared__ __align__(16) unsigned char smem[];
     PoseShared& ps = reinterpret_cast<PoseShared*>(smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
+    uint8_t* hist = warp_hist(hist_all);
     for (int q = next_pose(next, lane); q < n; q = next_pose(next, lane)) {
-        score_pose(S, W, W.pose_order[q], lane, ps);
+        score_pose(S, W, W.pose_order[q], lane, ps, hist);
         __syncwarp();
     }
 }
@@ -1354,14 +1429,16 @@ pose_kernel(DevSystem S, DevWork W, int n, int* next) {
 // The same over the poses of several jobs; the job's system and workspace descriptors are read
 // from the job table (they stay in L1), keeping shared memory for the polyhedron workspace.
 __global__ void __launch_bounds__(kVorWarps * 32)
-pose_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, int total, int* next, const int* __restrict__ order) {
+pose_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, int total, int* next, const int* __restrict__ order,
+                 uint8_t* hist_all) {
     extern __shared__ __align__(16) unsigned char smem[];
     PoseShared& ps = reinterpret_cast<PoseShared*>(smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
+    uint8_t* hist = warp_hist(hist_all);
     for (int q = next_pose(next, lane); q < total; q = next_pose(next, lane)) {
         const int gp = order[q];
         const Job& job = jobs[find_job(jobs, n_jobs, gp, false)];
-        score_pose(job.S, job.W, gp - job.pose0, lane, ps);
+        score_pose(job.S, job.W, gp - job.pose0, lane, ps, hist);
         __syncwarp();
     }
 }
@@ -1371,20 +1448,36 @@ size_t pose_jobs_smem_bytes() { return sizeof(PoseShared) * kVorWarps; }
 
 static int g_resident_blocks = 0;   // blocks of pose_kernel the device holds at once
 
-static unsigned pose_blocks(int n) {
-    const int want = (n + kVorWarps - 1) / kVorWarps;
-    return (unsigned)(g_resident_blocks > 0 && g_resident_blocks < want ? g_resident_blocks : want);
+// Blocks of a launch over n poses: no more than the device holds at once (the warps take poses
+// from a queue), and no more than the face history holds (hist_bytes; 0: no history).
+static unsigned pose_blocks(int n, size_t hist_bytes) {
+    int b = (n + kVorWarps - 1) / kVorWarps;
+    if (g_resident_blocks > 0 && g_resident_blocks < b) b = g_resident_blocks;
+    if (hist_bytes) {
+        const size_t cap = hist_bytes / (kVorWarps * kHistStride);
+        if ((size_t)b > cap) b = (int)cap;
+    }
+    return (unsigned)b;
 }
 
-void launch_poses(const DevSystem& S, const DevWork& W, int n, int* next, cudaStream_t st) {
+size_t pose_hist_bytes() { return (size_t)g_resident_blocks * kVorWarps * kHistStride; }
+
+// hist / hist_bytes: the launch's face history (reference face order), or null / 0.
+void launch_poses(const DevSystem& S, const DevWork& W, int n, int* next, uint8_t* hist, size_t hist_bytes,
+                  cudaStream_t st) {
+    if (hist_bytes < kVorWarps * kHistStride) hist = nullptr;
+    if (!hist) hist_bytes = 0;
     cudaMemsetAsync(next, 0, sizeof(int), st);
-    pose_kernel<<<pose_blocks(n), kVorWarps * 32, pose_smem_bytes(), st>>>(S, W, n, next);
+    pose_kernel<<<pose_blocks(n, hist_bytes), kVorWarps * 32, pose_smem_bytes(), st>>>(S, W, n, next, hist);
 }
 
-void launch_poses_jobs(const Job* jobs, int n_jobs, int total, int* next, const int* order, cudaStream_t st) {
+void launch_poses_jobs(const Job* jobs, int n_jobs, int total, int* next, const int* order, uint8_t* hist,
+                       size_t hist_bytes, cudaStream_t st) {
+    if (hist_bytes < kVorWarps * kHistStride) hist = nullptr;
+    if (!hist) hist_bytes = 0;
     cudaMemsetAsync(next, 0, sizeof(int), st);
-    pose_kernel_jobs<<<pose_blocks(total), kVorWarps * 32, pose_jobs_smem_bytes(), st>>>(jobs, n_jobs, total, next,
-                                                                                         order);
+    pose_kernel_jobs<<<pose_blocks(total, hist_bytes), kVorWarps * 32, pose_jobs_smem_bytes(), st>>>(
+        jobs, n_jobs, total, next, order, hist);
 }
 
 cudaError_t configure_voronoi() {

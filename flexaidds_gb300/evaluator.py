@@ -48,6 +48,7 @@ def load_library():
         lib.fxe_thermo_compute_device.argtypes = [vp, vp, C.c_int64, C.c_double, vp, vp]
         lib.fxe_thermo_weights.argtypes = [_d, _i, C.c_int64, C.c_double, _d]
         lib.fxe_context_set_precision.argtypes = [vp, C.c_int32]
+        lib.fxe_context_set_face_order.argtypes = [vp, C.c_int32]
         lib.fxe_context_enable_timing.argtypes = [vp, C.c_int32]
         lib.fxe_context_take_timing.argtypes = [vp, _d, C.POINTER(C.c_int64)]
         lib.fxe_context_create_shared.argtypes = [vp, vp, vp, vp, C.c_int32, C.POINTER(vp)]
@@ -90,9 +91,12 @@ class GPUEvaluator:
     """Evaluation context for one receptor, ligand and energy matrix."""
 
     REFERENCE, FAST = 0, 1
+    # how a face whose first point has no neighbour on its second plane is ordered
+    # (fxe_context_set_face_order): as the reference does it, or from the point's other plane
+    FACE_ORDER_REFERENCE, FACE_ORDER_GEOMETRIC = 0, 1
 
     def __init__(self, desc: Descriptor, max_poses: int = 2048, precision: int = 0,
-                 share_receptor_with: "GPUEvaluator | None" = None):
+                 share_receptor_with: "GPUEvaluator | None" = None, face_order: int = 0):
         """share_receptor_with: an evaluator on the same receptor whose device copy of the
         receptor, cell list and cleft grid this one reuses (fxe_context_create_shared)."""
         self.lib = load_library()
@@ -110,6 +114,7 @@ class GPUEvaluator:
                                                C.byref(pk.params), self.max_poses, C.byref(h)))
         self.handle = h
         _check(self.lib.fxe_context_set_precision(self.handle, int(precision)))
+        _check(self.lib.fxe_context_set_face_order(self.handle, int(face_order)))
 
     def close(self):
         if getattr(self, "handle", None):
@@ -198,7 +203,8 @@ class GPUEvaluator:
     def stats(self) -> dict:
         o = np.zeros(4, np.int32)
         _check(self.lib.fxe_last_stats(self.handle, ptr(o, _i)))
-        return {"hull_failures": int(o[1]), "capacity": int(o[2]), "no_partner_faces": int(o[3])}
+        return {"hull_failures": int(o[1]), "capacity": int(o[2]), "no_partner_faces": int(o[3]),
+                "unreplayed_faces": int(o[0])}
 
 
 class Job(C.Structure):

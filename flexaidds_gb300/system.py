@@ -200,17 +200,62 @@ def gene_bins(gmin: float, gmax: float, gdel: float, gmap: int) -> np.ndarray:
     while ``tot < u``; the index it stops at is the first k with ``T[k] >= u``. The table is
     extended until it reaches 1.0 so that every u in [0, 1) lands inside it.
     """
-    nbin = (gmax - gmin) / gdel
-    if nbin - int(nbin) > 0.0:
-        nbin += 1.0
-    if gmap:
-        nbin += 1.0
+    nbin = bin_count(gmin, gmax, gdel, gmap)
     b = 1.0 / nbin
     n = int(nbin) + 4
     t = np.cumsum(np.full(n, b, np.float64))   # numpy cumsum adds strictly left to right
     while t[-1] < 1.0:
         t = np.concatenate([t, t[-1] + np.cumsum(np.full(4, b))])
     return t
+
+
+MAX_RANDOM_VALUE = 2147483647   # LIB/gaboom.h:36
+RAND_MAX = 2147483647           # the C library's RAND_MAX on the reference's Linux builds
+
+
+def random_double(gene: int) -> float:
+    """RandomDouble(int32) (LIB/gaboom.cpp:2938-2940): a gene's place in [0, 1)."""
+    return int(gene) / (float(MAX_RANDOM_VALUE) + 1.0)
+
+
+def random_int(frac: float) -> int:
+    """RandomInt (LIB/gaboom.cpp:2930-2935): frac scaled to [0, RAND_MAX], saturating."""
+    raw = float(frac) * (float(RAND_MAX) + 1.0)
+    if raw >= float(RAND_MAX) + 1.0:
+        return RAND_MAX
+    if raw < 0.0:
+        return 0
+    return int(raw)
+
+
+def genetoic(tab: np.ndarray, gmin: float, gdel: float, gene: int) -> float:
+    """genetoic (LIB/gaboom.cpp:2887-2906) of one gene with its running bin totals (gene_bins):
+    min + del * (the first bin whose running total reaches RandomDouble(gene))."""
+    i = int(np.searchsorted(tab, random_double(gene), side="left"))
+    return float(gmin) + float(gdel) * float(i)
+
+
+def ic_to_gene(gmin: float, gmax: float, gdel: float, gmap: int, ic: float) -> int:
+    """ictogene (LIB/gaboom.cpp:2908-2927): the gene whose place is 1 - i * bin for the bin i
+    of ic, as RandomInt gives it (used by the reference to seed chromosomes with given ICs)."""
+    b = 1.0 / bin_count(gmin, gmax, gdel, gmap)
+    i = int((float(ic) - float(gmin)) / float(gdel))
+    tot = 1.0
+    while i > 0:
+        tot -= b
+        i -= 1
+    return random_int(tot)
+
+
+def bin_count(gmin: float, gmax: float, gdel: float, gmap: int) -> float:
+    """set_bins' nbin (LIB/gaboom.cpp:2295-2308): (max - min) / del, rounded up, one more for a
+    mapped (index) gene."""
+    nbin = (gmax - gmin) / gdel
+    if nbin - int(nbin) > 0.0:
+        nbin += 1.0
+    if gmap:
+        nbin += 1.0
+    return nbin
 
 
 def read_emat(path: str):

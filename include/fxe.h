@@ -167,6 +167,21 @@ fxe_status fxe_context_create_shared(const fxe_context* receptor_of, const fxe_l
 enum { FXE_PRECISION_REFERENCE = 0, FXE_PRECISION_FAST = 1 };
 fxe_status fxe_context_set_precision(fxe_context* ctx, int32_t precision);
 
+/* How a face whose first point has no other point on its second plane is ordered. order_faces
+ * (LIB/Vcontacts.cpp:800-812) then swaps point 1 with ptorder[X].pt[numpts], a slot past the
+ * face's own list that holds what an earlier atom of the pose left there.
+ * FXE_FACE_ORDER_REFERENCE (default): that read is replayed as the reference makes it on a
+ *   ptorder workspace cleared at the start of each pose: the device keeps each contact's last
+ *   point list for the pose (faces of at most 63 points; a longer one is counted in
+ *   fxe_last_stats out4[0] and ordered as below).
+ * FXE_FACE_ORDER_GEOMETRIC: point 1 is the first point sharing the first point's other plane, a
+ *   neighbour on the face, so the face's points are ordered by angle as the reference intends.
+ * Batched launches and the GA engine use the reference order unless every context of the launch
+ * asks for the geometric one; the GA engine reads the setting when its set of running jobs
+ * changes. No reference counterpart (the reference has no switch). */
+enum { FXE_FACE_ORDER_REFERENCE = 0, FXE_FACE_ORDER_GEOMETRIC = 1 };
+fxe_status fxe_context_set_face_order(fxe_context* ctx, int32_t mode);
+
 /* Scores n chromosomes given as int32 genes (n * n_genes, host memory), writing n records to
  * host memory. Synchronous, like cuda_eval_batch (LIB/cuda_eval.cuh:60-70). */
 fxe_status fxe_eval_genes(fxe_context* ctx, int32_t n, const int32_t* genes, fxe_cf* out);
@@ -191,9 +206,10 @@ fxe_status fxe_last_contacts(fxe_context* ctx, int32_t pose, int32_t atom, int32
 /* Built ligand coordinates of pose `pose` of the last evaluated batch (n_atoms * 3). */
 fxe_status fxe_last_ligand_xyz(fxe_context* ctx, int32_t pose, float* xyz);
 
-/* Work counters of the last evaluation call: out4[0] reserved (0), [1] poses whose hull walk
- * reached 200 edges, [2] poses over capacity, [3] faces whose first vertex had no neighbour on
- * its second plane. */
+/* Work counters of the last evaluation call: out4[0] faces whose read past the end of their
+ * point list could not be replayed (FXE_FACE_ORDER_REFERENCE; 0 in practice), [1] poses whose
+ * hull walk reached 200 edges, [2] poses over capacity, [3] faces whose first vertex had no
+ * neighbour on its second plane. */
 fxe_status fxe_last_stats(fxe_context* ctx, int32_t* out4);
 
 /* Thermodynamics of an ensemble of n energies (kcal/mol) with multiplicities (NULL = all 1)

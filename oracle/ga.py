@@ -103,6 +103,50 @@ def sig_share(desc, peaks: float = 5.0, scale: float = 10.0) -> float:
     return math.sqrt(s / ng) / (2.0 * math.pow(peaks, 1.0 / ng)) / scale
 
 
+def calc_rmsp(ic1, ic2) -> float:
+    """calc_rmsp (LIB/gaboom.cpp:2874-2885): root mean square of the IC differences, the squares
+    summed in gene order."""
+    acc = 0.0
+    for a, b in zip(ic1, ic2):
+        d = float(a) - float(b)
+        acc += d * d
+    return math.sqrt(acc / len(ic1))
+
+
+def fitness_stats(fit) -> tuple:
+    """fitness_stats (LIB/gaboom.cpp:818-840) over fitness values in roulette order: (running
+    sums, total, maximum, mean)."""
+    cum, mx, tot = [], float(fit[0]), 0.0
+    for f in fit:
+        tot += float(f)
+        cum.append(tot)
+        mx = max(mx, float(f))
+    return cum, tot, mx, tot / len(fit)
+
+
+def adapt_prob(fit_max: float, fit_avg: float, f1: float, f2: float, k) -> tuple:
+    """adapt_prob (LIB/gaboom.cpp:848-880): (crossover, mutation) probabilities of a pair whose
+    fitness is f1, f2; k = (k1, k2, k3, k4). The denominator is floored at 1e-15
+    (GA_FITNESS_DENOM_FLOOR, LIB/ga_constants.h:38)."""
+    hi, lo = max(f1, f2), min(f1, f2)
+    denom = max(fit_max - fit_avg, 1e-15)
+    crossp = k[0] * (fit_max - hi) / denom if hi > fit_avg else k[2]
+    mutp = k[1] * (fit_max - lo) / denom if lo > fit_avg else k[3]
+    return crossp, mutp
+
+
+def remove_dups(ic, tol: float = 0.1) -> list:
+    """remove_dups (LIB/gaboom.cpp:2728-2747) over chromosomes in their given order: a
+    chromosome is dropped when every gene is within tol of the last one kept. Returns the kept
+    indices."""
+    kept, last = [], None
+    for i, row in enumerate(ic):
+        if last is None or not all(abs(float(a) - float(b)) < tol for a, b in zip(row, last)):
+            kept.append(i)
+            last = row
+    return kept
+
+
 def clamped_ic(desc, genes) -> np.ndarray:
     """to_ic of evaluated chromosomes: decoded, then clamped by eval_chromosome
     (LIB/gaboom.cpp:1851-1859)."""
@@ -126,18 +170,7 @@ class Fitness:
             ic = clamped_ic(desc, pop)
             ng = ic.shape[1]
             sig = sig_share(desc, peaks, scale)
-            share = []
-            for i in range(P):
-                s = 0.0
-                for j in range(P):
-                    acc = 0.0
-                    for q in range(ng):
-                        dq = ic[i, q] - ic[j, q]
-                        acc += dq * dq
-                    r = math.sqrt(acc / ng)
-                    if r <= sig:
-                        s += 1.0 - (r / sig if alpha == 1.0 else math.pow(r / sig, alpha))
-                share.append(s)
+            share = niche_counts(ic, sig, alpha)
             if model == "PSHARE":
                 fit = [fit[i] / share[i] for i in range(P)]
             else:
@@ -155,23 +188,50 @@ class Fitness:
             order = sorted(range(P), key=lambda i: (-fit[i], i))
         self.order = order
         self.fit = [fit[i] for i in order]
-        cum, mx, tot = [], self.fit[0], 0.0
-        for f in self.fit:
-            tot += f
-            cum.append(tot)
-            mx = max(mx, f)
-        self.cum, self.total, self.max, self.avg = cum, tot, mx, tot / P
+        self.cum, self.total, self.max, self.avg = fitness_stats(self.fit)
+
+    @classmethod
+    def given(cls, fit, order=None) -> "Fitness":
+        """Fitness values given in roulette order (population positions `order`, default
+        0..P-1)."""
+        self = cls.__new__(cls)
+        self.fit = [float(f) for f in fit]
+        self.order = list(order) if order is not None else list(range(len(self.fit)))
+        self.cum, self.total, self.max, self.avg = fitness_stats(self.fit)
+        return self
 
     def roulette(self, u: float) -> int:
         """roulette_wheel (LIB/gaboom.cpp:1158-1186): a roulette position."""
-        P = len(self.cum)
-        if not self.total > 0.0:
-            return int(u * P) % P
-        r = u * self.total
-        for k, c in enumerate(self.cum):
-            if c > r:
-                return k
-        return P - 1
+        return roulette(self.cum, self.total, u)
+
+
+def niche_counts(ic, sig: float, alpha: float) -> list:
+    """PSHARE's niche count of each chromosome (LIB/gaboom.cpp:1652-1661): the sum over all j, in
+    order, of 1 - (rmsp / sig_share)^alpha for every rmsp within sig_share."""
+    P = len(ic)
+    share = []
+    for i in range(P):
+        s = 0.0
+        for j in range(P):
+            r = calc_rmsp(ic[i], ic[j])
+            if r <= sig:
+                s += 1.0 - (r / sig if alpha == 1.0 else math.pow(r / sig, alpha))
+        share.append(s)
+    return share
+
+
+def roulette(cum, total: float, u: float) -> int:
+    """roulette_wheel (LIB/gaboom.cpp:1158-1186) over running fitness sums: the first position
+    whose running sum exceeds u * total, the last if none does, a uniform position when the total
+    is not positive."""
+    P = len(cum)
+    if not total > 0.0:
+        return int(u * P) % P
+    r = u * total
+    for k, c in enumerate(cum):
+        if c > r:
+            return k
+    return P - 1
 
 
 def roulette_linear(P: int, u: float) -> int:
@@ -236,54 +296,65 @@ def pair(pop: np.ndarray, gen: int, seed: int, kk: int, cross_rate: float, mut_r
     a, b = fitness.order[pa], fitness.order[pb]
     crossp, mutp = cross_rate, mut_rate
     if adaptive:
-        f1, f2 = fitness.fit[pa], fitness.fit[pb]
-        hi, lo = max(f1, f2), min(f1, f2)
-        denom = max(fit_max - fit_avg, 1e-15)
-        crossp = k[0] * (fit_max - hi) / denom if hi > fit_avg else k[2]
-        mutp = k[1] * (fit_max - lo) / denom if lo > fit_avg else k[3]
+        crossp, mutp = adapt_prob(fit_max, fit_avg, fitness.fit[pa], fitness.fit[pb], k)
     john = [int(x) for x in u32[a]]
     mary = [int(x) for x in u32[b]]
     if draw() < crossp:
-        gen_a = min(int(draw() * ng), ng - 1)
-        gen_b = min(int(draw() * ng), ng - 1)
-        if intragenes:
-            pnt_a = int(draw() * 32.0)
-            pnt_b = int(draw() * 32.0)
-            if gen_a > gen_b:
-                gen_a, gen_b, pnt_a, pnt_b = gen_b, gen_a, pnt_b, pnt_a
-            if gen_a == gen_b and pnt_a < pnt_b:
-                pnt_a, pnt_b = pnt_b, pnt_a
-        else:
-            if gen_a > gen_b:
-                gen_a, gen_b = gen_b, gen_a
-            if gen_a != gen_b:
-                pnt_a = 32 if draw() < 0.5 else 0
-                pnt_b = 32 if draw() < 0.5 else 0
-                if gen_b - gen_a == 1 and pnt_a == 0 and pnt_b == 32:
-                    pnt_b = pnt_a
-            else:
-                pnt_a, pnt_b = 32, 0
-        for j in range(gen_a, gen_b + 1):
-            m = _mask(pnt_a if j == gen_a else 32)
-            uj, um = john[j], mary[j]
-            john[j] = (uj & ~m & 0xFFFFFFFF) | (um & m)
-            mary[j] = (uj & m) | (um & ~m & 0xFFFFFFFF)
-        if pnt_b > 0:
-            m = _mask(pnt_b - 1)
-            uj, um = john[gen_b], mary[gen_b]
-            john[gen_b] = (uj & ~m & 0xFFFFFFFF) | (um & m)
-            mary[gen_b] = (uj & m) | (um & ~m & 0xFFFFFFFF)
+        crossover(john, mary, intragenes, draw)
     for ch in (john, mary):
-        for q in range(ng):
-            # rotamer genes mutate with their side chain's probability (LIB/gaboom.cpp:944-966)
-            if prob[q] >= 0 and not draw() < prob[q]:
-                continue
-            m = 0
-            for bit in range(32):
-                if draw() < mutp:
-                    m |= 1 << bit
-            ch[q] ^= m
+        mutate(ch, mutp, draw, prob)
     return john, mary
+
+
+def crossover(john: list, mary: list, intragenes: bool, draw) -> None:
+    """crossover (LIB/gaboom.cpp:2517-2614) of two chromosomes' uint32 genes in place: two gene
+    draws, then two bit points (inside genes) or two gene-boundary choices, bits swapped between
+    the points. draw() gives the next uniform in [0, 1)."""
+    ng = len(john)
+    gen_a = min(int(draw() * ng), ng - 1)
+    gen_b = min(int(draw() * ng), ng - 1)
+    if intragenes:
+        pnt_a = int(draw() * 32.0)
+        pnt_b = int(draw() * 32.0)
+        if gen_a > gen_b:
+            gen_a, gen_b, pnt_a, pnt_b = gen_b, gen_a, pnt_b, pnt_a
+        if gen_a == gen_b and pnt_a < pnt_b:
+            pnt_a, pnt_b = pnt_b, pnt_a
+    else:
+        if gen_a > gen_b:
+            gen_a, gen_b = gen_b, gen_a
+        if gen_a != gen_b:
+            pnt_a = 32 if draw() < 0.5 else 0
+            pnt_b = 32 if draw() < 0.5 else 0
+            if gen_b - gen_a == 1 and pnt_a == 0 and pnt_b == 32:
+                pnt_b = pnt_a
+        else:
+            pnt_a, pnt_b = 32, 0
+    for j in range(gen_a, gen_b + 1):
+        m = _mask(pnt_a if j == gen_a else 32)
+        uj, um = john[j], mary[j]
+        john[j] = (uj & ~m & 0xFFFFFFFF) | (um & m)
+        mary[j] = (uj & m) | (um & ~m & 0xFFFFFFFF)
+    if pnt_b > 0:
+        m = _mask(pnt_b - 1)
+        uj, um = john[gen_b], mary[gen_b]
+        john[gen_b] = (uj & ~m & 0xFFFFFFFF) | (um & m)
+        mary[gen_b] = (uj & m) | (um & ~m & 0xFFFFFFFF)
+
+
+def mutate(ch: list, mutp: float, draw, prob=None) -> None:
+    """mutate (LIB/gaboom.cpp:2620-2641) of one chromosome's uint32 genes in place: each bit
+    flipped when its draw falls under mutp; a rotamer gene (prob[q] >= 0) only when a first draw
+    falls under its side chain's probability (LIB/gaboom.cpp:944-966)."""
+    prob = prob or [-1.0] * len(ch)
+    for q in range(len(ch)):
+        if prob[q] >= 0 and not draw() < prob[q]:
+            continue
+        m = 0
+        for bit in range(32):
+            if draw() < mutp:
+                m |= 1 << bit
+        ch[q] ^= m
 
 
 def steady(pop: np.ndarray, pop_e: np.ndarray, child: np.ndarray, child_e: np.ndarray):
@@ -318,9 +389,5 @@ def ensemble(snapshots, desc) -> np.ndarray:
     g = np.concatenate([s[0] for s in snapshots])
     e = np.concatenate([s[1] for s in snapshots])
     ic = clamped_ic(desc, g)
-    kept, last = [], None
-    for i in np.argsort(e, kind="stable"):
-        if last is None or not np.all(np.abs(ic[i] - last) < 0.1):
-            kept.append(e[i])
-            last = ic[i]
-    return np.asarray(kept)
+    order = np.argsort(e, kind="stable")
+    return np.asarray(e[order][remove_dups(ic[order])])

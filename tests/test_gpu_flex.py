@@ -23,7 +23,7 @@ def rel_err(a, b):
 
 
 def oracle_eval(d, ic, **kw):
-    port.set_reference_compat(False)
+    port.set_reference_compat(True)
     port.set_trig_rounding(False)
     return port.Oracle(d).eval_ic(ic, **kw)
 

@@ -39,7 +39,7 @@ def test_reference_precision_sweep(case):
         _density_curves()(inp, seed)
     d = prepare.prepare(inp)
     genes = synth.random_genes(3000, d.n_genes, seed=seed + 1)
-    port.set_reference_compat(False)
+    port.set_reference_compat(True)
     port.set_trig_rounding(False)
     r = port.Oracle(d).eval_ic(d.genes_to_ic(genes))["cf"]
     ev = evaluator.GPUEvaluator(d, max_poses=3000)
