@@ -15,7 +15,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # (source, extra flags): the pose build and the clustering RMSDs are evaluated without fused
 # multiply-adds, like the reference's single-precision arithmetic
 UNITS = [("fxe_build.cu", ["--fmad=false"]), ("fxe_contacts.cu", []), ("fxe_thermo.cu", []), ("fxe_ga.cu", []),
-         ("fxe_cluster.cu", ["--fmad=false"]),
+         ("fxe_cluster.cu", ["--fmad=false"]), ("fxe_ensemble.cu", []), ("fxe_prepare.cu", ["--fmad=false"]),
          ("fxe_capi.cu", []),
          # the polyhedron kernel twice: single precision, and double precision with the
          # reference's expressions and every operation rounded separately

@@ -151,4 +151,28 @@ void launch_build_jobs(const Job* jobs, int n_jobs, int total, cudaStream_t st) 
     build_kernel_jobs<<<blocks, kBuildWarps * 32, 0, st>>>(jobs, n_jobs, total);
 }
 
+// Gene decode alone (fxe_decode_genes): genetoic of every gene of n chromosomes, one thread per
+// gene, clamped into the gene limits as eval_chromosome leaves them when clamp is set.
+__global__ void decode_kernel(DevSystem S, long long n, const int32_t* __restrict__ genes, double* __restrict__ ic,
+                              int clamp) {
+    const long long total = n * S.n_genes;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        const int g = (int)(t % S.n_genes);
+        double v = S.gene_min[g] + S.gene_del[g] * (double)gene_bin(S, g, genes[t]);
+        if (clamp) {
+            if (v > S.gene_max[g]) v = S.gene_max[g];
+            else if (v < S.gene_min[g]) v = S.gene_min[g];
+        }
+        ic[t] = v;
+    }
+}
+
+void launch_decode(const DevSystem& S, long long n, const int32_t* genes, double* ic, int clamp, cudaStream_t st) {
+    const long long total = n * S.n_genes;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    if (blocks < 1) blocks = 1;
+    decode_kernel<<<(unsigned)blocks, 256, 0, st>>>(S, n, genes, ic, clamp);
+}
+
 }  // namespace fxe

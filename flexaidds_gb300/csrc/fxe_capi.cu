@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -38,6 +39,16 @@ inline size_t pose_hist_bytes() {
     return a > b ? a : b;
 }
 int cluster_blocks(int);
+size_t ensemble_scratch_bytes(long long, int);
+size_t grid_scratch_bytes(long long, long long);
+cudaError_t launch_cleft_grid(int, const float*, const long long*, const int*, const float*, long long, long long, void*,
+                              float*, long long*, cudaStream_t);
+void launch_cleft_ic(const float*, long long, const float*, float*, cudaStream_t);
+size_t cell_scratch_bytes(int, long long);
+cudaError_t launch_cell_list(const float4*, const int*, int, const float*, int, void*, int*, int*, float4*, int*,
+                             cudaStream_t);
+cudaError_t launch_ensemble(long long, int, const double*, const double*, const DevSystem*, const int32_t*, void*,
+                            long long*, double*, double*, int*, cudaStream_t);
 cudaError_t launch_cluster(const DevSystem&, const ClusterWork&, cudaStream_t);
 int thermo_blocks(long, int);
 void launch_thermo_partial(const double*, const int32_t*, long, double, LsePart*, int, cudaStream_t);
@@ -58,6 +69,31 @@ fxe_status cuda_fail(cudaError_t e, const char* what) {
     return fail(e == cudaErrorMemoryAllocation ? FXE_ERR_ALLOC : FXE_ERR_LAUNCH,
                 std::string(what) + ": " + cudaGetErrorString(e));
 }
+
+// Device buffers of one call, freed when the call returns.
+struct CallBuffers {
+    std::vector<void*> p;
+    template <typename T>
+    cudaError_t get(T** out, size_t count) {
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, count * sizeof(T) + 16);
+        if (e == cudaSuccess) {
+            p.push_back(q);
+            *out = reinterpret_cast<T*>(q);
+        }
+        return e;
+    }
+    template <typename T>
+    cudaError_t put(T** out, const T* src, size_t count) {
+        cudaError_t e = get(out, count);
+        if (e == cudaSuccess && count) e = cudaMemcpy(*out, src, count * sizeof(T), cudaMemcpyHostToDevice);
+        return e;
+    }
+    ~CallBuffers() {
+        for (void* q : p) cudaFree(q);
+    }
+};
+
 
 }  // namespace
 
@@ -81,8 +117,7 @@ struct fxe_context {
     std::shared_ptr<DevBlock> receptor = std::make_shared<DevBlock>();
     int rec_type_max = 0;             // largest receptor atom type (checked against each matrix)
     // host copies of the gene limits and genetoic tables (decoding snapshots on the host)
-    std::vector<double> h_gmin, h_gmax, h_gdel, h_dtab;
-    std::vector<int> h_doff;
+    std::vector<double> h_gmin, h_gmax, h_gdel;
     const void* rec_key = nullptr;    // identity of the receptor block (contexts sharing it)
     int32_t* d_genes = nullptr;
     double* d_icin = nullptr;
@@ -323,31 +358,35 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
             FXE_TRY(ctx->upload_receptor(&S.flex_bond_off, bond_off.data(), bond_off.size()), "side-chain upload");
             FXE_TRY(ctx->upload_receptor(&S.flex_bonded, fbonded.data(), fbonded.size()), "side-chain upload");
         }
-        const int dim = S.dim, dim2 = dim * dim;
-        const long dim3 = (long)dim2 * dim;
-        std::vector<int> cell(N), start(dim3 + 1, 0);
-        for (int i = 0; i < N; ++i) {
-            if (rec_mob[i] >= 0) continue;
-            const long bi = (long)(int)((pos[i].x - S.gmin[0]) / fxe::kCell) * dim2 +
-                            (long)(int)((pos[i].y - S.gmin[1]) / fxe::kCell) * dim +
-                            (int)((pos[i].z - S.gmin[2]) / fxe::kCell);
-            if (bi < 0 || bi >= dim3) return fail(FXE_ERR_INVALID_ARGS, "receptor atom outside its own cell grid");
-            cell[i] = (int)bi;
-            ++start[bi + 1];
-        }
-        for (long b = 0; b < dim3; ++b) start[b + 1] += start[b];
+        // the steady cell list of the rigid atoms, built on the device (fxe_prepare.cu)
+        const int dim = S.dim;
+        const long long dim3 = (long long)dim * dim * dim;
         const int n_rigid = N - S.n_sc;
-        std::vector<int> fill(start.begin(), start.end() - 1), catom(n_rigid);
-        std::vector<float4> cpos(n_rigid);
-        for (int i = 0; i < N; ++i) {
-            if (rec_mob[i] >= 0) continue;
-            const int w = fill[cell[i]]++;
-            catom[w] = i;
-            cpos[w] = pos[i];
+        {
+            int *d_catom = nullptr, *d_mob = nullptr;
+            float4* d_cpos = nullptr;
+            CallBuffers cb;
+            unsigned char* scratch = nullptr;
+            FXE_TRY(cb.get(&scratch, fxe::cell_scratch_bytes(N, dim3)), "cell list scratch");
+            if (S.n_sc) FXE_TRY(cb.put(&d_mob, rec_mob.data(), (size_t)N), "cell list");
+            void* q = nullptr;
+            FXE_TRY(cudaMalloc(&q, (size_t)(n_rigid > 0 ? n_rigid : 1) * sizeof(int) + 16), "cell list");
+            ctx->receptor->ptrs.push_back(q);
+            d_catom = static_cast<int*>(q);
+            FXE_TRY(cudaMalloc(&q, (size_t)(n_rigid > 0 ? n_rigid : 1) * sizeof(float4) + 16), "cell list");
+            ctx->receptor->ptrs.push_back(q);
+            d_cpos = static_cast<float4*>(q);
+            FXE_TRY(cudaMalloc(&q, ((size_t)dim3 + 1) * sizeof(int) + 16), "cell list");
+            ctx->receptor->ptrs.push_back(q);
+            int* d_start_keep = static_cast<int*>(q);
+            int bad = 0;
+            FXE_TRY(fxe::launch_cell_list(S.rec_pos, d_mob, N, S.gmin, dim, scratch, d_start_keep, d_catom, d_cpos, &bad,
+                                          ctx->stream), "cell list build");
+            if (bad) return fail(FXE_ERR_INVALID_ARGS, "receptor atom outside its own cell grid");
+            S.cell_start = d_start_keep;
+            S.cell_atom = d_catom;
+            S.cell_pos = d_cpos;
         }
-        FXE_TRY(ctx->upload_receptor(&S.cell_start, start.data(), dim3 + 1), "cell list upload");
-        FXE_TRY(ctx->upload_receptor(&S.cell_atom, catom.data(), n_rigid), "cell list upload");
-        FXE_TRY(ctx->upload_receptor(&S.cell_pos, cpos.data(), n_rigid), "cell list upload");
         // cleft grid
         std::vector<float4> gic(rec->n_grid);
         for (int g = 0; g < rec->n_grid; ++g)
@@ -440,8 +479,6 @@ fxe_status context_create(const fxe_receptor_desc* rec, const fxe_context* share
         ctx->h_gmin.assign(lig->gene_min, lig->gene_min + ng);
         ctx->h_gmax.assign(lig->gene_max, lig->gene_max + ng);
         ctx->h_gdel.assign(lig->gene_del, lig->gene_del + ng);
-        ctx->h_dtab = dtab;
-        ctx->h_doff = doff;
         {
             // which gene sets each atom's angle and dihedral last, and through which cascade
             // (the IC assignment of ic2cf, LIB/ic2cf.cpp:53-105, replayed symbolically)
@@ -788,31 +825,35 @@ extern "C" void fxe_context_destroy(fxe_context* ctx) { delete ctx; }
 
 namespace {
 
+// Block partials of the reduction, one buffer per device (a call reduces on the current device).
+// Calls hold the lock until their partials are back on the host.
 struct ThermoScratch {
-    std::mutex mu;
     fxe::LsePart* part = nullptr;
     int cap = 0;
 };
-ThermoScratch g_thermo;
+std::mutex g_thermo_mu;
+std::map<int, ThermoScratch> g_thermo;
 
 fxe_status thermo_run(const double* d_e, const int32_t* d_m, long n, double T, fxe_thermo* out,
                       double* d_w, cudaStream_t s) {
     int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    FXE_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+    FXE_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
     const int nb = fxe::thermo_blocks(n, sms);
-    std::lock_guard<std::mutex> lk(g_thermo.mu);
-    if (g_thermo.cap < nb) {
-        if (g_thermo.part) cudaFree(g_thermo.part);
-        g_thermo.part = nullptr;
-        FXE_TRY(cudaMalloc(&g_thermo.part, nb * sizeof(fxe::LsePart)), "thermo scratch");
-        g_thermo.cap = nb;
+    std::lock_guard<std::mutex> lk(g_thermo_mu);
+    ThermoScratch& sc = g_thermo[dev];
+    if (sc.cap < nb) {
+        if (sc.part) cudaFree(sc.part);
+        sc.part = nullptr;
+        sc.cap = 0;
+        FXE_TRY(cudaMalloc(&sc.part, nb * sizeof(fxe::LsePart)), "thermo scratch");
+        sc.cap = nb;
     }
     const double beta = 1.0 / (0.001987206 * T);
-    fxe::launch_thermo_partial(d_e, d_m, n, beta, g_thermo.part, nb, s);
+    fxe::launch_thermo_partial(d_e, d_m, n, beta, sc.part, nb, s);
     FXE_TRY(cudaGetLastError(), "thermo launch");
     std::vector<fxe::LsePart> part(nb);
-    FXE_TRY(cudaMemcpyAsync(part.data(), g_thermo.part, nb * sizeof(fxe::LsePart), cudaMemcpyDeviceToHost, s), "thermo");
+    FXE_TRY(cudaMemcpyAsync(part.data(), sc.part, nb * sizeof(fxe::LsePart), cudaMemcpyDeviceToHost, s), "thermo");
     FXE_TRY(cudaStreamSynchronize(s), "thermo");
     fxe_thermo th;
     fxe::thermo_finish(part.data(), nb, T, &th);
@@ -1683,49 +1724,33 @@ extern "C" fxe_status fxe_ga_finished(fxe_ga* e, int32_t* slots, int32_t cap, in
 }
 
 namespace {
-// genetoic on the host (LIB/gaboom.cpp:2887-2906): the first running bin total at or above u.
-double host_genetoic(const fxe_context* ctx, int g, int32_t gene) {
-    const double u = gene / (2147483647.0 + 1.0);
-    const double* lo = ctx->h_dtab.data() + ctx->h_doff[g];
-    const double* hi = ctx->h_dtab.data() + ctx->h_doff[g + 1];
-    const double* it = std::lower_bound(lo, hi, u);
-    // the IC as eval_chromosome leaves it in the gene, clamped (LIB/gaboom.cpp:1851-1859)
-    const double v = ctx->h_gmin[g] + ctx->h_gdel[g] * (double)(it - lo);
-    return v > ctx->h_gmax[g] ? ctx->h_gmax[g] : (v < ctx->h_gmin[g] ? ctx->h_gmin[g] : v);
-}
-
-// The ensemble of a job as the reference's GA assembles it (LIB/gaboom.cpp:520-540): every
-// generation's population, sorted by energy, chromosomes within 0.1 of the last one kept on every
-// decoded gene dropped (remove_dups, :2728-2747); ties in energy in snapshot order. The kept
-// chromosomes' decoded ICs (clamped as eval_chromosome leaves them) go to *ic when set.
-fxe_status ga_ensemble(const GaSlot& s, const fxe::GaJob& J, std::vector<double>* ic, std::vector<double>* kept_e) {
+// The ensemble of a job as the reference's GA assembles it (LIB/gaboom.cpp:520-540), on the
+// device (fxe_ensemble.cu): every generation's population, sorted by energy (ties in snapshot
+// order), chromosomes within 0.1 of the last one kept on every decoded gene dropped (remove_dups,
+// :2728-2747). Leaves the kept energies (energy order) in *d_e and, when want_ic, their decoded
+// ICs (clamped as eval_chromosome leaves them) in *d_ic; both are freed with `bufs`.
+fxe_status ga_ensemble(const GaSlot& s, const fxe::GaJob& J, cudaStream_t st, bool want_ic, CallBuffers& bufs,
+                       double** d_e, double** d_ic, int64_t* n_kept) {
     const int P = s.job.population, ng = s.ctx->S.n_genes, G = s.job.generations;
-    const size_t N = (size_t)G * P;
-    std::vector<int32_t> sg(N * ng);
-    std::vector<double> se(N);
-    if (N) {
-        FXE_TRY(cudaMemcpy(sg.data(), J.snap, sizeof(int32_t) * N * ng, cudaMemcpyDeviceToHost), "GA snapshots");
-        FXE_TRY(cudaMemcpy(se.data(), J.snap_e, sizeof(double) * N, cudaMemcpyDeviceToHost), "GA snapshots");
-    }
-    std::vector<size_t> ord(N);
-    for (size_t i = 0; i < N; ++i) ord[i] = i;
-    std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return se[a] < se[b]; });
-    std::vector<double> last(ng), cur(ng);
-    bool have = false;
-    kept_e->clear();
-    if (ic) ic->clear();
-    for (size_t i : ord) {
-        for (int g = 0; g < ng; ++g) cur[g] = host_genetoic(s.ctx, g, sg[i * ng + g]);
-        int same = 0;
-        if (have)
-            for (int g = 0; g < ng; ++g) same += std::fabs(cur[g] - last[g]) < 0.1;
-        if (!have || same != ng) {
-            kept_e->push_back(se[i]);
-            if (ic) ic->insert(ic->end(), cur.begin(), cur.end());
-            last = cur;
-            have = true;
-        }
-    }
+    const long long N = (long long)G * P;
+    if (N >= (1ll << 31)) return fail(FXE_ERR_CAPACITY, "ensemble larger than 2^31 chromosomes");
+    *n_kept = 0;
+    *d_e = nullptr;
+    if (d_ic) *d_ic = nullptr;
+    if (N == 0) return FXE_OK;
+    void* scratch = nullptr;
+    int* d_cnt = nullptr;
+    FXE_TRY(bufs.get(reinterpret_cast<unsigned char**>(&scratch), fxe::ensemble_scratch_bytes(N, ng)), "ensemble scratch");
+    FXE_TRY(bufs.get(d_e, (size_t)N), "ensemble output");
+    if (want_ic) FXE_TRY(bufs.get(d_ic, (size_t)N * ng), "ensemble output");
+    FXE_TRY(bufs.get(&d_cnt, 1), "ensemble output");
+    FXE_TRY(fxe::launch_ensemble(N, ng, J.snap_e, nullptr, &s.ctx->S, J.snap, scratch, nullptr, *d_e,
+                                 want_ic ? *d_ic : nullptr, d_cnt, st), "ensemble launch");
+    int cnt = 0;
+    FXE_TRY(cudaMemcpyAsync(&cnt, d_cnt, sizeof(int), cudaMemcpyDeviceToHost, st), "ensemble size");
+    FXE_TRY(cudaStreamSynchronize(st), "ensemble");
+    if (cnt < 0 || cnt > N) return fail(FXE_ERR_INTERNAL, "ensemble size out of range");
+    *n_kept = cnt;
     return FXE_OK;
 }
 
@@ -1745,13 +1770,16 @@ extern "C" fxe_status fxe_ga_collect(fxe_ga* e, int32_t slot, double temperature
     if (best_genes) FXE_TRY(cudaMemcpy(best_genes, J.pop, sizeof(int32_t) * ng, cudaMemcpyDeviceToHost), "GA result");
     if (best_energy) FXE_TRY(cudaMemcpy(best_energy, J.pop_e, sizeof(double), cudaMemcpyDeviceToHost), "GA result");
     if (thermo || n_ensemble) {
-        std::vector<double> kept_e;
-        fxe_status st = ga_ensemble(s, J, nullptr, &kept_e);
+        CallBuffers bufs;
+        double* d_e = nullptr;
+        int64_t nk = 0;
+        fxe_status st = ga_ensemble(s, J, e->stream, false, bufs, &d_e, nullptr, &nk);
         if (st != FXE_OK) return st;
-        if (n_ensemble) *n_ensemble = (int64_t)kept_e.size();
+        if (n_ensemble) *n_ensemble = nk;
         if (thermo) {
-            if (kept_e.empty()) return fail(FXE_ERR_INVALID_ARGS, "the job ran no generation: empty ensemble");
-            st = thermo_host(kept_e.data(), nullptr, (int64_t)kept_e.size(), temperature, thermo, nullptr);
+            if (nk == 0) return fail(FXE_ERR_INVALID_ARGS, "the job ran no generation: empty ensemble");
+            if (!(temperature > 0.0)) return fail(FXE_ERR_INVALID_ARGS, "temperature must be positive");
+            st = thermo_run(d_e, nullptr, (long)nk, temperature, thermo, nullptr, e->stream);
             if (st != FXE_OK) return st;
         }
     }
@@ -1770,14 +1798,18 @@ extern "C" fxe_status fxe_ga_ensemble(fxe_ga* e, int32_t slot, int64_t cap, doub
     FXE_TRY(cudaStreamSynchronize(e->stream), "GA step");
     fxe::GaJob J;
     FXE_TRY(cudaMemcpy(&J, e->d_all + slot, sizeof(J), cudaMemcpyDeviceToHost), "GA state");
-    std::vector<double> kic, ke;
-    fxe_status st = ga_ensemble(s, J, ic ? &kic : nullptr, &ke);
+    CallBuffers bufs;
+    double *d_e = nullptr, *d_ic = nullptr;
+    fxe_status st = ga_ensemble(s, J, e->stream, ic != nullptr, bufs, &d_e, &d_ic, n);
     if (st != FXE_OK) return st;
-    *n = (int64_t)ke.size();
     if (!ic && !energies) return FXE_OK;
     if (cap < *n) return fail(FXE_ERR_CAPACITY, "the ensemble holds more chromosomes than cap");
-    if (ic) std::copy(kic.begin(), kic.end(), ic);
-    if (energies) std::copy(ke.begin(), ke.end(), energies);
+    const int ng = s.ctx->S.n_genes;
+    if (*n > 0) {
+        if (ic) FXE_TRY(cudaMemcpyAsync(ic, d_ic, sizeof(double) * (size_t)*n * ng, cudaMemcpyDeviceToHost, e->stream), "ensemble ICs");
+        if (energies) FXE_TRY(cudaMemcpyAsync(energies, d_e, sizeof(double) * (size_t)*n, cudaMemcpyDeviceToHost, e->stream), "ensemble energies");
+        FXE_TRY(cudaStreamSynchronize(e->stream), "ensemble");
+    }
     return FXE_OK;
 }
 
@@ -1813,5 +1845,252 @@ extern "C" fxe_status fxe_ga_population(fxe_ga* e, int32_t slot, int32_t* genes,
     const int P = s.job.population, ng = s.ctx->S.n_genes;
     if (genes) FXE_TRY(cudaMemcpy(genes, J.pop, sizeof(int32_t) * P * ng, cudaMemcpyDeviceToHost), "GA population");
     if (energies) FXE_TRY(cudaMemcpy(energies, J.pop_e, sizeof(double) * P, cudaMemcpyDeviceToHost), "GA population");
+    return FXE_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// The GA operators and the gene decoder on caller-given inputs.
+// ------------------------------------------------------------------------------------------
+namespace fxe {
+void launch_decode(const DevSystem&, long long, const int32_t*, double*, int, cudaStream_t);
+void launch_ga_breed_draws(const GaJob*, const double*, long long, int, int*, cudaStream_t);
+void launch_ga_niche(const GaJob*, const int*, cudaStream_t);
+}  // namespace fxe
+
+
+extern "C" fxe_status fxe_decode_genes(fxe_context* ctx, int64_t n, const int32_t* genes, int32_t clamp, double* ic) {
+    g_err.clear();
+    if (!ctx || n < 0 || (n > 0 && (!genes || !ic))) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    if (n == 0 || ctx->S.n_genes == 0) return FXE_OK;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
+    const size_t cnt = (size_t)n * ctx->S.n_genes;
+    CallBuffers b;
+    int32_t* d_g = nullptr;
+    double* d_ic = nullptr;
+    FXE_TRY(b.put(&d_g, genes, cnt), "genes to device");
+    FXE_TRY(b.get(&d_ic, cnt), "decode buffer");
+    fxe::launch_decode(ctx->S, n, d_g, d_ic, clamp ? 1 : 0, ctx->stream);
+    FXE_TRY(cudaGetLastError(), "decode launch");
+    FXE_TRY(cudaMemcpyAsync(ic, d_ic, cnt * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "ICs to host");
+    FXE_TRY(cudaStreamSynchronize(ctx->stream), "decode");
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_ga_breed_draws(int32_t population, int32_t n_genes, const int32_t* pop,
+                                         const double* fitness, const int32_t* order, const float* gene_prob,
+                                         double cross_rate, double mut_rate, int32_t intragenes, int32_t adaptive,
+                                         const double* k4, int32_t n_pairs, const double* draws, int32_t* children,
+                                         int32_t* draws_used, double* fit_stats) {
+    g_err.clear();
+    const int P = population, ng = n_genes;
+    if (P < 1 || ng < 1 || ng > 1024 || n_pairs < 0 || !pop || !fitness || (n_pairs > 0 && (!draws || !children)) ||
+        (adaptive && !k4))
+        return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    std::vector<int32_t> ord(P);
+    for (int i = 0; i < P; ++i) {
+        ord[i] = order ? order[i] : i;
+        if (ord[i] < 0 || ord[i] >= P) return fail(FXE_ERR_INVALID_ARGS, "order names no chromosome");
+    }
+    std::vector<float> prob(ng, -1.0f);
+    if (gene_prob)
+        for (int q = 0; q < ng; ++q) prob[q] = gene_prob[q];
+    int dc = 0;
+    if (cudaGetDeviceCount(&dc) != cudaSuccess || dc == 0) return fail(FXE_ERR_NO_DEVICE, "no CUDA device");
+    const long long stride = FXE_GA_DRAWS_PER_PAIR(ng);
+    CallBuffers b;
+    fxe::GaJob J{};
+    J.P = P;
+    J.ng = ng;
+    J.cross_rate = cross_rate;
+    J.mut_rate = mut_rate;
+    J.intragenes = intragenes ? 1 : 0;
+    J.adaptive = adaptive ? 1 : 0;
+    for (int i = 0; i < 4; ++i) J.k[i] = adaptive ? k4[i] : 0.0;
+    const int np = n_pairs > 0 ? n_pairs : 1;
+    int32_t* d_pop = nullptr;
+    double* d_fit = nullptr;
+    int* d_ord = nullptr;
+    float* d_prob = nullptr;
+    FXE_TRY(b.put(&d_pop, pop, (size_t)P * ng), "GA buffers");
+    FXE_TRY(b.put(&d_fit, fitness, (size_t)P), "GA buffers");
+    FXE_TRY(b.put(&d_ord, ord.data(), (size_t)P), "GA buffers");
+    FXE_TRY(b.put(&d_prob, prob.data(), (size_t)ng), "GA buffers");
+    J.pop = d_pop;
+    J.fit = d_fit;
+    J.ford = d_ord;
+    J.gene_prob = d_prob;
+    FXE_TRY(b.get(&J.fcum, (size_t)P), "GA buffers");
+    FXE_TRY(b.get(&J.fstat, 4), "GA buffers");
+    FXE_TRY(b.get(&J.child, (size_t)2 * np * ng), "GA buffers");
+    double* d_draws = nullptr;
+    int* d_used = nullptr;
+    FXE_TRY(b.get(&d_used, (size_t)np), "GA buffers");
+    if (n_pairs > 0) FXE_TRY(b.put(&d_draws, draws, (size_t)n_pairs * stride), "draws to device");
+    fxe::GaJob* d_J = nullptr;
+    FXE_TRY(b.put(&d_J, &J, 1), "GA state");
+    fxe::launch_ga_breed_draws(d_J, d_draws, stride, n_pairs, d_used, nullptr);
+    FXE_TRY(cudaGetLastError(), "GA launch");
+    FXE_TRY(cudaDeviceSynchronize(), "GA breeding");
+    if (n_pairs > 0) {
+        FXE_TRY(cudaMemcpy(children, J.child, sizeof(int32_t) * 2 * (size_t)n_pairs * ng, cudaMemcpyDeviceToHost),
+                "children to host");
+        std::vector<int> used(n_pairs);
+        FXE_TRY(cudaMemcpy(used.data(), d_used, sizeof(int) * n_pairs, cudaMemcpyDeviceToHost), "draw counts");
+        for (int k = 0; k < n_pairs; ++k) {
+            if (used[k] < 0) return fail(FXE_ERR_INVALID_ARGS, "pair " + std::to_string(k) + " needed more draws than a row holds");
+            if (draws_used) draws_used[k] = used[k];
+        }
+    }
+    if (fit_stats) {
+        double st[4];
+        FXE_TRY(cudaMemcpy(st, J.fstat, sizeof(st), cudaMemcpyDeviceToHost), "fitness stats");
+        fit_stats[0] = st[0];
+        fit_stats[1] = st[1];
+        fit_stats[2] = st[2];
+    }
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_ga_niche_counts(int32_t population, int32_t n_genes, const double* ic, double sig_share,
+                                          double alpha, double* share) {
+    g_err.clear();
+    const int P = population, ng = n_genes;
+    if (P < 1 || P > 2048 || ng < 1 || !ic || !share || !(sig_share > 0.0))
+        return fail(FXE_ERR_INVALID_ARGS, "invalid arguments (population 1..2048, sig_share > 0)");
+    int dc = 0;
+    if (cudaGetDeviceCount(&dc) != cudaSuccess || dc == 0) return fail(FXE_ERR_NO_DEVICE, "no CUDA device");
+    CallBuffers b;
+    fxe::GaJob J{};
+    J.P = P;
+    J.ng = ng;
+    J.fitness = fxe::kFitPshare;
+    J.sig_share = sig_share;
+    J.share_alpha = alpha;
+    double* d_ic = nullptr;
+    FXE_TRY(b.put(&d_ic, ic, (size_t)P * ng), "ICs to device");
+    J.pic = d_ic;
+    FXE_TRY(b.get(&J.share, (size_t)P), "niche buffer");
+    fxe::GaJob* d_J = nullptr;
+    FXE_TRY(b.put(&d_J, &J, 1), "GA state");
+    const int zero = 0;
+    int* d_run = nullptr;
+    FXE_TRY(b.put(&d_run, &zero, 1), "GA state");
+    fxe::launch_ga_niche(d_J, d_run, nullptr);
+    FXE_TRY(cudaGetLastError(), "niche launch");
+    FXE_TRY(cudaDeviceSynchronize(), "niche counts");
+    FXE_TRY(cudaMemcpy(share, J.share, sizeof(double) * P, cudaMemcpyDeviceToHost), "niche counts to host");
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_ensemble_dedup(int64_t n, int32_t n_genes, const double* ic, const double* energies,
+                                         int64_t* kept_index, double* kept_energy, int64_t* n_kept) {
+    g_err.clear();
+    if (n < 0 || n >= ((int64_t)1 << 31) || n_genes < 1 || !n_kept || (n > 0 && (!ic || !energies)))
+        return fail(FXE_ERR_INVALID_ARGS, "invalid arguments (0 <= n < 2^31, n_genes >= 1)");
+    *n_kept = 0;
+    if (n == 0) return FXE_OK;
+    int dc = 0;
+    if (cudaGetDeviceCount(&dc) != cudaSuccess || dc == 0) return fail(FXE_ERR_NO_DEVICE, "no CUDA device");
+    CallBuffers b;
+    double *d_ic = nullptr, *d_e = nullptr, *d_eo = nullptr;
+    long long* d_idx = nullptr;
+    unsigned char* scratch = nullptr;
+    int* d_cnt = nullptr;
+    FXE_TRY(b.put(&d_ic, ic, (size_t)n * n_genes), "ensemble input");
+    FXE_TRY(b.put(&d_e, energies, (size_t)n), "ensemble input");
+    FXE_TRY(b.get(&d_eo, (size_t)n), "ensemble output");
+    FXE_TRY(b.get(&d_idx, (size_t)n), "ensemble output");
+    FXE_TRY(b.get(&d_cnt, 1), "ensemble output");
+    FXE_TRY(b.get(&scratch, fxe::ensemble_scratch_bytes(n, n_genes)), "ensemble scratch");
+    FXE_TRY(fxe::launch_ensemble(n, n_genes, d_e, d_ic, nullptr, nullptr, scratch, d_idx, d_eo, nullptr, d_cnt, nullptr),
+            "ensemble launch");
+    int cnt = 0;
+    FXE_TRY(cudaMemcpy(&cnt, d_cnt, sizeof(int), cudaMemcpyDeviceToHost), "ensemble size");
+    if (cnt < 0 || cnt > n) return fail(FXE_ERR_INTERNAL, "ensemble size out of range");
+    *n_kept = cnt;
+    if (cnt > 0 && kept_index) {
+        std::vector<long long> idx(cnt);
+        FXE_TRY(cudaMemcpy(idx.data(), d_idx, sizeof(long long) * cnt, cudaMemcpyDeviceToHost), "kept indices");
+        for (int i = 0; i < cnt; ++i) kept_index[i] = idx[i];
+    }
+    if (cnt > 0 && kept_energy) FXE_TRY(cudaMemcpy(kept_energy, d_eo, sizeof(double) * cnt, cudaMemcpyDeviceToHost), "kept energies");
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_cleft_grid(int32_t n_spheres, const float* centers, const float* radii, float spacing,
+                                     const float* ori, int64_t cap, float* xyz, float* ic, int64_t* n_points) {
+    g_err.clear();
+    if (n_spheres < 1 || !centers || !radii || !ori || !n_points || !(spacing > 0.0f) || cap < 0 ||
+        (cap > 0 && !xyz))
+        return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    *n_points = 0;
+    // the lattice of each sphere as generate_grid walks it (LIB/generate_grid.cpp:34-95), in float
+    const bool fractional = (float)(1.0 / spacing) - (float)((int)(1.0 / spacing)) > 0.001;
+    std::vector<float> axes, sph;
+    std::vector<long long> off;
+    std::vector<int> dims;
+    long long max_lattice = 0, total = 0;
+    for (int s = 0; s < n_spheres; ++s) {
+        const float r = radii[s];
+        if (!(r > 0.0f) || r > 1000.0f) return fail(FXE_ERR_INVALID_ARGS, "sphere radius outside (0, 1000] A");
+        off.push_back((long long)axes.size());
+        int n3[3];
+        for (int k = 0; k < 3; ++k) {
+            const float c = centers[3 * s + k];
+            if (!(c > -1000.0f && c < 1000.0f)) return fail(FXE_ERR_INVALID_ARGS, "sphere centre outside +-1000 A");
+            float mn, mx;
+            if (fractional) {
+                mn = (float)((int)((c - r) / spacing)) * spacing;
+                mx = (float)((int)((c + r) / spacing) + 1.0) * spacing;
+            } else {
+                mn = (float)((int)(c - r - spacing));
+                mx = (float)((int)(c + r + spacing) + 1.0);
+            }
+            int n = 0;
+            for (float v = mn; v < mx; v += spacing) {
+                axes.push_back(v);
+                if (++n > (1 << 20)) return fail(FXE_ERR_INVALID_ARGS, "lattice too large");
+            }
+            n3[k] = n;
+        }
+        dims.insert(dims.end(), n3, n3 + 3);
+        sph.insert(sph.end(), {centers[3 * s], centers[3 * s + 1], centers[3 * s + 2], r * r});
+        const long long lat = (long long)n3[0] * n3[1] * n3[2];
+        if (lat >= (1ll << 31)) return fail(FXE_ERR_INVALID_ARGS, "lattice too large");
+        max_lattice = lat > max_lattice ? lat : max_lattice;
+        total += lat;
+    }
+    int dc = 0;
+    if (cudaGetDeviceCount(&dc) != cudaSuccess || dc == 0) return fail(FXE_ERR_NO_DEVICE, "no CUDA device");
+    long long slots = 1024;
+    while (slots < 2 * total) slots <<= 1;
+    CallBuffers b;
+    float *d_axes = nullptr, *d_xyz = nullptr, *d_ic = nullptr;
+    unsigned char* scratch = nullptr;
+    FXE_TRY(b.put(&d_axes, axes.data(), axes.size()), "grid axes");
+    FXE_TRY(b.get(&d_xyz, (size_t)3 * (total > 0 ? total : 1)), "grid points");
+    FXE_TRY(b.get(&scratch, fxe::grid_scratch_bytes(max_lattice, slots)), "grid scratch");
+    cudaStream_t st = nullptr;
+    FXE_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
+    long long n = 0;
+    cudaError_t e = fxe::launch_cleft_grid(n_spheres, d_axes, off.data(), dims.data(), sph.data(), max_lattice, slots,
+                                           scratch, d_xyz, &n, st);
+    if (e == cudaSuccess && n > 0 && ic) {
+        e = cudaMalloc(reinterpret_cast<void**>(&d_ic), (size_t)3 * n * sizeof(float) + 16);
+        if (e == cudaSuccess) {
+            b.p.push_back(d_ic);
+            fxe::launch_cleft_ic(d_xyz, n, ori, d_ic, st);
+            e = cudaGetLastError();
+        }
+    }
+    if (e == cudaSuccess && n > 0 && n <= cap) {
+        e = cudaMemcpyAsync(xyz, d_xyz, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && ic) e = cudaMemcpyAsync(ic, d_ic, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    if (e != cudaSuccess) return cuda_fail(e, "cleft grid");
+    *n_points = n;
+    if (n > cap) return fail(FXE_ERR_CAPACITY, "the grid holds more points than cap");
     return FXE_OK;
 }

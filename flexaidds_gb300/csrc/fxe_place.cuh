@@ -75,6 +75,19 @@ __device__ __forceinline__ void build_trig(const DevSystem& S, const BuildShared
     trig_of(S, l, c, sh.gi, (src >= 0 && src < 64) ? sh.gbin[src] : -1, deg, cs, sn);
 }
 
+// genetoic's bin (LIB/gaboom.cpp:2887-2906) of gene value `gene` of gene g: the first running bin
+// total at or above RandomDouble(gene), found by binary search in the totals the host precomputes.
+__device__ __forceinline__ int gene_bin(const DevSystem& S, int g, int32_t gene) {
+    const double u = gene / (2147483647.0 + 1.0);
+    int lo = S.dec_off[g], hi = S.dec_off[g + 1];
+    const int base = lo;
+    while (lo < hi) {  // first entry >= u
+        const int mid = (lo + hi) >> 1;
+        if (S.dec_tab[mid] < u) lo = mid + 1; else hi = mid;
+    }
+    return lo - base;
+}
+
 // Step 1: genes -> ICs (genetoic, LIB/gaboom.cpp:2887-2906, as a binary search in the running bin
 // totals the host precomputes) or ICs as given, then the clamp of eval_chromosome
 // (LIB/gaboom.cpp:1845-1866) when `clamp`. The values go to sh.icv (genes < 64) and, when ic_out
@@ -86,15 +99,9 @@ __device__ __forceinline__ void decode_ics(const DevSystem& S, int p, const int3
     for (int g = lane; g < ng; g += 32) {
         double v;
         if (genes) {
-            const double u = genes[(size_t)p * ng + g] / (2147483647.0 + 1.0);
-            int lo = S.dec_off[g], hi = S.dec_off[g + 1];
-            const int base = lo;
-            while (lo < hi) {  // first entry >= u
-                const int mid = (lo + hi) >> 1;
-                if (S.dec_tab[mid] < u) lo = mid + 1; else hi = mid;
-            }
-            v = S.gene_min[g] + S.gene_del[g] * (double)(lo - base);
-            if (g < 64) sh.gbin[g] = lo - base;
+            const int bin = gene_bin(S, g, genes[(size_t)p * ng + g]);
+            v = S.gene_min[g] + S.gene_del[g] * (double)bin;
+            if (g < 64) sh.gbin[g] = bin;
         } else {
             v = ic_in[(size_t)p * ng + g];
             // the bin this value would come from; the table entry is used only if its angle matches

@@ -74,6 +74,13 @@ def load_library():
         lib.fxe_cluster.argtypes = [vp, C.c_int64, _d, _d, C.c_int32, C.c_float, C.c_int32, _i, _i, _d, _d,
                                     _i, _f, _f, _i]
         lib.fxe_last_cluster_time.argtypes = [vp, _d]
+        lib.fxe_decode_genes.argtypes = [vp, C.c_int64, _i, C.c_int32, _d]
+        lib.fxe_ga_breed_draws.argtypes = [C.c_int32, C.c_int32, _i, _d, _i, _f, C.c_double, C.c_double,
+                                           C.c_int32, C.c_int32, _d, C.c_int32, _d, _i, _i, _d]
+        lib.fxe_ga_niche_counts.argtypes = [C.c_int32, C.c_int32, _d, C.c_double, C.c_double, _d]
+        lib.fxe_ensemble_dedup.argtypes = [C.c_int64, C.c_int32, _d, _d, C.POINTER(C.c_int64), _d,
+                                           C.POINTER(C.c_int64)]
+        lib.fxe_cleft_grid.argtypes = [C.c_int32, _f, _f, C.c_float, _f, C.c_int64, _f, _f, C.POINTER(C.c_int64)]
         lib.fxe_context_destroy.argtypes = [vp]
         lib.fxe_context_destroy.restype = None
         lib.fxe_last_error.restype = C.c_char_p
@@ -199,6 +206,13 @@ class GPUEvaluator:
         ms = np.zeros(1, np.float64)
         _check(self.lib.fxe_last_cluster_time(self.handle, ptr(ms, _d)))
         return float(ms[0])
+
+    def decode_genes(self, genes: np.ndarray, clamp: bool = False) -> np.ndarray:
+        """genetoic of every gene on the device (fxe_decode_genes); clamp as eval_chromosome."""
+        genes = np.ascontiguousarray(genes, np.int32).reshape(-1, self.desc.n_genes)
+        out = np.empty(genes.shape, np.float64)
+        _check(self.lib.fxe_decode_genes(self.handle, genes.shape[0], ptr(genes, _i), int(bool(clamp)), ptr(out, _d)))
+        return out
 
     def stats(self) -> dict:
         o = np.zeros(4, np.int32)
@@ -371,6 +385,80 @@ class GAEngine:
             self.close()
         except Exception:
             pass
+
+
+def ga_draws_per_pair(n_genes: int) -> int:
+    """FXE_GA_DRAWS_PER_PAIR: the length of one pair's row of draws."""
+    return 7 + 2 * int(n_genes) * 33
+
+
+def ga_breed_draws(pop, fitness, draws, cross_rate, mut_rate, order=None, gene_prob=None,
+                   intragenes=False, adaptive=False, k=(1.0, 0.5, 1.0, 0.5)) -> dict:
+    """The GA engine's breeding on the device with the caller's draws (fxe_ga_breed_draws):
+    draws is (n_pairs, ga_draws_per_pair(ng)). Returns children (2 n_pairs, ng) as uint32,
+    draws used per pair and fitness_stats (total, max, mean)."""
+    lib = load_library()
+    pop = np.ascontiguousarray(np.asarray(pop, np.int64).astype(np.uint32).astype(np.int32))
+    P, ng = pop.shape
+    fit = np.ascontiguousarray(fitness, np.float64)
+    draws = np.ascontiguousarray(draws, np.float64).reshape(-1, ga_draws_per_pair(ng))
+    n_pairs = draws.shape[0]
+    ordr = None if order is None else np.ascontiguousarray(order, np.int32)
+    prob = None if gene_prob is None else np.ascontiguousarray(gene_prob, np.float32)
+    kk = np.ascontiguousarray(k, np.float64)
+    children = np.zeros((2 * max(n_pairs, 1), ng), np.int32)
+    used = np.zeros(max(n_pairs, 1), np.int32)
+    st = np.zeros(3, np.float64)
+    _check(lib.fxe_ga_breed_draws(P, ng, ptr(pop, _i), ptr(fit, _d), ptr(ordr, _i) if ordr is not None else None,
+                                  ptr(prob, _f) if prob is not None else None, float(cross_rate), float(mut_rate),
+                                  int(bool(intragenes)), int(bool(adaptive)), ptr(kk, _d), n_pairs, ptr(draws, _d),
+                                  ptr(children, _i), ptr(used, _i), ptr(st, _d)))
+    return {"children": children[:2 * n_pairs].astype(np.int64) & 0xFFFFFFFF, "draws_used": used[:n_pairs],
+            "total": float(st[0]), "max": float(st[1]), "mean": float(st[2])}
+
+
+def ga_niche_counts(ic, sig_share: float, alpha: float = 1.0) -> np.ndarray:
+    """PSHARE niche counts of a population given as ICs, on the device (fxe_ga_niche_counts)."""
+    lib = load_library()
+    ic = np.ascontiguousarray(ic, np.float64)
+    out = np.empty(ic.shape[0], np.float64)
+    _check(lib.fxe_ga_niche_counts(ic.shape[0], ic.shape[1], ptr(ic, _d), float(sig_share), float(alpha), ptr(out, _d)))
+    return out
+
+
+def ensemble_dedup(ic, energies) -> dict:
+    """The statmech ensemble of chromosomes given as ICs, on the device (fxe_ensemble_dedup):
+    sorted by energy, near-duplicates within 0.1 on every gene of the last one kept removed.
+    Returns the kept input indices and energies, in energy order."""
+    lib = load_library()
+    ic = np.ascontiguousarray(ic, np.float64)
+    e = np.ascontiguousarray(energies, np.float64)
+    n = e.shape[0]
+    ic = ic.reshape(n, -1)
+    idx = np.zeros(max(n, 1), np.int64)
+    ke = np.zeros(max(n, 1), np.float64)
+    cnt = C.c_int64()
+    _check(lib.fxe_ensemble_dedup(n, ic.shape[1], ptr(ic, _d), ptr(e, _d),
+                                  idx.ctypes.data_as(C.POINTER(C.c_int64)), ptr(ke, _d), C.byref(cnt)))
+    return {"index": idx[:cnt.value], "energy": ke[:cnt.value]}
+
+
+def cleft_grid(centers, radii, spacing: float, ori) -> tuple:
+    """The cleft grid of one or more spheres and its ICs, generated on the device
+    (fxe_cleft_grid): (points (M, 3) float32, ICs (M, 3) float32), grid entry 0 not included."""
+    lib = load_library()
+    c = np.ascontiguousarray(np.asarray(centers, np.float32).reshape(-1, 3))
+    r = np.ascontiguousarray(np.asarray(radii, np.float32).reshape(-1))
+    o = np.ascontiguousarray(np.asarray(ori, np.float32).reshape(3))
+    n = C.c_int64()
+    rc = lib.fxe_cleft_grid(c.shape[0], ptr(c, _f), ptr(r, _f), float(spacing), ptr(o, _f), 0, None, None, C.byref(n))
+    if rc not in (0, 6):      # FXE_ERR_CAPACITY: sized
+        _check(rc)
+    xyz = np.zeros((max(n.value, 1), 3), np.float32)
+    ic = np.zeros((max(n.value, 1), 3), np.float32)
+    _check(lib.fxe_cleft_grid(c.shape[0], ptr(c, _f), ptr(r, _f), float(spacing), ptr(o, _f), n.value,
+                              ptr(xyz, _f), ptr(ic, _f), C.byref(n)))
+    return xyz[:n.value], ic[:n.value]
 
 
 def ic2cf(evaluator: GPUEvaluator, icv) -> np.void:

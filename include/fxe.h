@@ -138,10 +138,26 @@ typedef struct fxe_thermo {
            entropy, std_energy;
 } fxe_thermo;
 
+/* Receptor preparation on the device: the cleft grid of generate_grid
+ * (LIB/generate_grid.cpp:18-107) and its internal coordinates (calc_cleftic,
+ * LIB/calc_cleftic.cpp:5-33), the fxe_receptor_desc grid entries 1.. (entry 0, the ligand's
+ * initial anchor, is the caller's). Spheres (centres n_spheres * 3, radii) are walked in the
+ * order given, as generate_grid walks its sphere list: the lattice of each (steps of `spacing`
+ * from the reference's rounded lower bound, x fastest) keeps the points strictly inside the
+ * sphere, and a point whose coordinates, snapped to 0.001 A (GridKey, LIB/maps.hpp:21-49),
+ * match a point of an earlier sphere is dropped. ICs against the frame ori + (1,0,0), ori,
+ * ori + (0,1,0) in single precision; the bond angle and dihedral round the double-precision
+ * acos and atan2, where the reference calls the C library's acosf and atan2f, so about one
+ * value in five can differ from the reference's in the last bit. xyz and ic: cap * 3 floats
+ * (host; ic may be NULL); *n_points the count (FXE_ERR_CAPACITY when it exceeds cap: call with
+ * cap 0 to size). Centres within +-1000 A, radii in (0, 1000]. */
+fxe_status fxe_cleft_grid(int32_t n_spheres, const float* centers, const float* radii, float spacing,
+                          const float* ori, int64_t cap, float* xyz, float* ic, int64_t* n_points);
+
 typedef struct fxe_context fxe_context;
 
 /* Creates an evaluation context on the current CUDA device: copies the descriptors into
- * device memory, builds the receptor cell list and the gene decode tables, and reserves
+ * device memory, builds the receptor cell list (on the device) and the gene decode tables, and reserves
  * workspace for up to max_poses poses per call. Replaces cuda_eval_init
  * (LIB/cuda_eval.cuh:46-58) and GPUContextPool::acquire_cuda (LIB/GPUContextPool.h:56-100). */
 fxe_status fxe_context_create(const fxe_receptor_desc* receptor, const fxe_ligand_desc* ligand,
@@ -390,7 +406,8 @@ fxe_status fxe_ga_finished(fxe_ga* ga, int32_t* slots, int32_t cap, int32_t* n);
  * its ensemble as the reference assembles it (every generation's population, sorted by energy,
  * near-duplicates within 0.1 on every decoded gene removed, LIB/gaboom.cpp:494,520-540,
  * 2728-2747; StatMechEngine::compute, LIB/statmech.cpp:73-174), with the ensemble size in
- * *n_ensemble; frees the slot. */
+ * *n_ensemble; frees the slot. The sort, the duplicate removal and the reduction run on the
+ * device (the snapshots stay in HBM). */
 fxe_status fxe_ga_collect(fxe_ga* ga, int32_t slot, double temperature, int32_t* best_genes,
                           double* best_energy, fxe_thermo* thermo, int64_t* n_ensemble);
 /* A finished job's ensemble as fxe_ga_collect assembles it (best first, near-duplicates
@@ -409,6 +426,53 @@ fxe_status fxe_ga_duplicates(fxe_ga* ga, int32_t slot, int64_t* rejected, int64_
 /* Kernels launched and graphs replayed since the previous call (resets both). */
 fxe_status fxe_ga_take_launches(fxe_ga* ga, int64_t* launches, int64_t* graphs);
 void fxe_ga_destroy(fxe_ga* ga);
+
+/* genetoic (LIB/gaboom.cpp:2887-2906) of n chromosomes' int32 genes (n * n_genes, host memory) with
+ * the context's gene limits, on the device: gene value g of gene q decodes to min + del * i for the
+ * first bin i whose running total (set_bins' bin = 1 / nbin, LIB/gaboom.cpp:2295-2308, added in
+ * order) reaches g / 2^31. clamp: 1 clamps into [min, max] as eval_chromosome does
+ * (LIB/gaboom.cpp:1845-1866), 0 returns genetoic's value. Writes n * n_genes doubles to ic. No
+ * separate reference entry point: the reference decodes inside its GA loop. */
+fxe_status fxe_decode_genes(fxe_context* ctx, int64_t n, const int32_t* genes, int32_t clamp, double* ic);
+
+/* One generation's breeding code of the GA engine run with the caller's draws in place of its
+ * counter-based ones: for callers that drive the GA from their own random stream (the reference
+ * draws from RandomDouble, LIB/gaboom.cpp:2942-2946) and for checking the operators alone.
+ * Pair k: two roulette_wheel draws over `fitness` (LIB/gaboom.cpp:1158-1186), adapt_prob when
+ * adaptive (:848-880, k4 = k1..k4), the crossover draw against the crossover probability, the
+ * crossover's gene and bit-point draws (:2517-2614), then for each child and gene a rotamer draw
+ * (rotamer genes only, :944-966) and 32 bit draws against the mutation probability (:2620-2641),
+ * read in that order from draws[k * FXE_GA_DRAWS_PER_PAIR(n_genes) ...] (uniforms in [0, 1)).
+ * pop: population * n_genes int32 genes; fitness: population values in roulette order; order: the
+ * population index at each roulette position (NULL: 0, 1, ...); gene_prob: n_genes side-chain
+ * probabilities of rotamer genes, -1 for the others (NULL: all -1). Outputs (host memory):
+ * children 2 * n_pairs * n_genes (pair k's first child, then its second); draws_used[n_pairs] (or
+ * NULL); fit_stats[3] (or NULL): fitness_stats' total, maximum and mean (LIB/gaboom.cpp:818-840).
+ * Synchronous; allocates its device buffers per call. */
+#define FXE_GA_DRAWS_PER_PAIR(ng) (7 + 2 * (int64_t)(ng) * 33)
+fxe_status fxe_ga_breed_draws(int32_t population, int32_t n_genes, const int32_t* pop, const double* fitness,
+                              const int32_t* order, const float* gene_prob, double cross_rate, double mut_rate,
+                              int32_t intragenes, int32_t adaptive, const double* k4, int32_t n_pairs,
+                              const double* draws, int32_t* children, int32_t* draws_used, double* fit_stats);
+
+/* PSHARE's niche counts (LIB/gaboom.cpp:1652-1661) of a population given as ICs
+ * (population * n_genes, host memory; population at most 2048): for each chromosome the sum over
+ * all chromosomes, in order, of 1 - (rmsp / sig_share)^alpha for every calc_rmsp
+ * (LIB/gaboom.cpp:2874-2885) within sig_share, computed by the GA engine's kernel. Writes
+ * population doubles to share. */
+fxe_status fxe_ga_niche_counts(int32_t population, int32_t n_genes, const double* ic, double sig_share,
+                               double alpha, double* share);
+
+/* The ensemble the reference's GA hands to statmech, assembled on the device from chromosomes given
+ * as ICs: sorted by energy (QuickSort of chrom_snapshot, LIB/gaboom.cpp:520; equal energies keep
+ * their input order, NaN sorts last), then remove_dups (LIB/gaboom.cpp:2728-2747): a chromosome is
+ * dropped when every gene lies within 0.1 of the last chromosome kept. ic: n * n_genes, energies:
+ * n (host memory, n < 2^31). Outputs (host memory, caller-owned, n entries suffice):
+ * kept_index, kept_energy (either may be NULL): the input index and energy of each kept
+ * chromosome in energy order; *n_kept their count. fxe_ga_collect and fxe_ga_ensemble run the
+ * same device code on a job's snapshots. Allocates its device buffers per call. */
+fxe_status fxe_ensemble_dedup(int64_t n, int32_t n_genes, const double* ic, const double* energies,
+                              int64_t* kept_index, double* kept_energy, int64_t* n_kept);
 
 /* Message describing the last error on the calling thread ("" if none). */
 const char* fxe_last_error(void);

@@ -275,14 +275,10 @@ def breed(pop: np.ndarray, gen: int, seed: int, cross_rate: float, mut_rate: flo
 def pair(pop: np.ndarray, gen: int, seed: int, kk: int, cross_rate: float, mut_rate: float,
          intragenes: bool, adaptive: bool, k, fitness: Fitness | None = None, prob=None):
     """Pair kk of generation gen + 1's children (two lists of uint32 genes)."""
-    P, ng = pop.shape
-    prob = prob or [-1.0] * ng
-    u32 = pop.astype(np.int64) & 0xFFFFFFFF
-    sb = (gen + 1) << 32
+    P = pop.shape[0]
     if fitness is None:
         fitness = Fitness(pop, np.zeros(P), None, "LINEAR")
-    fit_max, fit_avg = fitness.max, fitness.avg
-    st = sb + kk
+    st = ((gen + 1) << 32) + kk
     d = 0
 
     def draw():
@@ -291,18 +287,28 @@ def pair(pop: np.ndarray, gen: int, seed: int, kk: int, cross_rate: float, mut_r
         d += 1
         return v
 
+    return pair_with(pop, fitness, draw, cross_rate, mut_rate, intragenes, adaptive, k, prob)
+
+
+def pair_with(pop: np.ndarray, fitness: Fitness, draw, cross_rate: float, mut_rate: float,
+              intragenes: bool = False, adaptive: bool = False, k=(1.0, 0.5, 1.0, 0.5), prob=None):
+    """One pair of children from the draws draw() hands out, in the reference's order: two
+    roulette draws, adapt_prob when adaptive, the crossover draw and the crossover's own, then
+    each child's mutation draws (the reproduce loop, LIB/gaboom.cpp:918-964)."""
+    ng = pop.shape[1]
+    u32 = pop.astype(np.int64) & 0xFFFFFFFF
     pa = fitness.roulette(draw())
     pb = fitness.roulette(draw())
     a, b = fitness.order[pa], fitness.order[pb]
     crossp, mutp = cross_rate, mut_rate
     if adaptive:
-        crossp, mutp = adapt_prob(fit_max, fit_avg, fitness.fit[pa], fitness.fit[pb], k)
+        crossp, mutp = adapt_prob(fitness.max, fitness.avg, fitness.fit[pa], fitness.fit[pb], k)
     john = [int(x) for x in u32[a]]
     mary = [int(x) for x in u32[b]]
     if draw() < crossp:
         crossover(john, mary, intragenes, draw)
     for ch in (john, mary):
-        mutate(ch, mutp, draw, prob)
+        mutate(ch, mutp, draw, prob or [-1.0] * ng)
     return john, mary
 
 

@@ -15,6 +15,8 @@ from flexaidds_gb300.system import Descriptor, SystemInputs
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_ref", "libfxe_ref.so")
+# the reference checkout (its sources build oracle/_ref; its data files are read by some tests)
+REFERENCE_ROOT = os.environ.get("FXE_REFERENCE_ROOT", "/root/reference")
 _lib = None
 
 _f = C.POINTER(C.c_float)

@@ -258,10 +258,15 @@ def test_energy_matrix_file_format(tmp_path):
         system.read_emat(str(bad))
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/WRK/MC_st0r5.2_6.dat"),
+def _reference_file(*parts):
+    from oracle import ref
+    return os.path.join(ref.REFERENCE_ROOT, *parts)
+
+
+@pytest.mark.skipif(not os.path.exists(_reference_file("WRK", "MC_st0r5.2_6.dat")),
                     reason="the reference checkout is not present")
 def test_reference_energy_matrix_file_reads():
-    emat, w, curves = system.read_emat("/root/reference/WRK/MC_st0r5.2_6.dat")
+    emat, w, curves = system.read_emat(_reference_file("WRK", "MC_st0r5.2_6.dat"))
     assert emat.shape == (40, 40) and int(w.sum()) + 2 * len(curves) - sum(1 for (i, j) in curves if i == j) == 1600
 
 
