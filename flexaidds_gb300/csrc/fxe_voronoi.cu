@@ -51,8 +51,10 @@ using real = FXE_REAL;
 #ifndef FXE_FILTER
 #define FXE_FILTER (FXE_REFERENCE_FORMULAS)
 #endif
-// The double build's kernel outgrows the instruction cache (its top stall is instruction
-// fetch): its rarely taken or bulky helpers are called, not inlined.
+// The kernel outgrows the instruction cache (its top stall is instruction fetch): its rarely taken
+// or bulky helpers are called, not inlined (double build), and no loop is unrolled — every loop
+// carries `#pragma unroll 1` unless it says otherwise (measured on GB300, plain-scale workload:
+// 36.0 -> 30.4 ms per launch in double precision, 6.8 -> 4.9 ms in single).
 #if FXE_REFERENCE_FORMULAS
 #define FXE_COLD __noinline__
 #else
@@ -262,6 +264,7 @@ __device__ __forceinline__ real4 centre_of(const real4& pl) {
 
 // test_point (LIB/Vcontacts.cpp:1357-1372): true unless x lies behind a contact plane.
 __device__ FXE_COLD bool inside_all(const VorShared& sh, int NC, int skip, real x, real y, real z) {
+    #pragma unroll 1
     for (int cp = 0; cp < NC; ++cp) {
         if (cp == skip || sh.flag[cp] == 0) continue;
         if (dot3(sh.pl[cp], x, y, z) + sh.pl[cp].w > real(0.0)) return false;
@@ -324,6 +327,7 @@ __device__ FXE_COLD WalkStep walk_step_exact(const VorShared& sh, int NC, int e,
     const int pA = ep.x, pB = ep.y, oldC = ep.z;
     real vtmin = real(9.9e9);
     int pC = INT_MAX;
+    #pragma unroll 1
     for (int c = lane; c < NC; c += 32) {
         if (c == pA || c == pB || c == oldC) continue;
         const real4 P = sh.pl[c];
@@ -379,6 +383,7 @@ __device__ WalkStep walk_step(const VorShared& sh, int NC, int e, real rr, int l
     float best = 9.9e9f, beste = 0.0f;
     int bi = INT_MAX;
     bool unsure = false;
+    #pragma unroll 1
     for (int c = lane; c < NC; c += 32) {
         if (c == pA || c == pB || c == oldC) continue;
         float er;
@@ -395,6 +400,7 @@ __device__ WalkStep walk_step(const VorShared& sh, int NC, int e, real rr, int l
         if (b2 < best || (b2 == best && i2 < bi)) { best = b2; beste = e2; bi = i2; }
     }
     if (bi != INT_MAX && !(best - beste > 0.0f)) unsure = true;
+    #pragma unroll 1
     for (int c = lane; c < NC && !unsure; c += 32) {
         if (c == pA || c == pB || c == oldC || c == bi) continue;
         float er;
@@ -489,6 +495,7 @@ __device__ __forceinline__ void add_in_order(VorShared& sh, int X, real v, int l
     __syncwarp();
     if (X >= 0 && lane == __ffs(grp) - 1) {
         real acc = sh.area[X];
+        #pragma unroll 1
         for (unsigned m = grp; m; m &= m - 1) acc += sh.tmp[__ffs(m) - 1];
         sh.area[X] = acc;
     }
@@ -501,11 +508,13 @@ __device__ FXE_COLD void engulf_corrections(VorShared& sh, int NC, real rado, re
                                             int lane) {
     if (epi > 0) {
         if (lane == 0) {
+            #pragma unroll 1
             for (int X = 0; X < NC; ++X) {
                 if (!(sh.flag[X] & kEngulf)) continue;
                 const int np = sh.fnp[X];
                 const uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
                 const real4 cp = centre_of(sh.pl[X]);
+                #pragma unroll 1
                 for (int vi = 0; vi < np; ++vi) {
                     const int cur = pt[vi], nxt = pt[(vi + 1) % np];
                     const uchar4 qc = sh.vp[cur], qn = sh.vp[nxt];
@@ -543,6 +552,7 @@ __device__ FXE_COLD void engulf_corrections(VorShared& sh, int NC, real rado, re
         __syncwarp();
         if (epi >= 3) {
             const real share = real(4.0) * (real)kPi * rado * rado / epi;
+            #pragma unroll 1
             for (int X = lane; X < NC; X += 32) sh.area[X] = (sh.flag[X] & kEngulf) ? share : real(0.0);
         }
         __syncwarp();
@@ -587,6 +597,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
 #endif
         sh.flag[NC + lane] = 0;
     }
+    #pragma unroll 1
     for (int c = lane; c < NC; c += 32) sh.area[c] = real(0.0);
     __syncwarp();
 
@@ -600,6 +611,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     } else {
     real bv = real(9.9e9);
     int bi = INT_MAX;
+    #pragma unroll 1
     for (int c = lane; c < NC; c += 32) {
         const real d = fabs(sh.pl[c].w);
         if (d < bv) { bv = d; bi = c; }
@@ -610,6 +622,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     const real4 A = sh.pl[pA0];
     bv = real(9.9e9);
     bi = INT_MAX;
+    #pragma unroll 1
     for (int c = lane; c < NC + 4; c += 32) {
         if (c == pA0) continue;
         const real4 C = sh.pl[c];
@@ -629,6 +642,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     solve3(A, B, v, ptA);
     bv = real(9.9e9);
     bi = INT_MAX;
+    #pragma unroll 1
     for (int c = lane; c < NC + 4; c += 32) {
         if (c == pA0 || c == pB0) continue;
         const real4 C = sh.pl[c];
@@ -658,6 +672,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
 
     // ---- hull walk (LIB/Vcontacts.cpp:262-410) ----
     int edgenum = 3, startedge = 0, vn = 1;
+    #pragma unroll 1
     for (;;) {
         while (startedge < edgenum && sh.u.e.es[startedge].y != kNone) ++startedge;
         if (startedge >= edgenum) break;
@@ -669,6 +684,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         const int pA = ep.x, pB = ep.y;
         // edges (pA, pC) and (pB, pC): the first open match after startedge, else a new edge
         int mAC = INT_MAX, mBC = INT_MAX;
+        #pragma unroll 1
         for (int e0 = startedge + 1; e0 < edgenum; e0 += 32) {
             const int f = e0 + lane;
             bool ac = false, bc = false;
@@ -725,6 +741,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         __syncwarp();
     }
     // vertex distances to the centre, all at once
+    #pragma unroll 1
     for (int vi = 1 + lane; vi < vn; vi += 32) {
         const real4 X = sh.vx[vi];
         sh.vx[vi].w = sqrt(X.x * X.x + X.y * X.y + X.z * X.z);
@@ -732,6 +749,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     __syncwarp();
 
     // ---- arc points where edges leave the sphere (LIB/Vcontacts.cpp:418-462) ----
+    #pragma unroll 1
     for (int e0 = 0; e0 < edgenum; e0 += 32) {
         const int e = e0 + lane;
         int cnt = 0;
@@ -768,6 +786,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     }
     // ---- keep the vertices inside the sphere, in order ----
     int nv = 0;
+    #pragma unroll 1
     for (int v0 = 0; v0 < vn; v0 += 32) {
         const int vi = v0 + lane;
         real4 X = make_real4(0, 0, 0, 0);
@@ -793,10 +812,12 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     // ---- faces: points per plane in vertex order, plus an antipodal arc point ----
     // (the edge arrays are dead from here on; their storage holds the face lists)
     int tot_pts = 0;
+    #pragma unroll 1
     for (int x0 = 0; x0 < NC; x0 += 32) {
         const int X = x0 + lane;
         int cnt = 0;
         if (X < NC && sh.flag[X] != 0)
+            #pragma unroll 1
             for (int vi = 0; vi < NV; ++vi) {
                 const uchar4 P = sh.vp[vi];
                 cnt += (P.x == X || P.y == X || P.z == X);
@@ -813,6 +834,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     if (tot_pts > kMaxFacePts) return kAtomCapacity;
     __syncwarp();
     int n_extra = 0;
+    #pragma unroll 1
     for (int x0 = 0; x0 < NC; x0 += 32) {
         const int X = x0 + lane;
         bool extra = false;
@@ -820,12 +842,14 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         if (X < NC && sh.flag[X] != 0) {
             const int o = sh.foff[X];
             int k = 0;
+            #pragma unroll 1
             for (int vi = 0; vi < NV; ++vi) {
                 const uchar4 P = sh.vp[vi];
                 if (P.x == X || P.y == X || P.z == X) sh.u.f.pt[o + k++] = (uint8_t)vi;
             }
             if (k > 2) {
                 const real4 cp = centre_of(sh.pl[X]);
+                #pragma unroll 1
                 for (int q = 0; q < k; ++q) {
                     const int vi = sh.u.f.pt[o + q];
                     if (sh.vp[vi].z == kNone) {
@@ -858,6 +882,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     __syncwarp();
     // ordering around each face (pt[0], a neighbour of it, then decreasing cosine)
     int np_miss = 0, np_lost = 0;
+    #pragma unroll 1
     for (int X = lane; X < NC; X += 32) {
         if (sh.flag[X] == 0) continue;
         const int np = sh.fnp[X];
@@ -868,6 +893,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
             const uchar4 P0 = sh.vp[pt[0]];
             const int pY = (P0.x == X) ? P0.y : P0.x;
             int vi = 1;
+            #pragma unroll 1
             for (; vi < np; ++vi) {
                 const uchar4 q = sh.vp[pt[vi]];
                 if (q.x == pY || q.y == pY || q.z == pY) break;
@@ -892,6 +918,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
                     vi = 1;
                     if (pZ != kNone) {
                         int w = 1;
+                        #pragma unroll 1
                         for (; w < np; ++w) {
                             const uchar4 q = sh.vp[pt[w]];
                             if (q.x == pZ || q.y == pZ || q.z == pZ) break;
@@ -907,8 +934,11 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
                 v1 = sh.vx[pt[1]];
             }
             const real4 v0 = sh.vx[pt[0]];
+            #pragma unroll 1
             for (int k = 2; k < np; ++k) cs[k] = cos_pqr(v1, v0, sh.vx[pt[k]]);
+            #pragma unroll 1
             for (int a = 2; a < np - 1; ++a)
+                #pragma unroll 1
                 for (int b = a + 1; b < np; ++b)
                     if (cs[a] < cs[b]) {
                         const uint8_t t = pt[a];
@@ -922,6 +952,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         if (hist) {
             uint8_t* h = hist + X * kHistPts;
             const int nw = np < kHistPts ? np : kHistPts;
+            #pragma unroll 1
             for (int k = 0; k < nw; ++k) h[k] = pt[k];
             if (stale_prev >= 0) h[np] = (uint8_t)stale_prev;
         }
@@ -933,6 +964,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     // ---- areas (LIB/Vcontacts.cpp:838-1044) ----
     // the first three engulfing planes in plane order
     int epi = 0;
+    #pragma unroll 1
     for (int x0 = 0; x0 < NC && epi < 3; x0 += 32) {
         const int X = x0 + lane;
         const unsigned m = __ballot_sync(kFull, X < NC && (sh.flag[X] & kEngulf));
@@ -963,6 +995,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         } else {
             solve3(sh.pl[sh.eng[0]], sh.pl[sh.eng[1]], sh.pl[sh.eng[2]], pp);
         }
+        #pragma unroll 1
         for (int vi = lane; vi < NV; vi += 32) {
             if (sh.vp[vi].z == kNone) continue;
             real4 P = sh.vx[vi];
@@ -988,6 +1021,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     // segments of the other faces are laid out flat and spread over the lanes, then added to
     // their face's area in the reference's order (triangles, then arcs, each in point order).
     int t_run = 0, a_run = 0;
+    #pragma unroll 1
     for (int x0 = 0; x0 < NC; x0 += 32) {
         const int X = x0 + lane;
         int nt = 0, na = 0;
@@ -1005,6 +1039,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
             } else {
                 // (a face of one point has neither triangles nor arcs)
                 nt = np > 2 ? np - 2 : 0;
+                #pragma unroll 1
                 for (int vi = 0; vi < np; ++vi) na += arc_segment(sh, pt, np, vi);
             }
             sh.area[X] = area;
@@ -1021,6 +1056,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     }
     __syncwarp();
     // fan of spherical triangles from pt[0] (LIB/Vcontacts.cpp:906-940)
+    #pragma unroll 1
     for (int k0 = 0; k0 < t_run; k0 += 32) {
         const int k = k0 + lane;
         int X = -1;
@@ -1034,6 +1070,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         add_in_order(sh, X, v, lane);
     }
     // arc segments between consecutive arc points of different edges (:943-954)
+    #pragma unroll 1
     for (int k0 = 0; k0 < a_run; k0 += 32) {
         const int k = k0 + lane;
         int X = -1;
@@ -1043,6 +1080,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
             const int np = sh.fnp[X];
             const uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
             int j = k - sh.aoff[X], vi = 0;
+            #pragma unroll 1
             for (; vi < np - 1; ++vi)
                 if (arc_segment(sh, pt, np, vi) && j-- == 0) break;
             v = sph_arc(centre_of(sh.pl[X]), sh.vx[pt[vi]], sh.vx[pt[(vi + 1) % np]], rado);
@@ -1066,6 +1104,7 @@ __device__ int load_planes(VorShared& sh, const DevSystem& S, const DevWork& W, 
     const size_t cb = ((size_t)p * nm + a) * kMaxCand;
     const float rr = rado * rado;          // single-precision products, as in the reference
     int NC = 0;
+    #pragma unroll 1
     for (int c0 = 0; c0 < n_cand; c0 += 32) {
         const int c = c0 + lane;
         const bool keep = c < n_cand && !((excl[c >> 5] >> (c & 31)) & 1u);
@@ -1105,6 +1144,7 @@ __device__ int load_planes(VorShared& sh, const DevSystem& S, const DevWork& W, 
 __device__ double pose_clash_sum(const DevSystem& S, const DevWork& W, int p, int lane) {
     const int nm = n_mobile(S);
     double s = 0.0;
+    #pragma unroll 1
     for (int m = lane; m < nm; m += 32) s += W.clash_part[(size_t)p * nm + m];
     return warp_sum(s);
 }
@@ -1176,6 +1216,7 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         finish_failed(W, p, lane, FXE_POSE_CLASHED, clash);
         return;
     }
+    #pragma unroll 1
     for (int l = lane; l < nl; l += 32) {
         ps.order[W.mob_rank[lb + l]] = (uint8_t)l;
         seed[l][0] = seed[l][1] = seed[l][2] = -1;
@@ -1187,10 +1228,12 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
     // cleared before the pose
     if (hist) {
         uint4* h4 = reinterpret_cast<uint4*>(hist);
+        #pragma unroll 1
         for (int k = lane; k < kHistBytes / 16; k += 32) h4[k] = make_uint4(0u, 0u, 0u, 0u);
     }
     __syncwarp();
     // calc_region: atoms in Calclist order (LIB/Vcontacts.cpp:74-139)
+    #pragma unroll 1
     for (int r = 0; r < nl; ++r) {
         const int a = ps.order[r];
         const int n_cand = W.cand_n[lb + a];
@@ -1217,6 +1260,7 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
             kept_n += __popc(__ballot_sync(kFull, c < n_cand && !ex));
         }
         if (kept_n == 0) {   // no contacts: SAS -1, nothing saved, the atom is not marked done
+            #pragma unroll 1
             for (int c = lane; c < n_cand; c += 32) {
                 W.cand_area[cb + c] = 0.0;
                 W.cand_flag[cb + c] = 0;
@@ -1230,6 +1274,7 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         int sA = -1, sB = -1, sC = -1;
         if (seed[a][0] != -1) {
             const int s0 = seed[a][0], s1 = seed[a][1], s2 = seed[a][2];
+            #pragma unroll 1
             for (int c0 = 0; c0 < NC; c0 += 32) {
                 const int c = c0 + lane;
                 const int j = c < NC ? sh.cidx[c] : -2;
@@ -1258,12 +1303,14 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         // save_areas (LIB/Vcontacts.cpp:1149-1220): contacts with area > 0 on a contact plane;
         // candidates outside the contact list record nothing
         uint32_t keep_lig[kMaskWords] = {0, 0, 0, 0};
+        #pragma unroll 1
         for (int c = lane; c < n_cand; c += 32) {
             if ((excl[c >> 5] >> (c & 31)) & 1u) {
                 W.cand_area[cb + c] = 0.0;
                 W.cand_flag[cb + c] = 0;
             }
         }
+        #pragma unroll 1
         for (int k = lane; k < NC; k += 32) {
             const real ar = sh.area[k];
             const uint8_t f = sh.flag[k];
@@ -1284,6 +1331,7 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         // save_seeds (LIB/Vcontacts.cpp:601-629): first vertex naming each later atom's plane
         if (lane == 0) {
             const int az = slot_of(S, a);
+            #pragma unroll 1
             for (int vi = 0; vi < sh.nv; ++vi) {
                 const uchar4 q = sh.vp[vi];
                 if (q.z == kNone || q.x >= NC || q.y >= NC || q.z >= NC) continue;
@@ -1313,6 +1361,7 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
 #pragma unroll
     for (int r = 0; r < kMaxFlex; ++r) res_com[r] = res_wal[r] = res_sas[r] = 0.0;
     int cur_res = -1;
+    #pragma unroll 1
     for (int i = 0; i < nl; ++i) {
         const int NC = W.cand_n[lb + i];
         const size_t cb = (lb + i) * kMaxCand;
@@ -1332,6 +1381,7 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         const double surfA = 4.0 * kPi * radoA * radoA;
         const int ti = side ? S.rec_type[S.sc_slot[i]] : S.lig_type[i - nsc];
         double c_com = 0.0, c_wal = 0.0, c_area = 0.0;
+        #pragma unroll 1
         for (int c = lane; c < NC; c += 32) {
             if (!(W.cand_flag[cb + c] & kRecorded)) continue;
             const int j = W.cand_idx[cb + c];
@@ -1383,6 +1433,7 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         sas += contribution;
     }
     // the ligand's record (com/wal/sas hold it now), then each side chain's
+    #pragma unroll 1
     for (int r = 0; r < S.n_flex; ++r) {
         com += res_com[r];
         wal += res_wal[r];
@@ -1420,6 +1471,7 @@ pose_kernel(DevSystem S, DevWork W, int n, int* next, uint8_t* hist_all) {
     PoseShared& ps = reinterpret_cast<PoseShared*>(smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     uint8_t* hist = warp_hist(hist_all);
+    #pragma unroll 1
     for (int q = next_pose(next, lane); q < n; q = next_pose(next, lane)) {
         score_pose(S, W, W.pose_order[q], lane, ps, hist);
         __syncwarp();
@@ -1435,6 +1487,7 @@ pose_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, int total, int* next,
     PoseShared& ps = reinterpret_cast<PoseShared*>(smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     uint8_t* hist = warp_hist(hist_all);
+    #pragma unroll 1
     for (int q = next_pose(next, lane); q < total; q = next_pose(next, lane)) {
         const int gp = order[q];
         const Job& job = jobs[find_job(jobs, n_jobs, gp, false)];
