@@ -48,6 +48,9 @@ WORKLOAD_NAME = ("plain-scale: 6000-atom receptor (before carving the side chain
 N_POPULATIONS = 8           # distinct populations, cycled over the steps
 FLUSH_BYTES = 512 << 20     # L2 flush between timed steps (L2 is 129 MB)
 STATMECH_N = 1_000_000      # ensemble size of the thermodynamics reduction (all poses of a run)
+# FP64 work per energy of the reduction: the log-weight, the running maximum and its rescaling, one
+# exp (counted as 10), the three running sums
+STATMECH_FLOP = 20
 
 # DRAM bytes per launch of the dominant kernel from ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum), keyed by precision; from profiles/pose_kernel_plain_scale.md.
@@ -56,6 +59,13 @@ POSE_KERNEL_DRAM_BYTES = {"reference": 102_597_888, "fast": 85_202_176}
 # nominal non-tensor arithmetic peaks of GB300 (152 SMs at 2,070 MHz): FP32 152 x 128 lanes x 2
 # flops per FMA; FP64 1.25 TFLOP/s. There is no measured figure for either.
 NOMINAL_PEAK_TFLOPS = {"fast": 152 * 128 * 2 * 2.07e9 / 1e12, "reference": 1.25}
+
+
+def bench_config(prec: str) -> dict:
+    """The workload as both arms name it (the same dict in both JSON lines)."""
+    w = WORKLOAD
+    return {"workload": WORKLOAD_NAME, "population": w["population"], "precision": prec,
+            "side_chains": f"{w['side_chains']} residues x {w['rotamers']} rotamers"}
 
 
 def work_flops_per_pose(c: dict) -> float:
@@ -243,6 +253,16 @@ def run_gpu(args):
     barrier, max_over_ranks = ranks.barrier, ranks.max
 
     prec = args.precision
+    # receptors of the many-receptor legs, generated on the host cores before anything is timed
+    pool = futs4 = futs5 = None
+    if args.batched or args.served:
+        specs4 = receptor_specs(BATCH4["receptors"], BATCH4["seed"], side_chains=True) if args.batched else []
+        specs5 = receptor_specs(SERVE["receptors"], SERVE["seed"], side_chains=False) if args.served else []
+        pool, futs = start_receptor_pool(specs4 + specs5)
+        futs4, futs5 = futs[:len(specs4)], futs[len(specs4):]
+        rec4 = [f.result() for f in futs4]
+        rec5 = [f.result() for f in futs5]
+        pool.shutdown()
     d = make_system()
     pop = WORKLOAD["population"]
     ev = evaluator.GPUEvaluator(d, max_poses=pop,
@@ -313,35 +333,53 @@ def run_gpu(args):
     assert np.all(res["status"] != capi.POSE_CAPACITY)
 
     # --- statmech over a run's ensemble (1e6 poses, FP64) -------------------------------------
+    # fxe_thermo_compute_device_fixed: the reduction and its merge on the device, the record
+    # written to device memory (kernel time, no host round trip); fxe_thermo_compute_device: the
+    # same with the merge on the host (the call waits for it)
     from flexaidds_gb300.capi import Thermo
     energies = torch.from_numpy(np.random.default_rng(1).normal(-30.0, 5.0, STATMECH_N)).cuda()
     th = Thermo()
-    for _ in range(3):
+    d_th = torch.zeros(C.sizeof(Thermo), dtype=torch.uint8, device="cuda")
+
+    lib.fxe_thermo_compute_device_fixed.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_void_p,
+                                                    C.c_void_p]
+
+    def thermo_fixed():
+        rc = lib.fxe_thermo_compute_device_fixed(C.c_void_p(energies.data_ptr()), None, STATMECH_N, 300.0,
+                                                 C.c_void_p(d_th.data_ptr()), C.c_void_p(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(lib.fxe_last_error().decode())
+
+    def thermo_host_merge():
         lib.fxe_thermo_compute_device(C.c_void_p(energies.data_ptr()), None, STATMECH_N, 300.0,
                                       C.byref(th), C.c_void_p(stream.cuda_stream))
-    torch.cuda.synchronize()
-    sm_ms = []
-    for _ in range(10):
-        flush.zero_()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        lib.fxe_thermo_compute_device(C.c_void_p(energies.data_ptr()), None, STATMECH_N, 300.0,
-                                      C.byref(th), C.c_void_p(stream.cuda_stream))
-        b.record(stream)
-        b.synchronize()
-        sm_ms.append(a.elapsed_time(b))
-    sm_best = min(sm_ms)
+
+    sm = {}
+    for nm, fn in (("device_merge", thermo_fixed), ("host_merge", thermo_host_merge)):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(10):
+            flush.zero_()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            t = a.elapsed_time(b)
+            best = t if best is None else min(best, t)
+        sm[nm] = best
+    sm_best = sm["device_merge"]
 
     clustered = run_cluster(ev, d) if args.cluster else None
-    batched = run_batched(args, prec, flush, stream) if args.batched else None
-    served = None
-    if args.served:
-        from flexaidds_gb300.system import SystemInputs  # noqa: F401
-        w, b = WORKLOAD, BATCH
-        served = run_served(prec, {
-            "6000": system.make_inputs(w["n_rec"], w["cleft"], 12, 3, seed=w["seed"], edge=w["edge"],
-                                       side_chains=w["side_chains"], rotamers=w["rotamers"]),
-            "4000": system.make_inputs(b["n_rec"], b["cleft"], 12, 3, seed=b["seed"], edge=b["edge"])})
+    batched = batched4 = None
+    if args.batched:
+        batched = run_batched(args, prec, flush, stream, BATCH_NAME, c3_jobs(), BATCH["evolve"])
+        batched4 = run_batched(args, prec, flush, stream, BATCH4_NAME, c4_jobs(rec4), BATCH4["evolve"])
+    served = run_served(prec, rec5) if args.served else None
+    ga_runs = {k: run_ga(prec, k, d if k == "c2" else None) for k in ("c1", "c2")} if args.ga else None
 
     if rank != 0:
         ranks.close()
@@ -361,6 +399,7 @@ def run_gpu(args):
     traffic = POSE_KERNEL_DRAM_BYTES[prec]
     hbm = peaks.get("hbm_gbs")
     sm_gbs = 8.0 * STATMECH_N / (sm_best / 1e3) / 1e9
+    sm_tflops = STATMECH_FLOP * STATMECH_N / (sm_best / 1e3) / 1e12
     try:
         cpu = cpu_baseline_port(d, pops)
     except Exception as e:   # the oracle library could not be built or loaded
@@ -371,11 +410,9 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == "reference" else "f32",
         "data": "synthetic (seeded Poisson-disc receptor, seeded tree ligand, N(0,1) matrix)",
-        "config": {"workload": WORKLOAD_NAME, "population": pop, "precision": prec,
-                   "l2": f"flushed between timed steps ({FLUSH_BYTES >> 20} MB write)",
-                   "parallelism": f"replicas x{world}",
-                   "side_chains": f"{d.n_flex} residues x {int(d.flex_nrot[0]) if d.n_flex else 0} "
-                                  f"rotamers, {d.n_sc} scored side-chain atoms"},
+        "config": bench_config(prec),
+        "l2": f"flushed between timed steps ({FLUSH_BYTES >> 20} MB write)",
+        "parallelism": f"replicas x{world}",
         "e2e": {"value": world * pop * args.steps / e2e_s, "unit": "poses/s",
                 "h2d_bytes_per_step": pop * d.n_genes * 4, "d2h_bytes_per_step": pop * capi.CF_DTYPE.itemsize},
         "gpu_launches": launches,
@@ -390,10 +427,16 @@ def run_gpu(args):
                               "polyhedra_and_scoring": pose_ms},
         "wall_s_timed_region": wall,
         "statmech": {"poses": STATMECH_N, "ms": sm_best, "poses_per_s": STATMECH_N / (sm_best / 1e3),
-                     "roofline": {"bound": "hbm", "achieved": sm_gbs, "peak": hbm, "unit": "GB/s",
-                                  "frac": (sm_gbs / hbm) if hbm else None, "traffic": None}},
+                     "ms_host_merge": sm["host_merge"],
+                     "roofline": {"bound": "fp64", "achieved": sm_tflops, "peak": NOMINAL_PEAK_TFLOPS["reference"],
+                                  "unit": "TFLOP/s", "frac": sm_tflops / NOMINAL_PEAK_TFLOPS["reference"],
+                                  "flop_per_energy": STATMECH_FLOP, "peak_source": "nominal FP64",
+                                  "hbm_gbs": sm_gbs, "hbm_frac": (sm_gbs / hbm) if hbm else None,
+                                  "traffic": None}},
         "batched": batched,
+        "batched_c4": batched4,
         "served": served,
+        "ga": ga_runs,
         "cluster": clustered,
     }
     print(json.dumps(out), flush=True)
@@ -448,17 +491,52 @@ def run_cluster(ev, d, centres=None):
 
 
 # ---------------------------------------------------------------------------------------------
-# batched: many ligands on one receptor, one launch per generation
+# receptors of the many-receptor workloads: generated in worker processes (spawned, no CUDA)
+# ---------------------------------------------------------------------------------------------
+
+def receptor_specs(n, seed, side_chains):
+    """n seeded receptor shapes of 1,500-8,000 atoms and 6-14 A clefts; with side_chains, 0-4
+    flexible side chains of 4-12 rotamers each."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        out.append(dict(n_rec=int(rng.integers(1500, 8001)), cleft=float(rng.uniform(6.0, 14.0)),
+                        side_chains=int(rng.integers(0, 5)) if side_chains else 0,
+                        rotamers=int(rng.integers(4, 13)), seed=int(seed * 100 + k)))
+    return out
+
+
+def _gen_receptor(spec):
+    return system.make_inputs(spec["n_rec"], spec["cleft"], 12, 3, seed=spec["seed"],
+                              side_chains=spec["side_chains"], rotamers=spec["rotamers"])
+
+
+def start_receptor_pool(specs):
+    """Futures of the receptors' inputs, generated by a pool of spawned processes."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    ex = cf.ProcessPoolExecutor(max_workers=max(1, min(len(specs), os.cpu_count() or 1)),
+                                mp_context=mp.get_context("spawn"))
+    return ex, [ex.submit(_gen_receptor, s) for s in specs]
+
+
+# ---------------------------------------------------------------------------------------------
+# batched: many ligands (on one receptor, or on many), one launch per generation
 # ---------------------------------------------------------------------------------------------
 
 BATCH = dict(n_rec=4000, cleft=10.0, seed=31, edge=51.92391670510951, jobs=256, atoms=(10, 70),
-             torsions=(0, 15), population=(200, 2000))
-BATCH_NAME = ("batched: 4000-atom receptor, 10 A cleft (79501 grid points), 256 seeded ligands of "
-              "U[10,70] heavy atoms and U[0,15] torsions, populations U[200,2000] of uniform "
-              "(initial-generation) chromosomes; one GA generation of every job per step")
+             torsions=(0, 15), population=(200, 2000), evolve=5)
+BATCH_NAME = ("batched C3: 4000-atom receptor, 10 A cleft (79501 grid points), 256 seeded ligands of "
+              "U[10,70] heavy atoms and U[0,15] torsions, populations U[200,2000] after 5 GA "
+              "generations on the device; one generation's evaluation of every job per step")
+BATCH4 = dict(receptors=16, ligands=32, population=500, atoms=(10, 70), torsions=(0, 15), seed=44, evolve=5)
+BATCH4_NAME = ("batched C4: 16 seeded receptors of 1500-8000 atoms (6-14 A clefts, 0-4 flexible side "
+               "chains of 4-12 rotamers), 32 ligands each (U[10,70] heavy atoms, U[0,15] torsions), 512 "
+               "jobs of population 500 after 5 GA generations on the device; one generation's "
+               "evaluation of every job per step")
 
 
-def make_batch_jobs():
+def c3_jobs():
     from flexaidds_gb300.system import SystemInputs
     b = BATCH
     base = system.make_inputs(b["n_rec"], b["cleft"], 12, 3, seed=b["seed"], edge=b["edge"])
@@ -469,27 +547,64 @@ def make_batch_jobs():
         t = int(rng.integers(b["torsions"][0], b["torsions"][1] + 1))
         pop = int(rng.integers(b["population"][0], b["population"][1] + 1))
         lig = synth.random_ligand(n, t, seed=b["seed"] * 1000 + k)
-        d = prepare.prepare(SystemInputs(receptor=base.receptor, ligand=lig, grid_xyz=base.grid_xyz,
-                                         emat=base.emat))
-        out.append((d, pop, synth.random_genes(pop, d.n_genes, seed=b["seed"] * 5000 + k)))
+        out.append(("c3", SystemInputs(receptor=base.receptor, ligand=lig, grid_xyz=base.grid_xyz,
+                                       emat=base.emat), pop))
     return out
 
 
-def run_batched(args, prec, flush, stream):
-    """Poses/s of one generation of all jobs: one launch sequence per job (the plain path) and
-    one batched launch for all of them, same chromosomes, device-resident, L2 flushed."""
+def c4_jobs(receptors):
+    from flexaidds_gb300.system import SystemInputs
+    b = BATCH4
+    rng = np.random.default_rng(b["seed"])
+    out = []
+    for r, base in enumerate(receptors):
+        for k in range(b["ligands"]):
+            n = int(rng.integers(b["atoms"][0], b["atoms"][1] + 1))
+            t = int(rng.integers(b["torsions"][0], b["torsions"][1] + 1))
+            lig = synth.random_ligand(n, t, seed=b["seed"] * 100000 + r * 1000 + k)
+            out.append((f"r{r}", SystemInputs(receptor=base.receptor, ligand=lig, grid_xyz=base.grid_xyz,
+                                              emat=base.emat), b["population"]))
+    return out
+
+
+def evolved_populations(jobs, prec, generations, seed):
+    """Contexts of the jobs (one receptor copy per receptor key) and each job's population after
+    `generations` GA generations on the device (the reference's defaults)."""
+    from flexaidds_gb300 import evaluator
+    p = 0 if prec == "reference" else 1
+    bases, evs = {}, []
+    for key, inp, pop in jobs:
+        d = prepare.prepare(inp)
+        if key not in bases:
+            bases[key] = evaluator.GPUEvaluator(d, max_poses=pop, precision=p)
+            evs.append(bases[key])
+        else:
+            evs.append(evaluator.GPUEvaluator(d, max_poses=pop, precision=p, share_receptor_with=bases[key]))
+    eng = evaluator.GAEngine(max_jobs=len(jobs), precision=p)
+    slots = [eng.admit(eng.job(ev, pop, generations + 1, seed * 7919 + k), ev)
+             for k, (ev, (_, _, pop)) in enumerate(zip(evs, jobs))]
+    for _ in range(generations):
+        eng.step()
+    genes = [eng.read_population(sl, pop)[0] for sl, (_, _, pop) in zip(slots, jobs)]
+    eng.close()
+    return evs, genes
+
+
+def run_batched(args, prec, flush, stream, name, jobs, generations):
+    """Poses/s of one generation's evaluation of all jobs (their evolved populations): one launch
+    sequence per job (the plain path) and one batched launch for all of them, same chromosomes,
+    device-resident, L2 flushed."""
     import torch
     from flexaidds_gb300 import evaluator
-    jobs = make_batch_jobs()
-    p = 0 if prec == "reference" else 1
-    first = evaluator.GPUEvaluator(jobs[0][0], max_poses=jobs[0][1], precision=p)
-    evs = [first] + [evaluator.GPUEvaluator(d, max_poses=pop, precision=p, share_receptor_with=first)
-                     for d, pop, _ in jobs[1:]]
-    dg = [torch.from_numpy(np.ascontiguousarray(g)).cuda() for _, _, g in jobs]
-    do = [torch.empty(pop * capi.CF_DTYPE.itemsize, dtype=torch.uint8, device="cuda") for _, pop, _ in jobs]
-    total = sum(pop for _, pop, _ in jobs)
+    t_setup = time.perf_counter()
+    evs, genes = evolved_populations(jobs, prec, generations, seed=len(jobs))
+    setup_s = time.perf_counter() - t_setup
+    pops = [g.shape[0] for g in genes]
+    dg = [torch.from_numpy(np.ascontiguousarray(g)).cuda() for g in genes]
+    do = [torch.empty(pop * capi.CF_DTYPE.itemsize, dtype=torch.uint8, device="cuda") for pop in pops]
+    total = sum(pops)
     batch = evaluator.Batch(max_jobs=len(jobs), max_poses=total, max_genes=64)
-    table = [(ev, pop, g.data_ptr(), o.data_ptr()) for ev, (_, pop, _), g, o in zip(evs, jobs, dg, do)]
+    table = [(ev, pop, g.data_ptr(), o.data_ptr()) for ev, pop, g, o in zip(evs, pops, dg, do)]
 
     def plain():
         for ev, pop, g, o in table:
@@ -499,11 +614,10 @@ def run_batched(args, prec, flush, stream):
         batch.eval_genes_device(table, stream.cuda_stream)
 
     res = {}
-    steps = max(1, min(args.steps, 5))
-    for name, fn in (("plain", plain), ("batched", batched)):
+    steps = max(1, min(args.steps, 3))
+    for nm, fn in (("plain", plain), ("batched", batched)):
         with torch.cuda.stream(stream):
-            for _ in range(args.warmup):
-                fn()
+            fn()
         stream.synchronize()
         ms = 0.0
         for _ in range(steps):
@@ -515,7 +629,7 @@ def run_batched(args, prec, flush, stream):
                 b.record(stream)
             b.synchronize()
             ms += a.elapsed_time(b)
-        res[name] = {"poses_per_s": total * steps / (ms / 1e3), "ms_per_generation": ms / steps}
+        res[nm] = {"poses_per_s": total * steps / (ms / 1e3), "ms_per_generation": ms / steps}
     batched_out = [np.frombuffer(o.cpu().numpy().tobytes(), capi.CF_DTYPE) for o in do]
     plain()
     stream.synchronize()
@@ -525,24 +639,27 @@ def run_batched(args, prec, flush, stream):
     for ev in evs:
         ev.close()
     batch.close()
-    return {"workload": BATCH_NAME, "jobs": len(jobs), "poses_per_generation": total,
+    return {"workload": name, "jobs": len(jobs), "poses_per_generation": total,
             "scored_fraction": scored / total, "precision": prec, "steps": steps,
             "plain": res["plain"], "batched": res["batched"],
             "speedup": res["batched"]["poses_per_s"] / res["plain"]["poses_per_s"],
-            "results_identical": same}
+            "results_identical": same, "setup_s": setup_s}
 
 
 # ---------------------------------------------------------------------------------------------
 # served: Poisson arrivals of docking jobs, continuous batching on the device GA engine
 # ---------------------------------------------------------------------------------------------
 
-SERVE = dict(rates=(10.0, 50.0, 200.0), jobs=48, population=500, generations=20, budget=150e9,
-             atoms_median=30, atoms=(10, 70), torsions=(0, 15), seed=77)
-SERVE_NAME = ("served: Poisson arrivals at 10, 50 and 200 jobs/s, 48 jobs per rate, receptors from a "
-              "cache of two (6000 atoms with three flexible side chains of 8 rotamers, and 4000 "
-              "atoms), ligands lognormal median 30 heavy atoms (10-70) with U[0,15] torsions, "
-              "population 500 for 20 generations, the reference's GA defaults (PSHARE fitness, "
-              "BOOM, duplicates rejected), 150 GB admission budget")
+SERVE = dict(receptors=32, jobs=48, population=500, generations=100, budget=150e9, atoms_median=30,
+             atoms=(10, 70), torsions=(0, 15), seed=77, load=(0.5, 0.9, 1.5), plain_jobs=12)
+SERVE_NAME = ("served C5 (scaled: 48 jobs per stream where the config has 10,000): receptors from a "
+              "cache of 32 seeded receptors of 1500-8000 atoms (6-14 A clefts), ligands lognormal "
+              "median 30 heavy atoms (10-70) with U[0,15] torsions, population 500 for 100 generations, "
+              "the reference's GA defaults (PSHARE fitness, BOOM, duplicates rejected), 150 GB "
+              "admission budget; the receptor's grid and each job's descriptor prepared on admission, "
+              "inside the job's latency. Capacity first (all jobs at t = 0), then Poisson streams at "
+              "0.5, 0.9 and 1.5 times it, and the plain path (one job at a time, the first 12 jobs) at 0.5 "
+              "times it")
 
 
 def run_served(prec, receptors):
@@ -551,31 +668,92 @@ def run_served(prec, receptors):
     s = SERVE
     rng = np.random.default_rng(s["seed"])
     reqs = []
-    keys = list(receptors)
     for k in range(s["jobs"]):
-        key = keys[k % len(keys)]
-        base = receptors[key]
+        r = int(rng.integers(len(receptors)))
+        base = receptors[r]
         n = int(np.clip(round(rng.lognormal(np.log(s["atoms_median"]), 0.4)), *s["atoms"]))
         t = int(rng.integers(s["torsions"][0], s["torsions"][1] + 1))
         lig = synth.random_ligand(n, t, seed=s["seed"] * 1000 + k)
-        d = prepare.prepare(SystemInputs(receptor=base.receptor, ligand=lig, grid_xyz=base.grid_xyz, emat=base.emat))
-        reqs.append(serve.JobRequest(0.0, key, d, s["population"], s["generations"], seed=s["seed"] * 7919 + k))
+        inp = SystemInputs(receptor=base.receptor, ligand=lig, grid_xyz=base.grid_xyz, emat=base.emat)
+        reqs.append(serve.JobRequest(0.0, f"r{r}", inp, s["population"], s["generations"], seed=s["seed"] * 7919 + k))
     p = 0 if prec == "reference" else 1
-    out = {"workload": SERVE_NAME, "precision": prec, "rates": []}
-    for rate in s["rates"]:
-        arr = serve.poisson_arrivals(len(reqs), rate, seed=int(rate))
-        for r, t in zip(reqs, arr):
-            r.arrival = float(t)
-        srv = serve.DockingServer(max_jobs=256, hbm_budget=s["budget"], precision=p)
+
+    def serve_once(arrivals, max_jobs):
+        for q, t in zip(reqs, arrivals):
+            q.arrival = float(t)
+        srv = serve.DockingServer(max_jobs=max_jobs, hbm_budget=s["budget"], precision=p)
         res = srv.run(reqs)
         launches, graphs = srv.engine.take_launches()
         srv.close()
         summ = serve.latency_summary(res)
         poses = len(res) * s["population"] * (s["generations"] + 1)
-        summ.update({"arrival_rate": rate, "poses_per_s": poses / summ["makespan_s"],
-                     "graph_launches": graphs, "kernel_launches": launches})
+        summ.update({"poses_per_s": poses / summ["makespan_s"], "graph_launches": graphs,
+                     "kernel_launches": launches})
+        return summ
+
+    out = {"workload": SERVE_NAME, "precision": prec, "jobs_per_stream": s["jobs"]}
+    cap = serve_once(np.zeros(len(reqs)), 256)
+    capacity = cap["jobs_per_s"]
+    out["capacity"] = dict(cap, arrival_rate=None)
+    out["rates"] = []
+    for f in s["load"]:
+        rate = capacity * f
+        summ = serve_once(serve.poisson_arrivals(len(reqs), rate, seed=int(1000 * f)), 256)
+        summ.update({"arrival_rate": rate, "load": f})
         out["rates"].append(summ)
+    rate = capacity * s["load"][0]
+    del reqs[s["plain_jobs"]:]
+    plain = serve_once(serve.poisson_arrivals(len(reqs), rate, seed=int(1000 * s["load"][0])), 1)
+    plain.update({"arrival_rate": rate, "load": s["load"][0], "jobs": len(reqs)})
+    out["plain"] = plain
     return out
+
+
+# ---------------------------------------------------------------------------------------------
+# whole GA runs: C1 (500 x 100 generations) and C2 (2000 x 500 generations, 1e6 poses) on the
+# device GA engine, ensemble and thermodynamics included
+# ---------------------------------------------------------------------------------------------
+
+GA_RUNS = {
+    "c1": dict(n_rec=2000, cleft=8.0, n_lig=24, n_tor=6, seed=11, edge=None, side_chains=0, rotamers=8,
+               population=500, generations=100,
+               name="C1: 2000-atom receptor, 8 A cleft, 24-atom ligand, 6 torsions, population 500 for 100 generations"),
+    "c2": dict(n_rec=6000, cleft=12.0, n_lig=48, n_tor=12, seed=7, edge=WORKLOAD["edge"], side_chains=3, rotamers=8,
+               population=2000, generations=500,
+               name="C2: the plain-scale system (6000 atoms, 3 side chains of 8 rotamers, 48-atom ligand, 12 "
+                    "torsions), population 2000 for 500 generations (1e6 poses)"),
+}
+
+
+def run_ga(prec, key, d=None):
+    """One docking job's whole GA on the device: poses/s over the run, the ensemble's size and the
+    FP64 thermodynamics of it at 300 K."""
+    import torch
+    from flexaidds_gb300 import evaluator
+    g = GA_RUNS[key]
+    if d is None:
+        d = prepare.prepare(system.make_inputs(g["n_rec"], g["cleft"], g["n_lig"], g["n_tor"], seed=g["seed"],
+                                               edge=g["edge"], side_chains=g["side_chains"], rotamers=g["rotamers"]))
+    p = 0 if prec == "reference" else 1
+    ev = evaluator.GPUEvaluator(d, max_poses=g["population"], precision=p)
+    eng = evaluator.GAEngine(max_jobs=1, precision=p)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    slot = eng.admit(eng.job(ev, g["population"], g["generations"], seed=2024), ev)
+    for _ in range(g["generations"]):
+        eng.step()
+    assert eng.finished() == [slot]
+    t1 = time.perf_counter()
+    best_g, best_e, th = eng.collect(slot, 300.0)
+    t2 = time.perf_counter()
+    eng.close()
+    ev.close()
+    poses = g["population"] * (g["generations"] + 1)
+    return {"workload": g["name"], "precision": prec, "poses": poses, "seconds": t1 - t0,
+            "poses_per_s": poses / (t1 - t0), "collect_s": t2 - t1, "best_energy": best_e,
+            "n_ensemble": th["n_ensemble"], "free_energy": th["free_energy"],
+            "mean_energy": th["mean_energy"], "minus_T_dS": -300.0 * th["entropy"],
+            "heat_capacity": th["heat_capacity"]}
 
 
 # ---------------------------------------------------------------------------------------------
@@ -632,8 +810,8 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Poisson-disc receptor, seeded tree ligand, N(0,1) matrix)",
-        "config": {"workload": WORKLOAD_NAME, "population": pop, "precision": "reference",
-                   "parallelism": f"{cores} host processes"},
+        "config": bench_config(args.precision),
+        "parallelism": f"{cores} host processes",
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "poses/s", "cores": cores, "kind": "port",
                          "sample": f"one population of {pop} per step on {cores} processes of "
@@ -658,6 +836,8 @@ def main():
                     help="also time the batched many-ligand workload against one launch per job")
     ap.add_argument("--cluster", type=int, default=1,
                     help="also time the clustering of a 1e6-chromosome ensemble")
+    ap.add_argument("--ga", type=int, default=1,
+                    help="also run whole GA jobs: C1 (500 x 100 generations) and C2 (2000 x 500)")
     ap.add_argument("--cluster-only", type=int, default=0, metavar="CENTRES",
                     help="time only the clustering, of CENTRES x 500 chromosomes (a small case "
                          "for a profiler: few launches before the clustering kernels)")

@@ -276,9 +276,15 @@ def _receptor_setup(rec_xyz, grid_xyz):
     return c, ic
 
 
-def prepare(inp: SystemInputs) -> Descriptor:
+def prepare(inp: SystemInputs, receptor_setup=None) -> Descriptor:
+    """The descriptor of one docking system. receptor_setup: ((ori, globalmin, globalmax,
+    maxwidth), grid ICs) of the receptor and its grid when they are already known (the receptor
+    cache of a server computes the grid and its ICs once, on the device); else calc_center and
+    calc_cleftic here."""
     rec, lig = inp.receptor, inp.ligand
-    (ori, gmin, gmax, mw), grid_ic = _receptor_setup(rec.xyz, inp.grid_xyz)
+    if receptor_setup is None:
+        receptor_setup = _receptor_setup(rec.xyz, inp.grid_xyz)
+    (ori, gmin, gmax, mw), grid_ic = receptor_setup
     n = lig.xyz.shape[0]
     adj = [[] for _ in range(n)]
     for a, b in lig.bonds:

@@ -8,9 +8,14 @@ selection, `fxe_ga_step`), and a job leaves the engine as soon as its last gener
 freeing its slot and memory for the next arrivals. A job's result (best pose, best energy, the
 FP64 thermodynamics of everything it evaluated) depends only on the job, not on what else ran.
 
-Receptors are cached: the first job on a receptor creates a context holding the receptor, its
-cell list and cleft grid on the device; every later job on it shares them
-(`fxe_context_create_shared`).
+Receptors are cached: the first job on a receptor generates its cleft grid and the grid's
+internal coordinates on the device (`fxe_cleft_grid`) and creates a context holding the receptor,
+its cell list (built on the device) and the grid; every later job on it shares them
+(`fxe_context_create_shared`). A job's own preparation (the ligand's build tree, gene limits and
+descriptor) happens when it is admitted, so it counts in the job's latency.
+
+`DockingServer(max_jobs=1)` is the plain path served: one job at a time, one population per
+launch, the others waiting in arrival order.
 """
 from __future__ import annotations
 
@@ -19,16 +24,16 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import evaluator
+from . import evaluator, prepare
 from .evaluator import GAEngine, GPUEvaluator
-from .system import Descriptor
+from .system import Descriptor, SystemInputs
 
 
 @dataclass
 class JobRequest:
     arrival: float          # seconds after the start of the stream
     receptor: str           # key of the receptor in the server's cache
-    desc: Descriptor        # the job's prepared system (receptor, ligand, matrix)
+    inputs: SystemInputs    # the job's system (receptor, ligand, matrix), prepared on admission
     population: int = 500
     generations: int = 100
     seed: int = 0
@@ -68,12 +73,29 @@ class DockingServer:
         self.budget = float(hbm_budget)
         self.precision = int(precision)
         self.temperature = float(temperature)
-        self.receptors: dict[str, GPUEvaluator] = {}
+        self.receptors: dict[str, tuple] = {}   # key -> (receptor setup, context holding the receptor)
 
-    def _receptor(self, key: str, desc: Descriptor) -> GPUEvaluator:
+    def _receptor(self, key: str, inp: SystemInputs):
+        """The cached receptor: its frame and cleft grid ICs (grid on the device) and a context
+        whose device arrays later jobs share."""
         if key not in self.receptors:
-            self.receptors[key] = GPUEvaluator(desc, max_poses=2, precision=self.precision)
+            rec = inp.receptor
+            frame = prepare.calc_center(rec.xyz)
+            xyz, ic = evaluator.cleft_grid(rec.cleft_center, [rec.cleft_radius], 0.375, frame[0])
+            setup = (frame, ic)
+            inp = SystemInputs(receptor=rec, ligand=inp.ligand, grid_xyz=xyz, emat=inp.emat)
+            base = GPUEvaluator(prepare.prepare(inp, setup), max_poses=2, precision=self.precision)
+            self.receptors[key] = (setup, xyz, base)
         return self.receptors[key]
+
+    def _prepare(self, r: JobRequest) -> tuple:
+        setup, xyz, base = self._receptor(r.receptor, r.inputs)
+        inp = r.inputs
+        desc = prepare.prepare(SystemInputs(receptor=inp.receptor, ligand=inp.ligand, grid_xyz=xyz, emat=inp.emat,
+                                            permeability=inp.permeability, dee_clash=inp.dee_clash,
+                                            intramolecular=inp.intramolecular, solventterm=inp.solventterm),
+                               setup)
+        return desc, base
 
     def run(self, requests: list[JobRequest]) -> list[JobResult]:
         order = sorted(range(len(requests)), key=lambda i: requests[i].arrival)
@@ -88,11 +110,11 @@ class DockingServer:
             while pending and requests[pending[0]].arrival <= now and len(running) < self.max_jobs:
                 i = pending[0]
                 r = requests[i]
-                base = self._receptor(r.receptor, r.desc)
-                job_bytes = context_bytes(r.desc, r.population)
+                desc, base = self._prepare(r)
+                job_bytes = context_bytes(desc, r.population)
                 if used + job_bytes > self.budget and running:
                     break
-                ev = GPUEvaluator(r.desc, max_poses=r.population, precision=self.precision,
+                ev = GPUEvaluator(desc, max_poses=r.population, precision=self.precision,
                                   share_receptor_with=base)
                 job = self.engine.job(ev, r.population, r.generations, r.seed, r.cross_rate, r.mut_rate)
                 job_bytes += self.engine.job_bytes(job)
@@ -117,7 +139,7 @@ class DockingServer:
 
     def close(self):
         self.engine.close()
-        for ev in self.receptors.values():
+        for _, _, ev in self.receptors.values():
             ev.close()
 
 

@@ -101,70 +101,88 @@ def poisson_disc_receptor(n_atoms: int, cleft_radius: float, seed: int,
 
 
 def _poisson_disc(n_atoms, cleft_radius, seed, min_sep, edge):
+    """Bridson's sampling (k = 30 candidates in the shell [r, 2r] around a random active point),
+    then up to 20,000 uniform darts. Candidates are tested against the placed points in blocks
+    (a padded cell grid, cells of min_sep / sqrt(3), the 5^3 cells around each candidate) and
+    against the candidates of their own block accepted before them, so that every candidate is
+    accepted exactly when a one-at-a-time test would accept it."""
     rng = np.random.default_rng(seed)
     half = edge / 2.0
     r2min = min_sep * min_sep
+    rc2 = cleft_radius * cleft_radius
     cell = min_sep / math.sqrt(3.0)
     ng = int(math.ceil(edge / cell))
-    grid = -np.ones((ng, ng, ng), dtype=np.int64)
-    pts: list[np.ndarray] = []
-    arr = np.zeros((n_atoms + 1, 3), np.float64)   # pts as one array, for the distance checks
+    grid = -np.ones((ng + 4, ng + 4, ng + 4), dtype=np.int64)    # two cells of padding per side
+    arr = np.zeros((n_atoms + 1, 3), np.float64)
+    off = np.array([(a, b, c) for a in range(-2, 3) for b in range(-2, 3) for c in range(-2, 3)], np.int64)
+    state = {"n": 0, "last": 0}
 
-    def gidx(p):
-        return tuple(np.minimum(((p + half) / cell).astype(np.int64), ng - 1))
-
-    def ok(p):
-        if np.any(np.abs(p) > half) or float(p @ p) < cleft_radius * cleft_radius:
-            return False
-        gi = gidx(p)
-        lo = [max(0, g - 2) for g in gi]
-        hi = [min(ng, g + 3) for g in gi]
-        blk = grid[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]].ravel()
-        blk = blk[blk >= 0]
-        if blk.size == 0:
-            return True
-        d = arr[blk] - p
-        return bool(np.all(np.einsum('ij,ij->i', d, d) >= r2min))
-
-    def add(p):
-        grid[gidx(p)] = len(pts)
-        arr[len(pts)] = p
-        pts.append(p)
+    def add_block(C):
+        """Candidates C (k, 3) in order; returns the indices of the points placed."""
+        kk = C.shape[0]
+        inside = ~np.any(np.abs(C) > half, axis=1) & (np.einsum('ij,ij->i', C, C) >= rc2)
+        placed = []
+        if not inside.any():
+            return placed
+        G = np.clip(((C + half) / cell).astype(np.int64), 0, ng - 1)
+        nb = G[:, None, :] + off[None, :, :] + 2
+        idx = grid[nb[..., 0], nb[..., 1], nb[..., 2]]
+        valid = idx >= 0
+        d = arr[np.where(valid, idx, 0)] - C[:, None, :]
+        d2 = np.einsum('ij,ij->i', d.reshape(-1, 3), d.reshape(-1, 3)).reshape(kk, -1)
+        clear = ~np.any(valid & ~(d2 >= r2min), axis=1) & inside
+        taken = []
+        for i in np.nonzero(clear)[0]:
+            if taken:
+                e = C[taken] - C[i]
+                if not np.all(np.einsum('ij,ij->i', e, e) >= r2min):
+                    continue
+            g = G[i]
+            grid[g[0] + 2, g[1] + 2, g[2] + 2] = state["n"]
+            arr[state["n"]] = C[i]
+            placed.append(state["n"])
+            state["n"] += 1
+            taken.append(i)
+            state["last"] = int(i)
+            if state["n"] >= n_atoms:
+                break
+        return placed
 
     while True:
-        p0 = rng.uniform(-half, half, 3)
-        if ok(p0):
-            add(p0)
+        if add_block(rng.uniform(-half, half, 3)[None]):
             break
     active = [0]
     k = 30
-    while active and len(pts) < n_atoms:
+    while active and state["n"] < n_atoms:
         ai = int(rng.integers(len(active)))
-        base = pts[active[ai]]
-        found = False
+        base = arr[active[ai]].copy()
         # candidates in the spherical shell [r, 2r]
         dirs = rng.normal(size=(k, 3))
         dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
         radii = min_sep * (1.0 + rng.uniform(0.0, 1.0, k))
-        for c in base + dirs * radii[:, None]:
-            if ok(c):
-                add(c)
-                active.append(len(pts) - 1)
-                found = True
-                if len(pts) >= n_atoms:
-                    break
-        if not found:
+        placed = add_block(base + dirs * radii[:, None])
+        if placed:
+            active.extend(placed)
+        else:
             active[ai] = active[-1]
             active.pop()
-    # top up with random darts if the active list ran dry early
+    # top up with random darts if the active list ran dry early: one uniform triple per try, up
+    # to 20,000 tries; drawn in blocks, and when a block holds the dart that completes the set the
+    # generator is rewound and only the darts used are drawn again
     tries = 0
-    while len(pts) < n_atoms and tries < 20000:
-        c = rng.uniform(-half, half, 3)
-        if ok(c):
-            add(c)
-        tries += 1
-    if len(pts) < n_atoms:
-        raise ValueError(f"cube of edge {edge:.1f} A holds only {len(pts)} atoms at {min_sep} A")
+    while state["n"] < n_atoms and tries < 20000:
+        m = min(4096, 20000 - tries)
+        saved = rng.bit_generator.state
+        add_block(rng.uniform(-half, half, (m, 3)))
+        if state["n"] >= n_atoms:
+            used = state["last"] + 1
+            rng.bit_generator.state = saved
+            rng.uniform(-half, half, (used, 3))
+            break
+        tries += m
+    if state["n"] < n_atoms:
+        raise ValueError(f"cube of edge {edge:.1f} A holds only {state['n']} atoms at {min_sep} A")
+    pts = arr
     xyz = np.asarray(pts[:n_atoms], dtype=np.float64).astype(np.float32)
     types = rng.integers(1, NTYPES + 1, size=n_atoms).astype(np.int32)
     radius = np.asarray([type_radius(t, 0) for t in types], dtype=np.float32)

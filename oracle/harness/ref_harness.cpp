@@ -670,3 +670,112 @@ int ref_cluster(int32_t n, const double* ic, const double* app_evalue, int32_t t
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// The C++ adapter's packing (flexaidds_gb300/adapter/fxe_flexaid_pack.cpp) of this harness's
+// state, for the check that it packs what the reference's set-up produced.
+// ---------------------------------------------------------------------------------------------
+#include "fxe_flexaid.h"
+
+namespace {
+FxeFlexaidPacked g_packed;
+}
+
+extern "C" {
+
+// Packs the harness state; sizes[0..6] = receptor atoms, grid entries, ligand atoms, genes,
+// rebuild-list length, energy-matrix points, flexible side chains. Returns 0, or -1 with the
+// adapter's message in msg (cap bytes).
+int ref_adapter_pack(int32_t* sizes, char* msg, int32_t cap) {
+    if (!H) return -1;
+    std::string err;
+    if (!fxe_flexaid_pack(H->FA, H->atoms, H->residue, H->cleftgrid, &g_packed, &err)) {
+        if (msg && cap > 0) snprintf(msg, (size_t)cap, "%s", err.c_str());
+        return -1;
+    }
+    const FxeFlexaidPacked& P = g_packed;
+    sizes[0] = P.receptor.n_atoms;
+    sizes[1] = P.receptor.n_grid;
+    sizes[2] = P.ligand.n_atoms;
+    sizes[3] = P.ligand.n_genes;
+    sizes[4] = P.ligand.n_build;
+    sizes[5] = (int32_t)P.em_x.size();
+    sizes[6] = P.receptor.n_flex;
+    return 0;
+}
+
+// Copies one packed array by name into dst (sized by the caller from ref_adapter_pack's sizes).
+// Scalars: "frame" = ori, globalmin, globalmax, maxwidth (10 floats); "params" = permeability,
+// dee_clash, intramolecular, solventterm (4 floats). Flexible side chain r: "flex_info" (4 ints per
+// chain: first, atoms, rotamers, 0), "flex_backbone", "flex_xyz", "flex_bonded" concatenated.
+int ref_adapter_get(const char* name, void* dst) {
+    const FxeFlexaidPacked& P = g_packed;
+    const std::string k(name);
+    auto put = [&](const auto& v) {
+        memcpy(dst, v.data(), v.size() * sizeof(v[0]));
+        return (int)v.size();
+    };
+    if (k == "rec_xyz") return put(P.rec_xyz);
+    if (k == "rec_radius") return put(P.rec_radius);
+    if (k == "rec_type") return put(P.rec_type);
+    if (k == "grid_ic") return put(P.grid_ic);
+    if (k == "lig_radius") return put(P.lig_radius);
+    if (k == "lig_type") return put(P.lig_type);
+    if (k == "lig_rec") return put(P.lig_rec);
+    if (k == "lig_shift") return put(P.lig_shift);
+    if (k == "lig_ic") return put(P.lig_ic);
+    if (k == "build_order") return put(P.build_order);
+    if (k == "bonded") return put(P.bonded);
+    if (k == "gene_typ") return put(P.gene_type);
+    if (k == "gene_atm") return put(P.gene_atom);
+    if (k == "gene_min") return put(P.gene_min);
+    if (k == "gene_max") return put(P.gene_max);
+    if (k == "gene_del") return put(P.gene_del);
+    if (k == "gene_map") return put(P.gene_map);
+    if (k == "emat_weight") return put(P.em_weight);
+    if (k == "emat_off") return put(P.em_offset);
+    if (k == "emat_x") return put(P.em_x);
+    if (k == "emat_y") return put(P.em_y);
+    if (k == "frame") {
+        float* f = static_cast<float*>(dst);
+        for (int c = 0; c < 3; ++c) {
+            f[c] = P.receptor.ori[c];
+            f[3 + c] = P.receptor.globalmin[c];
+            f[6 + c] = P.receptor.globalmax[c];
+        }
+        f[9] = P.receptor.maxwidth;
+        return 10;
+    }
+    if (k == "params") {
+        float* f = static_cast<float*>(dst);
+        f[0] = P.params.permeability;
+        f[1] = P.params.dee_clash;
+        f[2] = (float)P.params.intramolecular;
+        f[3] = P.params.solventterm;
+        return 4;
+    }
+    if (k == "flex_info") {
+        int32_t* o = static_cast<int32_t*>(dst);
+        for (size_t r = 0; r < P.flex.size(); ++r) {
+            o[4 * r] = P.flex[r].first;
+            o[4 * r + 1] = P.flex[r].n_atoms;
+            o[4 * r + 2] = P.flex[r].n_rot;
+            o[4 * r + 3] = 0;
+        }
+        return (int)(4 * P.flex.size());
+    }
+    auto cat = [&](const auto& vv) {
+        size_t o = 0;
+        for (const auto& v : vv) {
+            memcpy(static_cast<char*>(dst) + o * sizeof(v[0]), v.data(), v.size() * sizeof(v[0]));
+            o += v.size();
+        }
+        return (int)o;
+    };
+    if (k == "flex_backbone") return cat(P.flex_backbone);
+    if (k == "flex_xyz") return cat(P.flex_xyz);
+    if (k == "flex_bonded") return cat(P.flex_bonded);
+    return -1;
+}
+
+}  // extern "C"

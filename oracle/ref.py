@@ -61,6 +61,8 @@ def _load():
         _lib.ref_last_contacts.argtypes = [C.c_int32, C.c_int32, _i, _d, _d]
         _lib.ref_export_flex_bonded.argtypes = [_b]
         _lib.ref_cluster.argtypes = [C.c_int32, _d, _d, C.c_int32, C.c_float, C.c_int32, C.c_char_p]
+        _lib.ref_adapter_pack.argtypes = [_i, C.c_char_p, C.c_int32]
+        _lib.ref_adapter_get.argtypes = [C.c_char_p, C.c_void_p]
     return _lib
 
 
@@ -178,6 +180,40 @@ class RefHarness:
             ntypes=int(self.inp.emat.shape[0]), emat_weight=w, emat_off=off, emat_x=ex,
             emat_y=ey, permeability=self.inp.permeability, dee_clash=self.inp.dee_clash,
             intramolecular=self.inp.intramolecular, solventterm=self.inp.solventterm)
+
+    def adapter_arrays(self) -> dict:
+        """What the product's C++ adapter (flexaidds_gb300/adapter/fxe_flexaid_pack.cpp) packs from
+        this harness's reference state, by descriptor field name."""
+        lib = _load()
+        sz = np.zeros(7, np.int32)
+        msg = C.create_string_buffer(512)
+        if lib.ref_adapter_pack(_p(sz, _i), msg, 512) != 0:
+            raise RuntimeError(msg.value.decode())
+        n_rec, n_grid, n, ng, n_build, n_pts, n_flex = (int(x) for x in sz)
+        spec = {"rec_xyz": (n_rec * 3, np.float32), "rec_radius": (n_rec, np.float32), "rec_type": (n_rec, np.int32),
+                "grid_ic": (n_grid * 3, np.float32), "lig_radius": (n, np.float32), "lig_type": (n, np.int32),
+                "lig_rec": (n * 4, np.int32), "lig_shift": (n, np.float32), "lig_ic": (n * 3, np.float32),
+                "build_order": (n_build, np.int32), "bonded": (n * n, np.int8), "gene_typ": (ng, np.int32),
+                "gene_atm": (ng, np.int32), "gene_min": (ng, np.float64), "gene_max": (ng, np.float64),
+                "gene_del": (ng, np.float64), "gene_map": (ng, np.int32), "emat_x": (n_pts, np.float32),
+                "emat_y": (n_pts, np.float32), "frame": (10, np.float32), "params": (4, np.float32),
+                "flex_info": (4 * n_flex, np.int32)}
+        t = int(self.inp.emat.shape[0])
+        spec["emat_weight"] = (t * t, np.int32)
+        spec["emat_off"] = (t * t + 1, np.int32)
+        if n_flex:
+            fl = self.inp.receptor.flex
+            spec["flex_backbone"] = (sum(f.natm for f in fl), np.int8)
+            spec["flex_xyz"] = (sum(f.natm * f.n_rot * 3 for f in fl), np.float32)
+            spec["flex_bonded"] = (sum(f.natm * f.natm for f in fl), np.int8)
+        out = {}
+        for k, (cnt, dt) in spec.items():
+            a = np.zeros(max(cnt, 1), dt)
+            got = lib.ref_adapter_get(k.encode(), a.ctypes.data_as(C.c_void_p))
+            if got != cnt:
+                raise RuntimeError(f"adapter array {k}: {got} entries, expected {cnt}")
+            out[k] = a[:cnt]
+        return out
 
     def eval(self, ic: np.ndarray, want_xyz: bool = False):
         """Scores poses given as decoded ICs. Returns (cf[n, 11], status[n], xyz or None)."""
