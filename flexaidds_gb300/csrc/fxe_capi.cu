@@ -23,14 +23,18 @@ void launch_build(const DevSystem&, const DevWork&, int, const int32_t*, const d
 void launch_contacts(const DevSystem&, const DevWork&, int, cudaStream_t);
 void launch_order_poses(const DevSystem&, const DevWork&, int, cudaStream_t);
 namespace f32 {
-void launch_poses(const DevSystem&, const DevWork&, int, int*, uint8_t*, size_t, cudaStream_t);
+void launch_poses(const DevSystem&, const DevWork&, int, int*, uint8_t*, size_t, int, cudaStream_t);
 cudaError_t configure_voronoi();
 size_t pose_hist_bytes();
+int pose_max_blocks_per_sm();
+int pose_warps_per_block();
 }
 namespace f64 {
-void launch_poses(const DevSystem&, const DevWork&, int, int*, uint8_t*, size_t, cudaStream_t);
+void launch_poses(const DevSystem&, const DevWork&, int, int*, uint8_t*, size_t, int, cudaStream_t);
 cudaError_t configure_voronoi();
 size_t pose_hist_bytes();
+int pose_max_blocks_per_sm();
+int pose_warps_per_block();
 }
 // Face history of a polyhedron launch, large enough for either precision's launch: the warps the
 // device holds at once, kHistStride bytes each (configure_voronoi first).
@@ -98,6 +102,26 @@ struct CallBuffers {
 }  // namespace
 
 // Device allocations freed together; a receptor's block is shared by every context built on it.
+// The autotuner's table: the polyhedron launch's occupancy cap (blocks per SM, 0 = as many as
+// fit) per size class, process-wide, so that every context, batch and GA engine of the class uses
+// what fxe_context_autotune measured for it. Classes: precision x scored atoms per pose (<= 16,
+// 32, 64, more) x poses per launch (<= 128, 512, 2048, 16384, more). The cap changes how many
+// poses run at once on an SM, never a result.
+std::mutex g_tune_mu;
+std::map<int, int> g_tune;
+
+int size_class(int precision, int mobile, long long poses) {
+    const int m = mobile <= 16 ? 0 : mobile <= 32 ? 1 : mobile <= 64 ? 2 : 3;
+    const int p = poses <= 128 ? 0 : poses <= 512 ? 1 : poses <= 2048 ? 2 : poses <= 16384 ? 3 : 4;
+    return precision * 100 + m * 10 + p;
+}
+
+int tuned_blocks(int precision, int mobile, long long poses) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    const auto it = g_tune.find(size_class(precision, mobile, poses));
+    return it == g_tune.end() ? 0 : it->second;
+}
+
 struct DevBlock {
     std::vector<void*> ptrs;
     std::vector<float4> grid_ic;   // host copy of the cleft-grid ICs
@@ -657,9 +681,10 @@ fxe_status run_chunk(fxe_context* ctx, int nb, const int32_t* d_genes, const dou
     if (t) cudaEventRecord(ctx->ev[2], s);
     fxe::launch_order_poses(ctx->S, ctx->W, nb, s);
     uint8_t* hist = ctx->face_order == FXE_FACE_ORDER_REFERENCE ? ctx->d_hist : nullptr;
+    const int bpsm = tuned_blocks(ctx->precision, ctx->S.n_sc + ctx->S.n_lig, nb);
     if (ctx->precision == FXE_PRECISION_FAST)
-        fxe::f32::launch_poses(ctx->S, ctx->W, nb, ctx->W.counters + 4, hist, ctx->hist_bytes, s);
-    else fxe::f64::launch_poses(ctx->S, ctx->W, nb, ctx->W.counters + 4, hist, ctx->hist_bytes, s);
+        fxe::f32::launch_poses(ctx->S, ctx->W, nb, ctx->W.counters + 4, hist, ctx->hist_bytes, bpsm, s);
+    else fxe::f64::launch_poses(ctx->S, ctx->W, nb, ctx->W.counters + 4, hist, ctx->hist_bytes, bpsm, s);
     if (t) cudaEventRecord(ctx->ev[3], s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
@@ -1165,10 +1190,10 @@ void launch_build_jobs(const Job*, int, int, cudaStream_t);
 void launch_contacts_jobs(const Job*, int, long long, cudaStream_t);
 void launch_order_poses_jobs(const Job*, int, int, int*, cudaStream_t);
 namespace f32 {
-void launch_poses_jobs(const Job*, int, int, int*, const int*, uint8_t*, size_t, cudaStream_t);
+void launch_poses_jobs(const Job*, int, int, int*, const int*, uint8_t*, size_t, int, cudaStream_t);
 }
 namespace f64 {
-void launch_poses_jobs(const Job*, int, int, int*, const int*, uint8_t*, size_t, cudaStream_t);
+void launch_poses_jobs(const Job*, int, int, int*, const int*, uint8_t*, size_t, int, cudaStream_t);
 }
 }  // namespace fxe
 
@@ -1251,7 +1276,7 @@ namespace {
 // genes_of / out_of give each job's device chromosomes and records.
 template <typename G, typename O>
 fxe_status batch_launch(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, cudaStream_t s, G genes_of, O out_of) {
-    int prec = -1, order = FXE_FACE_ORDER_REFERENCE, total = 0;
+    int prec = -1, order = FXE_FACE_ORDER_REFERENCE, total = 0, mobile = 0;
     long long items = 0;
     FXE_TRY(cudaEventSynchronize(b->staged), "batch staging");
     int k = 0;
@@ -1271,6 +1296,7 @@ fxe_status batch_launch(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, cudaS
         ctx->last_n = jobs[i].n;
         prec = ctx->precision;
         order = ctx->face_order;
+        mobile = std::max(mobile, ctx->S.n_sc + ctx->S.n_lig);
     }
     if (k == 0) return FXE_OK;
     FXE_TRY(cudaMemcpyAsync(b->d_jobs, b->h_jobs, sizeof(fxe::Job) * k, cudaMemcpyHostToDevice, s), "job table");
@@ -1279,9 +1305,10 @@ fxe_status batch_launch(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, cudaS
     fxe::launch_contacts_jobs(b->d_jobs, k, items, s);
     fxe::launch_order_poses_jobs(b->d_jobs, k, total, b->d_order, s);
     uint8_t* hist = order == FXE_FACE_ORDER_REFERENCE ? b->d_hist : nullptr;
+    const int bpsm = tuned_blocks(prec, mobile, total);
     if (prec == FXE_PRECISION_FAST)
-        fxe::f32::launch_poses_jobs(b->d_jobs, k, total, b->d_next, b->d_order, hist, b->hist_bytes, s);
-    else fxe::f64::launch_poses_jobs(b->d_jobs, k, total, b->d_next, b->d_order, hist, b->hist_bytes, s);
+        fxe::f32::launch_poses_jobs(b->d_jobs, k, total, b->d_next, b->d_order, hist, b->hist_bytes, bpsm, s);
+    else fxe::f64::launch_poses_jobs(b->d_jobs, k, total, b->d_next, b->d_order, hist, b->hist_bytes, bpsm, s);
     FXE_TRY(cudaGetLastError(), "batched kernel launch");
     b->launches += 4;
     return FXE_OK;
@@ -1683,9 +1710,13 @@ extern "C" fxe_status fxe_ga_step(fxe_ga* e) {
         bool ref_order = true;
         for (int sl : e->run) ref_order = ref_order && e->slots[sl].ctx->face_order == FXE_FACE_ORDER_REFERENCE;
         uint8_t* hist = ref_order ? e->d_hist : nullptr;
+        int mobile = 0;
+        for (int sl : e->run) mobile = std::max(mobile, e->slots[sl].ctx->S.n_sc + e->slots[sl].ctx->S.n_lig);
+        const int bpsm = tuned_blocks(e->precision, mobile, total);
         if (e->precision == FXE_PRECISION_FAST)
-            fxe::f32::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->d_order, hist, e->hist_bytes, e->stream);
-        else fxe::f64::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->d_order, hist, e->hist_bytes, e->stream);
+            fxe::f32::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->d_order, hist, e->hist_bytes, bpsm, e->stream);
+        else fxe::f64::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->d_order, hist, e->hist_bytes, bpsm,
+                                         e->stream);
         fxe::launch_ga_select(e->d_all, e->d_run, n, false, e->stream);
         fxe::launch_ga_fitness(e->d_all, e->d_run, n, false, e->stream);
         cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
@@ -2092,5 +2123,67 @@ extern "C" fxe_status fxe_cleft_grid(int32_t n_spheres, const float* centers, co
     if (e != cudaSuccess) return cuda_fail(e, "cleft grid");
     *n_points = n;
     if (n > cap) return fail(FXE_ERR_CAPACITY, "the grid holds more points than cap");
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_context_autotune(fxe_context* ctx, int32_t n, const int32_t* d_genes, int32_t reps,
+                                           int32_t* blocks_per_sm, double* ms_per_launch) {
+    g_err.clear();
+    if (!ctx || n <= 0 || !d_genes || reps < 1 || reps > 100) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    if (n > ctx->W.max_poses) return fail(FXE_ERR_INVALID_ARGS, "n exceeds the context's max_poses");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
+    cudaStream_t s = ctx->stream;
+    const bool fast = ctx->precision == FXE_PRECISION_FAST;
+    const int maxb = fast ? fxe::f32::pose_max_blocks_per_sm() : fxe::f64::pose_max_blocks_per_sm();
+    uint8_t* hist = ctx->face_order == FXE_FACE_ORDER_REFERENCE ? ctx->d_hist : nullptr;
+    // the candidates' work: this batch built, its contact candidates listed and ordered once
+    fxe::launch_build(ctx->S, ctx->W, n, d_genes, nullptr, s);
+    fxe::launch_contacts(ctx->S, ctx->W, n, s);
+    fxe::launch_order_poses(ctx->S, ctx->W, n, s);
+    FXE_TRY(cudaGetLastError(), "autotune launch");
+    cudaEvent_t a = nullptr, b = nullptr;
+    FXE_TRY(cudaEventCreate(&a), "cudaEventCreate");
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return fail(FXE_ERR_LAUNCH, "cudaEventCreate");
+    }
+    int best = 0;
+    float best_ms = 0.0f;
+    cudaError_t e = cudaSuccess;
+    for (int c = std::max(1, maxb / 2); c <= maxb && e == cudaSuccess; ++c) {
+        float cand = 0.0f;
+        for (int r = 0; r <= reps && e == cudaSuccess; ++r) {   // the first launch warms up
+            cudaEventRecord(a, s);
+            if (fast) fxe::f32::launch_poses(ctx->S, ctx->W, n, ctx->W.counters + 4, hist, ctx->hist_bytes, c, s);
+            else fxe::f64::launch_poses(ctx->S, ctx->W, n, ctx->W.counters + 4, hist, ctx->hist_bytes, c, s);
+            cudaEventRecord(b, s);
+            e = cudaEventSynchronize(b);
+            float ms = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+            if (r > 0 && (cand == 0.0f || ms < cand)) cand = ms;
+        }
+        if (e == cudaSuccess && (best == 0 || cand < best_ms)) {
+            best = c;
+            best_ms = cand;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (e != cudaSuccess) return cuda_fail(e, "autotune");
+    ctx->launches += 3 + (long long)(maxb - std::max(1, maxb / 2) + 1) * (reps + 1);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[size_class(ctx->precision, ctx->S.n_sc + ctx->S.n_lig, n)] = best;
+    }
+    if (blocks_per_sm) *blocks_per_sm = best;
+    if (ms_per_launch) *ms_per_launch = best_ms;
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_autotune_lookup(int32_t precision, int32_t scored_atoms, int64_t poses, int32_t* blocks_per_sm) {
+    g_err.clear();
+    if (!blocks_per_sm || (precision != FXE_PRECISION_REFERENCE && precision != FXE_PRECISION_FAST))
+        return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    *blocks_per_sm = tuned_blocks(precision, scored_atoms, poses);
     return FXE_OK;
 }

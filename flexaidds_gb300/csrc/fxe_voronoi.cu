@@ -1500,12 +1500,16 @@ size_t pose_smem_bytes() { return sizeof(PoseShared) * kVorWarps; }
 size_t pose_jobs_smem_bytes() { return sizeof(PoseShared) * kVorWarps; }
 
 static int g_resident_blocks = 0;   // blocks of pose_kernel the device holds at once
+static int g_sms = 0, g_per_sm = 0;  // SMs, and blocks of pose_kernel one SM holds
 
 // Blocks of a launch over n poses: no more than the device holds at once (the warps take poses
-// from a queue), and no more than the face history holds (hist_bytes; 0: no history).
-static unsigned pose_blocks(int n, size_t hist_bytes) {
+// from a queue), no more than blocks_per_sm per SM when that is set (> 0; the autotuner's
+// occupancy cap), and no more than the face history holds (hist_bytes; 0: no history).
+static unsigned pose_blocks(int n, size_t hist_bytes, int blocks_per_sm) {
     int b = (n + kVorWarps - 1) / kVorWarps;
     if (g_resident_blocks > 0 && g_resident_blocks < b) b = g_resident_blocks;
+    if (blocks_per_sm > 0 && g_sms > 0 && blocks_per_sm < g_per_sm && g_sms * blocks_per_sm < b)
+        b = g_sms * blocks_per_sm;
     if (hist_bytes) {
         const size_t cap = hist_bytes / (kVorWarps * kHistStride);
         if ((size_t)b > cap) b = (int)cap;
@@ -1514,22 +1518,26 @@ static unsigned pose_blocks(int n, size_t hist_bytes) {
 }
 
 size_t pose_hist_bytes() { return (size_t)g_resident_blocks * kVorWarps * kHistStride; }
+int pose_max_blocks_per_sm() { return g_per_sm; }
+int pose_warps_per_block() { return kVorWarps; }
 
-// hist / hist_bytes: the launch's face history (reference face order), or null / 0.
+// hist / hist_bytes: the launch's face history (reference face order), or null / 0;
+// blocks_per_sm: occupancy cap (0: as many as fit).
 void launch_poses(const DevSystem& S, const DevWork& W, int n, int* next, uint8_t* hist, size_t hist_bytes,
-                  cudaStream_t st) {
+                  int blocks_per_sm, cudaStream_t st) {
     if (hist_bytes < kVorWarps * kHistStride) hist = nullptr;
     if (!hist) hist_bytes = 0;
     cudaMemsetAsync(next, 0, sizeof(int), st);
-    pose_kernel<<<pose_blocks(n, hist_bytes), kVorWarps * 32, pose_smem_bytes(), st>>>(S, W, n, next, hist);
+    pose_kernel<<<pose_blocks(n, hist_bytes, blocks_per_sm), kVorWarps * 32, pose_smem_bytes(), st>>>(S, W, n, next,
+                                                                                                       hist);
 }
 
 void launch_poses_jobs(const Job* jobs, int n_jobs, int total, int* next, const int* order, uint8_t* hist,
-                       size_t hist_bytes, cudaStream_t st) {
+                       size_t hist_bytes, int blocks_per_sm, cudaStream_t st) {
     if (hist_bytes < kVorWarps * kHistStride) hist = nullptr;
     if (!hist) hist_bytes = 0;
     cudaMemsetAsync(next, 0, sizeof(int), st);
-    pose_kernel_jobs<<<pose_blocks(total, hist_bytes), kVorWarps * 32, pose_jobs_smem_bytes(), st>>>(
+    pose_kernel_jobs<<<pose_blocks(total, hist_bytes, blocks_per_sm), kVorWarps * 32, pose_jobs_smem_bytes(), st>>>(
         jobs, n_jobs, total, next, order, hist);
 }
 
@@ -1543,7 +1551,9 @@ cudaError_t configure_voronoi() {
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pose_kernel, kVorWarps * 32, pose_smem_bytes())) != cudaSuccess)
         return e;
-    g_resident_blocks = sms * (per_sm > 0 ? per_sm : 1);
+    g_sms = sms;
+    g_per_sm = per_sm > 0 ? per_sm : 1;
+    g_resident_blocks = sms * g_per_sm;
     return cudaSuccess;
 }
 

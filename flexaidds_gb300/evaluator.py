@@ -81,6 +81,9 @@ def load_library():
         lib.fxe_ensemble_dedup.argtypes = [C.c_int64, C.c_int32, _d, _d, C.POINTER(C.c_int64), _d,
                                            C.POINTER(C.c_int64)]
         lib.fxe_cleft_grid.argtypes = [C.c_int32, _f, _f, C.c_float, _f, C.c_int64, _f, _f, C.POINTER(C.c_int64)]
+        lib.fxe_context_autotune.argtypes = [vp, C.c_int32, vp, C.c_int32, C.POINTER(C.c_int32),
+                                             C.POINTER(C.c_double)]
+        lib.fxe_autotune_lookup.argtypes = [C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_int32)]
         lib.fxe_context_destroy.argtypes = [vp]
         lib.fxe_context_destroy.restype = None
         lib.fxe_last_error.restype = C.c_char_p
@@ -206,6 +209,13 @@ class GPUEvaluator:
         ms = np.zeros(1, np.float64)
         _check(self.lib.fxe_last_cluster_time(self.handle, ptr(ms, _d)))
         return float(ms[0])
+
+    def autotune(self, d_genes: int, n: int, reps: int = 2) -> tuple:
+        """fxe_context_autotune over n device chromosomes: (blocks per SM chosen, its launch ms)."""
+        b, ms = C.c_int32(0), C.c_double(0.0)
+        _check(self.lib.fxe_context_autotune(self.handle, int(n), C.c_void_p(d_genes), int(reps), C.byref(b),
+                                             C.byref(ms)))
+        return int(b.value), float(ms.value)
 
     def decode_genes(self, genes: np.ndarray, clamp: bool = False) -> np.ndarray:
         """genetoic of every gene on the device (fxe_decode_genes); clamp as eval_chromosome."""
@@ -385,6 +395,13 @@ class GAEngine:
             self.close()
         except Exception:
             pass
+
+
+def autotune_lookup(precision: int, scored_atoms: int, poses: int) -> int:
+    """The occupancy cap the autotuner's table holds for a size class (0: not tuned)."""
+    b = C.c_int32(0)
+    _check(load_library().fxe_autotune_lookup(int(precision), int(scored_atoms), int(poses), C.byref(b)))
+    return int(b.value)
 
 
 def ga_draws_per_pair(n_genes: int) -> int:

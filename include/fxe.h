@@ -254,7 +254,9 @@ fxe_status fxe_thermo_compute_device(const double* d_energies, const int32_t* d_
  *   energies); larger n is rejected with FXE_ERR_INVALID_ARGS before any work is queued.
  * - The first call on a device looks up the array's address (cudaGetSymbolAddress, with that
  *   device current) and loads the library's device code; make that first call before any stream
- *   capture and before memory is handed out.
+ *   capture and before memory is handed out. The address is kept for the life of the process:
+ *   after a cudaDeviceReset the library's device code is loaded anew and the kept address no
+ *   longer names the array, so do not call this entry point on a device that was reset.
  * - Nothing needs to start at zero: every partial a call reads is written by that call.
  * - Calls on one device share the array: calls whose work overlaps (different streams, or
  *   host threads without ordering) race and give wrong results. Serialise them on one stream.
@@ -473,6 +475,22 @@ fxe_status fxe_ga_niche_counts(int32_t population, int32_t n_genes, const double
  * same device code on a job's snapshots. Allocates its device buffers per call. */
 fxe_status fxe_ensemble_dedup(int64_t n, int32_t n_genes, const double* ic, const double* energies,
                               int64_t* kept_index, double* kept_energy, int64_t* n_kept);
+
+/* Autotuner of the polyhedron launch. The launch hands poses to as many warps as the SMs hold; how
+ * many run at once on an SM (the occupancy cap) trades latency hiding against contention for the
+ * SM's double-precision pipe and instruction cache, differently for different ligand sizes and
+ * batch sizes. fxe_context_autotune times the launch over this context's batch (d_genes: n int32
+ * chromosomes in device memory, n <= max_poses) at every cap from half the SM's capacity to all of
+ * it, `reps` timed launches each after one warm-up, and records the fastest in a process-wide table
+ * keyed by size class: precision x scored atoms per pose (<= 16, 32, 64, more) x poses per launch
+ * (<= 128, 512, 2048, 16384, more). Every later launch of that class, by any context, batch or GA
+ * engine (captured when its set of jobs changes), uses it. Results never depend on the cap.
+ * Outputs: the cap chosen (blocks per SM), and its fastest launch time (ms). Synchronous. No
+ * reference counterpart. */
+fxe_status fxe_context_autotune(fxe_context* ctx, int32_t n, const int32_t* d_genes, int32_t reps,
+                                int32_t* blocks_per_sm, double* ms_per_launch);
+/* The cap the table holds for a size class (0: not tuned, as many blocks as fit). */
+fxe_status fxe_autotune_lookup(int32_t precision, int32_t scored_atoms, int64_t poses, int32_t* blocks_per_sm);
 
 /* Message describing the last error on the calling thread ("" if none). */
 const char* fxe_last_error(void);
