@@ -136,6 +136,7 @@ struct VorShared {
     float4 plf[kMaxPlanes];        // the planes rounded to single precision, for pre-tests
 #endif
     uint8_t flag[kMaxPlanes];
+    uint8_t sprev[kMaxCand];       // per face: point 1 before a replayed stale read (kNone: none)
     int eng[4];
     int epi;
     int nv;
@@ -230,9 +231,11 @@ __device__ __forceinline__ real angle_between(real ux, real uy, real uz, real vx
 __device__ FXE_COLD real sph_arc(const real4& ao, const real4& b, const real4& c, real rado) {
     const real cosAOB = (ao.x * b.x + ao.y * b.y + ao.z * b.z) / (ao.w * b.w);
     const real cosBOC = (b.x * c.x + b.y * c.y + b.z * c.z) / (b.w * c.w);
-    const real U = (1 + cosAOB) * sqrt((1 + cosBOC) / real(8.0));
-    const real V = (1 - cosAOB) * sqrt((1 + cosBOC) / real(8.0));
-    const real W = sqrt((1 - cosAOB) * (1 + cosAOB) * (1 - cosBOC) / real(8.0));
+    // (x / 8 and x * 0.125 are the same correctly rounded value: the multiply is the cheaper)
+    const real h = sqrt((1 + cosBOC) * real(0.125));
+    const real U = (1 + cosAOB) * h;
+    const real V = (1 - cosAOB) * h;
+    const real W = sqrt((1 - cosAOB) * (1 + cosAOB) * (1 - cosBOC) * real(0.125));
     const real tS = (1 - U + V + W + W) / (1 + U - V - W - W);
     const real tSB = (1 - U - V) / (1 + U + V);
     const real tSA = (1 - U + V - W - W) / (1 + U - V + W + W);
@@ -368,61 +371,104 @@ __device__ FXE_COLD WalkStep walk_step_exact(const VorShared& sh, int NC, int e,
     return r;
 }
 
-// The same step with the plane tests decided in single precision (double builds): each lane
-// pre-tests its planes; when the winner is surely positive and every other plane is surely not
-// positive or surely farther, only the winner's vt is evaluated in double. Otherwise, and for
-// the bounding planes when the pre-test cannot rule them out, the step is redone in double.
-__device__ WalkStep walk_step(const VorShared& sh, int NC, int e, real rr, int lane) {
-#if FXE_FILTER
-    const uchar4 ep = sh.u.e.ep[e];
-    const real3 V = sh.u.e.ev[e];
-    const real4 s = sh.vx[sh.u.e.es[e].x];
+// The hull walk steps several open edges at once: a step's result depends only on its edge (start
+// vertex, direction, planes), all fixed when the edge was made, and the reference takes every edge
+// that is open now, in index order, before any edge the steps append (those get higher indices).
+// So the first kWalkGroups open edges are stepped together, one group of kWalkLanes lanes each (the
+// double-precision arithmetic of the step then serves four edges per warp instruction), and their
+// results are booked one after another in index order, skipping an edge an earlier one closed.
+constexpr int kWalkGroups = 4;
+constexpr int kWalkLanes = 32 / kWalkGroups;
+
+struct GroupStep {
+    real x, y, z;
+    int pc;        // closing plane, -1 if none
+    bool unsure;   // the single-precision pre-tests did not decide it: redo with walk_step_exact
+};
+
+// Argmin over the lanes of one group (ties to the lower plane index, as the reference's strict
+// less-than over planes in index order keeps the first).
+template <typename V>
+__device__ __forceinline__ void group_argmin(V& v, int& i) {
+#pragma unroll
+    for (int o = kWalkLanes / 2; o > 0; o >>= 1) {
+        const V v2 = __shfl_xor_sync(kFull, v, o);
+        const int i2 = __shfl_xor_sync(kFull, i, o);
+        if (v2 < v || (v2 == v && i2 < i)) {
+            v = v2;
+            i = i2;
+        }
+    }
+}
+
+// One step for the group's edge e (e < 0: the group idles; every lane still joins the shuffles).
+// sub: the lane's index in its group; gmask: the group's lanes.
+__device__ GroupStep walk_step_group(const VorShared& sh, int NC, int e, real rr, int sub, unsigned gmask) {
+    const bool has = e >= 0;
+    uchar4 ep = make_uchar4(kNone, kNone, kNone, kNone);
+    real3 V = real3{real(0.0), real(0.0), real(0.0)};
+    real4 s = make_real4(real(0.0), real(0.0), real(0.0), real(0.0));
+    if (has) {
+        ep = sh.u.e.ep[e];
+        V = sh.u.e.ev[e];
+        s = sh.vx[sh.u.e.es[e].x];
+    }
     const int pA = ep.x, pB = ep.y, oldC = ep.z;
+    GroupStep r;
+#if FXE_FILTER
+    // planes pre-tested in single precision; when the winner is surely positive and every other
+    // plane surely not positive or surely farther, only the winner's vt is evaluated in double
     const float sx = (float)s.x, sy = (float)s.y, sz = (float)s.z;
     const float Vx = (float)V.x, Vy = (float)V.y, Vz = (float)V.z;
     float best = 9.9e9f, beste = 0.0f;
     int bi = INT_MAX;
     bool unsure = false;
-    #pragma unroll 1
-    for (int c = lane; c < NC; c += 32) {
-        if (c == pA || c == pB || c == oldC) continue;
-        float er;
-        bool ok;
-        const float vt = vt_pretest(sh.plf[c], sx, sy, sz, Vx, Vy, Vz, &er, &ok);
-        if (!ok) unsure = true;
-        else if (vt > 0.0f && vt < best) { best = vt; beste = er; bi = c; }
+    if (has) {
+        #pragma unroll 1
+        for (int c = sub; c < NC; c += kWalkLanes) {
+            if (c == pA || c == pB || c == oldC) continue;
+            float er;
+            bool ok;
+            const float vt = vt_pretest(sh.plf[c], sx, sy, sz, Vx, Vy, Vz, &er, &ok);
+            if (!ok) unsure = true;
+            else if (vt > 0.0f && vt < best) { best = vt; beste = er; bi = c; }
+        }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int o = kWalkLanes / 2; o > 0; o >>= 1) {
         const float b2 = __shfl_xor_sync(kFull, best, o);
         const float e2 = __shfl_xor_sync(kFull, beste, o);
         const int i2 = __shfl_xor_sync(kFull, bi, o);
         if (b2 < best || (b2 == best && i2 < bi)) { best = b2; beste = e2; bi = i2; }
     }
     if (bi != INT_MAX && !(best - beste > 0.0f)) unsure = true;
-    #pragma unroll 1
-    for (int c = lane; c < NC && !unsure; c += 32) {
-        if (c == pA || c == pB || c == oldC || c == bi) continue;
-        float er;
-        bool ok;
-        const float vt = vt_pretest(sh.plf[c], sx, sy, sz, Vx, Vy, Vz, &er, &ok);
-        if (ok && (vt + er <= 0.0f || (bi != INT_MAX && vt - er > best + beste))) continue;
-        unsure = true;
+    if (has) {
+        #pragma unroll 1
+        for (int c = sub; c < NC && !unsure; c += kWalkLanes) {
+            if (c == pA || c == pB || c == oldC || c == bi) continue;
+            float er;
+            bool ok;
+            const float vt = vt_pretest(sh.plf[c], sx, sy, sz, Vx, Vy, Vz, &er, &ok);
+            if (ok && (vt + er <= 0.0f || (bi != INT_MAX && vt - er > best + beste))) continue;
+            unsure = true;
+        }
     }
-    if (__any_sync(kFull, unsure)) return walk_step_exact(sh, NC, e, rr, lane);
+    unsure = (__ballot_sync(kFull, unsure) & gmask) != 0u;
     real vtmin = real(9.9e9);
-    int pC = bi;
-    if (bi != INT_MAX) {
+    if (!unsure && bi != INT_MAX) {
         const real4 P = sh.pl[bi];
         const real den = P.x * V.x + P.y * V.y + P.z * V.z;
         vtmin = -(P.x * s.x + P.y * s.y + P.z * s.z + P.w) / den;
     }
-    real x = s.x + vtmin * V.x, y = s.y + vtmin * V.y, z = s.z + vtmin * V.z;
-    if (x * x + y * y + z * z > rr) {
-        // the bounding planes lie 10 A out: most of the time surely farther than vtmin
-        bool need = bi == INT_MAX;
-        if (!need && lane < 4) {
-            const int c = NC + lane;
+    r.x = s.x + vtmin * V.x;
+    r.y = s.y + vtmin * V.y;
+    r.z = s.z + vtmin * V.z;
+    // outside the sphere: the bounding planes (10 A out) are most of the time surely farther
+    bool need = false;
+    if (has && !unsure && r.x * r.x + r.y * r.y + r.z * r.z > rr) {
+        need = bi == INT_MAX;
+        if (!need && sub < 4) {
+            const int c = NC + sub;
             if (c != pA && c != pB && c != oldC) {
                 float er;
                 bool ok;
@@ -430,17 +476,52 @@ __device__ WalkStep walk_step(const VorShared& sh, int NC, int e, real rr, int l
                 need = !(ok && (vt + er <= 0.0f || vt - er > (float)vtmin * 1.0000005f));
             }
         }
-        if (__any_sync(kFull, need)) return walk_step_exact(sh, NC, e, rr, lane);
     }
-    WalkStep r;
-    r.x = x;
-    r.y = y;
-    r.z = z;
-    r.pc = pC == INT_MAX ? -1 : pC;
-    return r;
+    // (every lane takes part in the ballot: it must not sit behind a short-circuit)
+    const unsigned need_lanes = __ballot_sync(kFull, need);
+    r.unsure = unsure || (need_lanes & gmask) != 0u;
+    r.pc = bi == INT_MAX ? -1 : bi;
 #else
-    return walk_step_exact(sh, NC, e, rr, lane);
+    real vtmin = real(9.9e9);
+    int pC = INT_MAX;
+    if (has) {
+        #pragma unroll 1
+        for (int c = sub; c < NC; c += kWalkLanes) {
+            if (c == pA || c == pB || c == oldC) continue;
+            const real4 P = sh.pl[c];
+            const real den = P.x * V.x + P.y * V.y + P.z * V.z;
+            if (den != real(0.0)) {
+                const real vt = -(P.x * s.x + P.y * s.y + P.z * s.z + P.w) / den;
+                if (vt < vtmin && vt > real(0.0)) { vtmin = vt; pC = c; }
+            }
+        }
+    }
+    group_argmin(vtmin, pC);
+    r.x = s.x + vtmin * V.x;
+    r.y = s.y + vtmin * V.y;
+    r.z = s.z + vtmin * V.z;
+    const bool out = has && r.x * r.x + r.y * r.y + r.z * r.z > rr;
+    if (out && sub < 4) {
+        const int c = NC + sub;
+        if (c != pA && c != pB && c != oldC) {
+            const real4 P = sh.pl[c];
+            const real den = P.x * V.x + P.y * V.y + P.z * V.z;
+            if (den != real(0.0)) {
+                const real vt = -(P.x * s.x + P.y * s.y + P.z * s.z + P.w) / den;
+                if (vt < vtmin && vt > real(0.0)) { vtmin = vt; pC = c; }
+            }
+        }
+    }
+    group_argmin(vtmin, pC);
+    if (out) {
+        r.x = s.x + vtmin * V.x;
+        r.y = s.y + vtmin * V.y;
+        r.z = s.z + vtmin * V.z;
+    }
+    r.pc = pC == INT_MAX ? -1 : pC;
+    r.unsure = false;
 #endif
+    return r;
 }
 
 // Face of flat item k: the last face X in [0, NC) whose first item is at or before k.
@@ -471,10 +552,11 @@ __device__ __forceinline__ real fan_triangle(const real4& v0, const real4& va, c
     const real cNN1 = (va.x * vb.x + va.y * vb.y + va.z * vb.z) / (va.w * vb.w);
     const real cN0a = (v0.x * va.x + v0.y * va.y + v0.z * va.z) / (v0.w * va.w);
     const real cN0b = (v0.x * vb.x + v0.y * vb.y + v0.z * vb.z) / (v0.w * vb.w);
-    const real U = sqrt((1 + cN0a) * (1 + cNN1) * (1 + cN0b) / real(8.0));
-    const real V = sqrt((1 - cN0a) * (1 - cNN1) * (1 + cN0b) / real(8.0));
-    const real W = sqrt((1 - cN0a) * (1 + cNN1) * (1 - cN0b) / real(8.0));
-    const real Xv = sqrt((1 + cN0a) * (1 - cNN1) * (1 - cN0b) / real(8.0));
+    // (x / 8 and x * 0.125 are the same correctly rounded value: the multiply is the cheaper)
+    const real U = sqrt((1 + cN0a) * (1 + cNN1) * (1 + cN0b) * real(0.125));
+    const real V = sqrt((1 - cN0a) * (1 - cNN1) * (1 + cN0b) * real(0.125));
+    const real W = sqrt((1 - cN0a) * (1 + cNN1) * (1 - cN0b) * real(0.125));
+    const real Xv = sqrt((1 + cN0a) * (1 - cNN1) * (1 - cN0b) * real(0.125));
     const real tS = (1 - U + V + W + Xv) / (1 + U - V - W - Xv);
     const real tSA = (1 - U - V - W + Xv) / (1 + U + V + W - Xv);
     const real tSB = (1 - U - V + W - Xv) / (1 + U + V - W + Xv);
@@ -502,48 +584,73 @@ __device__ __forceinline__ void add_in_order(VorShared& sh, int X, real v, int l
     __syncwarp();
 }
 
+// The face that the arc between points cur and nxt of engulfed face X is credited to
+// (LIB/Vcontacts.cpp:971-1000): the plane the two points share besides X, when it is neither the
+// sphere nor an engulfing plane; -1 when the reference moves on without crediting anything.
+__device__ __forceinline__ int engulf_comm(const VorShared& sh, int NC, int X, int cur, int nxt) {
+    const uchar4 qc = sh.vp[cur], qn = sh.vp[nxt];
+    int pa1, pa2;
+    if (qc.x == X) { pa1 = qc.y; pa2 = qc.z; }
+    else { pa1 = qc.x; pa2 = (qc.y == X) ? qc.z : qc.y; }
+    int comm;
+    if (pa1 == qn.x || pa1 == qn.y || pa1 == qn.z) comm = pa1;
+    else if (pa2 == qn.x || pa2 == qn.y || pa2 == qn.z) comm = pa2;
+    else return -1;
+    return (comm != kNone && !(comm < NC && (sh.flag[comm] & kEngulf))) ? comm : -1;
+}
+
 // Corrections for engulfing planes (LIB/Vcontacts.cpp:963-1041): arcs of the engulfed faces
-// credited to their neighbours, then the engulfing faces' own areas.
-__device__ FXE_COLD void engulf_corrections(VorShared& sh, int NC, real rado, real rr, real two_pi_r, int epi,
-                                            int lane) {
+// credited to their neighbours, then the engulfing faces' own areas. The reference walks the
+// engulfed faces' points one after another; here each (face, point) item of the flat face lists
+// goes to a lane, the arcs are evaluated together, and each neighbour's sum is formed in the
+// reference's order. tot_pts: the length of the flat face lists.
+__device__ FXE_COLD void engulf_corrections(VorShared& sh, int NC, int tot_pts, real rado, real rr, real two_pi_r,
+                                            int epi, int lane) {
     if (epi > 0) {
-        if (lane == 0) {
-            #pragma unroll 1
-            for (int X = 0; X < NC; ++X) {
-                if (!(sh.flag[X] & kEngulf)) continue;
+        #pragma unroll 1
+        for (int k0 = 0; k0 < tot_pts; k0 += 32) {
+            const int k = k0 + lane;
+            int comm = -1, X = 0, cur = 0, nxt = 0;
+            if (k < tot_pts) {
+                X = face_of(sh.foff, NC, k);
+                const int vi = k - sh.foff[X];
                 const int np = sh.fnp[X];
-                const uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
-                const real4 cp = centre_of(sh.pl[X]);
-                #pragma unroll 1
-                for (int vi = 0; vi < np; ++vi) {
-                    const int cur = pt[vi], nxt = pt[(vi + 1) % np];
-                    const uchar4 qc = sh.vp[cur], qn = sh.vp[nxt];
-                    int pa1, pa2;
-                    if (qc.x == X) { pa1 = qc.y; pa2 = qc.z; }
-                    else { pa1 = qc.x; pa2 = (qc.y == X) ? qc.z : qc.y; }
-                    int comm;
-                    if (pa1 == qn.x || pa1 == qn.y || pa1 == qn.z) comm = pa1;
-                    else if (pa2 == qn.x || pa2 == qn.y || pa2 == qn.z) comm = pa2;
-                    else continue;
-                    if (comm != kNone && !(comm < NC && (sh.flag[comm] & kEngulf))) {
-                        if (comm < NC) sh.area[comm] += sph_arc(cp, sh.vx[cur], sh.vx[nxt], rado);
-                        if (np == 2) break;
+                if ((sh.flag[X] & kEngulf) && vi < np) {
+                    const uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
+                    // a face of two points stops after its first credited (or sphere-bound) arc
+                    if (!(np == 2 && vi == 1 && engulf_comm(sh, NC, X, pt[0], pt[1]) >= 0)) {
+                        cur = pt[vi];
+                        nxt = pt[(vi + 1) % np];
+                        const int c = engulf_comm(sh, NC, X, cur, nxt);
+                        if (c >= 0 && c < NC) comm = c;
                     }
                 }
             }
-            if (epi == 1) {
-                sh.area[sh.eng[0]] = two_pi_r * (rado + fabs(sh.pl[sh.eng[0]].w));
-            } else if (epi == 2) {
-                real q0[3], q1[3];
-                const real full = two_pi_r * rado;
-                if (!solve2s(sh.pl[sh.eng[0]], sh.pl[sh.eng[1]], rr, q0, q1)) {
+            if (__any_sync(kFull, comm >= 0)) {
+                real v = real(0.0);
+                if (comm >= 0) v = sph_arc(centre_of(sh.pl[X]), sh.vx[cur], sh.vx[nxt], rado);
+                add_in_order(sh, comm, v, lane);
+            }
+        }
+        if (epi == 1) {
+            if (lane == 0) sh.area[sh.eng[0]] = two_pi_r * (rado + fabs(sh.pl[sh.eng[0]].w));
+        } else if (epi == 2) {
+            real q0[3], q1[3];
+            const real full = two_pi_r * rado;
+            const bool ok = solve2s(sh.pl[sh.eng[0]], sh.pl[sh.eng[1]], rr, q0, q1);
+            real m = real(0.0);
+            if (ok && lane < 2) {
+                const real4 Bp = make_real4(q0[0], q0[1], q0[2], rado);
+                const real4 Cp = make_real4(q1[0], q1[1], q1[2], rado);
+                m = sph_arc(centre_of(sh.pl[sh.eng[lane]]), Bp, Cp, rado);
+            }
+            const real m1 = __shfl_sync(kFull, m, 1);
+            if (lane == 0) {
+                if (!ok) {
                     sh.area[sh.eng[0]] = full;
                     sh.area[sh.eng[1]] = full;
                 } else {
-                    const real4 Bp = make_real4(q0[0], q0[1], q0[2], rado);
-                    const real4 Cp = make_real4(q1[0], q1[1], q1[2], rado);
-                    real m = sph_arc(centre_of(sh.pl[sh.eng[0]]), Bp, Cp, rado);
-                    m += sph_arc(centre_of(sh.pl[sh.eng[1]]), Bp, Cp, rado);
+                    m += m1;
                     sh.area[sh.eng[0]] = full - real(0.5) * m;
                     sh.area[sh.eng[1]] = full - real(0.5) * m;
                 }
@@ -670,74 +777,117 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     }
     __syncwarp();
 
-    // ---- hull walk (LIB/Vcontacts.cpp:262-410) ----
+    // ---- hull walk (LIB/Vcontacts.cpp:262-410), the open edges stepped kWalkGroups at a time ----
     int edgenum = 3, startedge = 0, vn = 1;
+    const int sub = lane & (kWalkLanes - 1);
+    const unsigned gmask = ((1u << kWalkLanes) - 1u) << (lane & ~(kWalkLanes - 1));
     #pragma unroll 1
     for (;;) {
         while (startedge < edgenum && sh.u.e.es[startedge].y != kNone) ++startedge;
         if (startedge >= edgenum) break;
-        const WalkStep r = walk_step(sh, NC, startedge, rr, lane);
-        const int pC = r.pc;
-        if (pC < 0) return kAtomHullFail;
-        if (vn >= kMaxVerts - 1) return kAtomCapacity;
-        const uchar4 ep = sh.u.e.ep[startedge];
-        const int pA = ep.x, pB = ep.y;
-        // edges (pA, pC) and (pB, pC): the first open match after startedge, else a new edge
-        int mAC = INT_MAX, mBC = INT_MAX;
+        // the first kWalkGroups open edges, in index order (one byte each)
+        unsigned batch = 0u;
+        int nb = 0;
         #pragma unroll 1
-        for (int e0 = startedge + 1; e0 < edgenum; e0 += 32) {
+        for (int e0 = startedge; e0 < edgenum && nb < kWalkGroups; e0 += 32) {
             const int f = e0 + lane;
-            bool ac = false, bc = false;
-            if (f < edgenum) {
-                const uchar4 q = sh.u.e.ep[f];
-                ac = (q.x == pA && q.y == pC) || (q.x == pC && q.y == pA);
-                bc = (q.x == pB && q.y == pC) || (q.x == pC && q.y == pB);
+            unsigned m = __ballot_sync(kFull, f < edgenum && sh.u.e.es[f].y == kNone);
+            while (m && nb < kWalkGroups) {
+                batch |= (unsigned)(e0 + __ffs(m) - 1) << (8 * nb);
+                m &= m - 1;
+                ++nb;
             }
-            const unsigned ma = __ballot_sync(kFull, ac), mb = __ballot_sync(kFull, bc);
-            if (ma && mAC == INT_MAX) mAC = e0 + __ffs(ma) - 1;
-            if (mb && mBC == INT_MAX) mBC = e0 + __ffs(mb) - 1;
         }
-        __syncwarp();
-        // lane 0 books the vertex and edge (pA, pC), lane 1 edge (pB, pC); a new edge's direction
-        // comes from the vertex just found (its distance is filled in after the walk)
-        // a walk that keeps opening edges past the reference's 200-edge check ends here: as a
-        // hull failure when the reference's check fails it at this step, else over capacity
-        const int n_new = (mAC == INT_MAX) + (mBC == INT_MAX);
-        if (edgenum + n_new > kMaxEdges + 2) return mBC == INT_MAX ? kAtomHullFail : kAtomCapacity;
-        const int eAC = mAC != INT_MAX ? mAC : edgenum;
-        const int eBC = mBC != INT_MAX ? mBC : edgenum + (mAC == INT_MAX ? 1 : 0);
-        if (lane == 0) {
-            sh.vx[vn] = make_real4(r.x, r.y, r.z, real(0.0));
-            sh.vp[vn] = make_uchar4((uint8_t)pA, (uint8_t)pB, (uint8_t)pC, 0);
-            sh.u.e.es[startedge].y = (uint8_t)vn;
-            sh.u.e.ep[startedge].w = (uint8_t)pC;
-            sh.flag[pC] |= kOnHull;
-        }
-        if (lane < 2) {
-            const bool match = lane == 0 ? mAC != INT_MAX : mBC != INT_MAX;
-            const int e = lane == 0 ? eAC : eBC;
-            const int p0 = lane == 0 ? pA : pB, tp = lane == 0 ? pB : pA;
-            if (match) {
+        const int grp = lane / kWalkLanes;
+        const GroupStep gs = walk_step_group(sh, NC, grp < nb ? (int)((batch >> (8 * grp)) & 0xffu) : -1, rr, sub, gmask);
+        // book the steps in index order; a new edge's direction is set after the batch (lane j
+        // holds the j-th new edge: slot, planes, start vertex)
+        int n_pend = 0, pe = 0, p0e = 0, pce = 0, tpe = 0, pve = 0;
+        #pragma unroll 1
+        for (int g = 0; g < nb; ++g) {
+            const int e = (batch >> (8 * g)) & 0xffu;
+            real rx = __shfl_sync(kFull, gs.x, g * kWalkLanes);
+            real ry = __shfl_sync(kFull, gs.y, g * kWalkLanes);
+            real rz = __shfl_sync(kFull, gs.z, g * kWalkLanes);
+            int pC = __shfl_sync(kFull, gs.pc, g * kWalkLanes);
+            const bool unsure = __shfl_sync(kFull, (int)gs.unsure, g * kWalkLanes) != 0;
+            if (sh.u.e.es[e].y != kNone) continue;   // closed by an earlier edge of the batch
+            startedge = e;
+            if (unsure) {
+                const WalkStep w = walk_step_exact(sh, NC, e, rr, lane);
+                rx = w.x;
+                ry = w.y;
+                rz = w.z;
+                pC = w.pc;
+            }
+            if (pC < 0) return kAtomHullFail;
+            if (vn >= kMaxVerts - 1) return kAtomCapacity;
+            const uchar4 ep = sh.u.e.ep[e];
+            const int pA = ep.x, pB = ep.y;
+            // edges (pA, pC) and (pB, pC): the first match after this edge, else a new edge
+            int mAC = INT_MAX, mBC = INT_MAX;
+            #pragma unroll 1
+            for (int e0 = e + 1; e0 < edgenum; e0 += 32) {
+                const int f = e0 + lane;
+                bool ac = false, bc = false;
+                if (f < edgenum) {
+                    const uchar4 q = sh.u.e.ep[f];
+                    ac = (q.x == pA && q.y == pC) || (q.x == pC && q.y == pA);
+                    bc = (q.x == pB && q.y == pC) || (q.x == pC && q.y == pB);
+                }
+                const unsigned ma = __ballot_sync(kFull, ac), mb = __ballot_sync(kFull, bc);
+                if (ma && mAC == INT_MAX) mAC = e0 + __ffs(ma) - 1;
+                if (mb && mBC == INT_MAX) mBC = e0 + __ffs(mb) - 1;
+            }
+            __syncwarp();
+            // a walk that keeps opening edges past the reference's 200-edge check ends here: as a
+            // hull failure when the reference's check fails it at this step, else over capacity
+            const int n_new = (mAC == INT_MAX) + (mBC == INT_MAX);
+            if (edgenum + n_new > kMaxEdges + 2) return mBC == INT_MAX ? kAtomHullFail : kAtomCapacity;
+            const int eAC = mAC != INT_MAX ? mAC : edgenum;
+            const int eBC = mBC != INT_MAX ? mBC : edgenum + (mAC == INT_MAX ? 1 : 0);
+            if (lane == 0) {
+                sh.vx[vn] = make_real4(rx, ry, rz, real(0.0));
+                sh.vp[vn] = make_uchar4((uint8_t)pA, (uint8_t)pB, (uint8_t)pC, 0);
                 sh.u.e.es[e].y = (uint8_t)vn;
-                sh.u.e.ep[e].w = (uint8_t)tp;
-            } else {
-                const real4 a = sh.pl[p0], b = sh.pl[pC], t = sh.pl[tp];
-                real vx = a.y * b.z - a.z * b.y;
-                real vy = a.z * b.x - a.x * b.z;
-                real vz = a.x * b.y - a.y * b.x;
-                const real tv = t.x * (r.x + vx) + t.y * (r.y + vy) + t.z * (r.z + vz) + t.w;
-                if (tv > real(0.0)) { vx = -vx; vy = -vy; vz = -vz; }
-                sh.u.e.ev[e] = real3{vx, vy, vz};
-                sh.u.e.ep[e] = make_uchar4((uint8_t)p0, (uint8_t)pC, (uint8_t)tp, kNone);
-                sh.u.e.es[e] = make_uchar2((uint8_t)vn, kNone);
+                sh.u.e.ep[e].w = (uint8_t)pC;
+                sh.flag[pC] |= kOnHull;
             }
+            if (lane < 2) {
+                const bool match = lane == 0 ? mAC != INT_MAX : mBC != INT_MAX;
+                const int ee = lane == 0 ? eAC : eBC;
+                const int p0 = lane == 0 ? pA : pB, tp = lane == 0 ? pB : pA;
+                if (match) {
+                    sh.u.e.es[ee].y = (uint8_t)vn;
+                    sh.u.e.ep[ee].w = (uint8_t)tp;
+                } else {
+                    sh.u.e.ep[ee] = make_uchar4((uint8_t)p0, (uint8_t)pC, (uint8_t)tp, kNone);
+                    sh.u.e.es[ee] = make_uchar2((uint8_t)vn, kNone);
+                }
+            }
+            const int jAC = n_pend, jBC = n_pend + (mAC == INT_MAX ? 1 : 0);
+            if (mAC == INT_MAX && lane == jAC) { pe = eAC; p0e = pA; pce = pC; tpe = pB; pve = vn; }
+            if (mBC == INT_MAX && lane == jBC) { pe = eBC; p0e = pB; pce = pC; tpe = pA; pve = vn; }
+            n_pend += n_new;
+            if (mAC == INT_MAX) ++edgenum;
+            if (mBC == INT_MAX) {
+                ++edgenum;
+                if (edgenum >= kMaxEdges) return kAtomHullFail;
+            }
+            ++vn;
+            __syncwarp();
         }
-        if (mAC == INT_MAX) ++edgenum;
-        if (mBC == INT_MAX) {
-            ++edgenum;
-            if (edgenum >= kMaxEdges) return kAtomHullFail;
+        // the new edges' directions, oriented away from their third plane (add_vedge)
+        if (lane < n_pend) {
+            const real4 a = sh.pl[p0e], b = sh.pl[pce], t = sh.pl[tpe];
+            const real4 r = sh.vx[pve];
+            real vx = a.y * b.z - a.z * b.y;
+            real vy = a.z * b.x - a.x * b.z;
+            real vz = a.x * b.y - a.y * b.x;
+            const real tv = t.x * (r.x + vx) + t.y * (r.y + vy) + t.z * (r.z + vz) + t.w;
+            if (tv > real(0.0)) { vx = -vx; vy = -vy; vz = -vz; }
+            sh.u.e.ev[pe] = real3{vx, vy, vz};
         }
-        ++vn;
         __syncwarp();
     }
     // vertex distances to the centre, all at once
@@ -880,16 +1030,17 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         n_extra += t;
     }
     __syncwarp();
-    // ordering around each face (pt[0], a neighbour of it, then decreasing cosine)
+    // ordering around each face (pt[0], a neighbour of it, then decreasing cosine): the second
+    // point per face (one face per lane), the cosines of all faces' points spread over the lanes,
+    // then each face's sort and its history (one face per lane)
     int np_miss = 0, np_lost = 0;
     #pragma unroll 1
     for (int X = lane; X < NC; X += 32) {
         if (sh.flag[X] == 0) continue;
         const int np = sh.fnp[X];
         uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
-        int stale_prev = -1;   // point 1 of the face before a replayed read of the slot past its end
+        int stale_prev = kNone;   // point 1 of the face before a replayed read of the slot past its end
         if (np > 3) {
-            real* cs = &sh.u.f.cosv[sh.foff[X]];
             const uchar4 P0 = sh.vp[pt[0]];
             const int pY = (P0.x == X) ? P0.y : P0.x;
             int vi = 1;
@@ -898,20 +1049,16 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
                 const uchar4 q = sh.vp[pt[vi]];
                 if (q.x == pY || q.y == pY || q.z == pY) break;
             }
-            real4 v1;
             bool replayed = false;
             if (vi == np) {
                 ++np_miss;
                 const int s = (hist && np < kHistPts) ? (int)hist[X * kHistPts + np] : -1;
                 if (s >= 0 && s < kMaxVerts - 1) {
                     // the reference swaps pt[1] with the stale slot: the slot's vertex becomes
-                    // point 1, the old point 1 stays behind in the slot. The vertex is read as it
-                    // stood when this face was ordered: an antipodal point a later face appends
-                    // had not yet replaced the slot's old contents.
+                    // point 1, the old point 1 stays behind in the slot
                     replayed = true;
                     stale_prev = pt[1];
                     pt[1] = (uint8_t)s;
-                    v1 = (s >= NV && s < NV + n_extra && sh.vp[s].x > X) ? hist_vx(hist)[s - NV] : sh.vx[s];
                 } else {
                     if (hist) ++np_lost;
                     const int pZ = (P0.x == X || P0.y == X) ? P0.z : P0.y;
@@ -931,11 +1078,39 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
                 const uint8_t tmp = pt[vi];
                 pt[vi] = pt[1];
                 pt[1] = tmp;
-                v1 = sh.vx[pt[1]];
             }
-            const real4 v0 = sh.vx[pt[0]];
-            #pragma unroll 1
-            for (int k = 2; k < np; ++k) cs[k] = cos_pqr(v1, v0, sh.vx[pt[k]]);
+        }
+        sh.sprev[X] = (uint8_t)stale_prev;
+    }
+    *no_partner += warp_sum(np_miss);
+    *unreplayed += warp_sum(np_lost);
+    __syncwarp();
+    #pragma unroll 1
+    for (int k0 = 0; k0 < tot_pts; k0 += 32) {
+        const int k = k0 + lane;
+        if (k < tot_pts) {
+            const int X = face_of(sh.foff, NC, k);
+            const int j = k - sh.foff[X];
+            const int np = sh.fnp[X];
+            if (sh.flag[X] != 0 && np > 3 && j >= 2 && j < np) {
+                const uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
+                // point 1 is read as it stood when the reference ordered this face: a replayed
+                // slot that a later face's antipodal point takes still held its old vertex
+                const int s1 = pt[1];
+                const real4 v1 = (hist && s1 >= NV && s1 < NV + n_extra && sh.vp[s1].x > X) ? hist_vx(hist)[s1 - NV]
+                                                                                          : sh.vx[s1];
+                sh.u.f.cosv[sh.foff[X] + j] = cos_pqr(v1, sh.vx[pt[0]], sh.vx[pt[j]]);
+            }
+        }
+    }
+    __syncwarp();
+    #pragma unroll 1
+    for (int X = lane; X < NC; X += 32) {
+        if (sh.flag[X] == 0) continue;
+        const int np = sh.fnp[X];
+        uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
+        if (np > 3) {
+            real* cs = &sh.u.f.cosv[sh.foff[X]];
             #pragma unroll 1
             for (int a = 2; a < np - 1; ++a)
                 #pragma unroll 1
@@ -954,11 +1129,9 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
             const int nw = np < kHistPts ? np : kHistPts;
             #pragma unroll 1
             for (int k = 0; k < nw; ++k) h[k] = pt[k];
-            if (stale_prev >= 0) h[np] = (uint8_t)stale_prev;
+            if (sh.sprev[X] != kNone) h[np] = sh.sprev[X];
         }
     }
-    *no_partner += warp_sum(np_miss);
-    *unreplayed += warp_sum(np_lost);
     __syncwarp();
 
     // ---- areas (LIB/Vcontacts.cpp:838-1044) ----
@@ -990,7 +1163,9 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
                 pp[1] = sh.vx[kMaxVerts - 1].y;
                 pp[2] = sh.vx[kMaxVerts - 1].z;
             } else {
-                pp[0] = (q0[0] + q1[0]) / 2; pp[1] = (q0[1] + q1[1]) / 2; pp[2] = (q0[2] + q1[2]) / 2;
+                pp[0] = (q0[0] + q1[0]) * real(0.5);   // the same value as / 2
+                pp[1] = (q0[1] + q1[1]) * real(0.5);
+                pp[2] = (q0[2] + q1[2]) * real(0.5);
             }
         } else {
             solve3(sh.pl[sh.eng[0]], sh.pl[sh.eng[1]], sh.pl[sh.eng[2]], pp);
@@ -1088,7 +1263,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         add_in_order(sh, X, v, lane);
     }
     __syncwarp();
-    engulf_corrections(sh, NC, rado, rr, two_pi_r, epi, lane);
+    engulf_corrections(sh, NC, tot_pts, rado, rr, two_pi_r, epi, lane);
     sh.nv = NV;
     __syncwarp();
     return kAtomOk;
