@@ -280,7 +280,9 @@ def run_gpu(args):
         ev.eval_genes_device(dgen[k % N_POPULATIONS].data_ptr(), pop, dout.data_ptr(), stream.cuda_stream)
 
     # the polyhedron launch's occupancy cap for this size class, tuned on the first population
-    tuned_cap, tuned_ms = ev.autotune(dgen[0].data_ptr(), pop, reps=2)
+    sweep = ev.autotune_sweep(dgen[0].data_ptr(), pop, reps=2)
+    tuned_cap = min(sweep, key=lambda c: (sweep[c], c))
+    tuned_ms = sweep[tuned_cap]
 
     # --- device-resident: inputs in HBM, timed on the launching stream -----------------------
     with torch.cuda.stream(stream):
@@ -419,7 +421,8 @@ def run_gpu(args):
         "e2e": {"value": world * pop * args.steps / e2e_s, "unit": "poses/s",
                 "h2d_bytes_per_step": pop * d.n_genes * 4, "d2h_bytes_per_step": pop * capi.CF_DTYPE.itemsize},
         "gpu_launches": launches,
-        "autotune": {"pose_blocks_per_sm": tuned_cap, "launch_ms": tuned_ms},
+        "autotune": {"pose_blocks_per_sm": tuned_cap, "launch_ms": tuned_ms,
+                     "sweep_ms": {str(c): round(t, 3) for c, t in sorted(sweep.items())}},
         "clocks": clk.summary(),
         "roofline": {"bound": "fp64" if prec == "reference" else "fp32", "achieved": achieved,
                      "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,

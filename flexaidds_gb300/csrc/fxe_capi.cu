@@ -2126,10 +2126,15 @@ extern "C" fxe_status fxe_cleft_grid(int32_t n_spheres, const float* centers, co
     return FXE_OK;
 }
 
-extern "C" fxe_status fxe_context_autotune(fxe_context* ctx, int32_t n, const int32_t* d_genes, int32_t reps,
-                                           int32_t* blocks_per_sm, double* ms_per_launch) {
+// The autotuner's sweep: times the polyhedron launch over the context's batch at every cap from
+// half the SM's capacity to all of it; fills caps/ms (up to max_out entries, may be null) and
+// records the fastest cap for the context's size class.
+static fxe_status autotune_sweep(fxe_context* ctx, int32_t n, const int32_t* d_genes, int32_t reps, int32_t* caps,
+                                 double* ms_out, int32_t max_out, int32_t* n_out, int32_t* blocks_per_sm,
+                                 double* ms_per_launch) {
     g_err.clear();
-    if (!ctx || n <= 0 || !d_genes || reps < 1 || reps > 100) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    if (!ctx || n <= 0 || !d_genes || reps < 1 || reps > 100 || max_out < 0)
+        return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
     if (n > ctx->W.max_poses) return fail(FXE_ERR_INVALID_ARGS, "n exceeds the context's max_poses");
     if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
     cudaStream_t s = ctx->stream;
@@ -2147,7 +2152,7 @@ extern "C" fxe_status fxe_context_autotune(fxe_context* ctx, int32_t n, const in
         cudaEventDestroy(a);
         return fail(FXE_ERR_LAUNCH, "cudaEventCreate");
     }
-    int best = 0;
+    int best = 0, n_done = 0;
     float best_ms = 0.0f;
     cudaError_t e = cudaSuccess;
     for (int c = std::max(1, maxb / 2); c <= maxb && e == cudaSuccess; ++c) {
@@ -2162,7 +2167,13 @@ extern "C" fxe_status fxe_context_autotune(fxe_context* ctx, int32_t n, const in
             if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
             if (r > 0 && (cand == 0.0f || ms < cand)) cand = ms;
         }
-        if (e == cudaSuccess && (best == 0 || cand < best_ms)) {
+        if (e != cudaSuccess) break;
+        if (n_done < max_out) {
+            if (caps) caps[n_done] = c;
+            if (ms_out) ms_out[n_done] = cand;
+            ++n_done;
+        }
+        if (best == 0 || cand < best_ms) {
             best = c;
             best_ms = cand;
         }
@@ -2175,9 +2186,20 @@ extern "C" fxe_status fxe_context_autotune(fxe_context* ctx, int32_t n, const in
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune[size_class(ctx->precision, ctx->S.n_sc + ctx->S.n_lig, n)] = best;
     }
+    if (n_out) *n_out = n_done;
     if (blocks_per_sm) *blocks_per_sm = best;
     if (ms_per_launch) *ms_per_launch = best_ms;
     return FXE_OK;
+}
+
+extern "C" fxe_status fxe_context_autotune(fxe_context* ctx, int32_t n, const int32_t* d_genes, int32_t reps,
+                                           int32_t* blocks_per_sm, double* ms_per_launch) {
+    return autotune_sweep(ctx, n, d_genes, reps, nullptr, nullptr, 0, nullptr, blocks_per_sm, ms_per_launch);
+}
+
+extern "C" fxe_status fxe_context_autotune_sweep(fxe_context* ctx, int32_t n, const int32_t* d_genes, int32_t reps,
+                                                 int32_t* caps, double* ms, int32_t max_out, int32_t* n_out) {
+    return autotune_sweep(ctx, n, d_genes, reps, caps, ms, max_out, n_out, nullptr, nullptr);
 }
 
 extern "C" fxe_status fxe_autotune_lookup(int32_t precision, int32_t scored_atoms, int64_t poses, int32_t* blocks_per_sm) {

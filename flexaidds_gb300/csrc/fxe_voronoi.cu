@@ -24,6 +24,7 @@ namespace fxe {
 namespace FXE_VARIANT {
 
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kFaceWords = (kMaxCand + 31) / 32;
 constexpr uint8_t kNone = 255;
 // Poses (warps) per block of pose_kernel. Two per block fit eight double-precision workspaces
 // (23 KB each) or twenty single-precision ones (10.6 KB) on an SM; the double kernel measured no
@@ -131,12 +132,19 @@ struct VorShared {
     uint8_t fnp[kMaxCand];
     uint16_t toff[kMaxCand + 1];   // per face: first fan triangle / arc segment in the flat lists
     uint16_t aoff[kMaxCand + 1];
-    real tmp[32];                  // one value per lane, for in-order sums
+    union {
+        real tmp[32];                  // one value per lane, for in-order sums
+        uint8_t elist[kMaxEdges + 8];  // the hull edges with an end outside the sphere
+    };
 #if FXE_FILTER
     float4 plf[kMaxPlanes];        // the planes rounded to single precision, for pre-tests
 #endif
     uint8_t flag[kMaxPlanes];
     uint8_t sprev[kMaxCand];       // per face: point 1 before a replayed stale read (kNone: none)
+    uint8_t flist[kMaxCand];       // faces whose test point is checked against the other planes
+    uint8_t llist[kMaxCand];       // faces of two points (lenses), in face order
+    uint32_t cmask[kFaceWords];    // faces with a test point
+    uint32_t bad[kFaceWords];      // faces whose test point lies in front of another plane
     int eng[4];
     int epi;
     int nv;
@@ -265,24 +273,34 @@ __device__ __forceinline__ real4 centre_of(const real4& pl) {
     return make_real4(-pl.x * pl.w, -pl.y * pl.w, -pl.z * pl.w, fabs(pl.w));
 }
 
-// test_point (LIB/Vcontacts.cpp:1357-1372): true unless x lies behind a contact plane.
-__device__ FXE_COLD bool inside_all(const VorShared& sh, int NC, int skip, real x, real y, real z) {
+// test_point (LIB/Vcontacts.cpp:1357-1372) for several faces at once: face X of sh.flist[0, nf) keeps its test point, held in
+// sh.u.f.cosv[3X .. 3X+2], when the point lies behind every flagged contact plane other than X.
+// The (face, plane) pairs are spread over the lanes; a face with a plane in front of its point
+// gets its bit in sh.bad.
+__device__ void faces_inside(VorShared& sh, int NC, int nf, int lane) {
+    if (lane < kFaceWords) sh.bad[lane] = 0u;
+    __syncwarp();
+    const int n = nf * NC;
     #pragma unroll 1
-    for (int cp = 0; cp < NC; ++cp) {
-        if (cp == skip || sh.flag[cp] == 0) continue;
-        if (dot3(sh.pl[cp], x, y, z) + sh.pl[cp].w > real(0.0)) return false;
+    for (int k = lane; k < n; k += 32) {
+        const int fi = k / NC, cp = k - fi * NC;
+        const int X = sh.flist[fi];
+        if (cp == X || sh.flag[cp] == 0) continue;
+        const real* q = &sh.u.f.cosv[3 * X];
+        if (dot3(sh.pl[cp], q[0], q[1], q[2]) + sh.pl[cp].w > real(0.0)) atomicOr(&sh.bad[X >> 5], 1u << (X & 31));
     }
-    return true;
+    __syncwarp();
 }
 
-__device__ void add_edge(VorShared& sh, int en, int p0, int p1, int tp, int sp) {
+// add_vedge (LIB/Vcontacts.cpp:633-660): edge en along planes p0 and p1 from vertex sp (at s),
+// pointing away from plane tp.
+__device__ void add_edge(VorShared& sh, int en, int p0, int p1, int tp, int sp, const real* s) {
     const real4 a = sh.pl[p0], b = sh.pl[p1];
     real vx = a.y * b.z - a.z * b.y;
     real vy = a.z * b.x - a.x * b.z;
     real vz = a.x * b.y - a.y * b.x;
-    const real4 s = sh.vx[sp];
     const real4 t = sh.pl[tp];
-    const real tv = t.x * (s.x + vx) + t.y * (s.y + vy) + t.z * (s.z + vz) + t.w;
+    const real tv = t.x * (s[0] + vx) + t.y * (s[1] + vy) + t.z * (s[2] + vz) + t.w;
     if (tv > real(0.0)) { vx = -vx; vy = -vy; vz = -vz; }
     sh.u.e.ev[en] = real3{vx, vy, vz};
     sh.u.e.ep[en] = make_uchar4((uint8_t)p0, (uint8_t)p1, (uint8_t)tp, kNone);
@@ -607,6 +625,10 @@ __device__ __forceinline__ int engulf_comm(const VorShared& sh, int NC, int X, i
 __device__ FXE_COLD void engulf_corrections(VorShared& sh, int NC, int tot_pts, real rado, real rr, real two_pi_r,
                                             int epi, int lane) {
     if (epi > 0) {
+        // the items that credit an arc, in order, packed (face, current point, next point,
+        // neighbour) into the cosine scratch (free by now), then their arcs a warp at a time
+        uint32_t* items = reinterpret_cast<uint32_t*>(sh.u.f.cosv);
+        int n_items = 0;
         #pragma unroll 1
         for (int k0 = 0; k0 < tot_pts; k0 += 32) {
             const int k = k0 + lane;
@@ -626,11 +648,24 @@ __device__ FXE_COLD void engulf_corrections(VorShared& sh, int NC, int tot_pts, 
                     }
                 }
             }
-            if (__any_sync(kFull, comm >= 0)) {
-                real v = real(0.0);
-                if (comm >= 0) v = sph_arc(centre_of(sh.pl[X]), sh.vx[cur], sh.vx[nxt], rado);
-                add_in_order(sh, comm, v, lane);
+            const unsigned m = __ballot_sync(kFull, comm >= 0);
+            if (comm >= 0)
+                items[n_items + __popc(m & lanemask_lt())] =
+                    (uint32_t)X | ((uint32_t)cur << 8) | ((uint32_t)nxt << 16) | ((uint32_t)comm << 24);
+            n_items += __popc(m);
+        }
+        __syncwarp();
+        #pragma unroll 1
+        for (int k0 = 0; k0 < n_items; k0 += 32) {
+            const int k = k0 + lane;
+            int comm = -1;
+            real v = real(0.0);
+            if (k < n_items) {
+                const uint32_t it = items[k];
+                comm = (int)(it >> 24);
+                v = sph_arc(centre_of(sh.pl[it & 0xffu]), sh.vx[(it >> 8) & 0xffu], sh.vx[(it >> 16) & 0xffu], rado);
             }
+            add_in_order(sh, comm, v, lane);
         }
         if (epi == 1) {
             if (lane == 0) sh.area[sh.eng[0]] = two_pi_r * (rado + fabs(sh.pl[sh.eng[0]].w));
@@ -763,17 +798,23 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     pC0 = bi;
     if (pC0 == INT_MAX) return kAtomCapacity;
     }
-    if (lane == 0) {
-        real t[3];
+    {
+        // the vertex on every lane (one warp instruction either way), then its three edges at once
+        real t[3] = {real(0.0), real(0.0), real(0.0)};
         solve3(sh.pl[pA0], sh.pl[pB0], sh.pl[pC0], t);
-        sh.vx[0] = make_real4(t[0], t[1], t[2], sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]));
-        sh.vp[0] = make_uchar4((uint8_t)pA0, (uint8_t)pB0, (uint8_t)pC0, 0);
-        sh.flag[pA0] |= kOnHull;
-        sh.flag[pB0] |= kOnHull;
-        sh.flag[pC0] |= kOnHull;
-        add_edge(sh, 0, pA0, pB0, pC0, 0);
-        add_edge(sh, 1, pB0, pC0, pA0, 0);
-        add_edge(sh, 2, pC0, pA0, pB0, 0);
+        if (lane == 0) {
+            sh.vx[0] = make_real4(t[0], t[1], t[2], sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]));
+            sh.vp[0] = make_uchar4((uint8_t)pA0, (uint8_t)pB0, (uint8_t)pC0, 0);
+            sh.flag[pA0] |= kOnHull;
+            sh.flag[pB0] |= kOnHull;
+            sh.flag[pC0] |= kOnHull;
+        }
+        if (lane < 3) {
+            const int p0 = lane == 0 ? pA0 : lane == 1 ? pB0 : pC0;
+            const int p1 = lane == 0 ? pB0 : lane == 1 ? pC0 : pA0;
+            const int tp = lane == 0 ? pC0 : lane == 1 ? pA0 : pB0;
+            add_edge(sh, lane, p0, p1, tp, 0, t);
+        }
     }
     __syncwarp();
 
@@ -898,36 +939,50 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     }
     __syncwarp();
 
-    // ---- arc points where edges leave the sphere (LIB/Vcontacts.cpp:418-462) ----
+    // ---- arc points where edges leave the sphere (LIB/Vcontacts.cpp:418-462): the edges with an
+    //      end outside the sphere listed in order, then their
+    //      sphere intersections a warp at a time ----
+    uint8_t* elist = sh.elist;
+    int n_out = 0;
     #pragma unroll 1
     for (int e0 = 0; e0 < edgenum; e0 += 32) {
         const int e = e0 + lane;
+        bool out = false;
+        if (e < edgenum) {
+            const uchar2 se = sh.u.e.es[e];
+            out = rado < sh.vx[se.x].w || rado < sh.vx[se.y].w;
+        }
+        const unsigned m = __ballot_sync(kFull, out);
+        if (out) elist[n_out + __popc(m & lanemask_lt())] = (uint8_t)e;
+        n_out += __popc(m);
+    }
+    __syncwarp();
+    #pragma unroll 1
+    for (int k0 = 0; k0 < n_out; k0 += 32) {
+        const int k = k0 + lane;
         int cnt = 0;
         real a0[3], a1[3];
-        bool k0 = false, k1 = false;
+        bool k0v = false, k1v = false;
         uchar4 q = make_uchar4(0, 0, 0, 0);
-        if (e < edgenum) {
-            q = sh.u.e.ep[e];
-            const uchar2 se = sh.u.e.es[e];
-            if (rado < sh.vx[se.x].w || rado < sh.vx[se.y].w) {
-                if (solve2s(sh.pl[q.x], sh.pl[q.y], rr, a0, a1)) {
-                    const real4 ta = sh.pl[q.z], tb = sh.pl[q.w];
-                    k0 = (dot3(ta, a0[0], a0[1], a0[2]) + ta.w < real(0.0)) && (dot3(tb, a0[0], a0[1], a0[2]) + tb.w < real(0.0));
-                    k1 = (dot3(ta, a1[0], a1[1], a1[2]) + ta.w < real(0.0)) && (dot3(tb, a1[0], a1[1], a1[2]) + tb.w < real(0.0));
-                    cnt = (int)k0 + (int)k1;
-                }
+        if (k < n_out) {
+            q = sh.u.e.ep[elist[k]];
+            if (solve2s(sh.pl[q.x], sh.pl[q.y], rr, a0, a1)) {
+                const real4 ta = sh.pl[q.z], tb = sh.pl[q.w];
+                k0v = (dot3(ta, a0[0], a0[1], a0[2]) + ta.w < real(0.0)) && (dot3(tb, a0[0], a0[1], a0[2]) + tb.w < real(0.0));
+                k1v = (dot3(ta, a1[0], a1[1], a1[2]) + ta.w < real(0.0)) && (dot3(tb, a1[0], a1[1], a1[2]) + tb.w < real(0.0));
+                cnt = (int)k0v + (int)k1v;
             }
         }
         int tot;
         const int off = warp_excl_scan(cnt, lane, &tot);
         if (vn + tot > kMaxVerts - 1) return kAtomCapacity;
         int w = vn + off;
-        if (k0) {
+        if (k0v) {
             sh.vx[w] = make_real4(a0[0], a0[1], a0[2], rado);
             sh.vp[w] = make_uchar4(q.x, q.y, kNone, 0);
             ++w;
         }
-        if (k1) {
+        if (k1v) {
             sh.vx[w] = make_real4(a1[0], a1[1], a1[2], rado);
             sh.vp[w] = make_uchar4(q.x, q.y, kNone, 0);
         }
@@ -983,12 +1038,13 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     }
     if (tot_pts > kMaxFacePts) return kAtomCapacity;
     __syncwarp();
-    int n_extra = 0;
+    // the faces' point lists and, for a face of more than two points, the antipode of its first
+    // sphere point, which joins the face when it lies behind every other plane (test_point)
+    int nf = 0;
     #pragma unroll 1
     for (int x0 = 0; x0 < NC; x0 += 32) {
         const int X = x0 + lane;
-        bool extra = false;
-        real ex[3] = {real(0.), real(0.), real(0.)};
+        bool cand = false;
         if (X < NC && sh.flag[X] != 0) {
             const int o = sh.foff[X];
             int k = 0;
@@ -1004,15 +1060,28 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
                     const int vi = sh.u.f.pt[o + q];
                     if (sh.vp[vi].z == kNone) {
                         const real4 pv = sh.vx[vi];
+                        real* ex = &sh.u.f.cosv[3 * X];
                         ex[0] = real(2.0) * cp.x - pv.x;
                         ex[1] = real(2.0) * cp.y - pv.y;
                         ex[2] = real(2.0) * cp.z - pv.z;
-                        extra = inside_all(sh, NC, X, ex[0], ex[1], ex[2]);
+                        cand = true;
                         break;
                     }
                 }
             }
         }
+        const unsigned m = __ballot_sync(kFull, cand);
+        if (lane == 0) sh.cmask[x0 >> 5] = m;
+        if (cand) sh.flist[nf + __popc(m & lanemask_lt())] = (uint8_t)X;
+        nf += __popc(m);
+    }
+    __syncwarp();
+    faces_inside(sh, NC, nf, lane);
+    int n_extra = 0;
+    #pragma unroll 1
+    for (int x0 = 0; x0 < NC; x0 += 32) {
+        const int X = x0 + lane;
+        const bool extra = X < NC && ((sh.cmask[x0 >> 5] >> lane) & 1u) && !((sh.bad[x0 >> 5] >> lane) & 1u);
         int t;
         const int off = warp_excl_scan(extra ? 1 : 0, lane, &t);
         if (NV + n_extra + t > kMaxVerts - 1) return kAtomCapacity;
@@ -1022,6 +1091,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
                 hist_vx(hist)[w - NV] = sh.vx[w];
                 hist_vp(hist)[w - NV] = sh.vp[w];
             }
+            const real* ex = &sh.u.f.cosv[3 * X];
             sh.vx[w] = make_real4(ex[0], ex[1], ex[2], rado);
             sh.vp[w] = make_uchar4((uint8_t)X, kNone, kNone, 0);
             sh.u.f.pt[sh.foff[X] + sh.fnp[X]] = (uint8_t)w;
@@ -1192,33 +1262,42 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         __syncwarp();
     }
     const real two_pi_r = real(2.0) * (real)kPi * rado;
-    // Caps and lenses (faces of 0 and 2 points) one face per lane; the fan triangles and arc
-    // segments of the other faces are laid out flat and spread over the lanes, then added to
-    // their face's area in the reference's order (triangles, then arcs, each in point order).
-    int t_run = 0, a_run = 0;
+    // Caps and lenses (faces of 0 and 2 points) test their plane's centre against the other planes
+    // (all faces' tests spread over the lanes); the fan triangles and arc segments of the other
+    // faces, and the lenses' arcs, are laid out flat and spread over the lanes, then added to their
+    // face's area in the reference's order (triangles, then arcs, each in point order).
+    int t_run = 0, a_run = 0, nf2 = 0, n_lens = 0;
     #pragma unroll 1
     for (int x0 = 0; x0 < NC; x0 += 32) {
         const int X = x0 + lane;
         int nt = 0, na = 0;
+        bool ring = false;
         if (X < NC && sh.flag[X] != 0) {
             const int np = sh.fnp[X];
-            const uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
-            const real4 cp = centre_of(sh.pl[X]);
-            real area = real(0.0);
-            if (np == 0) {
-                if (inside_all(sh, NC, X, cp.x, cp.y, cp.z)) area = two_pi_r * (rado - cp.w);
-            } else if (np == 2) {
-                const real arc = sph_arc(cp, sh.vx[pt[0]], sh.vx[pt[1]], rado);
-                if (inside_all(sh, NC, X, cp.x, cp.y, cp.z)) area = two_pi_r * (rado - cp.w) - arc;
-                else area = arc;
+            if (np == 0 || np == 2) {
+                ring = true;
+                const real4 cp = centre_of(sh.pl[X]);
+                real* q = &sh.u.f.cosv[3 * X];
+                q[0] = cp.x;
+                q[1] = cp.y;
+                q[2] = cp.z;
             } else {
                 // (a face of one point has neither triangles nor arcs)
+                const uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
                 nt = np > 2 ? np - 2 : 0;
                 #pragma unroll 1
                 for (int vi = 0; vi < np; ++vi) na += arc_segment(sh, pt, np, vi);
             }
-            sh.area[X] = area;
+            sh.area[X] = real(0.0);
         }
+        const unsigned m = __ballot_sync(kFull, ring);
+        if (lane == 0) sh.cmask[x0 >> 5] = m;
+        if (ring) sh.flist[nf2 + __popc(m & lanemask_lt())] = (uint8_t)X;
+        nf2 += __popc(m);
+        const bool lens = ring && sh.fnp[X] == 2;
+        const unsigned ml = __ballot_sync(kFull, lens);
+        if (lens) sh.llist[n_lens + __popc(ml & lanemask_lt())] = (uint8_t)X;
+        n_lens += __popc(ml);
         int tt, ta;
         const int ot = warp_excl_scan(nt, lane, &tt);
         const int oa = warp_excl_scan(na, lane, &ta);
@@ -1229,6 +1308,13 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         t_run += tt;
         a_run += ta;
     }
+    __syncwarp();
+    faces_inside(sh, NC, nf2, lane);
+    // caps: the whole cap when its centre is inside the polyhedron
+    #pragma unroll 1
+    for (int X = lane; X < NC; X += 32)
+        if (((sh.cmask[X >> 5] >> (X & 31)) & 1u) && sh.fnp[X] == 0 && !((sh.bad[X >> 5] >> (X & 31)) & 1u))
+            sh.area[X] = two_pi_r * (rado - fabs(sh.pl[X].w));
     __syncwarp();
     // fan of spherical triangles from pt[0] (LIB/Vcontacts.cpp:906-940)
     #pragma unroll 1
@@ -1244,23 +1330,35 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         }
         add_in_order(sh, X, v, lane);
     }
-    // arc segments between consecutive arc points of different edges (:943-954)
+    // arc segments between consecutive arc points of different edges (:943-954), then the
+    // lenses' arcs (the cap less the arc when the centre is inside, else the arc alone)
     #pragma unroll 1
-    for (int k0 = 0; k0 < a_run; k0 += 32) {
+    for (int k0 = 0; k0 < a_run + n_lens; k0 += 32) {
         const int k = k0 + lane;
-        int X = -1;
-        real v = real(0.0);
+        int F = -1, ia = 0, ib = 0;
+        bool lens = false;
         if (k < a_run) {
-            X = face_of(sh.aoff, NC, k);
-            const int np = sh.fnp[X];
-            const uint8_t* pt = &sh.u.f.pt[sh.foff[X]];
-            int j = k - sh.aoff[X], vi = 0;
+            F = face_of(sh.aoff, NC, k);
+            const int np = sh.fnp[F];
+            const uint8_t* pt = &sh.u.f.pt[sh.foff[F]];
+            int j = k - sh.aoff[F], vi = 0;
             #pragma unroll 1
             for (; vi < np - 1; ++vi)
                 if (arc_segment(sh, pt, np, vi) && j-- == 0) break;
-            v = sph_arc(centre_of(sh.pl[X]), sh.vx[pt[vi]], sh.vx[pt[(vi + 1) % np]], rado);
+            ia = pt[vi];
+            ib = pt[(vi + 1) % np];
+        } else if (k < a_run + n_lens) {
+            F = sh.llist[k - a_run];
+            const uint8_t* pt = &sh.u.f.pt[sh.foff[F]];
+            ia = pt[0];
+            ib = pt[1];
+            lens = true;
         }
-        add_in_order(sh, X, v, lane);
+        real v = real(0.0);
+        if (F >= 0) v = sph_arc(centre_of(sh.pl[F]), sh.vx[ia], sh.vx[ib], rado);
+        add_in_order(sh, lens ? -1 : F, v, lane);
+        if (lens)
+            sh.area[F] = ((sh.bad[F >> 5] >> (F & 31)) & 1u) ? v : two_pi_r * (rado - fabs(sh.pl[F].w)) - v;
     }
     __syncwarp();
     engulf_corrections(sh, NC, tot_pts, rado, rr, two_pi_r, epi, lane);
@@ -1327,11 +1425,12 @@ __device__ double pose_clash_sum(const DevSystem& S, const DevWork& W, int p, in
 // ------------------------------------------------------------------------------------------
 // pose_kernel: calc_region + vcfunction for one pose per warp
 // ------------------------------------------------------------------------------------------
-// Shared memory per warp sets how many poses an SM holds at once. The single-precision kernel is
-// latency-bound and gains from more warps, so it keeps the per-pose seeds and record masks in the
-// workspace (W.pose_seed, W.pose_rec); the double-precision kernel is bound by the FP64 pipe and
-// keeps them in shared memory.
-#define FXE_SEEDS_SHARED (FXE_REFERENCE_FORMULAS)
+// Shared memory per warp sets how many poses an SM holds at once. Both kernels gain from more
+// warps (latency-bound), so they keep the per-pose seeds and record masks in the workspace
+// (W.pose_seed, W.pose_rec): ten double-precision or twenty single-precision poses per SM.
+#ifndef FXE_SEEDS_SHARED
+#define FXE_SEEDS_SHARED 0
+#endif
 struct PoseShared {
     VorShared v;
     uint8_t order[kMaxLig];          // mobile atoms in Calclist order

@@ -83,6 +83,8 @@ def load_library():
         lib.fxe_cleft_grid.argtypes = [C.c_int32, _f, _f, C.c_float, _f, C.c_int64, _f, _f, C.POINTER(C.c_int64)]
         lib.fxe_context_autotune.argtypes = [vp, C.c_int32, vp, C.c_int32, C.POINTER(C.c_int32),
                                              C.POINTER(C.c_double)]
+        lib.fxe_context_autotune_sweep.argtypes = [vp, C.c_int32, vp, C.c_int32, _i, _d, C.c_int32,
+                                                   C.POINTER(C.c_int32)]
         lib.fxe_autotune_lookup.argtypes = [C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_int32)]
         lib.fxe_context_destroy.argtypes = [vp]
         lib.fxe_context_destroy.restype = None
@@ -216,6 +218,13 @@ class GPUEvaluator:
         _check(self.lib.fxe_context_autotune(self.handle, int(n), C.c_void_p(d_genes), int(reps), C.byref(b),
                                              C.byref(ms)))
         return int(b.value), float(ms.value)
+
+    def autotune_sweep(self, d_genes: int, n: int, reps: int = 2) -> dict:
+        """fxe_context_autotune_sweep: {blocks per SM: fastest launch ms} for every cap timed."""
+        caps, ms, k = np.zeros(32, np.int32), np.zeros(32, np.float64), C.c_int32(0)
+        _check(self.lib.fxe_context_autotune_sweep(self.handle, int(n), C.c_void_p(d_genes), int(reps), ptr(caps, _i),
+                                                   ptr(ms, _d), 32, C.byref(k)))
+        return {int(c): float(t) for c, t in zip(caps[:k.value], ms[:k.value])}
 
     def decode_genes(self, genes: np.ndarray, clamp: bool = False) -> np.ndarray:
         """genetoic of every gene on the device (fxe_decode_genes); clamp as eval_chromosome."""

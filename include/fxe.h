@@ -489,6 +489,11 @@ fxe_status fxe_ensemble_dedup(int64_t n, int32_t n_genes, const double* ic, cons
  * reference counterpart. */
 fxe_status fxe_context_autotune(fxe_context* ctx, int32_t n, const int32_t* d_genes, int32_t reps,
                                 int32_t* blocks_per_sm, double* ms_per_launch);
+/* The same sweep, reporting every cap it timed: caps[i] (blocks per SM) and ms[i] (fastest launch
+ * time) for i < *n_out (at most max_out entries; the SM's capacity is at most 32 blocks). Records
+ * the fastest in the table like fxe_context_autotune. */
+fxe_status fxe_context_autotune_sweep(fxe_context* ctx, int32_t n, const int32_t* d_genes, int32_t reps,
+                                      int32_t* caps, double* ms, int32_t max_out, int32_t* n_out);
 /* The cap the table holds for a size class (0: not tuned, as many blocks as fit). */
 fxe_status fxe_autotune_lookup(int32_t precision, int32_t scored_atoms, int64_t poses, int32_t* blocks_per_sm);
 
