@@ -315,8 +315,11 @@ struct WalkStep {
 #if FXE_FILTER
 // Single-precision value of vt = -(P.s + w) / (P.V) and a bound on its distance from the same
 // expression evaluated in double: every input is rounded once to float and every operation
-// rounds, 16 units of roundoff (2^-20) per sum of absolute terms covers both. den_ok is false
-// when the sign of P.V is not certain (the double test skips P.V == 0 exactly).
+// rounds, 16 units of roundoff (2^-20) per sum of absolute terms covers both; the quotients use
+// the fast reciprocal (at most 2 units in the last place off, covered by 4 units of |vt| and the
+// 1/16 margin on the bound). den_ok is false when the sign of P.V is not certain (the double test
+// skips P.V == 0 exactly), when |P.V| is too small for the fast quotient, or when the bound is
+// not finite.
 __device__ __forceinline__ float vt_pretest(const float4& P, float sx, float sy, float sz, float Vx,
                                             float Vy, float Vz, float* err, bool* den_ok) {
     const float g = 9.5367431640625e-07f;   // 2^-20
@@ -331,9 +334,11 @@ __device__ __forceinline__ float vt_pretest(const float4& P, float sx, float sy,
         *err = 0.0f;
         return -1.0f;
     }
-    *den_ok = fabsf(den) > 2.0f * eden;
-    const float vt = -num / den;
-    *err = (enm + fabsf(vt) * eden) / (fabsf(den) - eden) * 1.0625f + fabsf(vt) * 2.4e-7f;
+    const bool ok = fabsf(den) > 2.0f * eden && fabsf(den) > 1e-30f;
+    const float vt = __fdividef(-num, den);
+    const float er = __fdividef(enm + fabsf(vt) * eden, fabsf(den) - eden) * 1.0625f + fabsf(vt) * 4.8e-7f;
+    *den_ok = ok && er < 3.0e38f;
+    *err = er;
     return vt;
 }
 #endif
@@ -440,6 +445,10 @@ __device__ GroupStep walk_step_group(const VorShared& sh, int NC, int e, real rr
     const float Vx = (float)V.x, Vy = (float)V.y, Vz = (float)V.z;
     float best = 9.9e9f, beste = 0.0f;
     int bi = INT_MAX;
+    // and the two smallest lower bounds (vt - err) over the planes whose vt may be positive: every
+    // plane but the winner must be surely not positive or surely farther
+    float lo1 = 3.0e38f, lo2 = 3.0e38f;
+    int lo1i = INT_MAX;
     bool unsure = false;
     if (has) {
         #pragma unroll 1
@@ -448,8 +457,16 @@ __device__ GroupStep walk_step_group(const VorShared& sh, int NC, int e, real rr
             float er;
             bool ok;
             const float vt = vt_pretest(sh.plf[c], sx, sy, sz, Vx, Vy, Vz, &er, &ok);
-            if (!ok) unsure = true;
-            else if (vt > 0.0f && vt < best) { best = vt; beste = er; bi = c; }
+            if (!ok) {
+                unsure = true;
+                continue;
+            }
+            if (vt > 0.0f && vt < best) { best = vt; beste = er; bi = c; }
+            if (vt + er > 0.0f) {
+                const float lo = vt - er;
+                if (lo < lo1) { lo2 = lo1; lo1 = lo; lo1i = c; }
+                else if (lo < lo2) lo2 = lo;
+            }
         }
     }
 #pragma unroll
@@ -460,17 +477,8 @@ __device__ GroupStep walk_step_group(const VorShared& sh, int NC, int e, real rr
         if (b2 < best || (b2 == best && i2 < bi)) { best = b2; beste = e2; bi = i2; }
     }
     if (bi != INT_MAX && !(best - beste > 0.0f)) unsure = true;
-    if (has) {
-        #pragma unroll 1
-        for (int c = sub; c < NC && !unsure; c += kWalkLanes) {
-            if (c == pA || c == pB || c == oldC || c == bi) continue;
-            float er;
-            bool ok;
-            const float vt = vt_pretest(sh.plf[c], sx, sy, sz, Vx, Vy, Vz, &er, &ok);
-            if (ok && (vt + er <= 0.0f || (bi != INT_MAX && vt - er > best + beste))) continue;
-            unsure = true;
-        }
-    }
+    const float mylo = lo1i == bi ? lo2 : lo1;
+    if (mylo < 3.0e38f && !(bi != INT_MAX && mylo > best + beste)) unsure = true;
     unsure = (__ballot_sync(kFull, unsure) & gmask) != 0u;
     real vtmin = real(9.9e9);
     if (!unsure && bi != INT_MAX) {
@@ -655,40 +663,53 @@ __device__ FXE_COLD void engulf_corrections(VorShared& sh, int NC, int tot_pts, 
             n_items += __popc(m);
         }
         __syncwarp();
+        // two engulfing planes: the lens their circles cut, its two arcs evaluated with the items
+        // (the last two of the list)
+        real q0[3] = {real(0.0), real(0.0), real(0.0)}, q1[3] = {real(0.0), real(0.0), real(0.0)};
+        const bool lens2 = epi == 2 && solve2s(sh.pl[sh.eng[0]], sh.pl[sh.eng[1]], rr, q0, q1);
+        const int n_all = n_items + (lens2 ? 2 : 0);
+        real m = real(0.0);   // lane 0: the sum of the two lens arcs
         #pragma unroll 1
-        for (int k0 = 0; k0 < n_items; k0 += 32) {
+        for (int k0 = 0; k0 < n_all; k0 += 32) {
             const int k = k0 + lane;
             int comm = -1;
             real v = real(0.0);
-            if (k < n_items) {
-                const uint32_t it = items[k];
-                comm = (int)(it >> 24);
-                v = sph_arc(centre_of(sh.pl[it & 0xffu]), sh.vx[(it >> 8) & 0xffu], sh.vx[(it >> 16) & 0xffu], rado);
+            if (k < n_all) {
+                real4 ao, b, c;
+                if (k < n_items) {
+                    const uint32_t it = items[k];
+                    comm = (int)(it >> 24);
+                    ao = centre_of(sh.pl[it & 0xffu]);
+                    b = sh.vx[(it >> 8) & 0xffu];
+                    c = sh.vx[(it >> 16) & 0xffu];
+                } else {
+                    ao = centre_of(sh.pl[sh.eng[k - n_items]]);
+                    b = make_real4(q0[0], q0[1], q0[2], rado);
+                    c = make_real4(q1[0], q1[1], q1[2], rado);
+                }
+                v = sph_arc(ao, b, c, rado);
             }
             add_in_order(sh, comm, v, lane);
+            if (lens2) {
+                // the reference adds the second arc to the first
+                const real a0 = __shfl_sync(kFull, v, n_items & 31);
+                const real a1 = __shfl_sync(kFull, v, (n_items + 1) & 31);
+                if (lane == 0) {
+                    if (k0 <= n_items && n_items < k0 + 32) m = a0;
+                    if (k0 <= n_items + 1 && n_items + 1 < k0 + 32) m += a1;
+                }
+            }
         }
         if (epi == 1) {
             if (lane == 0) sh.area[sh.eng[0]] = two_pi_r * (rado + fabs(sh.pl[sh.eng[0]].w));
-        } else if (epi == 2) {
-            real q0[3], q1[3];
+        } else if (epi == 2 && lane == 0) {
             const real full = two_pi_r * rado;
-            const bool ok = solve2s(sh.pl[sh.eng[0]], sh.pl[sh.eng[1]], rr, q0, q1);
-            real m = real(0.0);
-            if (ok && lane < 2) {
-                const real4 Bp = make_real4(q0[0], q0[1], q0[2], rado);
-                const real4 Cp = make_real4(q1[0], q1[1], q1[2], rado);
-                m = sph_arc(centre_of(sh.pl[sh.eng[lane]]), Bp, Cp, rado);
-            }
-            const real m1 = __shfl_sync(kFull, m, 1);
-            if (lane == 0) {
-                if (!ok) {
-                    sh.area[sh.eng[0]] = full;
-                    sh.area[sh.eng[1]] = full;
-                } else {
-                    m += m1;
-                    sh.area[sh.eng[0]] = full - real(0.5) * m;
-                    sh.area[sh.eng[1]] = full - real(0.5) * m;
-                }
+            if (!lens2) {
+                sh.area[sh.eng[0]] = full;
+                sh.area[sh.eng[1]] = full;
+            } else {
+                sh.area[sh.eng[0]] = full - real(0.5) * m;
+                sh.area[sh.eng[1]] = full - real(0.5) * m;
             }
         }
         __syncwarp();
@@ -841,24 +862,26 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         }
         const int grp = lane / kWalkLanes;
         const GroupStep gs = walk_step_group(sh, NC, grp < nb ? (int)((batch >> (8 * grp)) & 0xffu) : -1, rr, sub, gmask);
-        // book the steps in index order; a new edge's direction is set after the batch (lane j
-        // holds the j-th new edge: slot, planes, start vertex)
+        // book the steps in index order; a new vertex's coordinates are stored by its group's
+        // first lane and a new edge's direction is set after the batch (lane j holds the j-th new
+        // edge: slot, planes, start vertex)
+        real gx = gs.x, gy = gs.y, gz = gs.z;
+        int my_vn = -1;
         int n_pend = 0, pe = 0, p0e = 0, pce = 0, tpe = 0, pve = 0;
         #pragma unroll 1
         for (int g = 0; g < nb; ++g) {
             const int e = (batch >> (8 * g)) & 0xffu;
-            real rx = __shfl_sync(kFull, gs.x, g * kWalkLanes);
-            real ry = __shfl_sync(kFull, gs.y, g * kWalkLanes);
-            real rz = __shfl_sync(kFull, gs.z, g * kWalkLanes);
             int pC = __shfl_sync(kFull, gs.pc, g * kWalkLanes);
             const bool unsure = __shfl_sync(kFull, (int)gs.unsure, g * kWalkLanes) != 0;
             if (sh.u.e.es[e].y != kNone) continue;   // closed by an earlier edge of the batch
             startedge = e;
             if (unsure) {
                 const WalkStep w = walk_step_exact(sh, NC, e, rr, lane);
-                rx = w.x;
-                ry = w.y;
-                rz = w.z;
+                if (lane == g * kWalkLanes) {
+                    gx = w.x;
+                    gy = w.y;
+                    gz = w.z;
+                }
                 pC = w.pc;
             }
             if (pC < 0) return kAtomHullFail;
@@ -879,6 +902,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
                 const unsigned ma = __ballot_sync(kFull, ac), mb = __ballot_sync(kFull, bc);
                 if (ma && mAC == INT_MAX) mAC = e0 + __ffs(ma) - 1;
                 if (mb && mBC == INT_MAX) mBC = e0 + __ffs(mb) - 1;
+                if (mAC != INT_MAX && mBC != INT_MAX) break;
             }
             __syncwarp();
             // a walk that keeps opening edges past the reference's 200-edge check ends here: as a
@@ -887,8 +911,8 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
             if (edgenum + n_new > kMaxEdges + 2) return mBC == INT_MAX ? kAtomHullFail : kAtomCapacity;
             const int eAC = mAC != INT_MAX ? mAC : edgenum;
             const int eBC = mBC != INT_MAX ? mBC : edgenum + (mAC == INT_MAX ? 1 : 0);
+            if (lane == g * kWalkLanes) my_vn = vn;
             if (lane == 0) {
-                sh.vx[vn] = make_real4(rx, ry, rz, real(0.0));
                 sh.vp[vn] = make_uchar4((uint8_t)pA, (uint8_t)pB, (uint8_t)pC, 0);
                 sh.u.e.es[e].y = (uint8_t)vn;
                 sh.u.e.ep[e].w = (uint8_t)pC;
@@ -918,6 +942,8 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
             ++vn;
             __syncwarp();
         }
+        if (my_vn >= 0) sh.vx[my_vn] = make_real4(gx, gy, gz, real(0.0));
+        __syncwarp();
         // the new edges' directions, oriented away from their third plane (add_vedge)
         if (lane < n_pend) {
             const real4 a = sh.pl[p0e], b = sh.pl[pce], t = sh.pl[tpe];
