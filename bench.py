@@ -54,7 +54,7 @@ STATMECH_FLOP = 20
 
 # DRAM bytes per launch of the dominant kernel from ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum), keyed by precision; from profiles/pose_kernel_plain_scale.md.
-POSE_KERNEL_DRAM_BYTES = {"reference": 115_325_440, "fast": 85_202_176}
+POSE_KERNEL_DRAM_BYTES = {"reference": 113_323_776, "fast": 85_202_176}
 
 # nominal non-tensor arithmetic peaks of GB300 (152 SMs at 2,070 MHz): FP32 152 x 128 lanes x 2
 # flops per FMA; FP64 1.25 TFLOP/s. There is no measured figure for either.
@@ -379,10 +379,12 @@ def run_gpu(args):
     sm_best = sm["device_merge"]
 
     clustered = run_cluster(ev, d) if args.cluster else None
-    batched = batched4 = None
+    batched = batched4 = batched_fp32 = None
     if args.batched:
         batched = run_batched(args, prec, flush, stream, BATCH_NAME, c3_jobs(), BATCH["evolve"])
         batched4 = run_batched(args, prec, flush, stream, BATCH4_NAME, c4_jobs(rec4), BATCH4["evolve"])
+        # the 256-ligand workload names FP32 geometry: the same comparison in fast precision
+        batched_fp32 = run_batched(args, "fast", flush, stream, BATCH_NAME, c3_jobs(), BATCH["evolve"])
     served = run_served(prec, rec5) if args.served else None
     ga_runs = {k: run_ga(prec, k, d if k == "c2" else None) for k in ("c1", "c2")} if args.ga else None
 
@@ -442,6 +444,7 @@ def run_gpu(args):
                                   "traffic": None}},
         "batched": batched,
         "batched_c4": batched4,
+        "batched_fp32": batched_fp32,
         "served": served,
         "ga": ga_runs,
         "cluster": clustered,

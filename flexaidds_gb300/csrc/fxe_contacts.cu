@@ -95,8 +95,13 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
                 const double rAB = (double)rABf;
                 const double cd = permea * rAB;
                 const double dist = sqrt((double)sq);
-                if (dist < cd && residue_pair(S, a, j) != 1)
-                    clash += (double)kKwall * (pow(dist, -12.0) - pow(cd, -12.0));
+                if (dist < cd && residue_pair(S, a, j) != 1) {
+                    // pow(x, -12) as 1 / (x^6)^2: within a few units in the last place of the C
+                    // library's pow (which the reference calls) and a tenth of the work
+                    const double d2 = dist * dist, d6 = d2 * d2 * d2;
+                    const double c2 = cd * cd, c6 = c2 * c2 * c2;
+                    clash += (double)kKwall * (1.0 / (d6 * d6) - 1.0 / (c6 * c6));
+                }
             }
         }
         nc += __popc(m);
@@ -174,7 +179,7 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
         }
         consider(pos >= 0, pos, m < nm ? slot_of(S, m) : 0, pj);
     }
-    clash = warp_sum_d(clash);
+    if (__any_sync(kFull, clash != 0.0)) clash = warp_sum_d(clash);
     // into the reference's order: bitonic sort of the staged keys
     if (nc <= kMaxCand) {
         int len = 32;

@@ -173,6 +173,26 @@ __device__ FXE_COLD bool solve3(const real4& e0, const real4& e1, const real4& e
     return true;
 }
 
+// Coordinate i (0..2) of solve3's solution, with the same operations in the same order: each
+// lane of a warp can take one coordinate with one instruction stream (the cofactors of column i
+// as P*Q - R*S on operands chosen per lane; -a*b + c*d is that value exactly). 0 when det is 0.
+__device__ __forceinline__ real solve3_coord(const real4& e0, const real4& e1, const real4& e2, int i) {
+    const real c00 = e1.y * e2.z - e2.y * e1.z;
+    const real c01 = -e1.x * e2.z + e2.x * e1.z;
+    const real c02 = e1.x * e2.y - e2.x * e1.y;
+    const real det = e0.x * c00 + e0.y * c01 + e0.z * c02;
+    // column i of the cofactors of rows 1 and 2
+    const real p1 = i == 0 ? e2.y : i == 1 ? e0.x : e2.x, q1 = i == 0 ? e0.z : i == 1 ? e2.z : e0.y;
+    const real r1 = i == 0 ? e0.y : i == 1 ? e2.x : e0.x, s1 = i == 0 ? e2.z : i == 1 ? e0.z : e2.y;
+    const real p2 = i == 0 ? e0.y : i == 1 ? e1.x : e0.x, q2 = i == 0 ? e1.z : i == 1 ? e0.z : e1.y;
+    const real r2 = i == 0 ? e1.y : i == 1 ? e0.x : e1.x, s2 = i == 0 ? e0.z : i == 1 ? e1.z : e0.y;
+    const real c0i = i == 0 ? c00 : i == 1 ? c01 : c02;
+    const real c1i = p1 * q1 - r1 * s1;
+    const real c2i = p2 * q2 - r2 * s2;
+    if (det == real(0.0)) return real(0.0);
+    return -(e0.w * c0i + e1.w * c1i + e2.w * c2i) / det;
+}
+
 // solve_2xS (LIB/Vcontacts.cpp:1427-1476) in FP32.
 // rr is the square of the radius as the reference forms it: a single-precision product.
 __device__ FXE_COLD bool solve2s(const real4& a, const real4& b, real rr, real* p0, real* p1) {
@@ -820,11 +840,14 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     if (pC0 == INT_MAX) return kAtomCapacity;
     }
     {
-        // the vertex on every lane (one warp instruction either way), then its three edges at once
-        real t[3] = {real(0.0), real(0.0), real(0.0)};
-        solve3(sh.pl[pA0], sh.pl[pB0], sh.pl[pC0], t);
+        // the vertex's coordinates on lanes 0..2, then its three edges at once
+        const real ti = solve3_coord(sh.pl[pA0], sh.pl[pB0], sh.pl[pC0], lane < 3 ? lane : 0);
+        real t[3];
+        t[0] = __shfl_sync(kFull, ti, 0);
+        t[1] = __shfl_sync(kFull, ti, 1);
+        t[2] = __shfl_sync(kFull, ti, 2);
         if (lane == 0) {
-            sh.vx[0] = make_real4(t[0], t[1], t[2], sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]));
+            sh.vx[0] = make_real4(t[0], t[1], t[2], real(0.0));   // (its distance comes with the others')
             sh.vp[0] = make_uchar4((uint8_t)pA0, (uint8_t)pB0, (uint8_t)pC0, 0);
             sh.flag[pA0] |= kOnHull;
             sh.flag[pB0] |= kOnHull;
@@ -871,8 +894,9 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
         #pragma unroll 1
         for (int g = 0; g < nb; ++g) {
             const int e = (batch >> (8 * g)) & 0xffu;
-            int pC = __shfl_sync(kFull, gs.pc, g * kWalkLanes);
-            const bool unsure = __shfl_sync(kFull, (int)gs.unsure, g * kWalkLanes) != 0;
+            const int pu = __shfl_sync(kFull, (gs.pc << 1) | (int)gs.unsure, g * kWalkLanes);
+            int pC = pu >> 1;   // (an arithmetic shift keeps -1)
+            const bool unsure = (pu & 1) != 0;
             if (sh.u.e.es[e].y != kNone) continue;   // closed by an earlier edge of the batch
             startedge = e;
             if (unsure) {
@@ -959,7 +983,7 @@ __device__ int voronoi_warp(VorShared& sh, int NC, real rado, int lane, int* no_
     }
     // vertex distances to the centre, all at once
     #pragma unroll 1
-    for (int vi = 1 + lane; vi < vn; vi += 32) {
+    for (int vi = lane; vi < vn; vi += 32) {
         const real4 X = sh.vx[vi];
         sh.vx[vi].w = sqrt(X.x * X.x + X.y * X.y + X.z * X.z);
     }
