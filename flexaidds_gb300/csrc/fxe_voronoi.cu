@@ -26,10 +26,6 @@ namespace FXE_VARIANT {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kFaceWords = (kMaxCand + 31) / 32;
 constexpr uint8_t kNone = 255;
-// Poses (warps) per block of pose_kernel. Two per block fit eight double-precision workspaces
-// (23 KB each) or twenty single-precision ones (10.6 KB) on an SM; the double kernel measured no
-// faster with nine (three per block) than with seven or eight.
-constexpr int kVorWarps = 2;
 
 // Floating-point type of the polyhedron arithmetic: single precision by default; building
 // with -DFXE_REAL=double gives the same algorithm in double precision (for comparisons).
@@ -52,6 +48,16 @@ using real = FXE_REAL;
 #ifndef FXE_FILTER
 #define FXE_FILTER (FXE_REFERENCE_FORMULAS)
 #endif
+// Poses (warps) per block of pose_kernel, and whether the block's warps meet after every atom.
+// The double kernel's code (about 220 KB) outgrows the SM's instruction caches, and its top stall
+// was instruction fetch with eight warps of an SM at unrelated points of it: eight warps per block
+// (one block per SM, 20 KB of workspace each) that take eight neighbouring poses of the queue and
+// meet at a block barrier after each atom fetch the same code at about the same time (measured on
+// GB300, plain-scale workload: 22.9 -> 19.2 ms per launch; four warps per block 20.5 ms, ten
+// 21.7 ms). The single-precision kernel is not fetch-bound: two warps per block, twenty per SM,
+// each taking the next pose on its own.
+constexpr bool kLockstep = FXE_REFERENCE_FORMULAS;
+constexpr int kVorWarps = kLockstep ? 8 : 2;
 // The kernel outgrows the instruction cache (its top stall is instruction fetch): its rarely taken
 // or bulky helpers are called, not inlined (double build), and no loop is unrolled — every loop
 // carries `#pragma unroll 1` unless it says otherwise (measured on GB300, plain-scale workload:
@@ -1517,9 +1523,14 @@ __device__ void finish_failed(const DevWork& W, int p, int lane, int status, dou
     if (lane == 0) W.out[p] = cf;
 }
 
+// p < 0: no pose (the warp only keeps its block's barriers). n_iter: the atom steps the block
+// takes together in lockstep (at least this pose's scored atoms; unused otherwise).
 __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W, int p, int lane,
-                                           PoseShared& ps, uint8_t* hist) {
+                                           PoseShared& ps, uint8_t* hist, int n_iter) {
     VorShared& sh = ps.v;
+    // a pose that fails stops here; in lockstep its warp still meets the block after every step
+    bool alive = p >= 0;
+    if (p < 0) p = 0;
     const int nl = n_mobile(S);      // the scored atoms: side-chain atoms, then the ligand
     // polyhedron seeds (Calc indices, -1 = none) and the mobile partners each processed atom kept
 #if FXE_SEEDS_SHARED
@@ -1530,27 +1541,30 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
     uint32_t (*const rec)[kMaskWords] = reinterpret_cast<uint32_t (*)[kMaskWords]>(W.pose_rec + (size_t)p * kMaxLig * kMaskWords);
 #endif
     const size_t lb = (size_t)p * nl;
-    if (W.pose_grid[p].z) {
+    if (alive && W.pose_grid[p].z) {
         finish_failed(W, p, lane, FXE_POSE_CAPACITY, 0.0);
-        return;
+        alive = false;
     }
     // clash pre-filter (LIB/Vcontacts.cpp:36-51)
-    const double clash = pose_clash_sum(S, W, p, lane);
-    if (clash >= kClashThreshold) {
-        finish_failed(W, p, lane, FXE_POSE_CLASHED, clash);
-        return;
+    if (alive) {
+        const double clash = pose_clash_sum(S, W, p, lane);
+        if (clash >= kClashThreshold) {
+            finish_failed(W, p, lane, FXE_POSE_CLASHED, clash);
+            alive = false;
+        }
     }
+    if (!kLockstep && !alive) return;
     #pragma unroll 1
-    for (int l = lane; l < nl; l += 32) {
+    for (int l = lane; alive && l < nl; l += 32) {
         ps.order[W.mob_rank[lb + l]] = (uint8_t)l;
         seed[l][0] = seed[l][1] = seed[l][2] = -1;
 #pragma unroll
         for (int w = 0; w < kMaskWords; ++w) rec[l][w] = 0;
     }
-    if (lane < kMaskWords) ps.done[lane] = 0;
+    if (alive && lane < kMaskWords) ps.done[lane] = 0;
     // the face history starts the pose at zero, as the reference's ptorder does on a workspace
     // cleared before the pose
-    if (hist) {
+    if (alive && hist) {
         uint4* h4 = reinterpret_cast<uint4*>(hist);
         #pragma unroll 1
         for (int k = lane; k < kHistBytes / 16; k += 32) h4[k] = make_uint4(0u, 0u, 0u, 0u);
@@ -1558,13 +1572,16 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
     __syncwarp();
     // calc_region: atoms in Calclist order (LIB/Vcontacts.cpp:74-139)
     #pragma unroll 1
-    for (int r = 0; r < nl; ++r) {
+    for (int r = 0; r < (kLockstep ? n_iter : nl); ++r) {
+        if (!alive || r >= nl) goto atom_end;
+        {
         const int a = ps.order[r];
         const int n_cand = W.cand_n[lb + a];
         if (n_cand < 0) {
             if (lane == 0) atomicAdd(&W.counters[2], 1);
             finish_failed(W, p, lane, FXE_POSE_CAPACITY, 0.0);
-            return;
+            alive = false;
+            goto atom_end;
         }
         const size_t cb = (lb + a) * kMaxCand;
         // get_contlist4's list: saved atoms drop out unless they kept a contact with this one, and
@@ -1589,7 +1606,7 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
                 W.cand_area[cb + c] = 0.0;
                 W.cand_flag[cb + c] = 0;
             }
-            continue;
+            goto atom_end;
         }
         const float4 me = W.mob_pos[lb + a];
         const float rado = me.w + kRw;
@@ -1617,12 +1634,14 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         if (st == kAtomCapacity) {
             if (lane == 0) atomicAdd(&W.counters[2], 1);
             finish_failed(W, p, lane, FXE_POSE_CAPACITY, 0.0);
-            return;
+            alive = false;
+            goto atom_end;
         }
         if (st == kAtomHullFail) {
             if (lane == 0) atomicAdd(&W.counters[1], 1);
             finish_failed(W, p, lane, FXE_POSE_POLYHEDRON_FAILED, (double)kPolyPenalty);
-            return;
+            alive = false;
+            goto atom_end;
         }
         // save_areas (LIB/Vcontacts.cpp:1149-1220): contacts with area > 0 on a contact plane;
         // candidates outside the contact list record nothing
@@ -1675,6 +1694,11 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
         }
         __syncwarp();
     }
+    atom_end:
+        if (kLockstep) __syncthreads();
+        if (!kLockstep && !alive) return;
+    }
+    if (!alive) return;
     // vcfunction (LIB/vcfunction.cpp:84-513): scored atoms in Calc order (side-chain atoms,
     // then the ligand), their kept contacts; each residue's terms are summed on their own and the
     // records added up ligand first, then the side chains in order (LIB/ic2cf.cpp:133-245)
@@ -1795,10 +1819,26 @@ pose_kernel(DevSystem S, DevWork W, int n, int* next, uint8_t* hist_all) {
     PoseShared& ps = reinterpret_cast<PoseShared*>(smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     uint8_t* hist = warp_hist(hist_all);
-    #pragma unroll 1
-    for (int q = next_pose(next, lane); q < n; q = next_pose(next, lane)) {
-        score_pose(S, W, W.pose_order[q], lane, ps, hist);
-        __syncwarp();
+    if (kLockstep) {
+        // the block takes kVorWarps neighbouring poses of the queue at once
+        __shared__ int base_s;
+        #pragma unroll 1
+        for (;;) {
+            if (threadIdx.x == 0) base_s = atomicAdd(next, kVorWarps);
+            __syncthreads();
+            const int base = base_s;
+            __syncthreads();
+            if (base >= n) break;
+            const int q = base + (int)(threadIdx.x >> 5);
+            score_pose(S, W, q < n ? W.pose_order[q] : -1, lane, ps, hist, n_mobile(S));
+            __syncwarp();
+        }
+    } else {
+        #pragma unroll 1
+        for (int q = next_pose(next, lane); q < n; q = next_pose(next, lane)) {
+            score_pose(S, W, W.pose_order[q], lane, ps, hist, 0);
+            __syncwarp();
+        }
     }
 }
 
@@ -1811,12 +1851,41 @@ pose_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, int total, int* next,
     PoseShared& ps = reinterpret_cast<PoseShared*>(smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     uint8_t* hist = warp_hist(hist_all);
-    #pragma unroll 1
-    for (int q = next_pose(next, lane); q < total; q = next_pose(next, lane)) {
-        const int gp = order[q];
-        const Job& job = jobs[find_job(jobs, n_jobs, gp, false)];
-        score_pose(job.S, job.W, gp - job.pose0, lane, ps, hist);
-        __syncwarp();
+    if (kLockstep) {
+        // the block takes kVorWarps neighbouring poses of the queue at once and steps through as
+        // many atoms as the largest of them has
+        __shared__ int base_s, steps_s;
+        #pragma unroll 1
+        for (;;) {
+            if (threadIdx.x == 0) {
+                base_s = atomicAdd(next, kVorWarps);
+                steps_s = 0;
+            }
+            __syncthreads();
+            const int base = base_s;
+            const int q = base + (int)(threadIdx.x >> 5);
+            int gp = -1, j = 0;
+            if (q < total) {
+                gp = order[q];
+                j = find_job(jobs, n_jobs, gp, false);
+                if (lane == 0) atomicMax(&steps_s, n_mobile(jobs[j].S));
+            }
+            __syncthreads();
+            const int steps = steps_s;
+            __syncthreads();
+            if (base >= total) break;
+            const Job& job = jobs[j];
+            score_pose(job.S, job.W, gp < 0 ? -1 : gp - job.pose0, lane, ps, hist, steps);
+            __syncwarp();
+        }
+    } else {
+        #pragma unroll 1
+        for (int q = next_pose(next, lane); q < total; q = next_pose(next, lane)) {
+            const int gp = order[q];
+            const Job& job = jobs[find_job(jobs, n_jobs, gp, false)];
+            score_pose(job.S, job.W, gp - job.pose0, lane, ps, hist, 0);
+            __syncwarp();
+        }
     }
 }
 
