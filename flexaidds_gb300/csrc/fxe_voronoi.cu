@@ -58,10 +58,10 @@ using real = FXE_REAL;
 // each taking the next pose on its own.
 constexpr bool kLockstep = FXE_REFERENCE_FORMULAS;
 constexpr int kVorWarps = kLockstep ? 8 : 2;
-// The kernel outgrows the instruction cache (its top stall is instruction fetch): its rarely taken
-// or bulky helpers are called, not inlined (double build), and no loop is unrolled — every loop
-// carries `#pragma unroll 1` unless it says otherwise (measured on GB300, plain-scale workload:
-// 36.0 -> 30.4 ms per launch in double precision, 6.8 -> 4.9 ms in single).
+// The kernel outgrows the instruction cache: its rarely taken or bulky helpers are called, not
+// inlined (double build; measured one by one), and no loop is unrolled — every loop carries
+// `#pragma unroll 1` unless it says otherwise (measured on GB300, plain-scale workload: 36.0 ->
+// 30.4 ms per launch in double precision, 6.8 -> 4.9 ms in single).
 #if FXE_REFERENCE_FORMULAS
 #define FXE_COLD __noinline__
 #else
@@ -224,7 +224,7 @@ __device__ FXE_COLD bool solve2s(const real4& a, const real4& b, real rr, real* 
     return true;
 }
 
-__device__ FXE_COLD real cos_pqr(const real4& p, const real4& q, const real4& r) {
+__device__ __forceinline__ real cos_pqr(const real4& p, const real4& q, const real4& r) {
     const real ax = p.x - q.x, ay = p.y - q.y, az = p.z - q.z;
     const real bx = r.x - q.x, by = r.y - q.y, bz = r.z - q.z;
     return (ax * bx + ay * by + az * bz) / sqrt((ax * ax + ay * ay + az * az) * (bx * bx + by * by + bz * bz));
@@ -1499,7 +1499,7 @@ struct PoseShared {
 
 __device__ __forceinline__ bool bit(const uint32_t* m, int l) { return (m[l >> 5] >> (l & 31)) & 1u; }
 
-__device__ FXE_COLD double get_yval(const DevSystem& S, int idx, double rel) {
+__device__ __forceinline__ double get_yval(const DevSystem& S, int idx, double rel) {
     const int o = S.em_off[idx], e = S.em_off[idx + 1];
     if (S.em_weight[idx]) return (double)S.em_y[o];
     int k = o;
