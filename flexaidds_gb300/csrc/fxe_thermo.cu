@@ -19,27 +19,60 @@ struct LseState {
     double m, s, e1, e2;
 };
 
+// One energy into the state. Both cases take exp(-|lw - m|): the rescale factor of the sums when
+// lw is a new maximum, the weight of the energy otherwise; one exp per energy and no divergent
+// exp between the lanes of a warp. (With no energy yet, m = -inf and the factor is exp(-inf) = 0.)
 __device__ __forceinline__ void lse_push(LseState& st, double lw, double e) {
-    if (lw > st.m) {
-        const double sc = st.m == -INFINITY ? 0.0 : exp(st.m - lw);
-        st.s = st.s * sc + 1.0;
-        st.e1 = st.e1 * sc + e;
-        st.e2 = st.e2 * sc + e * e;
+    const double d = lw - st.m;
+    const double x = exp(-fabs(d));
+    if (d > 0.0) {
+        st.s = st.s * x + 1.0;
+        st.e1 = st.e1 * x + e;
+        st.e2 = st.e2 * x + e * e;
         st.m = lw;
     } else {
-        const double w = exp(lw - st.m);
-        st.s += w;
-        st.e1 += w * e;
-        st.e2 += w * e * e;
+        st.s += x;
+        st.e1 += x * e;
+        st.e2 += x * e * e;
     }
 }
 
-__device__ __forceinline__ LseState lse_merge(const LseState& a, const LseState& b) {
-    if (b.m == -INFINITY) return a;
-    if (a.m == -INFINITY) return b;
-    const double M = fmax(a.m, b.m);
-    const double fa = exp(a.m - M), fb = exp(b.m - M);
-    return {M, a.s * fa + b.s * fb, a.e1 * fa + b.e1 * fb, a.e2 * fa + b.e2 * fb};
+// The block's states merged, max first: the block's maximum M by shuffles, then each thread's
+// sums rescaled once by exp(m - M) and added up (one exp per thread instead of one per merge).
+// Every thread of the block calls it; thread 0 gets the result.
+__device__ LseState block_merge(const LseState& st) {
+    __shared__ double wm[kThermoThreads / 32];
+    __shared__ double ws[3][kThermoThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double m = st.m;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) wm[warp] = m;
+    __syncthreads();
+    double M = wm[0];
+    for (int w = 1; w < kThermoThreads / 32; ++w) M = fmax(M, wm[w]);
+    const double f = st.m == -INFINITY ? 0.0 : exp(st.m - M);
+    double a = st.s * f, b = st.e1 * f, c = st.e2 * f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
+    if (lane == 0) {
+        ws[0][warp] = a;
+        ws[1][warp] = b;
+        ws[2][warp] = c;
+    }
+    __syncthreads();
+    LseState t{M, 0.0, 0.0, 0.0};
+    if (threadIdx.x == 0)
+        for (int w = 0; w < kThermoThreads / 32; ++w) {
+            t.s += ws[0][w];
+            t.e1 += ws[1][w];
+            t.e2 += ws[2][w];
+        }
+    return t;
 }
 
 __global__ void __launch_bounds__(kThermoThreads)
@@ -52,20 +85,8 @@ thermo_partial_kernel(const double* __restrict__ e, const int32_t* __restrict__ 
         const double lw = (mult ? log((double)mult[i]) : 0.0) - beta * ei;
         lse_push(st, lw, ei);
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        LseState other{__shfl_xor_sync(0xffffffffu, st.m, o), __shfl_xor_sync(0xffffffffu, st.s, o),
-                       __shfl_xor_sync(0xffffffffu, st.e1, o), __shfl_xor_sync(0xffffffffu, st.e2, o)};
-        st = lse_merge(st, other);
-    }
-    __shared__ LseState ws[kThermoThreads / 32];
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = st;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        LseState t = ws[0];
-        for (int w = 1; w < kThermoThreads / 32; ++w) t = lse_merge(t, ws[w]);
-        part[blockIdx.x] = {t.m, t.s, t.e1, t.e2};
-    }
+    const LseState t = block_merge(st);
+    if (threadIdx.x == 0) part[blockIdx.x] = {t.m, t.s, t.e1, t.e2};
 }
 
 __global__ void thermo_weights_kernel(const double* __restrict__ e, const int32_t* __restrict__ mult,
@@ -131,64 +152,84 @@ void thermo_finish(const LsePart* part, int nb, double T, fxe_thermo* out) {
 // ------------------------------------------------------------------------------------------
 namespace fxe {
 
-constexpr long kFixedPerBlock = (long)kThermoThreads * FXE_THERMO_FIXED_PER_THREAD;
+// One partial per block, and after them one slot for the maximum; every slot a call reads is
+// written (or, the maximum, cleared) by that call first, so nothing here needs to start at zero.
+static __device__ __align__(256) LsePart g_fixed_part[FXE_THERMO_FIXED_MAX_BLOCKS + 1];
 
-// One partial per block; every slot a call reads is written by that call first, so nothing
-// here needs to start at zero.
-static __device__ __align__(256) LsePart g_fixed_part[FXE_THERMO_FIXED_MAX_BLOCKS];
+// Order-preserving 64-bit key of a double (atomicMax on keys is a maximum on doubles; key 0 is
+// below every number).
+__device__ __forceinline__ unsigned long long order_key(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double from_order_key(unsigned long long k) {
+    return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
 
 cudaError_t fixed_scratch_address(LsePart** p) {
     return cudaGetSymbolAddress(reinterpret_cast<void**>(p), g_fixed_part);
 }
 
-__global__ void __launch_bounds__(kThermoThreads)
-thermo_fixed_partial_kernel(const double* __restrict__ e, const int32_t* __restrict__ mult, long n,
-                            double beta, LsePart* __restrict__ part) {
-    LseState st{-INFINITY, 0.0, 0.0, 0.0};
-    const long lo = (long)blockIdx.x * kFixedPerBlock;
-    const long hi = lo + kFixedPerBlock < n ? lo + kFixedPerBlock : n;
-    for (long i = lo + threadIdx.x; i < hi; i += kThermoThreads) {
-        const double ei = e[i];
-        const double lw = (mult ? log((double)mult[i]) : 0.0) - beta * ei;
-        lse_push(st, lw, ei);
-    }
+// The block maximum of a double over all its threads (every thread calls it; all get it).
+__device__ double block_max(double m) {
+    __shared__ double wm[kThermoThreads / 32];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        LseState other{__shfl_xor_sync(0xffffffffu, st.m, o), __shfl_xor_sync(0xffffffffu, st.s, o),
-                       __shfl_xor_sync(0xffffffffu, st.e1, o), __shfl_xor_sync(0xffffffffu, st.e2, o)};
-        st = lse_merge(st, other);
-    }
-    __shared__ LseState ws[kThermoThreads / 32];
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = st;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        LseState t = ws[0];
-        for (int w = 1; w < kThermoThreads / 32; ++w) t = lse_merge(t, ws[w]);
-        part[blockIdx.x] = {t.m, t.s, t.e1, t.e2};
-    }
+    double M = wm[0];
+    for (int w = 1; w < kThermoThreads / 32; ++w) M = fmax(M, wm[w]);
+    __syncthreads();
+    return M;
 }
 
-// One block merges the partials and writes the record (the host merge of thermo_finish, done
-// as a tree).
+// The fixed-scratch reduction runs max first, so that the pass with the exps has no chain between
+// its energies: (1) the maximum log-weight M (each block's, into one slot by atomicMax on order
+// keys; the slot is cleared before); (2) each block sums exp(lw - M) and its energy moments;
+// (3) one block adds the blocks' sums. Each block covers a contiguous run of per_block energies.
+__global__ void __launch_bounds__(kThermoThreads)
+thermo_fixed_max_kernel(const double* __restrict__ e, const int32_t* __restrict__ mult, long n,
+                        long per_block, double beta, unsigned long long* __restrict__ max_key) {
+    const long lo = (long)blockIdx.x * per_block;
+    const long hi = lo + per_block < n ? lo + per_block : n;
+    double m = -INFINITY;
+    for (long i = lo + threadIdx.x; i < hi; i += kThermoThreads)
+        m = fmax(m, (mult ? log((double)mult[i]) : 0.0) - beta * e[i]);
+    m = block_max(m);
+    if (threadIdx.x == 0) atomicMax(max_key, order_key(m));
+}
+
+__global__ void __launch_bounds__(kThermoThreads)
+thermo_fixed_sum_kernel(const double* __restrict__ e, const int32_t* __restrict__ mult, long n,
+                        long per_block, double beta, const unsigned long long* __restrict__ max_key,
+                        LsePart* __restrict__ part) {
+    const double M = from_order_key(*max_key);
+    const long lo = (long)blockIdx.x * per_block;
+    const long hi = lo + per_block < n ? lo + per_block : n;
+    LseState st{M, 0.0, 0.0, 0.0};
+    for (long i = lo + threadIdx.x; i < hi; i += kThermoThreads) {
+        const double ei = e[i];
+        const double w = exp((mult ? log((double)mult[i]) : 0.0) - beta * ei - M);
+        st.s += w;
+        st.e1 += w * ei;
+        st.e2 += w * ei * ei;
+    }
+    const LseState t = block_merge(st);
+    if (threadIdx.x == 0) part[blockIdx.x] = {M, t.s, t.e1, t.e2};
+}
+
+// One block adds the blocks' sums (all relative to the same maximum) and writes the record.
 __global__ void __launch_bounds__(kThermoThreads)
 thermo_fixed_finish_kernel(const LsePart* __restrict__ part, int nb, double T, fxe_thermo* __restrict__ out) {
-    LseState st{-INFINITY, 0.0, 0.0, 0.0};
+    LseState st{part[0].m, 0.0, 0.0, 0.0};
     for (int b = threadIdx.x; b < nb; b += kThermoThreads) {
         const LsePart q = part[b];
-        st = lse_merge(st, LseState{q.m, q.s, q.e1, q.e2});
+        st.s += q.s;
+        st.e1 += q.e1;
+        st.e2 += q.e2;
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        LseState other{__shfl_xor_sync(0xffffffffu, st.m, o), __shfl_xor_sync(0xffffffffu, st.s, o),
-                       __shfl_xor_sync(0xffffffffu, st.e1, o), __shfl_xor_sync(0xffffffffu, st.e2, o)};
-        st = lse_merge(st, other);
-    }
-    __shared__ LseState ws[kThermoThreads / 32];
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = st;
-    __syncthreads();
+    const LseState t = block_merge(st);
     if (threadIdx.x == 0) {
-        LseState t = ws[0];
-        for (int w = 1; w < kThermoThreads / 32; ++w) t = lse_merge(t, ws[w]);
         const double kB = 0.001987206;  // LIB/statmech.h:26
         const double lnZ = t.m + log(t.s);
         const double Ea = t.e1 / t.s, E2 = t.e2 / t.s;
@@ -207,11 +248,22 @@ thermo_fixed_finish_kernel(const LsePart* __restrict__ part, int nb, double T, f
     }
 }
 
+// Blocks of the fixed-scratch passes: about four energies per thread, within the
+// FXE_THERMO_FIXED_MAX_BLOCKS partials.
 void launch_thermo_fixed(const double* e, const int32_t* mult, long n, double beta, double T,
                          LsePart* scratch, fxe_thermo* d_out, cudaStream_t st) {
-    const int nb = (int)((n + kFixedPerBlock - 1) / kFixedPerBlock);
-    thermo_fixed_partial_kernel<<<nb, kThermoThreads, 0, st>>>(e, mult, n, beta, scratch);
-    thermo_fixed_finish_kernel<<<1, kThermoThreads, 0, st>>>(scratch, nb, T, d_out);
+    long nb = (n + 4 * kThermoThreads - 1) / (4 * kThermoThreads);
+    if (nb > FXE_THERMO_FIXED_MAX_BLOCKS) nb = FXE_THERMO_FIXED_MAX_BLOCKS;
+    if (nb < 1) nb = 1;
+    long per_block = (n + nb - 1) / nb;
+    if (per_block < 1) per_block = 1;
+    nb = (n + per_block - 1) / per_block;
+    if (nb < 1) nb = 1;
+    unsigned long long* max_key = reinterpret_cast<unsigned long long*>(scratch + FXE_THERMO_FIXED_MAX_BLOCKS);
+    cudaMemsetAsync(max_key, 0, sizeof(unsigned long long), st);
+    thermo_fixed_max_kernel<<<(int)nb, kThermoThreads, 0, st>>>(e, mult, n, per_block, beta, max_key);
+    thermo_fixed_sum_kernel<<<(int)nb, kThermoThreads, 0, st>>>(e, mult, n, per_block, beta, max_key, scratch);
+    thermo_fixed_finish_kernel<<<1, kThermoThreads, 0, st>>>(scratch, (int)nb, T, d_out);
 }
 
 }  // namespace fxe

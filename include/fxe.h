@@ -245,13 +245,15 @@ fxe_status fxe_thermo_compute_device(const double* d_energies, const int32_t* d_
  * memory: code running under a fixed device-memory budget that has handed all free memory to
  * its own pools (an admission-controlled serving loop), and code that may not synchronise the
  * device, which every cudaMalloc/cudaFree can do. The block partials live in a fixed array
- * inside the library (FXE_THERMO_FIXED_MAX_BLOCKS partials of 32 bytes, 2 MiB, one array per
- * device), the merge runs on the device, and the record is written to d_out (device memory).
+ * inside the library (FXE_THERMO_FIXED_MAX_BLOCKS partials of 32 bytes and one slot for the
+ * maximum, 2 MiB, one array per device), the merge runs on the device, and the record is written
+ * to d_out (device memory).
  * Work is queued on `stream` (cudaStream_t or NULL for the legacy default stream) and not
  * waited for.
  *
- * - n may be at most FXE_THERMO_FIXED_MAX_N (each block covers FXE_THERMO_FIXED_PER_THREAD x 256
- *   energies); larger n is rejected with FXE_ERR_INVALID_ARGS before any work is queued.
+ * - n may be at most FXE_THERMO_FIXED_MAX_N (FXE_THERMO_FIXED_MAX_BLOCKS partials, each of at most
+ *   FXE_THERMO_FIXED_PER_THREAD x 256 energies); larger n is rejected with FXE_ERR_INVALID_ARGS
+ *   before any work is queued.
  * - The first call on a device looks up the array's address (cudaGetSymbolAddress, with that
  *   device current) and loads the library's device code; make that first call before any stream
  *   capture and before memory is handed out. The address is kept for the life of the process:
