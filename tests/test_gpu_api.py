@@ -101,6 +101,23 @@ def test_thermo_known_answers():
     assert all(math.isfinite(v) for v in th.values())
 
 
+def test_boltzmann_weights_over_the_double_range():
+    """Weights from 1 down past the double range against the host's exp: within 1e-12 where the
+    weight is a normal double, 0 where it underflows."""
+    e = np.linspace(-1000.0, 0.0, 20001)
+    w = evaluator.boltzmann_weights(e, None, 300.0)
+    beta = 1.0 / (KB * 300.0)
+    lw = -beta * e
+    m = lw.max()
+    lnz = m + math.log(np.exp(lw - m).sum())
+    want = np.exp(lw - lnz)
+    normal = want > 1e-290
+    assert normal.sum() > 5000 and (want == 0.0).sum() > 5000
+    np.testing.assert_allclose(w[normal], want[normal], rtol=1e-12, atol=0.0)
+    assert np.all(w[want == 0.0] == 0.0)
+    assert np.all((w >= 0.0) & (w <= 1.0))
+
+
 def test_boltzmann_weights_and_engine():
     rng = np.random.default_rng(9)
     e = rng.normal(-20.0, 2.0, 50_000)
