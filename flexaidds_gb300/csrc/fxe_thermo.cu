@@ -152,118 +152,118 @@ void thermo_finish(const LsePart* part, int nb, double T, fxe_thermo* out) {
 // ------------------------------------------------------------------------------------------
 namespace fxe {
 
-// One partial per block, and after them one slot for the maximum; every slot a call reads is
-// written (or, the maximum, cleared) by that call first, so nothing here needs to start at zero.
+// One partial per block, and after them one slot for the count of finished blocks; every slot a
+// call reads is written (or, the count, cleared) by that call first, so nothing here needs to
+// start at zero.
 static __device__ __align__(256) LsePart g_fixed_part[FXE_THERMO_FIXED_MAX_BLOCKS + 1];
-
-// Order-preserving 64-bit key of a double (atomicMax on keys is a maximum on doubles; key 0 is
-// below every number).
-__device__ __forceinline__ unsigned long long order_key(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
-}
-__device__ __forceinline__ double from_order_key(unsigned long long k) {
-    return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
-}
 
 cudaError_t fixed_scratch_address(LsePart** p) {
     return cudaGetSymbolAddress(reinterpret_cast<void**>(p), g_fixed_part);
 }
 
-// The block maximum of a double over all its threads (every thread calls it; all get it).
-__device__ double block_max(double m) {
-    __shared__ double wm[kThermoThreads / 32];
+// The fixed-scratch reduction in one launch: each thread takes its energies four at a time (their
+// log-weights' maximum rescales the thread's sums at most once, then four independent exps), the
+// blocks merge max first and write their partials, and the last block to finish (a counter in
+// the scratch, cleared before the launch) merges the partials and writes the record. Each block
+// covers a contiguous run of per_block energies.
+constexpr int kFixedChunk = 4;
+
+__global__ void __launch_bounds__(kThermoThreads)
+thermo_fixed_kernel(const double* __restrict__ e, const int32_t* __restrict__ mult, long n, long per_block,
+                    double beta, double T, LsePart* __restrict__ part, unsigned* __restrict__ done,
+                    fxe_thermo* __restrict__ out) {
+    const long lo = (long)blockIdx.x * per_block;
+    const long hi = lo + per_block < n ? lo + per_block : n;
+    LseState st{-INFINITY, 0.0, 0.0, 0.0};
+    #pragma unroll 1
+    for (long i0 = lo + threadIdx.x; i0 < hi; i0 += (long)kFixedChunk * kThermoThreads) {
+        double ev[kFixedChunk], lw[kFixedChunk];
+        double m4 = -INFINITY;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
-    __syncthreads();
-    double M = wm[0];
-    for (int w = 1; w < kThermoThreads / 32; ++w) M = fmax(M, wm[w]);
-    __syncthreads();
-    return M;
-}
-
-// The fixed-scratch reduction runs max first, so that the pass with the exps has no chain between
-// its energies: (1) the maximum log-weight M (each block's, into one slot by atomicMax on order
-// keys; the slot is cleared before); (2) each block sums exp(lw - M) and its energy moments;
-// (3) one block adds the blocks' sums. Each block covers a contiguous run of per_block energies.
-__global__ void __launch_bounds__(kThermoThreads)
-thermo_fixed_max_kernel(const double* __restrict__ e, const int32_t* __restrict__ mult, long n,
-                        long per_block, double beta, unsigned long long* __restrict__ max_key) {
-    const long lo = (long)blockIdx.x * per_block;
-    const long hi = lo + per_block < n ? lo + per_block : n;
-    double m = -INFINITY;
-    for (long i = lo + threadIdx.x; i < hi; i += kThermoThreads)
-        m = fmax(m, (mult ? log((double)mult[i]) : 0.0) - beta * e[i]);
-    m = block_max(m);
-    if (threadIdx.x == 0) atomicMax(max_key, order_key(m));
-}
-
-__global__ void __launch_bounds__(kThermoThreads)
-thermo_fixed_sum_kernel(const double* __restrict__ e, const int32_t* __restrict__ mult, long n,
-                        long per_block, double beta, const unsigned long long* __restrict__ max_key,
-                        LsePart* __restrict__ part) {
-    const double M = from_order_key(*max_key);
-    const long lo = (long)blockIdx.x * per_block;
-    const long hi = lo + per_block < n ? lo + per_block : n;
-    LseState st{M, 0.0, 0.0, 0.0};
-    for (long i = lo + threadIdx.x; i < hi; i += kThermoThreads) {
-        const double ei = e[i];
-        const double w = exp((mult ? log((double)mult[i]) : 0.0) - beta * ei - M);
-        st.s += w;
-        st.e1 += w * ei;
-        st.e2 += w * ei * ei;
+        for (int j = 0; j < kFixedChunk; ++j) {
+            const long i = i0 + (long)j * kThermoThreads;
+            ev[j] = 0.0;
+            lw[j] = -INFINITY;
+            if (i < hi) {
+                ev[j] = e[i];
+                lw[j] = (mult ? log((double)mult[i]) : 0.0) - beta * ev[j];
+                m4 = fmax(m4, lw[j]);
+            }
+        }
+        if (m4 > st.m) {
+            const double f = st.m == -INFINITY ? 0.0 : exp(st.m - m4);
+            st.s *= f;
+            st.e1 *= f;
+            st.e2 *= f;
+            st.m = m4;
+        }
+#pragma unroll
+        for (int j = 0; j < kFixedChunk; ++j) {
+            if (lw[j] == -INFINITY) continue;
+            const double w = exp(lw[j] - st.m);
+            st.s += w;
+            st.e1 += w * ev[j];
+            st.e2 += w * ev[j] * ev[j];
+        }
     }
     const LseState t = block_merge(st);
-    if (threadIdx.x == 0) part[blockIdx.x] = {M, t.s, t.e1, t.e2};
-}
-
-// One block adds the blocks' sums (all relative to the same maximum) and writes the record.
-__global__ void __launch_bounds__(kThermoThreads)
-thermo_fixed_finish_kernel(const LsePart* __restrict__ part, int nb, double T, fxe_thermo* __restrict__ out) {
-    LseState st{part[0].m, 0.0, 0.0, 0.0};
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = {t.m, t.s, t.e1, t.e2};
+        __threadfence();
+        last = atomicAdd(done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // the last block: every partial, rescaled to their largest maximum, then the block's
+    const int nb = (int)gridDim.x;
+    double mt = -INFINITY;
+    for (int b = threadIdx.x; b < nb; b += kThermoThreads) mt = fmax(mt, ((volatile LsePart*)part)[b].m);
+    LseState sp{mt, 0.0, 0.0, 0.0};
     for (int b = threadIdx.x; b < nb; b += kThermoThreads) {
-        const LsePart q = part[b];
-        st.s += q.s;
-        st.e1 += q.e1;
-        st.e2 += q.e2;
+        const volatile LsePart* q = (volatile LsePart*)part + b;
+        const double qm = q->m;
+        if (qm == -INFINITY) continue;
+        const double f = exp(qm - mt);
+        sp.s += q->s * f;
+        sp.e1 += q->e1 * f;
+        sp.e2 += q->e2 * f;
     }
-    const LseState t = block_merge(st);
+    const LseState r = block_merge(sp);
     if (threadIdx.x == 0) {
         const double kB = 0.001987206;  // LIB/statmech.h:26
-        const double lnZ = t.m + log(t.s);
-        const double Ea = t.e1 / t.s, E2 = t.e2 / t.s;
+        const double lnZ = r.m + log(r.s);
+        const double Ea = r.e1 / r.s, E2 = r.e2 / r.s;
         const double kT = kB * T;
         const double var = E2 - Ea * Ea;
-        fxe_thermo r;
-        r.temperature = T;
-        r.log_Z = lnZ;
-        r.free_energy = -kT * lnZ;
-        r.mean_energy = Ea;
-        r.mean_energy_sq = E2;
-        r.heat_capacity = var / (kT * kT);
-        r.entropy = (Ea - r.free_energy) / T;
-        r.std_energy = sqrt(var > 0.0 ? var : 0.0);
-        *out = r;
+        fxe_thermo rec;
+        rec.temperature = T;
+        rec.log_Z = lnZ;
+        rec.free_energy = -kT * lnZ;
+        rec.mean_energy = Ea;
+        rec.mean_energy_sq = E2;
+        rec.heat_capacity = var / (kT * kT);
+        rec.entropy = (Ea - rec.free_energy) / T;
+        rec.std_energy = sqrt(var > 0.0 ? var : 0.0);
+        *out = rec;
     }
 }
 
-// Blocks of the fixed-scratch passes: about four energies per thread, within the
-// FXE_THERMO_FIXED_MAX_BLOCKS partials.
+// Blocks of the fixed-scratch pass: one chunk of four energies per thread when the partials allow
+// it, within the FXE_THERMO_FIXED_MAX_BLOCKS partials.
 void launch_thermo_fixed(const double* e, const int32_t* mult, long n, double beta, double T,
                          LsePart* scratch, fxe_thermo* d_out, cudaStream_t st) {
-    long nb = (n + 4 * kThermoThreads - 1) / (4 * kThermoThreads);
+    long nb = (n + (long)kFixedChunk * kThermoThreads - 1) / ((long)kFixedChunk * kThermoThreads);
     if (nb > FXE_THERMO_FIXED_MAX_BLOCKS) nb = FXE_THERMO_FIXED_MAX_BLOCKS;
     if (nb < 1) nb = 1;
     long per_block = (n + nb - 1) / nb;
     if (per_block < 1) per_block = 1;
     nb = (n + per_block - 1) / per_block;
     if (nb < 1) nb = 1;
-    unsigned long long* max_key = reinterpret_cast<unsigned long long*>(scratch + FXE_THERMO_FIXED_MAX_BLOCKS);
-    cudaMemsetAsync(max_key, 0, sizeof(unsigned long long), st);
-    thermo_fixed_max_kernel<<<(int)nb, kThermoThreads, 0, st>>>(e, mult, n, per_block, beta, max_key);
-    thermo_fixed_sum_kernel<<<(int)nb, kThermoThreads, 0, st>>>(e, mult, n, per_block, beta, max_key, scratch);
-    thermo_fixed_finish_kernel<<<1, kThermoThreads, 0, st>>>(scratch, (int)nb, T, d_out);
+    unsigned* done = reinterpret_cast<unsigned*>(scratch + FXE_THERMO_FIXED_MAX_BLOCKS);
+    cudaMemsetAsync(done, 0, sizeof(unsigned), st);
+    thermo_fixed_kernel<<<(int)nb, kThermoThreads, 0, st>>>(e, mult, n, per_block, beta, T, scratch, done, d_out);
 }
 
 }  // namespace fxe

@@ -245,8 +245,8 @@ fxe_status fxe_thermo_compute_device(const double* d_energies, const int32_t* d_
  * memory: code running under a fixed device-memory budget that has handed all free memory to
  * its own pools (an admission-controlled serving loop), and code that may not synchronise the
  * device, which every cudaMalloc/cudaFree can do. The block partials live in a fixed array
- * inside the library (FXE_THERMO_FIXED_MAX_BLOCKS partials of 32 bytes and one slot for the
- * maximum, 2 MiB, one array per device), the merge runs on the device, and the record is written
+ * inside the library (FXE_THERMO_FIXED_MAX_BLOCKS partials of 32 bytes and one slot for a
+ * counter, 2 MiB, one array per device), the merge runs on the device, and the record is written
  * to d_out (device memory).
  * Work is queued on `stream` (cudaStream_t or NULL for the legacy default stream) and not
  * waited for.
