@@ -44,7 +44,7 @@ using real = FXE_REAL;
 #endif
 // Double builds decide the hull walk's plane tests in single precision first and redo a test
 // in double only when its single-precision result is within its error bound of deciding the
-// other way (see walk_step).
+// other way (see walk_step_group).
 #ifndef FXE_FILTER
 #define FXE_FILTER (FXE_REFERENCE_FORMULAS)
 #endif
@@ -1481,20 +1481,13 @@ __device__ double pose_clash_sum(const DevSystem& S, const DevWork& W, int p, in
 // ------------------------------------------------------------------------------------------
 // pose_kernel: calc_region + vcfunction for one pose per warp
 // ------------------------------------------------------------------------------------------
-// Shared memory per warp sets how many poses an SM holds at once. Both kernels gain from more
-// warps (latency-bound), so they keep the per-pose seeds and record masks in the workspace
-// (W.pose_seed, W.pose_rec): ten double-precision or twenty single-precision poses per SM.
-#ifndef FXE_SEEDS_SHARED
-#define FXE_SEEDS_SHARED 0
-#endif
+// Shared memory per warp sets how many poses an SM holds at once, so the per-pose seeds and
+// record masks live in the workspace (W.pose_seed, W.pose_rec); 20.0 KB of shared memory per pose
+// in double precision, 11.1 KB in single.
 struct PoseShared {
     VorShared v;
     uint8_t order[kMaxLig];          // mobile atoms in Calclist order
     uint32_t done[kMaskWords];       // mobile atoms whose contacts are saved
-#if FXE_SEEDS_SHARED
-    int seed[kMaxLig][3];
-    uint32_t rec[kMaxLig][kMaskWords];
-#endif
 };
 
 __device__ __forceinline__ bool bit(const uint32_t* m, int l) { return (m[l >> 5] >> (l & 31)) & 1u; }
@@ -1533,13 +1526,8 @@ __device__ __forceinline__ void score_pose(const DevSystem& S, const DevWork& W,
     if (p < 0) p = 0;
     const int nl = n_mobile(S);      // the scored atoms: side-chain atoms, then the ligand
     // polyhedron seeds (Calc indices, -1 = none) and the mobile partners each processed atom kept
-#if FXE_SEEDS_SHARED
-    int (*const seed)[3] = ps.seed;
-    uint32_t (*const rec)[kMaskWords] = ps.rec;
-#else
     int (*const seed)[3] = reinterpret_cast<int (*)[3]>(W.pose_seed + (size_t)p * kMaxLig * 3);
     uint32_t (*const rec)[kMaskWords] = reinterpret_cast<uint32_t (*)[kMaskWords]>(W.pose_rec + (size_t)p * kMaxLig * kMaskWords);
-#endif
     const size_t lb = (size_t)p * nl;
     if (alive && W.pose_grid[p].z) {
         finish_failed(W, p, lane, FXE_POSE_CAPACITY, 0.0);
