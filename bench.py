@@ -54,7 +54,7 @@ STATMECH_FLOP = 20
 
 # DRAM bytes per launch of the dominant kernel from ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum), keyed by precision; from profiles/pose_kernel_plain_scale.md.
-POSE_KERNEL_DRAM_BYTES = {"reference": 106_995_968, "fast": 85_202_176}
+POSE_KERNEL_DRAM_BYTES = {"reference": 106_995_968, "fast": 99_187_200}
 
 # nominal non-tensor arithmetic peaks of GB300 (152 SMs at 2,070 MHz): FP32 152 x 128 lanes x 2
 # flops per FMA; FP64 1.25 TFLOP/s. There is no measured figure for either.
