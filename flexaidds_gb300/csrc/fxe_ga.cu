@@ -141,9 +141,10 @@ __device__ __forceinline__ int32_t uniform_gene(const GaJob& J, uint64_t i) {
 // stream kInitRotStream.
 constexpr uint64_t kInitRotStream = 0xFFFFFFFEull;
 
-__device__ void initial_candidates(const GaJob& J, long long c0, int npairs) {
+// (the candidates first, first + stride, ... of the batch: the threads of a block, or of a grid)
+__device__ void initial_candidates(const GaJob& J, long long c0, int npairs, int first, int stride) {
     const int ng = J.ng;
-    for (int c = threadIdx.x; c < 2 * npairs; c += blockDim.x) {
+    for (int c = first; c < 2 * npairs; c += stride) {
         int32_t* g = J.cand + (size_t)c * ng;
         for (int q = 0; q < ng; ++q) {
             const uint64_t i = (uint64_t)(c0 + c) * ng + q;
@@ -155,8 +156,8 @@ __device__ void initial_candidates(const GaJob& J, long long c0, int npairs) {
 }
 
 __global__ void __launch_bounds__(kGaThreads) ga_init_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
-    const GaJob& J = all[run[blockIdx.x]];
-    initial_candidates(J, 0, min(J.ncand, J.gen[1]));
+    const GaJob& J = all[run[blockIdx.y]];
+    initial_candidates(J, 0, min(J.ncand, J.gen[1]), blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 // One pair of children: two roulette draws, optional adaptive probabilities, crossover with
@@ -259,9 +260,10 @@ __device__ void breed_pair(const GaJob& J, int g, int k, int32_t* john, int32_t*
 
 // Pairs k0 .. k0 + npairs - 1 of the running generation's children as candidates, with their
 // signatures.
-__device__ void bred_candidates(const GaJob& J, int g, long long k0, int npairs) {
+// (the pairs first, first + stride, ... of the batch: the threads of a block, or of a grid)
+__device__ void bred_candidates(const GaJob& J, int g, long long k0, int npairs, int first, int stride) {
     const int ng = J.ng;
-    for (int k = threadIdx.x; k < npairs; k += blockDim.x) {
+    for (int k = first; k < npairs; k += stride) {
         int32_t* john = J.cand + (size_t)(2 * k) * ng;
         int32_t* mary = john + ng;
         breed_pair(J, g, (int)(k0 + k), john, mary);
@@ -271,9 +273,13 @@ __device__ void bred_candidates(const GaJob& J, int g, long long k0, int npairs)
 }
 
 __global__ void __launch_bounds__(kGaThreads) ga_breed_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
-    const GaJob& J = all[run[blockIdx.x]];
-    bred_candidates(J, J.gen[0], 0, min(J.ncand, J.gen[1]));
+    const GaJob& J = all[run[blockIdx.y]];
+    bred_candidates(J, J.gen[0], 0, min(J.ncand, J.gen[1]), blockIdx.x * blockDim.x + threadIdx.x,
+                    gridDim.x * blockDim.x);
 }
+
+// Blocks per job of the first candidate batch (pairs up to P + 8 with P <= 2048; one pair per thread).
+constexpr int kGaBatchBlocks = (2048 + 8 + kGaThreads - 1) / kGaThreads;
 
 constexpr int kGaMaxBatches = 16;   // candidate batches before duplicates are let through
 
@@ -313,8 +319,8 @@ __global__ void __launch_bounds__(kGaThreads) ga_accept_kernel(const GaJob* __re
         if (s_done) break;
         base += 2 * npairs;
         npairs = J.ncand;
-        if (kInitial) initial_candidates(J, base, npairs);
-        else bred_candidates(J, g, base >> 1, npairs);
+        if (kInitial) initial_candidates(J, base, npairs, threadIdx.x, blockDim.x);
+        else bred_candidates(J, g, base >> 1, npairs, threadIdx.x, blockDim.x);
         __syncthreads();
     }
     if (threadIdx.x == 0) {
@@ -407,31 +413,40 @@ __global__ void __launch_bounds__(kGaThreads) ga_decode_kernel(const GaJob* __re
     }
 }
 
-constexpr int kNicheThreads = 64;
-constexpr int kNicheBlocks = (2048 + kNicheThreads - 1) / kNicheThreads;
+constexpr int kNicheWarps = 8;
+constexpr int kNicheBlocks = (2048 + kNicheWarps - 1) / kNicheWarps;
 
 // Niche count of chromosome i: the sum over all j of 1 - (rmsp / sig_share)^alpha where rmsp
 // (calc_rmsp, LIB/gaboom.cpp:2874-2885: root mean square of the IC differences) is within
-// sig_share (LIB/gaboom.cpp:1652-1661). One thread per i, j in order.
-__global__ void __launch_bounds__(kNicheThreads) ga_niche_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
+// sig_share (LIB/gaboom.cpp:1652-1661). One warp per i: the lanes form the terms of 32 j's at a
+// time, and the sum takes them in j order (a pair beyond sig_share adds 0, which changes no sum
+// of these non-negative terms), so every count is the one a thread walking j in order forms.
+__global__ void __launch_bounds__(kNicheWarps * 32) ga_niche_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
     const GaJob& J = all[run[blockIdx.y]];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.x * kNicheWarps + (int)(threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
     if (J.fitness == kFitLinear || i >= J.P) return;
-    const int ng = J.ng;
+    const int ng = J.ng, P = J.P;
     const double* xi = J.pic + (size_t)i * ng;
     const double sig = J.sig_share, alpha = J.share_alpha;
     double s = 0.0;
-    for (int j = 0; j < J.P; ++j) {
-        const double* xj = J.pic + (size_t)j * ng;
-        double acc = 0.0;
-        for (int q = 0; q < ng; ++q) {
-            const double dq = xi[q] - xj[q];
-            acc += dq * dq;
+    for (int j0 = 0; j0 < P; j0 += 32) {
+        const int j = j0 + lane;
+        double term = 0.0;
+        if (j < P) {
+            const double* xj = J.pic + (size_t)j * ng;
+            double acc = 0.0;
+            for (int q = 0; q < ng; ++q) {
+                const double dq = xi[q] - xj[q];
+                acc += dq * dq;
+            }
+            const double r = sqrt(acc / (double)ng);
+            if (r <= sig) term = 1.0 - (alpha == 1.0 ? r / sig : pow(r / sig, alpha));
         }
-        const double r = sqrt(acc / (double)ng);
-        if (r <= sig) s += 1.0 - (alpha == 1.0 ? r / sig : pow(r / sig, alpha));
+        const int m = P - j0 < 32 ? P - j0 : 32;
+        for (int k = 0; k < m; ++k) s += __shfl_sync(0xffffffffu, term, k);
     }
-    J.share[i] = s;
+    if (lane == 0) J.share[i] = s;
 }
 
 // Running sums of the fitness in roulette order (roullete_wheel's walk, LIB/gaboom.cpp:1158-1186)
@@ -503,17 +518,17 @@ __global__ void __launch_bounds__(kGaThreads) ga_fitness_kernel(const GaJob* __r
 
 void launch_ga_fitness(const GaJob* all, const int* run, int n_jobs, bool initial, cudaStream_t st) {
     ga_decode_kernel<<<dim3(8, n_jobs), kGaThreads, 0, st>>>(all, run);
-    ga_niche_kernel<<<dim3(kNicheBlocks, n_jobs), kNicheThreads, 0, st>>>(all, run);
+    ga_niche_kernel<<<dim3(kNicheBlocks, n_jobs), kNicheWarps * 32, 0, st>>>(all, run);
     if (initial) ga_fitness_kernel<true><<<n_jobs, kGaThreads, 0, st>>>(all, run);
     else ga_fitness_kernel<false><<<n_jobs, kGaThreads, 0, st>>>(all, run);
 }
 
 void launch_ga_init(const GaJob* all, const int* run, int n_jobs, cudaStream_t st) {
-    ga_init_kernel<<<n_jobs, kGaThreads, 0, st>>>(all, run);
+    ga_init_kernel<<<dim3(2 * kGaBatchBlocks, n_jobs), kGaThreads, 0, st>>>(all, run);
     ga_accept_kernel<true><<<n_jobs, kGaThreads, 0, st>>>(all, run);
 }
 void launch_ga_breed(const GaJob* all, const int* run, int n_jobs, cudaStream_t st) {
-    ga_breed_kernel<<<n_jobs, kGaThreads, 0, st>>>(all, run);
+    ga_breed_kernel<<<dim3(kGaBatchBlocks, n_jobs), kGaThreads, 0, st>>>(all, run);
     ga_accept_kernel<false><<<n_jobs, kGaThreads, 0, st>>>(all, run);
 }
 // Breeding with the caller's draws (fxe_ga_breed_draws): J.fit and J.ford given, one block forms
@@ -547,7 +562,7 @@ void launch_ga_breed_draws(const GaJob* J, const double* draws, long long stride
 // Niche counts of a population whose ICs are given (fxe_ga_niche_counts): the generation's kernel
 // on one job.
 void launch_ga_niche(const GaJob* all, const int* run, cudaStream_t st) {
-    ga_niche_kernel<<<dim3(kNicheBlocks, 1), kNicheThreads, 0, st>>>(all, run);
+    ga_niche_kernel<<<dim3(kNicheBlocks, 1), kNicheWarps * 32, 0, st>>>(all, run);
 }
 
 void launch_ga_select(GaJob* all, const int* run, int n_jobs, bool initial, cudaStream_t st) {
