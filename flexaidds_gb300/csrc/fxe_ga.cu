@@ -110,24 +110,33 @@ __device__ __forceinline__ uint64_t signature(const GaJob& J, const int32_t* gen
     return h;
 }
 
-// Inserts a signature; false if it was there already. 0 marks an empty slot of the open-addressing
-// table, so the signature 0 is kept in gen[4] instead.
-__device__ bool seen_insert(const GaJob& J, uint64_t h) {
-    if (h == 0) {
-        if (J.gen[4]) return false;
-        J.gen[4] = 1;
-        return true;
-    }
+// The signature set: open addressing in HBM; 0 marks an empty slot of the table, so the signature
+// 0 is kept in gen[4] instead.
+// Whether a signature is in the set (no insertion).
+__device__ bool seen_contains(const GaJob& J, uint64_t h) {
+    if (h == 0) return J.gen[4] != 0;
     unsigned long long i = mix64(h) & J.hmask;
     for (unsigned long long n = 0; n <= J.hmask; ++n, i = (i + 1) & J.hmask) {
         const uint64_t v = J.seen[i];
-        if (v == h) return false;
-        if (v == 0) {
-            J.seen[i] = h;
-            return true;
-        }
+        if (v == h) return true;
+        if (v == 0) return false;
     }
-    return true;   // full table: cannot happen, it has twice the slots of the chromosomes a job makes
+    return false;
+}
+
+// Inserts a signature the set does not hold, safe beside other threads inserting other
+// signatures (the table's layout may differ from one-at-a-time insertion; membership does not).
+__device__ void seen_insert_concurrent(const GaJob& J, uint64_t h) {
+    if (h == 0) {
+        J.gen[4] = 1;
+        return;
+    }
+    unsigned long long i = mix64(h) & J.hmask;
+    for (unsigned long long n = 0; n <= J.hmask; ++n, i = (i + 1) & J.hmask) {
+        const unsigned long long prev = atomicCAS(reinterpret_cast<unsigned long long*>(J.seen) + i, 0ull,
+                                                  (unsigned long long)h);
+        if (prev == 0ull || prev == h) return;
+    }
 }
 
 __device__ __forceinline__ int32_t uniform_gene(const GaJob& J, uint64_t i) {
@@ -285,38 +294,133 @@ constexpr int kGaMaxBatches = 16;   // candidate batches before duplicates are l
 
 // Acceptance in the reference's order (child 1, then child 2 of each pair, until the generation
 // has nnew children; the initial population: P chromosomes): a candidate is taken unless its
-// signature was seen before in the job, and taken signatures join the set. Thread 0 walks the
-// batch; when it runs out, the block breeds the next batch of pairs. After kGaMaxBatches batches
-// candidates are taken as they come (counted in gen[2]), where the reference would loop until
-// mutation finds new genes. gen[1] sizes the next generation's first batch from what this one
-// used; gen[3] counts rejected candidates.
+// signature was seen before in the job, and taken signatures join the set. Walked one candidate
+// at a time, candidate c is taken exactly when its signature is in neither the set the batch
+// started from nor at an earlier candidate of the batch (an earlier copy joined the set or was in
+// it), up to the candidate that completes the generation; candidates after it are not looked at.
+// So the block decides all of a batch's candidates at once: the first occurrences by a sort of
+// (signature, index) pairs in shared memory, the set by read-only probes, the cut by an ordered
+// scan; then it copies the taken ones into place and inserts their signatures. When a batch runs
+// out, the block breeds the next batch of pairs. After kGaMaxBatches batches candidates are taken
+// as they come (counted in gen[2]), where the reference would loop until mutation finds new genes.
+// gen[1] sizes the next generation's first batch from what this one used; gen[3] counts rejected
+// candidates.
+constexpr int kAcceptThreads = 1024;
+constexpr int kAcceptSort = 8192;                  // >= 2 (P + 8) candidates with P <= 2048
+constexpr size_t kAcceptSmem = (size_t)kAcceptSort * (sizeof(uint64_t) + sizeof(uint16_t)) + kAcceptSort;
+
 template <bool kInitial>
-__global__ void __launch_bounds__(kGaThreads) ga_accept_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
-    __shared__ int s_done;
+__global__ void __launch_bounds__(kAcceptThreads) ga_accept_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
+    extern __shared__ __align__(16) unsigned char acc_smem[];
+    uint64_t* skey = reinterpret_cast<uint64_t*>(acc_smem);
+    uint16_t* sidx = reinterpret_cast<uint16_t*>(skey + kAcceptSort);
+    uint8_t* take = reinterpret_cast<uint8_t*>(sidx + kAcceptSort);
+    __shared__ int wsum[kAcceptThreads / 32];
+    __shared__ int s_cut, s_taken, s_rej;
     const GaJob& J = all[run[blockIdx.x]];
     const int ng = J.ng, g = J.gen[0];
     const int need = kInitial ? J.P : J.nnew;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int npairs = min(J.ncand, J.gen[1]);
     long long base = 0;   // candidate index of the batch's first entry
     int i = 0, used = 0, forced = 0, rejected = 0;
     for (int batch = 0;; ++batch) {
-        if (threadIdx.x == 0) {
-            const bool force = !J.reject || batch >= kGaMaxBatches;
-            int c = 0;
-            for (; c < 2 * npairs; ++c) {
-                if (force || seen_insert(J, J.cand_sig[c])) {
-                    for (int q = 0; q < ng; ++q) J.child[(size_t)i * ng + q] = J.cand[(size_t)c * ng + q];
-                    if (J.reject && force) ++forced;
-                    if (++i == need) break;
-                } else {
-                    ++rejected;
-                }
+        const bool force = !J.reject || batch >= kGaMaxBatches;
+        const int ncb = 2 * npairs;
+        // 1. which candidates would be taken (before the cut)
+        if (force) {
+            for (int c = tid; c < ncb; c += kAcceptThreads) take[c] = 1;
+        } else {
+            int n2 = 1;
+            while (n2 < ncb) n2 <<= 1;
+            for (int k = tid; k < n2; k += kAcceptThreads) {
+                skey[k] = k < ncb ? J.cand_sig[k] : ~0ull;
+                sidx[k] = (uint16_t)k;
             }
-            used = (int)(base + c + 1);
-            s_done = i == need;
+            __syncthreads();
+            for (int len = 2; len <= n2; len <<= 1)
+                for (int j = len >> 1; j > 0; j >>= 1) {
+                    for (int k = tid; k < n2; k += kAcceptThreads) {
+                        const int l = k ^ j;
+                        if (l > k) {
+                            const bool up = (k & len) == 0;
+                            const uint64_t ka = skey[k], kb = skey[l];
+                            const bool gt = ka > kb || (ka == kb && sidx[k] > sidx[l]);
+                            if (gt == up) {
+                                skey[k] = kb;
+                                skey[l] = ka;
+                                const uint16_t t = sidx[k];
+                                sidx[k] = sidx[l];
+                                sidx[l] = t;
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+            for (int k = tid; k < n2; k += kAcceptThreads) {
+                const int c = sidx[k];
+                if (c >= ncb) continue;
+                const bool first = k == 0 || skey[k] != skey[k - 1];
+                take[c] = first && !seen_contains(J, skey[k]) ? 1 : 0;
+            }
         }
         __syncthreads();
-        if (s_done) break;
+        // 2. the cut: the candidate that takes the generation to `need`, by an ordered scan over
+        // contiguous runs of candidates per thread
+        const int per = (ncb + kAcceptThreads - 1) / kAcceptThreads;
+        const int c0 = tid * per, c1 = min(ncb, c0 + per);
+        int cnt = 0;
+        for (int c = c0; c < c1; ++c) cnt += take[c];
+        int inc = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
+        }
+        if (lane == 31) wsum[warp] = inc;
+        if (tid == 0) {
+            s_cut = ncb;
+            s_taken = 0;
+            s_rej = 0;
+        }
+        __syncthreads();
+        int wbase = 0;
+        for (int w = 0; w < warp; ++w) wbase += wsum[w];
+        const int left = need - i;
+        int rank = wbase + inc - cnt;   // taken candidates before c0
+        for (int c = c0; c < c1; ++c)
+            if (take[c]) {
+                if (rank == left - 1) s_cut = c;   // (one thread holds the cut, if any)
+                ++rank;
+            }
+        __syncthreads();
+        const int cut = s_cut;                  // last candidate looked at (ncb: none)
+        // 3. copy the taken candidates up to the cut into place, insert their signatures, count
+        int my_taken = 0, my_rej = 0;
+        rank = wbase + inc - cnt;
+        for (int c = c0; c < c1 && c <= cut; ++c) {
+            if (c >= ncb) break;
+            if (take[c]) {
+                const int slot = i + rank;
+                for (int q = 0; q < ng; ++q) J.child[(size_t)slot * ng + q] = J.cand[(size_t)c * ng + q];
+                if (!force) seen_insert_concurrent(J, J.cand_sig[c]);
+                ++rank;
+                ++my_taken;
+            } else {
+                ++my_rej;
+            }
+        }
+        if (my_taken) atomicAdd(&s_taken, my_taken);
+        if (my_rej) atomicAdd(&s_rej, my_rej);
+        __syncthreads();
+        const int taken = s_taken;
+        if (J.reject && force) forced += taken;
+        rejected += s_rej;
+        i += taken;
+        used = (int)(base + cut + 1);
+        const bool done = i == need;
+        __syncthreads();
+        if (done) break;
         base += 2 * npairs;
         npairs = J.ncand;
         if (kInitial) initial_candidates(J, base, npairs, threadIdx.x, blockDim.x);
@@ -523,13 +627,26 @@ void launch_ga_fitness(const GaJob* all, const int* run, int n_jobs, bool initia
     else ga_fitness_kernel<false><<<n_jobs, kGaThreads, 0, st>>>(all, run);
 }
 
+// The acceptance kernels' shared memory (beyond the default 48 KB), allowed once per device.
+static void accept_smem_attribute() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+    static bool done[64] = {false};
+    if (done[dev]) return;
+    cudaFuncSetAttribute(ga_accept_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAcceptSmem);
+    cudaFuncSetAttribute(ga_accept_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kAcceptSmem);
+    done[dev] = true;
+}
+
 void launch_ga_init(const GaJob* all, const int* run, int n_jobs, cudaStream_t st) {
     ga_init_kernel<<<dim3(2 * kGaBatchBlocks, n_jobs), kGaThreads, 0, st>>>(all, run);
-    ga_accept_kernel<true><<<n_jobs, kGaThreads, 0, st>>>(all, run);
+    accept_smem_attribute();
+    ga_accept_kernel<true><<<n_jobs, kAcceptThreads, kAcceptSmem, st>>>(all, run);
 }
 void launch_ga_breed(const GaJob* all, const int* run, int n_jobs, cudaStream_t st) {
     ga_breed_kernel<<<dim3(kGaBatchBlocks, n_jobs), kGaThreads, 0, st>>>(all, run);
-    ga_accept_kernel<false><<<n_jobs, kGaThreads, 0, st>>>(all, run);
+    accept_smem_attribute();
+    ga_accept_kernel<false><<<n_jobs, kAcceptThreads, kAcceptSmem, st>>>(all, run);
 }
 // Breeding with the caller's draws (fxe_ga_breed_draws): J.fit and J.ford given, one block forms
 // the running sums and fitness_stats, then one thread per pair breeds from its row of draws.
