@@ -766,6 +766,42 @@ def run_ga(prec, key, d=None):
             "heat_capacity": th["heat_capacity"]}
 
 
+def run_thermo_only(n, reps=20):
+    """fxe_thermo_compute_device_fixed over n seeded energies (N(-30, 5) kcal/mol) at 300 K: the
+    best CUDA-event time of reps calls after three warm-up calls, and the record it wrote."""
+    import ctypes as C
+    import torch
+    from flexaidds_gb300 import evaluator
+    from flexaidds_gb300.capi import Thermo
+    lib = evaluator.load_library()
+    lib.fxe_thermo_compute_device_fixed.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_void_p,
+                                                    C.c_void_p]
+    e = torch.from_numpy(np.random.default_rng(1).normal(-30.0, 5.0, n)).cuda()
+    d_th = torch.zeros(C.sizeof(Thermo), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def call():
+        rc = lib.fxe_thermo_compute_device_fixed(C.c_void_p(e.data_ptr()), None, n, 300.0,
+                                                 C.c_void_p(d_th.data_ptr()), C.c_void_p(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(lib.fxe_last_error().decode())
+
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    best = None
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        call()
+        b.record(stream)
+        b.synchronize()
+        t = a.elapsed_time(b)
+        best = t if best is None else min(best, t)
+    th = Thermo.from_buffer_copy(d_th.cpu().numpy().tobytes())
+    return {"n": n, "best_ms": best, "free_energy": th.free_energy, "mean_energy": th.mean_energy}
+
+
 # ---------------------------------------------------------------------------------------------
 # reference arm: the reference's algorithm on the host cores
 # ---------------------------------------------------------------------------------------------
@@ -851,7 +887,22 @@ def main():
     ap.add_argument("--cluster-only", type=int, default=0, metavar="CENTRES",
                     help="time only the clustering, of CENTRES x 500 chromosomes (a small case "
                          "for a profiler: few launches before the clustering kernels)")
+    ap.add_argument("--ga-only", default="", metavar="KEY:GENERATIONS",
+                    help="run only one whole GA job, e.g. c2:40 (a small case for a profiler)")
+    ap.add_argument("--thermo-only", type=int, default=0, metavar="N",
+                    help="time only the device-merged thermodynamics of N energies (a small case "
+                         "for a profiler)")
     args = ap.parse_args()
+    if args.ga_only:
+        key, _, gens = args.ga_only.partition(":")
+        if gens:
+            GA_RUNS[key]["generations"] = int(gens)
+            GA_RUNS[key]["name"] += f"; this run: {int(gens)} generations"
+        print(json.dumps({"ga": run_ga(args.precision, key)}), flush=True)
+        return
+    if args.thermo_only:
+        print(json.dumps({"thermo": run_thermo_only(args.thermo_only)}), flush=True)
+        return
     if args.cluster_only:
         from flexaidds_gb300 import evaluator
         d = make_system()

@@ -38,23 +38,53 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
     return z ^ (z >> 31);
 }
 
-// Uniform double in [0, 1) for draw `k` of stream `s` of a job: 53 random bits.
+// The 53 random bits of draw `k` of stream `s` of a job.
+__device__ __forceinline__ uint64_t uniform_bits(uint64_t seed, uint64_t s, uint64_t k) {
+    return mix64(seed ^ mix64(s * 0x100000001B3ull + k)) >> 11;
+}
+
+// Uniform double in [0, 1) for draw `k` of stream `s` of a job: its 53 bits times 2^-53 (both
+// steps exact).
 __device__ __forceinline__ double uniform(uint64_t seed, uint64_t s, uint64_t k) {
-    return (double)(mix64(seed ^ mix64(s * 0x100000001B3ull + k)) >> 11) * 0x1.0p-53;
+    return (double)uniform_bits(seed, s, k) * 0x1.0p-53;
+}
+
+// A probability p with the integer form of the test u < p for draws u = b 2^-53 (b < 2^53 an
+// integer): u < p exactly when b < ceil(p 2^53), the scaling by 2^53 being exact. Tests with it
+// stay on the integer units (a mutation makes 32 such tests per gene).
+struct DrawThreshold {
+    double p;
+    uint64_t bits;
+};
+__device__ __forceinline__ DrawThreshold draw_threshold(double p) {
+    const double t = p * 0x1.0p53;
+    uint64_t b = 0;                                  // p <= 0 or NaN: no draw is below
+    if (t >= 0x1.0p53) b = 1ull << 53;               // p >= 1: every draw is
+    else if (t > 0.0) b = (uint64_t)ceil(t);
+    return {p, b};
 }
 
 constexpr int kGaThreads = 256;
 constexpr int kGaMaxSort = 4096;   // 2P entries sorted in shared memory: P <= 2048
 
+// Order-preserving 64-bit image of a double that is not a NaN: the images compare as unsigned
+// integers in the order the values compare (-0 and +0, which compare equal, share one image), so
+// the sorts below run on the integer units rather than on the narrow double-precision pipe.
+__device__ __forceinline__ uint64_t order_key(double x) {
+    uint64_t b = (uint64_t)__double_as_longlong(x);
+    if ((b << 1) == 0) b = 0;
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
 // Ascending bitonic sort of (key, index) pairs in shared memory, n a power of two.
-__device__ void bitonic_sort(double* key, int* idx, int n) {
+__device__ void bitonic_sort(uint64_t* key, int* idx, int n) {
     for (int k = 2; k <= n; k <<= 1) {
         for (int j = k >> 1; j > 0; j >>= 1) {
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
                 const int l = i ^ j;
                 if (l > i) {
                     const bool up = (i & k) == 0;
-                    const double a = key[i], b = key[l];
+                    const uint64_t a = key[i], b = key[l];
                     const int ia = idx[i], ib = idx[l];
                     // order by key, then by index, so equal energies keep a fixed order
                     const bool gt = a > b || (a == b && ia > ib);
@@ -90,11 +120,14 @@ __device__ __forceinline__ int roulette(const GaJob& J, double u) {
 // genetoic (LIB/gaboom.cpp:2887-2906): the first running bin total at or above u.
 __device__ __forceinline__ double gene_ic(const GaJob& J, int g, int32_t gene) {
     const double u = gene / (2147483647.0 + 1.0);
+    // the totals are positive: as signed 64-bit integers their bit patterns compare with u's as
+    // the values do (a negative gene's u lies below them all), on the integer units
+    const long long ub = __double_as_longlong(u);
     int lo = J.dec_off[g], hi = J.dec_off[g + 1];
     const int base = lo;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (J.dec_tab[mid] < u) lo = mid + 1;
+        if (__double_as_longlong(J.dec_tab[mid]) < ub) lo = mid + 1;
         else hi = mid;
     }
     return J.gene_min[g] + J.gene_del[g] * (double)(lo - base);
@@ -189,6 +222,7 @@ __device__ __forceinline__ void breed_pair_with(const GaJob& J, Draw&& draw, int
         crossp = hi > fit_avg ? J.k[0] * (fit_max - hi) / denom : J.k[2];
         mutp = lo > fit_avg ? J.k[1] * (fit_max - lo) / denom : J.k[3];
     }
+    const DrawThreshold mut = draw_threshold(mutp);
     int32_t* m = mary;
     for (int q = 0; q < ng; ++q) {
         john[q] = J.pop[(size_t)a * ng + q];
@@ -254,17 +288,23 @@ __device__ __forceinline__ void breed_pair_with(const GaJob& J, Draw&& draw, int
             if (pr >= 0.0f && !(draw() < (double)pr)) continue;
             uint32_t optr = 0u;
             for (int bit = 0; bit < 32; ++bit)
-                if (draw() < mutp) optr |= 1u << bit;
+                if (draw.below(mut)) optr |= 1u << bit;
             ch[q] ^= (int32_t)optr;
         }
     }
 }
 
+// The draws of one pair: its counter-based stream.
+struct StreamDraws {
+    uint64_t seed, st, d;
+    __device__ __forceinline__ double operator()() { return uniform(seed, st, d++); }
+    __device__ __forceinline__ bool below(const DrawThreshold& t) { return uniform_bits(seed, st, d++) < t.bits; }
+};
+
 // Pair k of the children of generation g + 1, from the generation's counter-based stream.
 __device__ void breed_pair(const GaJob& J, int g, int k, int32_t* john, int32_t* mary) {
     const uint64_t st = ((uint64_t)(g + 1) << 32) + (uint64_t)k;   // streams of generation g + 1
-    uint64_t d = 0;
-    breed_pair_with(J, [&]() { return uniform(J.seed, st, d++); }, john, mary);
+    breed_pair_with(J, StreamDraws{J.seed, st, 0}, john, mary);
 }
 
 // Pairs k0 .. k0 + npairs - 1 of the running generation's children as candidates, with their
@@ -448,7 +488,7 @@ __global__ void __launch_bounds__(kAcceptThreads) ga_accept_kernel(const GaJob* 
 // generation counter advanced.
 template <bool kInitial>
 __global__ void __launch_bounds__(kGaThreads) ga_select_kernel(GaJob* __restrict__ all, const int* __restrict__ run) {
-    __shared__ double key[kGaMaxSort];
+    __shared__ uint64_t key[kGaMaxSort];
     __shared__ int idx[kGaMaxSort];
     GaJob& J = all[run[blockIdx.x]];
     const int P = J.P, ng = J.ng, nnew = J.nnew;
@@ -472,7 +512,7 @@ __global__ void __launch_bounds__(kGaThreads) ga_select_kernel(GaJob* __restrict
             if (e != e) e = INFINITY;   // a NaN energy sorts last
             id = i;
         }
-        key[i] = e;
+        key[i] = order_key(e);
         idx[i] = id;
     }
     __syncthreads();
@@ -489,8 +529,12 @@ __global__ void __launch_bounds__(kGaThreads) ga_select_kernel(GaJob* __restrict
         if (!kInitial) sg[t] = v;
     }
     for (int r = threadIdx.x; r < P; r += blockDim.x) {
-        nxt_e[r] = key[r];
-        if (!kInitial) se[r] = key[r];
+        const int src = idx[r];
+        const int c = kInitial ? src : (J.steady ? (P - 1 - src) : (src - np_));
+        double e = src < np_ ? pe[src] : J.child_cf[c].evalue;
+        if (e != e) e = INFINITY;
+        nxt_e[r] = e;
+        if (!kInitial) se[r] = e;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -556,24 +600,26 @@ __global__ void __launch_bounds__(kNicheWarps * 32) ga_niche_kernel(const GaJob*
 // Running sums of the fitness in roulette order (roullete_wheel's walk, LIB/gaboom.cpp:1158-1186)
 // and fitness_stats' total, maximum and mean (LIB/gaboom.cpp:818-840), in order.
 __device__ void fitness_sums(const GaJob& J, const double* fit, int P) {
-    double cum = 0.0, mx = fit[0], sum = 0.0;
+    // (fitness_stats' total adds the same terms in the same order as the running sum: one sum)
+    double cum = 0.0, mx = fit[0];
     for (int i = 0; i < P; ++i) {
         cum += fit[i];
         J.fcum[i] = cum;
         if (fit[i] > mx) mx = fit[i];
-        sum += fit[i];
     }
     J.fstat[0] = cum;
     J.fstat[1] = mx;
-    J.fstat[2] = sum / (double)P;
+    J.fstat[2] = cum / (double)P;
 }
 
 // Fitness of the population (sorted by energy), the roulette order, running sums and
 // fitness_stats. kInitial: the initial population, walked in energy order whatever the model.
 template <bool kInitial>
 __global__ void __launch_bounds__(kGaThreads) ga_fitness_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
-    __shared__ double key[kGaMaxSort];
-    __shared__ int idx[kGaMaxSort];
+    // P <= kGaMaxSort / 2: the fitness, the sort keys (then the sorted fitness) and the order
+    __shared__ double fval[kGaMaxSort / 2];
+    __shared__ uint64_t key[kGaMaxSort / 2];
+    __shared__ int idx[kGaMaxSort / 2];
     const GaJob& J = all[run[blockIdx.x]];
     const int P = J.P, model = J.fitness;
     const bool rank_only = model == kFitLinear || (model == kFitSmfree && !(J.beta > 0.0));
@@ -593,31 +639,31 @@ __global__ void __launch_bounds__(kGaThreads) ga_fitness_kernel(const GaJob* __r
                 f = blended * (double)P / J.share[i];
             }
         }
-        key[i] = f;
+        fval[i] = f;
         idx[i] = i;
     }
     __syncthreads();
-    if (!kInitial && model == kFitPshare) {
+    const bool sorted = !kInitial && model == kFitPshare;
+    if (sorted) {
         // QuickSort by fitness, descending (LIB/gaboom.cpp:499); equal fitness keeps energy order
         int n = 1;
         while (n < P) n <<= 1;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            if (i < P) key[i] = -key[i];
-            else {
-                key[i] = INFINITY;
-                idx[i] = i;
-            }
+            key[i] = i < P ? order_key(-fval[i]) : order_key(INFINITY);
+            idx[i] = i;
         }
         __syncthreads();
         bitonic_sort(key, idx, n);
-        for (int i = threadIdx.x; i < P; i += blockDim.x) key[i] = -key[i];
-        __syncthreads();
     }
+    double* const fs = reinterpret_cast<double*>(key);   // the fitness in roulette order
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
-        J.fit[i] = key[i];
+        const double f = fval[sorted ? idx[i] : i];
+        fs[i] = f;
+        J.fit[i] = f;
         J.ford[i] = idx[i];
     }
-    if (threadIdx.x == 0) fitness_sums(J, key, P);
+    __syncthreads();
+    if (threadIdx.x == 0) fitness_sums(J, fs, P);
 }
 
 void launch_ga_fitness(const GaJob* all, const int* run, int n_jobs, bool initial, cudaStream_t st) {
@@ -659,15 +705,20 @@ __global__ void __launch_bounds__(kGaThreads) ga_breed_draws_kernel(const GaJob*
     const GaJob& J = *Jp;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n_pairs) return;
-    const double* row = draws + (size_t)k * stride;
-    long long d = 0;
-    bool over = false;
+    // the draws of one pair: its row of the caller's draws
+    struct RowDraws {
+        const double* row;
+        long long stride, d;
+        bool over;
+        __device__ double operator()() {
+            if (d >= stride) { over = true; return 0.0; }
+            return row[d++];
+        }
+        __device__ bool below(const DrawThreshold& t) { return (*this)() < t.p; }
+    } draw{draws + (size_t)k * stride, stride, 0, false};
     int32_t* john = J.child + (size_t)(2 * k) * J.ng;
-    breed_pair_with(J, [&]() {
-        if (d >= stride) { over = true; return 0.0; }
-        return row[d++];
-    }, john, john + J.ng);
-    used[k] = over ? -1 : (int)d;
+    breed_pair_with(J, draw, john, john + J.ng);
+    used[k] = draw.over ? -1 : (int)draw.d;
 }
 
 void launch_ga_breed_draws(const GaJob* J, const double* draws, long long stride, int n_pairs, int* used,
