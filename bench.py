@@ -283,6 +283,8 @@ def run_gpu(args):
     sweep = ev.autotune_sweep(dgen[0].data_ptr(), pop, reps=2)
     tuned_cap = min(sweep, key=lambda c: (sweep[c], c))
     tuned_ms = sweep[tuned_cap]
+    # and the contact scan's form (cell entries read in place, or staged in shared memory)
+    cells = ev.autotune_contacts(dgen[0].data_ptr(), pop, reps=3)
 
     # --- device-resident: inputs in HBM, timed on the launching stream -----------------------
     with torch.cuda.stream(stream):
@@ -424,7 +426,10 @@ def run_gpu(args):
                 "h2d_bytes_per_step": pop * d.n_genes * 4, "d2h_bytes_per_step": pop * capi.CF_DTYPE.itemsize},
         "gpu_launches": launches,
         "autotune": {"pose_blocks_per_sm": tuned_cap, "launch_ms": tuned_ms,
-                     "sweep_ms": {str(c): round(t, 3) for c, t in sorted(sweep.items())}},
+                     "sweep_ms": {str(c): round(t, 3) for c, t in sorted(sweep.items())},
+                     "contacts_ms": {"in_place": round(cells["in_place_ms"], 4),
+                                     "staged": round(cells["staged_ms"], 4)},
+                     "contacts_staged": cells["staged"]},
         "clocks": clk.summary(),
         "roofline": {"bound": "fp64" if prec == "reference" else "fp32", "achieved": achieved,
                      "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,

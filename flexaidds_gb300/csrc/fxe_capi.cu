@@ -20,7 +20,7 @@
 
 namespace fxe {
 void launch_build(const DevSystem&, const DevWork&, int, const int32_t*, const double*, cudaStream_t);
-void launch_contacts(const DevSystem&, const DevWork&, int, cudaStream_t);
+void launch_contacts(const DevSystem&, const DevWork&, int, cudaStream_t, bool);
 void launch_order_poses(const DevSystem&, const DevWork&, int, cudaStream_t);
 namespace f32 {
 void launch_poses(const DevSystem&, const DevWork&, int, int*, uint8_t*, size_t, int, cudaStream_t);
@@ -102,13 +102,18 @@ struct CallBuffers {
 }  // namespace
 
 // Device allocations freed together; a receptor's block is shared by every context built on it.
-// The autotuner's table: the polyhedron launch's occupancy cap (blocks per SM, 0 = as many as
-// fit) per size class, process-wide, so that every context, batch and GA engine of the class uses
-// what fxe_context_autotune measured for it. Classes: precision x scored atoms per pose (<= 16,
-// 32, 64, more) x poses per launch (<= 128, 512, 2048, 16384, more). The cap changes how many
-// poses run at once on an SM, never a result.
+// The autotuner's table: per size class, the polyhedron launch's occupancy cap (blocks per SM, 0 =
+// as many as fit) and the form of the contact-candidate scan (staged: the rigid cell entries
+// staged in shared memory by bulk copies, 0 = read in place), process-wide, so that every
+// context, batch and GA engine of the class uses what fxe_context_autotune measured for it.
+// Classes: precision x scored atoms per pose (<= 16, 32, 64, more) x poses per launch (<= 128,
+// 512, 2048, 16384, more). Neither choice changes a result.
+struct Tune {
+    int blocks = 0;
+    int staged = 0;
+};
 std::mutex g_tune_mu;
-std::map<int, int> g_tune;
+std::map<int, Tune> g_tune;
 
 int size_class(int precision, int mobile, long long poses) {
     const int m = mobile <= 16 ? 0 : mobile <= 32 ? 1 : mobile <= 64 ? 2 : 3;
@@ -119,7 +124,20 @@ int size_class(int precision, int mobile, long long poses) {
 int tuned_blocks(int precision, int mobile, long long poses) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     const auto it = g_tune.find(size_class(precision, mobile, poses));
-    return it == g_tune.end() ? 0 : it->second;
+    return it == g_tune.end() ? 0 : it->second.blocks;
+}
+
+bool tuned_staged(int precision, int mobile, long long poses) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    const auto it = g_tune.find(size_class(precision, mobile, poses));
+    return it != g_tune.end() && it->second.staged != 0;
+}
+
+// The contact scan's form for a setting (FXE_CELLS_*) and the launch's size class.
+bool resolve_staged(int mode, int precision, int mobile, long long poses) {
+    if (mode == FXE_CELLS_STAGED) return true;
+    if (mode == FXE_CELLS_IN_PLACE) return false;
+    return tuned_staged(precision, mobile, poses);
 }
 
 struct DevBlock {
@@ -149,6 +167,7 @@ struct fxe_context {
     int counters[4] = {0, 0, 0, 0};
     int precision = FXE_PRECISION_REFERENCE;
     int face_order = FXE_FACE_ORDER_REFERENCE;
+    int cell_staging = FXE_CELLS_AUTO;
     uint8_t* d_hist = nullptr;        // face history of the polyhedron launch
     size_t hist_bytes = 0;
     // per-stage timing (fxe_context_enable_timing) and the count of kernels launched
@@ -677,7 +696,8 @@ fxe_status run_chunk(fxe_context* ctx, int nb, const int32_t* d_genes, const dou
     if (t) cudaEventRecord(ctx->ev[0], s);
     fxe::launch_build(ctx->S, ctx->W, nb, d_genes, d_ic, s);
     if (t) cudaEventRecord(ctx->ev[1], s);
-    fxe::launch_contacts(ctx->S, ctx->W, nb, s);
+    fxe::launch_contacts(ctx->S, ctx->W, nb, s,
+                         resolve_staged(ctx->cell_staging, ctx->precision, ctx->S.n_sc + ctx->S.n_lig, nb));
     if (t) cudaEventRecord(ctx->ev[2], s);
     fxe::launch_order_poses(ctx->S, ctx->W, nb, s);
     uint8_t* hist = ctx->face_order == FXE_FACE_ORDER_REFERENCE ? ctx->d_hist : nullptr;
@@ -843,6 +863,14 @@ extern "C" fxe_status fxe_context_set_face_order(fxe_context* ctx, int32_t mode)
     if (!ctx || (mode != FXE_FACE_ORDER_REFERENCE && mode != FXE_FACE_ORDER_GEOMETRIC))
         return fail(FXE_ERR_INVALID_ARGS, "invalid face order mode");
     ctx->face_order = mode;
+    return FXE_OK;
+}
+
+extern "C" fxe_status fxe_context_set_cell_staging(fxe_context* ctx, int32_t mode) {
+    g_err.clear();
+    if (!ctx || (mode != FXE_CELLS_AUTO && mode != FXE_CELLS_IN_PLACE && mode != FXE_CELLS_STAGED))
+        return fail(FXE_ERR_INVALID_ARGS, "invalid cell staging mode");
+    ctx->cell_staging = mode;
     return FXE_OK;
 }
 
@@ -1187,7 +1215,7 @@ extern "C" fxe_status fxe_thermo_compute_device_fixed(const double* d_energies, 
 // ------------------------------------------------------------------------------------------
 namespace fxe {
 void launch_build_jobs(const Job*, int, int, cudaStream_t);
-void launch_contacts_jobs(const Job*, int, long long, cudaStream_t);
+void launch_contacts_jobs(const Job*, int, long long, cudaStream_t, bool);
 void launch_order_poses_jobs(const Job*, int, int, int*, cudaStream_t);
 namespace f32 {
 void launch_poses_jobs(const Job*, int, int, int*, const int*, uint8_t*, size_t, int, cudaStream_t);
@@ -1276,7 +1304,7 @@ namespace {
 // genes_of / out_of give each job's device chromosomes and records.
 template <typename G, typename O>
 fxe_status batch_launch(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, cudaStream_t s, G genes_of, O out_of) {
-    int prec = -1, order = FXE_FACE_ORDER_REFERENCE, total = 0, mobile = 0;
+    int prec = -1, order = FXE_FACE_ORDER_REFERENCE, total = 0, mobile = 0, cells = -1;
     long long items = 0;
     FXE_TRY(cudaEventSynchronize(b->staged), "batch staging");
     int k = 0;
@@ -1297,12 +1325,14 @@ fxe_status batch_launch(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, cudaS
         prec = ctx->precision;
         order = ctx->face_order;
         mobile = std::max(mobile, ctx->S.n_sc + ctx->S.n_lig);
+        // the contexts' common cell-staging setting, else the autotuner's choice
+        cells = cells < 0 || cells == ctx->cell_staging ? ctx->cell_staging : FXE_CELLS_AUTO;
     }
     if (k == 0) return FXE_OK;
     FXE_TRY(cudaMemcpyAsync(b->d_jobs, b->h_jobs, sizeof(fxe::Job) * k, cudaMemcpyHostToDevice, s), "job table");
     FXE_TRY(cudaEventRecord(b->staged, s), "cudaEventRecord");
     fxe::launch_build_jobs(b->d_jobs, k, total, s);
-    fxe::launch_contacts_jobs(b->d_jobs, k, items, s);
+    fxe::launch_contacts_jobs(b->d_jobs, k, items, s, resolve_staged(cells, prec, mobile, total));
     fxe::launch_order_poses_jobs(b->d_jobs, k, total, b->d_order, s);
     uint8_t* hist = order == FXE_FACE_ORDER_REFERENCE ? b->d_hist : nullptr;
     const int bpsm = tuned_blocks(prec, mobile, total);
@@ -1704,14 +1734,19 @@ extern "C" fxe_status fxe_ga_step(fxe_ga* e) {
         FXE_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
         fxe::launch_ga_breed(e->d_all, e->d_run, n, e->stream);
         fxe::launch_build_jobs(e->d_eval, n, total, e->stream);
-        fxe::launch_contacts_jobs(e->d_eval, n, items, e->stream);
+        // the running jobs' largest scored-atom count, and their common cell-staging setting
+        int mobile = 0, cells = -1;
+        for (int sl : e->run) {
+            const fxe_context* c = e->slots[sl].ctx;
+            mobile = std::max(mobile, c->S.n_sc + c->S.n_lig);
+            cells = cells < 0 || cells == c->cell_staging ? c->cell_staging : FXE_CELLS_AUTO;
+        }
+        fxe::launch_contacts_jobs(e->d_eval, n, items, e->stream, resolve_staged(cells, e->precision, mobile, total));
         fxe::launch_order_poses_jobs(e->d_eval, n, total, e->d_order, e->stream);
         // the GA engine keeps the reference's face order unless a running job's context asks otherwise
         bool ref_order = true;
         for (int sl : e->run) ref_order = ref_order && e->slots[sl].ctx->face_order == FXE_FACE_ORDER_REFERENCE;
         uint8_t* hist = ref_order ? e->d_hist : nullptr;
-        int mobile = 0;
-        for (int sl : e->run) mobile = std::max(mobile, e->slots[sl].ctx->S.n_sc + e->slots[sl].ctx->S.n_lig);
         const int bpsm = tuned_blocks(e->precision, mobile, total);
         if (e->precision == FXE_PRECISION_FAST)
             fxe::f32::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->d_order, hist, e->hist_bytes, bpsm, e->stream);
@@ -2143,7 +2178,7 @@ static fxe_status autotune_sweep(fxe_context* ctx, int32_t n, const int32_t* d_g
     uint8_t* hist = ctx->face_order == FXE_FACE_ORDER_REFERENCE ? ctx->d_hist : nullptr;
     // the candidates' work: this batch built, its contact candidates listed and ordered once
     fxe::launch_build(ctx->S, ctx->W, n, d_genes, nullptr, s);
-    fxe::launch_contacts(ctx->S, ctx->W, n, s);
+    fxe::launch_contacts(ctx->S, ctx->W, n, s, false);
     fxe::launch_order_poses(ctx->S, ctx->W, n, s);
     FXE_TRY(cudaGetLastError(), "autotune launch");
     cudaEvent_t a = nullptr, b = nullptr;
@@ -2184,7 +2219,7 @@ static fxe_status autotune_sweep(fxe_context* ctx, int32_t n, const int32_t* d_g
     ctx->launches += 3 + (long long)(maxb - std::max(1, maxb / 2) + 1) * (reps + 1);
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
-        g_tune[size_class(ctx->precision, ctx->S.n_sc + ctx->S.n_lig, n)] = best;
+        g_tune[size_class(ctx->precision, ctx->S.n_sc + ctx->S.n_lig, n)].blocks = best;
     }
     if (n_out) *n_out = n_done;
     if (blocks_per_sm) *blocks_per_sm = best;
@@ -2192,9 +2227,65 @@ static fxe_status autotune_sweep(fxe_context* ctx, int32_t n, const int32_t* d_g
     return FXE_OK;
 }
 
+// The contact-candidate launch over the context's built batch of n poses timed in both forms
+// (rigid cell entries read in place, and staged in shared memory), reps timed launches each after
+// one warm-up; records the faster form for the context's size class. ms2: the two fastest times.
+static fxe_status tune_contacts(fxe_context* ctx, int32_t n, int32_t reps, double* ms2, int32_t* staged) {
+    cudaStream_t s = ctx->stream;
+    cudaEvent_t a = nullptr, b = nullptr;
+    FXE_TRY(cudaEventCreate(&a), "cudaEventCreate");
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return fail(FXE_ERR_LAUNCH, "cudaEventCreate");
+    }
+    float best[2] = {0.0f, 0.0f};
+    cudaError_t e = cudaSuccess;
+    for (int form = 0; form < 2 && e == cudaSuccess; ++form) {
+        for (int r = 0; r <= reps && e == cudaSuccess; ++r) {   // the first launch warms up
+            cudaEventRecord(a, s);
+            fxe::launch_contacts(ctx->S, ctx->W, n, s, form == 1);
+            cudaEventRecord(b, s);
+            e = cudaEventSynchronize(b);
+            float ms = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+            if (r > 0 && (best[form] == 0.0f || ms < best[form])) best[form] = ms;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (e != cudaSuccess) return cuda_fail(e, "autotune");
+    ctx->launches += 2LL * (reps + 1);
+    const bool st = best[1] < best[0];
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[size_class(ctx->precision, ctx->S.n_sc + ctx->S.n_lig, n)].staged = st ? 1 : 0;
+    }
+    if (ms2) {
+        ms2[0] = best[0];
+        ms2[1] = best[1];
+    }
+    if (staged) *staged = st ? 1 : 0;
+    return FXE_OK;
+}
+
 extern "C" fxe_status fxe_context_autotune(fxe_context* ctx, int32_t n, const int32_t* d_genes, int32_t reps,
                                            int32_t* blocks_per_sm, double* ms_per_launch) {
-    return autotune_sweep(ctx, n, d_genes, reps, nullptr, nullptr, 0, nullptr, blocks_per_sm, ms_per_launch);
+    const fxe_status st = autotune_sweep(ctx, n, d_genes, reps, nullptr, nullptr, 0, nullptr, blocks_per_sm,
+                                         ms_per_launch);
+    if (st != FXE_OK) return st;
+    return tune_contacts(ctx, n, reps, nullptr, nullptr);
+}
+
+extern "C" fxe_status fxe_context_autotune_contacts(fxe_context* ctx, int32_t n, const int32_t* d_genes, int32_t reps,
+                                                    double* ms2, int32_t* staged) {
+    g_err.clear();
+    if (!ctx || n <= 0 || !d_genes || reps < 1 || reps > 100) return fail(FXE_ERR_INVALID_ARGS, "invalid arguments");
+    if (n > ctx->W.max_poses) return fail(FXE_ERR_INVALID_ARGS, "n exceeds the context's max_poses");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(FXE_ERR_NO_DEVICE, "cudaSetDevice");
+    fxe::launch_build(ctx->S, ctx->W, n, d_genes, nullptr, ctx->stream);
+    FXE_TRY(cudaGetLastError(), "autotune launch");
+    ++ctx->launches;
+    return tune_contacts(ctx, n, reps, ms2, staged);
 }
 
 extern "C" fxe_status fxe_context_autotune_sweep(fxe_context* ctx, int32_t n, const int32_t* d_genes, int32_t reps,

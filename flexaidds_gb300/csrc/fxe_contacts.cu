@@ -9,6 +9,11 @@
 // plus the atom's share of the clash pre-filter (LIB/Vcontacts.cpp:36-51): rigid partners and
 // the mobile partners processed after it in Calclist order, pairs of one residue within bloops
 // bonds left out.
+//
+// Two forms of the rigid scan, chosen per launch (the autotuner's choice for the size class, or
+// the context's setting): the entries read in place from the cell list (global memory, through
+// L1 and L2), or staged first in shared memory by bulk copies (cp.async.bulk, one per contiguous
+// row of three cells, completing on an mbarrier). Results are the same.
 #include "fxe_common.cuh"
 
 namespace fxe {
@@ -34,8 +39,45 @@ struct ContactStage {
     int cst[27];    // their first entries in the cell list
 };
 
+// The 27 cells' rigid entries staged in shared memory: scan position 3r + k of the flat list is
+// cell k of row r (r = 0..8 over the two slower axes, k over the fastest), and the three cells of
+// a row are neighbours in the cell list too, so each row is one contiguous run of entries, moved
+// by one bulk copy (positions: 16-byte entries in place at the row's first scan position; Calc
+// indices: the run widened to 16-byte boundaries, its entry t at abase[r] + t).
+constexpr int kStageCap = 256;                 // entries staged per atom; more: read in place
+constexpr int kStageAtoms = kStageCap + 9 * 8;
+constexpr long long kStageSpin = 1ll << 22;    // bounded wait for the copies
+struct __align__(16) RigidStage {
+    float4 pos[kStageCap];
+    int atom[kStageAtoms];
+    int abase[9];
+    unsigned long long bar;
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void bulk_to_shared(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool bar_try_wait(unsigned long long* bar, unsigned phase) {
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}" : "=r"(ok) : "r"(smem_addr(bar)), "r"(phase) : "memory");
+    return ok != 0;
+}
+// Waits, at most kStageSpin polls, for the copies of phase 0 of the warp's barrier.
+__device__ __forceinline__ bool stage_wait(unsigned long long* bar) {
+    bool ok = false;
+    for (long long it = 0; it < kStageSpin && !ok; ++it) ok = bar_try_wait(bar, 0u);
+    return __all_sync(0xffffffffu, ok);
+}
+
+// kStaged: the rigid entries are read from shared memory after bulk copies (rs), else in place.
+template <bool kStaged>
 __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork& W, int p, int a, int lane,
-                                              ContactStage& cs) {
+                                              ContactStage& cs, RigidStage* rs) {
     const int nsc = S.n_sc, nm = nsc + S.n_lig;
     const size_t lb = (size_t)p * nm;
     const int4 pg = W.pose_grid[p];
@@ -129,6 +171,43 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
         }
         if (lane == 0) cs.coff[0] = 0;
         __syncwarp();
+        // stage the nine rows' entries when they fit
+        const bool staged = kStaged && total > 0 && total <= kStageCap;
+        bool ready = false;
+        if constexpr (kStaged) if (staged) {
+            int n_r = 0, st_r = 0, lo4 = 0, len4 = 0;
+            if (lane < 9) {
+                n_r = cs.coff[3 * lane + 3] - cs.coff[3 * lane];
+                const int bi = box0 + dim2 * ((lane / 3) - 1) + dim * ((lane % 3) - 1) - 1;
+                const int c0 = bi < 0 ? 0 : bi;
+                st_r = c0 < dim3 ? S.cell_start[c0] : 0;
+                lo4 = st_r & ~3;
+                len4 = n_r > 0 ? ((st_r + n_r + 3) & ~3) - lo4 : 0;
+            }
+            int aoff = len4;   // exclusive prefix of the widened runs
+#pragma unroll
+            for (int o = 1; o < 16; o <<= 1) {
+                const int v = __shfl_up_sync(kFull, aoff, o);
+                if (lane >= o) aoff += v;
+            }
+            aoff -= len4;
+            const int aints = __shfl_sync(kFull, aoff + len4, 8);
+            if (lane == 0) {
+                asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&rs->bar)) : "memory");
+                asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                             :: "r"(smem_addr(&rs->bar)), "r"((unsigned)(16 * total + 4 * aints)) : "memory");
+            }
+            __syncwarp();
+            if (lane < 9) {
+                rs->abase[lane] = aoff + (st_r - lo4) - cs.coff[3 * lane];
+                if (n_r > 0) {
+                    bulk_to_shared(&rs->pos[cs.coff[3 * lane]], S.cell_pos + st_r, 16u * n_r, &rs->bar);
+                    bulk_to_shared(&rs->atom[aoff], S.cell_atom + lo4, 4u * len4, &rs->bar);
+                }
+            }
+            ready = stage_wait(&rs->bar);
+        }
         for (int t0 = 0; t0 < total; t0 += 32) {
             const int t = t0 + lane;
             const bool in = t < total;
@@ -142,11 +221,24 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
                     else hi = mid - 1;
                 }
                 pos = lo;
-                const int k = cs.cst[lo] + (t - cs.coff[lo]);
-                j = S.cell_atom[k];
-                pj = S.cell_pos[k];
+                if (kStaged && ready) {
+                    j = rs->atom[rs->abase[lo / 3] + t];
+                    pj = rs->pos[t];
+                } else {
+                    const int k = cs.cst[lo] + (t - cs.coff[lo]);
+                    j = S.cell_atom[k];
+                    pj = S.cell_pos[k];
+                }
             }
             consider(in, pos, j, pj);
+        }
+        if constexpr (kStaged) if (staged) {
+            // the copies are done before the barrier is retired (a second bounded wait when the
+            // first gave up)
+            if (!ready) ready = stage_wait(&rs->bar);
+            if (ready && lane == 0)
+                asm volatile("mbarrier.inval.shared::cta.b64 [%0];" :: "r"(smem_addr(&rs->bar)) : "memory");
+            __syncwarp();
         }
     } else {
         // a grid re-derived for this pose: every rigid atom, binned on that grid
@@ -218,20 +310,25 @@ __device__ __forceinline__ void contacts_atom(const DevSystem& S, const DevWork&
     }
 }
 
+template <bool kStaged>
 __global__ void __launch_bounds__(128)
 contacts_kernel(DevSystem S, DevWork W, int n) {
     __shared__ ContactStage stage[4];
+    __shared__ RigidStage rstage[kStaged ? 4 : 1];
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nm = n_mobile(S);
     if (gw >= n * nm) return;
-    contacts_atom(S, W, gw / nm, gw % nm, threadIdx.x & 31, stage[threadIdx.x >> 5]);
+    contacts_atom<kStaged>(S, W, gw / nm, gw % nm, threadIdx.x & 31, stage[threadIdx.x >> 5],
+                           &rstage[kStaged ? threadIdx.x >> 5 : 0]);
 }
 
 // The same over the (pose, mobile atom) items of several jobs.
+template <bool kStaged>
 __global__ void __launch_bounds__(128)
 contacts_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, long long total) {
     __shared__ Job job_all[4];
     __shared__ ContactStage stage[4];
+    __shared__ RigidStage rstage[kStaged ? 4 : 1];
     const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (gw >= total) return;
@@ -240,7 +337,7 @@ contacts_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, long long total) 
     copy_job(&job, &jobs[j], lane);
     const int nm = n_mobile(job.S);
     const long long r = gw - job.warp0;
-    contacts_atom(job.S, job.W, (int)(r / nm), (int)(r % nm), lane, stage[wib]);
+    contacts_atom<kStaged>(job.S, job.W, (int)(r / nm), (int)(r % nm), lane, stage[wib], &rstage[kStaged ? wib : 0]);
 }
 
 // The order pose_kernel takes the poses in: costliest first (sum over the pose's atoms of the
@@ -351,13 +448,17 @@ void launch_order_poses(const DevSystem& S, const DevWork& W, int n, cudaStream_
     order_poses_kernel<<<(n + kOrderSeg - 1) / kOrderSeg, 1024, 0, st>>>(W.cand_n, S.n_sc + S.n_lig, n, W.pose_order);
 }
 
-void launch_contacts(const DevSystem& S, const DevWork& W, int n, cudaStream_t st) {
+void launch_contacts(const DevSystem& S, const DevWork& W, int n, cudaStream_t st, bool staged) {
     const long warps = (long)n * (S.n_sc + S.n_lig);
-    contacts_kernel<<<(unsigned)((warps + 3) / 4), 128, 0, st>>>(S, W, n);
+    const unsigned blocks = (unsigned)((warps + 3) / 4);
+    if (staged) contacts_kernel<true><<<blocks, 128, 0, st>>>(S, W, n);
+    else contacts_kernel<false><<<blocks, 128, 0, st>>>(S, W, n);
 }
 
-void launch_contacts_jobs(const Job* jobs, int n_jobs, long long total_items, cudaStream_t st) {
-    contacts_kernel_jobs<<<(unsigned)((total_items + 3) / 4), 128, 0, st>>>(jobs, n_jobs, total_items);
+void launch_contacts_jobs(const Job* jobs, int n_jobs, long long total_items, cudaStream_t st, bool staged) {
+    const unsigned blocks = (unsigned)((total_items + 3) / 4);
+    if (staged) contacts_kernel_jobs<true><<<blocks, 128, 0, st>>>(jobs, n_jobs, total_items);
+    else contacts_kernel_jobs<false><<<blocks, 128, 0, st>>>(jobs, n_jobs, total_items);
 }
 
 }  // namespace fxe

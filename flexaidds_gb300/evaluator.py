@@ -49,6 +49,7 @@ def load_library():
         lib.fxe_thermo_weights.argtypes = [_d, _i, C.c_int64, C.c_double, _d]
         lib.fxe_context_set_precision.argtypes = [vp, C.c_int32]
         lib.fxe_context_set_face_order.argtypes = [vp, C.c_int32]
+        lib.fxe_context_set_cell_staging.argtypes = [vp, C.c_int32]
         lib.fxe_context_enable_timing.argtypes = [vp, C.c_int32]
         lib.fxe_context_take_timing.argtypes = [vp, _d, C.POINTER(C.c_int64)]
         lib.fxe_context_create_shared.argtypes = [vp, vp, vp, vp, C.c_int32, C.POINTER(vp)]
@@ -86,6 +87,7 @@ def load_library():
         lib.fxe_context_autotune_sweep.argtypes = [vp, C.c_int32, vp, C.c_int32, _i, _d, C.c_int32,
                                                    C.POINTER(C.c_int32)]
         lib.fxe_autotune_lookup.argtypes = [C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_int32)]
+        lib.fxe_context_autotune_contacts.argtypes = [vp, C.c_int32, vp, C.c_int32, _d, C.POINTER(C.c_int32)]
         lib.fxe_context_destroy.argtypes = [vp]
         lib.fxe_context_destroy.restype = None
         lib.fxe_last_error.restype = C.c_char_p
@@ -106,9 +108,13 @@ class GPUEvaluator:
     # how a face whose first point has no neighbour on its second plane is ordered
     # (fxe_context_set_face_order): as the reference does it, or from the point's other plane
     FACE_ORDER_REFERENCE, FACE_ORDER_GEOMETRIC = 0, 1
+    # how the contact-candidate scan reads the cell list (fxe_context_set_cell_staging): the
+    # autotuner's choice, in place, or staged in shared memory by bulk copies
+    CELLS_AUTO, CELLS_IN_PLACE, CELLS_STAGED = 0, 1, 2
 
     def __init__(self, desc: Descriptor, max_poses: int = 2048, precision: int = 0,
-                 share_receptor_with: "GPUEvaluator | None" = None, face_order: int = 0):
+                 share_receptor_with: "GPUEvaluator | None" = None, face_order: int = 0,
+                 cell_staging: int = 0):
         """share_receptor_with: an evaluator on the same receptor whose device copy of the
         receptor, cell list and cleft grid this one reuses (fxe_context_create_shared)."""
         self.lib = load_library()
@@ -127,6 +133,7 @@ class GPUEvaluator:
         self.handle = h
         _check(self.lib.fxe_context_set_precision(self.handle, int(precision)))
         _check(self.lib.fxe_context_set_face_order(self.handle, int(face_order)))
+        _check(self.lib.fxe_context_set_cell_staging(self.handle, int(cell_staging)))
 
     def close(self):
         if getattr(self, "handle", None):
@@ -218,6 +225,14 @@ class GPUEvaluator:
         _check(self.lib.fxe_context_autotune(self.handle, int(n), C.c_void_p(d_genes), int(reps), C.byref(b),
                                              C.byref(ms)))
         return int(b.value), float(ms.value)
+
+    def autotune_contacts(self, d_genes: int, n: int, reps: int = 2) -> dict:
+        """fxe_context_autotune_contacts: the contact launch's fastest ms with the cell entries read
+        in place and staged in shared memory, and whether staging was chosen."""
+        ms, st = np.zeros(2, np.float64), C.c_int32(0)
+        _check(self.lib.fxe_context_autotune_contacts(self.handle, int(n), C.c_void_p(d_genes), int(reps), ptr(ms, _d),
+                                                      C.byref(st)))
+        return {"in_place_ms": float(ms[0]), "staged_ms": float(ms[1]), "staged": bool(st.value)}
 
     def autotune_sweep(self, d_genes: int, n: int, reps: int = 2) -> dict:
         """fxe_context_autotune_sweep: {blocks per SM: fastest launch ms} for every cap timed."""

@@ -198,6 +198,19 @@ fxe_status fxe_context_set_precision(fxe_context* ctx, int32_t precision);
 enum { FXE_FACE_ORDER_REFERENCE = 0, FXE_FACE_ORDER_GEOMETRIC = 1 };
 fxe_status fxe_context_set_face_order(fxe_context* ctx, int32_t mode);
 
+/* How the contact-candidate scan reads the receptor's cell list. The scan of an atom's 27
+ * neighbouring cells (get_contlist4, LIB/Vcontacts.cpp:1725-1839) takes their rigid entries
+ * FXE_CELLS_IN_PLACE: from global memory where they lie (through L1 and L2);
+ * FXE_CELLS_STAGED: from shared memory, staged first by bulk copies (one cp.async.bulk per row of
+ *   three neighbouring cells, which lie together in the cell list) when the 27 cells hold at most
+ *   256 entries, in place otherwise;
+ * FXE_CELLS_AUTO (default): the form fxe_context_autotune measured faster for the launch's size
+ *   class, in place when the class is not tuned.
+ * Results are the same in every form. Batched launches and the GA engine use the contexts' common
+ * setting, else AUTO. No reference counterpart. */
+enum { FXE_CELLS_AUTO = 0, FXE_CELLS_IN_PLACE = 1, FXE_CELLS_STAGED = 2 };
+fxe_status fxe_context_set_cell_staging(fxe_context* ctx, int32_t mode);
+
 /* Scores n chromosomes given as int32 genes (n * n_genes, host memory), writing n records to
  * host memory. Synchronous, like cuda_eval_batch (LIB/cuda_eval.cuh:60-70). */
 fxe_status fxe_eval_genes(fxe_context* ctx, int32_t n, const int32_t* genes, fxe_cf* out);
@@ -487,10 +500,19 @@ fxe_status fxe_ensemble_dedup(int64_t n, int32_t n_genes, const double* ic, cons
  * keyed by size class: precision x scored atoms per pose (<= 16, 32, 64, more) x poses per launch
  * (<= 128, 512, 2048, 16384, more). Every later launch of that class, by any context, batch or GA
  * engine (captured when its set of jobs changes), uses it. Results never depend on the cap.
+ * It then times the contact-candidate launch in both forms of fxe_context_set_cell_staging, as
+ * fxe_context_autotune_contacts does, and records the faster for the class.
  * Outputs: the cap chosen (blocks per SM), and its fastest launch time (ms). Synchronous. No
  * reference counterpart. */
 fxe_status fxe_context_autotune(fxe_context* ctx, int32_t n, const int32_t* d_genes, int32_t reps,
                                 int32_t* blocks_per_sm, double* ms_per_launch);
+/* Times the contact-candidate launch over this context's batch (d_genes: n int32 chromosomes in
+ * device memory, n <= max_poses) with the cell entries read in place and staged in shared memory,
+ * `reps` timed launches each after one warm-up, and records the faster form in the table for the
+ * size class. ms2 (may be null): the fastest launch times in place and staged (ms); staged (may be
+ * null): 1 when the staged form was the faster. Synchronous. */
+fxe_status fxe_context_autotune_contacts(fxe_context* ctx, int32_t n, const int32_t* d_genes, int32_t reps,
+                                         double* ms2, int32_t* staged);
 /* The same sweep, reporting every cap it timed: caps[i] (blocks per SM) and ms[i] (fastest launch
  * time) for i < *n_out (at most max_out entries; the SM's capacity is at most 32 blocks). Records
  * the fastest in the table like fxe_context_autotune. */
