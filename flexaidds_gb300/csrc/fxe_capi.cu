@@ -21,13 +21,15 @@
 namespace fxe {
 void launch_build(const DevSystem&, const DevWork&, int, const int32_t*, const double*, cudaStream_t);
 void launch_contacts(const DevSystem&, const DevWork&, int, cudaStream_t, bool);
-void launch_order_poses(const DevSystem&, const DevWork&, int, cudaStream_t);
+void launch_order_poses(const DevSystem&, const DevWork&, int, cudaStream_t, int, int);
 namespace f32 {
 void launch_poses(const DevSystem&, const DevWork&, int, int*, uint8_t*, size_t, int, cudaStream_t);
 cudaError_t configure_voronoi();
 size_t pose_hist_bytes();
 int pose_max_blocks_per_sm();
 int pose_warps_per_block();
+int pose_tile();
+int pose_launch_blocks(int, size_t, int);
 }
 namespace f64 {
 void launch_poses(const DevSystem&, const DevWork&, int, int*, uint8_t*, size_t, int, cudaStream_t);
@@ -35,6 +37,24 @@ cudaError_t configure_voronoi();
 size_t pose_hist_bytes();
 int pose_max_blocks_per_sm();
 int pose_warps_per_block();
+int pose_tile();
+int pose_launch_blocks(int, size_t, int);
+}
+
+// How the pose order of a polyhedron launch over n poses is dealt: {full tiles to deal the sorted
+// poses over (0: kept sorted), poses per tile}. Only lockstep launches whose tiles all run at
+// once are dealt (launch_order_poses).
+struct Deal {
+    int deal, tile;
+};
+inline Deal order_deal(int precision, int n, size_t hist_bytes, int blocks_per_sm) {
+    const bool fast = precision == FXE_PRECISION_FAST;
+    const int tile = fast ? f32::pose_tile() : f64::pose_tile();
+    if (tile < 1) return {0, 0};
+    const int blocks = fast ? f32::pose_launch_blocks(n, hist_bytes, blocks_per_sm)
+                            : f64::pose_launch_blocks(n, hist_bytes, blocks_per_sm);
+    const int full = n / tile;
+    return {full <= blocks ? full : 0, tile};
 }
 // Face history of a polyhedron launch, large enough for either precision's launch: the warps the
 // device holds at once, kHistStride bytes each (configure_voronoi first).
@@ -699,9 +719,10 @@ fxe_status run_chunk(fxe_context* ctx, int nb, const int32_t* d_genes, const dou
     fxe::launch_contacts(ctx->S, ctx->W, nb, s,
                          resolve_staged(ctx->cell_staging, ctx->precision, ctx->S.n_sc + ctx->S.n_lig, nb));
     if (t) cudaEventRecord(ctx->ev[2], s);
-    fxe::launch_order_poses(ctx->S, ctx->W, nb, s);
     uint8_t* hist = ctx->face_order == FXE_FACE_ORDER_REFERENCE ? ctx->d_hist : nullptr;
     const int bpsm = tuned_blocks(ctx->precision, ctx->S.n_sc + ctx->S.n_lig, nb);
+    const fxe::Deal dl = fxe::order_deal(ctx->precision, nb, hist ? ctx->hist_bytes : 0, bpsm);
+    fxe::launch_order_poses(ctx->S, ctx->W, nb, s, dl.deal, dl.tile);
     if (ctx->precision == FXE_PRECISION_FAST)
         fxe::f32::launch_poses(ctx->S, ctx->W, nb, ctx->W.counters + 4, hist, ctx->hist_bytes, bpsm, s);
     else fxe::f64::launch_poses(ctx->S, ctx->W, nb, ctx->W.counters + 4, hist, ctx->hist_bytes, bpsm, s);
@@ -1216,7 +1237,7 @@ extern "C" fxe_status fxe_thermo_compute_device_fixed(const double* d_energies, 
 namespace fxe {
 void launch_build_jobs(const Job*, int, int, cudaStream_t);
 void launch_contacts_jobs(const Job*, int, long long, cudaStream_t, bool);
-void launch_order_poses_jobs(const Job*, int, int, int*, cudaStream_t);
+void launch_order_poses_jobs(const Job*, int, int, int*, cudaStream_t, int, int);
 namespace f32 {
 void launch_poses_jobs(const Job*, int, int, int*, const int*, uint8_t*, size_t, int, cudaStream_t);
 }
@@ -1333,9 +1354,10 @@ fxe_status batch_launch(fxe_batch* b, const fxe_job* jobs, int32_t n_jobs, cudaS
     FXE_TRY(cudaEventRecord(b->staged, s), "cudaEventRecord");
     fxe::launch_build_jobs(b->d_jobs, k, total, s);
     fxe::launch_contacts_jobs(b->d_jobs, k, items, s, resolve_staged(cells, prec, mobile, total));
-    fxe::launch_order_poses_jobs(b->d_jobs, k, total, b->d_order, s);
     uint8_t* hist = order == FXE_FACE_ORDER_REFERENCE ? b->d_hist : nullptr;
     const int bpsm = tuned_blocks(prec, mobile, total);
+    const fxe::Deal dl = fxe::order_deal(prec, total, hist ? b->hist_bytes : 0, bpsm);
+    fxe::launch_order_poses_jobs(b->d_jobs, k, total, b->d_order, s, dl.deal, dl.tile);
     if (prec == FXE_PRECISION_FAST)
         fxe::f32::launch_poses_jobs(b->d_jobs, k, total, b->d_next, b->d_order, hist, b->hist_bytes, bpsm, s);
     else fxe::f64::launch_poses_jobs(b->d_jobs, k, total, b->d_next, b->d_order, hist, b->hist_bytes, bpsm, s);
@@ -1742,12 +1764,13 @@ extern "C" fxe_status fxe_ga_step(fxe_ga* e) {
             cells = cells < 0 || cells == c->cell_staging ? c->cell_staging : FXE_CELLS_AUTO;
         }
         fxe::launch_contacts_jobs(e->d_eval, n, items, e->stream, resolve_staged(cells, e->precision, mobile, total));
-        fxe::launch_order_poses_jobs(e->d_eval, n, total, e->d_order, e->stream);
         // the GA engine keeps the reference's face order unless a running job's context asks otherwise
         bool ref_order = true;
         for (int sl : e->run) ref_order = ref_order && e->slots[sl].ctx->face_order == FXE_FACE_ORDER_REFERENCE;
         uint8_t* hist = ref_order ? e->d_hist : nullptr;
         const int bpsm = tuned_blocks(e->precision, mobile, total);
+        const fxe::Deal dl = fxe::order_deal(e->precision, total, hist ? e->hist_bytes : 0, bpsm);
+        fxe::launch_order_poses_jobs(e->d_eval, n, total, e->d_order, e->stream, dl.deal, dl.tile);
         if (e->precision == FXE_PRECISION_FAST)
             fxe::f32::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->d_order, hist, e->hist_bytes, bpsm, e->stream);
         else fxe::f64::launch_poses_jobs(e->d_eval, n, total, e->d_next, e->d_order, hist, e->hist_bytes, bpsm,
@@ -2179,7 +2202,8 @@ static fxe_status autotune_sweep(fxe_context* ctx, int32_t n, const int32_t* d_g
     // the candidates' work: this batch built, its contact candidates listed and ordered once
     fxe::launch_build(ctx->S, ctx->W, n, d_genes, nullptr, s);
     fxe::launch_contacts(ctx->S, ctx->W, n, s, false);
-    fxe::launch_order_poses(ctx->S, ctx->W, n, s);
+    const fxe::Deal dl = fxe::order_deal(ctx->precision, n, hist ? ctx->hist_bytes : 0, 0);
+    fxe::launch_order_poses(ctx->S, ctx->W, n, s, dl.deal, dl.tile);
     FXE_TRY(cudaGetLastError(), "autotune launch");
     cudaEvent_t a = nullptr, b = nullptr;
     FXE_TRY(cudaEventCreate(&a), "cudaEventCreate");

@@ -342,12 +342,42 @@ contacts_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, long long total) 
 
 // The order pose_kernel takes the poses in: costliest first (sum over the pose's atoms of the
 // squared candidate count, which the hull walk's plane tests grow with), so that the slowest
-// poses start early and the launch does not end on one of them while the SMs run dry. Sorted in
-// segments of kOrderSeg poses, one block each.
+// poses start early and the launch does not end on one of them while the SMs run dry; then the
+// poses that need no polyhedra (the clash pre-filter rejects them, or they left the grid), so
+// that the warps of a block, which step through the atoms together, are not held by poses that
+// have nothing to do. Sorted in segments of kOrderSeg poses, one block each. The order changes
+// no result.
+// A launch of lockstep blocks (tiles of `tile` neighbouring queue entries) with no more tiles
+// than the device runs at once takes every tile at the same time, and lasts as long as its
+// slowest tile: there the sorted poses are dealt round-robin over its deal = n / tile full tiles
+// (tile t gets sorted entries t, t + deal, ...), so each tile holds one of the costliest poses and
+// the rejected ones spread over the tiles' last slots.
 constexpr int kOrderSeg = 4096;
 
-__global__ void __launch_bounds__(1024) order_poses_kernel(const int* __restrict__ cand_n, int nm, int n,
-                                                           int* __restrict__ order) {
+// Queue position of sorted entry i of a segment.
+__device__ __forceinline__ int dealt_position(int i, int deal, int tile) {
+    return deal > 0 && i < deal * tile ? (i % deal) * tile + i / deal : i;
+}
+
+// The sort key of pose p: minus its cost, or 1 for a pose the polyhedron launch rejects at once.
+__device__ __forceinline__ long long pose_order_key(const DevWork& W, int nm, int p) {
+    if (W.pose_grid[p].z) return 1;
+    const int* cn = W.cand_n + (size_t)p * nm;
+    const double* cp = W.clash_part + (size_t)p * nm;
+    long long cost = 0;
+    double clash = 0.0;
+    for (int a = 0; a < nm; ++a) {
+        const int k = cn[a];
+        if (k > 0) cost += (long long)k * k;
+        clash += cp[a];
+    }
+    // (the launch's own test sums the same terms in another order: a pose within rounding of the
+    // threshold may be placed on the other side, which only moves it in the queue)
+    return clash >= kClashThreshold ? 1 : -cost;
+}
+
+__global__ void __launch_bounds__(1024) order_poses_kernel(DevWork W, int nm, int n, int* __restrict__ order, int deal,
+                                                           int tile) {
     __shared__ long long key[kOrderSeg];
     __shared__ int idx[kOrderSeg];
     const int base = blockIdx.x * kOrderSeg;
@@ -356,15 +386,7 @@ __global__ void __launch_bounds__(1024) order_poses_kernel(const int* __restrict
     while (len < m) len <<= 1;
     for (int i = threadIdx.x; i < len; i += blockDim.x) {
         long long c = 0x7FFFFFFFFFFFFFFFll;   // padding sorts last
-        if (i < m) {
-            const int* cn = cand_n + (size_t)(base + i) * nm;
-            long long cost = 0;
-            for (int a = 0; a < nm; ++a) {
-                const int k = cn[a];
-                if (k > 0) cost += (long long)k * k;
-            }
-            c = -cost;
-        }
+        if (i < m) c = pose_order_key(W, nm, base + i);
         key[i] = c;
         idx[i] = i;
     }
@@ -388,12 +410,12 @@ __global__ void __launch_bounds__(1024) order_poses_kernel(const int* __restrict
             }
             __syncthreads();
         }
-    for (int i = threadIdx.x; i < m; i += blockDim.x) order[base + i] = base + idx[i];
+    for (int i = threadIdx.x; i < m; i += blockDim.x) order[base + dealt_position(i, deal, tile)] = base + idx[i];
 }
 
 // The same over the poses of several jobs (global pose index gp of the launch).
 __global__ void __launch_bounds__(1024) order_poses_jobs_kernel(const Job* __restrict__ jobs, int n_jobs, int n,
-                                                                int* __restrict__ order) {
+                                                                int* __restrict__ order, int deal, int tile) {
     __shared__ long long key[kOrderSeg];
     __shared__ int idx[kOrderSeg];
     const int base = blockIdx.x * kOrderSeg;
@@ -405,14 +427,7 @@ __global__ void __launch_bounds__(1024) order_poses_jobs_kernel(const Job* __res
         if (i < m) {
             const int gp = base + i;
             const Job& J = jobs[find_job(jobs, n_jobs, gp, false)];
-            const int nm = J.S.n_sc + J.S.n_lig;
-            const int* cn = J.W.cand_n + (size_t)(gp - J.pose0) * nm;
-            long long cost = 0;
-            for (int a = 0; a < nm; ++a) {
-                const int k = cn[a];
-                if (k > 0) cost += (long long)k * k;
-            }
-            c = -cost;
+            c = pose_order_key(J.W, J.S.n_sc + J.S.n_lig, gp - J.pose0);
         }
         key[i] = c;
         idx[i] = i;
@@ -437,15 +452,22 @@ __global__ void __launch_bounds__(1024) order_poses_jobs_kernel(const Job* __res
             }
             __syncthreads();
         }
-    for (int i = threadIdx.x; i < m; i += blockDim.x) order[base + i] = base + idx[i];
+    for (int i = threadIdx.x; i < m; i += blockDim.x) order[base + dealt_position(i, deal, tile)] = base + idx[i];
 }
 
-void launch_order_poses_jobs(const Job* jobs, int n_jobs, int total, int* order, cudaStream_t st) {
-    order_poses_jobs_kernel<<<(total + kOrderSeg - 1) / kOrderSeg, 1024, 0, st>>>(jobs, n_jobs, total, order);
+// deal: full tiles to deal the sorted poses over (one segment only; 0 keeps the sorted order);
+// tile: poses per tile.
+void launch_order_poses_jobs(const Job* jobs, int n_jobs, int total, int* order, cudaStream_t st, int deal,
+                             int tile) {
+    if (total > kOrderSeg || tile < 1) deal = 0;
+    order_poses_jobs_kernel<<<(total + kOrderSeg - 1) / kOrderSeg, 1024, 0, st>>>(jobs, n_jobs, total, order, deal,
+                                                                                  tile);
 }
 
-void launch_order_poses(const DevSystem& S, const DevWork& W, int n, cudaStream_t st) {
-    order_poses_kernel<<<(n + kOrderSeg - 1) / kOrderSeg, 1024, 0, st>>>(W.cand_n, S.n_sc + S.n_lig, n, W.pose_order);
+void launch_order_poses(const DevSystem& S, const DevWork& W, int n, cudaStream_t st, int deal, int tile) {
+    if (n > kOrderSeg || tile < 1) deal = 0;
+    order_poses_kernel<<<(n + kOrderSeg - 1) / kOrderSeg, 1024, 0, st>>>(W, S.n_sc + S.n_lig, n, W.pose_order, deal,
+                                                                         tile);
 }
 
 void launch_contacts(const DevSystem& S, const DevWork& W, int n, cudaStream_t st, bool staged) {

@@ -1899,6 +1899,12 @@ static unsigned pose_blocks(int n, size_t hist_bytes, int blocks_per_sm) {
 }
 
 size_t pose_hist_bytes() { return (size_t)g_resident_blocks * kVorWarps * kHistStride; }
+// Poses per lockstep block (0: the warps take poses one at a time), and the blocks of a launch.
+int pose_tile() { return kLockstep ? kVorWarps : 0; }
+int pose_launch_blocks(int n, size_t hist_bytes, int blocks_per_sm) {
+    if (hist_bytes < kVorWarps * kHistStride) hist_bytes = 0;
+    return (int)pose_blocks(n, hist_bytes, blocks_per_sm);
+}
 int pose_max_blocks_per_sm() { return g_per_sm; }
 int pose_warps_per_block() { return kVorWarps; }
 
