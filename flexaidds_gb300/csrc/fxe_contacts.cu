@@ -340,9 +340,11 @@ contacts_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, long long total) 
     contacts_atom<kStaged>(job.S, job.W, (int)(r / nm), (int)(r % nm), lane, stage[wib], &rstage[kStaged ? wib : 0]);
 }
 
-// The order pose_kernel takes the poses in: costliest first (sum over the pose's atoms of the
-// squared candidate count, which the hull walk's plane tests grow with), so that the slowest
-// poses start early and the launch does not end on one of them while the SMs run dry; then the
+// The order pose_kernel takes the poses in: the poses with the most scored atoms first, among
+// them the costliest first (sum over the pose's atoms of the squared candidate count, which the
+// hull walk's plane tests grow with), so that the slowest poses start early and the launch does
+// not end on one of them while the SMs run dry, and the poses a lockstep block steps through
+// together have as many atoms; then the
 // poses that need no polyhedra (the clash pre-filter rejects them, or they left the grid), so
 // that the warps of a block, which step through the atoms together, are not held by poses that
 // have nothing to do. Sorted in segments of kOrderSeg poses, one block each. The order changes
@@ -373,7 +375,10 @@ __device__ __forceinline__ long long pose_order_key(const DevWork& W, int nm, in
     }
     // (the launch's own test sums the same terms in another order: a pose within rounding of the
     // threshold may be placed on the other side, which only moves it in the queue)
-    return clash >= kClashThreshold ? 1 : -cost;
+    if (clash >= kClashThreshold) return 1;
+    // scored poses with more atoms first (a lockstep block steps through as many atoms as its
+    // largest pose has), then the costliest
+    return -(((long long)nm << 40) | cost);
 }
 
 __global__ void __launch_bounds__(1024) order_poses_kernel(DevWork W, int nm, int n, int* __restrict__ order, int deal,
