@@ -324,6 +324,7 @@ def run_gpu(args):
         lib.fxe_eval_genes(ev.handle, pop, C.cast(hgen[k % N_POPULATIONS].data_ptr(), capi._i),
                            C.c_void_p(hout.data_ptr()))
     e2e_s = 0.0
+    e2e_steps = []
     barrier()
     for k in range(args.steps):
         flush.zero_()
@@ -331,7 +332,8 @@ def run_gpu(args):
         t = time.perf_counter()
         rc = lib.fxe_eval_genes(ev.handle, pop, C.cast(hgen[k % N_POPULATIONS].data_ptr(), capi._i),
                                 C.c_void_p(hout.data_ptr()))
-        e2e_s += time.perf_counter() - t
+        e2e_steps.append(time.perf_counter() - t)
+        e2e_s += e2e_steps[-1]
         if rc != 0:
             raise RuntimeError(lib.fxe_last_error().decode())
     barrier()
@@ -423,6 +425,8 @@ def run_gpu(args):
         "l2": f"flushed between timed steps ({FLUSH_BYTES >> 20} MB write)",
         "parallelism": f"replicas x{world}",
         "e2e": {"value": world * pop * args.steps / e2e_s, "unit": "poses/s",
+                "step_ms": {"median": 1e3 * float(np.median(e2e_steps)), "min": 1e3 * min(e2e_steps),
+                            "max": 1e3 * max(e2e_steps)},
                 "h2d_bytes_per_step": pop * d.n_genes * 4, "d2h_bytes_per_step": pop * capi.CF_DTYPE.itemsize},
         "gpu_launches": launches,
         "autotune": {"pose_blocks_per_sm": tuned_cap, "launch_ms": tuned_ms,
