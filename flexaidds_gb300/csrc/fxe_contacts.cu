@@ -314,12 +314,15 @@ template <bool kStaged>
 __global__ void __launch_bounds__(128)
 contacts_kernel(DevSystem S, DevWork W, int n) {
     __shared__ ContactStage stage[4];
-    __shared__ RigidStage rstage[kStaged ? 4 : 1];
+    RigidStage* rs = nullptr;
+    if constexpr (kStaged) {   // (the in-place form allocates no staging)
+        __shared__ RigidStage rstage[4];
+        rs = &rstage[threadIdx.x >> 5];
+    }
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nm = n_mobile(S);
     if (gw >= n * nm) return;
-    contacts_atom<kStaged>(S, W, gw / nm, gw % nm, threadIdx.x & 31, stage[threadIdx.x >> 5],
-                           &rstage[kStaged ? threadIdx.x >> 5 : 0]);
+    contacts_atom<kStaged>(S, W, gw / nm, gw % nm, threadIdx.x & 31, stage[threadIdx.x >> 5], rs);
 }
 
 // The same over the (pose, mobile atom) items of several jobs.
@@ -328,7 +331,11 @@ __global__ void __launch_bounds__(128)
 contacts_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, long long total) {
     __shared__ Job job_all[4];
     __shared__ ContactStage stage[4];
-    __shared__ RigidStage rstage[kStaged ? 4 : 1];
+    RigidStage* rs = nullptr;
+    if constexpr (kStaged) {
+        __shared__ RigidStage rstage[4];
+        rs = &rstage[threadIdx.x >> 5];
+    }
     const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (gw >= total) return;
@@ -337,7 +344,7 @@ contacts_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, long long total) 
     copy_job(&job, &jobs[j], lane);
     const int nm = n_mobile(job.S);
     const long long r = gw - job.warp0;
-    contacts_atom<kStaged>(job.S, job.W, (int)(r / nm), (int)(r % nm), lane, stage[wib], &rstage[kStaged ? wib : 0]);
+    contacts_atom<kStaged>(job.S, job.W, (int)(r / nm), (int)(r % nm), lane, stage[wib], rs);
 }
 
 // The order pose_kernel takes the poses in: the poses with the most scored atoms first, among
