@@ -65,6 +65,9 @@ __device__ __forceinline__ DrawThreshold draw_threshold(double p) {
 }
 
 constexpr int kGaThreads = 256;
+// The one-block-per-job sorts (replacement, fitness): a wider block, so that each bitonic stage
+// is a couple of exchanges per thread.
+constexpr int kGaSortThreads = 1024;
 constexpr int kGaMaxSort = 4096;   // 2P entries sorted in shared memory: P <= 2048
 
 // Order-preserving 64-bit image of a double that is not a NaN: the images compare as unsigned
@@ -487,7 +490,7 @@ __global__ void __launch_bounds__(kAcceptThreads) ga_accept_kernel(const GaJob* 
 // set is sorted by energy, the best P kept, saved as the generation's snapshot, and the
 // generation counter advanced.
 template <bool kInitial>
-__global__ void __launch_bounds__(kGaThreads) ga_select_kernel(GaJob* __restrict__ all, const int* __restrict__ run) {
+__global__ void __launch_bounds__(kGaSortThreads) ga_select_kernel(GaJob* __restrict__ all, const int* __restrict__ run) {
     __shared__ uint64_t key[kGaMaxSort];
     __shared__ int idx[kGaMaxSort];
     GaJob& J = all[run[blockIdx.x]];
@@ -600,22 +603,33 @@ __global__ void __launch_bounds__(kNicheWarps * 32) ga_niche_kernel(const GaJob*
 // Running sums of the fitness in roulette order (roullete_wheel's walk, LIB/gaboom.cpp:1158-1186)
 // and fitness_stats' total, maximum and mean (LIB/gaboom.cpp:818-840), in order.
 __device__ void fitness_sums(const GaJob& J, const double* fit, int P) {
-    // (fitness_stats' total adds the same terms in the same order as the running sum: one sum)
-    double cum = 0.0, mx = fit[0];
+    // (fitness_stats' total adds the same terms in the same order as the running sum: one sum;
+    // the largest value, the first of equal ones, is found on the order keys, off the
+    // double-precision pipe)
+    double cum = 0.0;
+    uint64_t mk = order_key(fit[0]);
+    int mi = 0;
+#pragma unroll 8
     for (int i = 0; i < P; ++i) {
-        cum += fit[i];
+        const double f = fit[i];
+        cum += f;
         J.fcum[i] = cum;
-        if (fit[i] > mx) mx = fit[i];
+        const uint64_t k = order_key(f);
+        const bool nan = ((uint64_t)__double_as_longlong(f) << 1) > (0x7FF0000000000000ull << 1);
+        if (k > mk && !nan) {   // (a NaN never compares greater)
+            mk = k;
+            mi = i;
+        }
     }
     J.fstat[0] = cum;
-    J.fstat[1] = mx;
+    J.fstat[1] = fit[mi];
     J.fstat[2] = cum / (double)P;
 }
 
 // Fitness of the population (sorted by energy), the roulette order, running sums and
 // fitness_stats. kInitial: the initial population, walked in energy order whatever the model.
 template <bool kInitial>
-__global__ void __launch_bounds__(kGaThreads) ga_fitness_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
+__global__ void __launch_bounds__(kGaSortThreads) ga_fitness_kernel(const GaJob* __restrict__ all, const int* __restrict__ run) {
     // P <= kGaMaxSort / 2: the fitness, the sort keys (then the sorted fitness) and the order
     __shared__ double fval[kGaMaxSort / 2];
     __shared__ uint64_t key[kGaMaxSort / 2];
@@ -669,8 +683,8 @@ __global__ void __launch_bounds__(kGaThreads) ga_fitness_kernel(const GaJob* __r
 void launch_ga_fitness(const GaJob* all, const int* run, int n_jobs, bool initial, cudaStream_t st) {
     ga_decode_kernel<<<dim3(8, n_jobs), kGaThreads, 0, st>>>(all, run);
     ga_niche_kernel<<<dim3(kNicheBlocks, n_jobs), kNicheWarps * 32, 0, st>>>(all, run);
-    if (initial) ga_fitness_kernel<true><<<n_jobs, kGaThreads, 0, st>>>(all, run);
-    else ga_fitness_kernel<false><<<n_jobs, kGaThreads, 0, st>>>(all, run);
+    if (initial) ga_fitness_kernel<true><<<n_jobs, kGaSortThreads, 0, st>>>(all, run);
+    else ga_fitness_kernel<false><<<n_jobs, kGaSortThreads, 0, st>>>(all, run);
 }
 
 // The acceptance kernels' shared memory (beyond the default 48 KB), allowed once per device.
@@ -734,8 +748,8 @@ void launch_ga_niche(const GaJob* all, const int* run, cudaStream_t st) {
 }
 
 void launch_ga_select(GaJob* all, const int* run, int n_jobs, bool initial, cudaStream_t st) {
-    if (initial) ga_select_kernel<true><<<n_jobs, kGaThreads, 0, st>>>(all, run);
-    else ga_select_kernel<false><<<n_jobs, kGaThreads, 0, st>>>(all, run);
+    if (initial) ga_select_kernel<true><<<n_jobs, kGaSortThreads, 0, st>>>(all, run);
+    else ga_select_kernel<false><<<n_jobs, kGaSortThreads, 0, st>>>(all, run);
 }
 
 }  // namespace fxe
