@@ -41,9 +41,10 @@ int pose_tile();
 int pose_launch_blocks(int, size_t, int);
 }
 
-// How the pose order of a polyhedron launch over n poses is dealt: {full tiles to deal the sorted
-// poses over (0: kept sorted), poses per tile}. Only lockstep launches whose tiles all run at
-// once are dealt (launch_order_poses).
+// How the pose order of a polyhedron launch over n poses may be dealt: {full tiles that start
+// together (0: none, the order stays sorted), poses per tile}; the order kernel deals when those
+// tiles are all the launch has or its scored poses do not fill them (launch_order_poses). Only
+// lockstep launches have tiles.
 struct Deal {
     int deal, tile;
 };
@@ -53,8 +54,7 @@ inline Deal order_deal(int precision, int n, size_t hist_bytes, int blocks_per_s
     if (tile < 1) return {0, 0};
     const int blocks = fast ? f32::pose_launch_blocks(n, hist_bytes, blocks_per_sm)
                             : f64::pose_launch_blocks(n, hist_bytes, blocks_per_sm);
-    const int full = n / tile;
-    return {full <= blocks ? full : 0, tile};
+    return {std::min(n / tile, blocks), tile};
 }
 // Face history of a polyhedron launch, large enough for either precision's launch: the warps the
 // device holds at once, kHistStride bytes each (configure_voronoi first).

@@ -356,16 +356,23 @@ contacts_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, long long total) 
 // that the warps of a block, which step through the atoms together, are not held by poses that
 // have nothing to do. Sorted in segments of kOrderSeg poses, one block each. The order changes
 // no result.
-// A launch of lockstep blocks (tiles of `tile` neighbouring queue entries) with no more tiles
-// than the device runs at once takes every tile at the same time, and lasts as long as its
-// slowest tile: there the sorted poses are dealt round-robin over its deal = n / tile full tiles
-// (tile t gets sorted entries t, t + deal, ...), so each tile holds one of the costliest poses and
-// the rejected ones spread over the tiles' last slots.
+// A launch of lockstep blocks takes tiles of `tile` neighbouring queue entries; its first `deal`
+// tiles (as many full tiles as the device runs at once) start together. When they are all the
+// launch has, or when its scored poses do not fill them, the launch lasts about as long as its
+// slowest first tile: there the sorted poses are dealt round-robin over those tiles (tile t gets
+// sorted entries t, t + deal, ...), so each holds one of the costliest poses and the scored poses
+// spread over every SM, the rejected ones taking the tiles' last slots and the later tiles.
+// Otherwise (the scored poses fill more than the first tiles) the sorted order stands.
 constexpr int kOrderSeg = 4096;
 
 // Queue position of sorted entry i of a segment.
 __device__ __forceinline__ int dealt_position(int i, int deal, int tile) {
     return deal > 0 && i < deal * tile ? (i % deal) * tile + i / deal : i;
+}
+
+// Whether a sorted single segment of m poses, n_scored of them scored, is dealt over `deal` tiles.
+__device__ __forceinline__ int deal_tiles(int m, int n_scored, int deal, int tile) {
+    return deal > 0 && (deal == m / tile || n_scored < deal * tile) ? deal : 0;
 }
 
 // The sort key of pose p: minus its cost, or 1 for a pose the polyhedron launch rejects at once.
@@ -392,6 +399,8 @@ __global__ void __launch_bounds__(1024) order_poses_kernel(DevWork W, int nm, in
                                                            int tile) {
     __shared__ long long key[kOrderSeg];
     __shared__ int idx[kOrderSeg];
+    __shared__ int n_scored;
+    if (threadIdx.x == 0) n_scored = 0;
     const int base = blockIdx.x * kOrderSeg;
     const int m = min(kOrderSeg, n - base);
     int len = 1;
@@ -422,7 +431,13 @@ __global__ void __launch_bounds__(1024) order_poses_kernel(DevWork W, int nm, in
             }
             __syncthreads();
         }
-    for (int i = threadIdx.x; i < m; i += blockDim.x) order[base + dealt_position(i, deal, tile)] = base + idx[i];
+    // the scored poses (keys <= 0) of the segment
+    int c = 0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) c += key[i] <= 0;
+    if (c) atomicAdd(&n_scored, c);
+    __syncthreads();
+    const int dl = deal_tiles(m, n_scored, deal, tile);
+    for (int i = threadIdx.x; i < m; i += blockDim.x) order[base + dealt_position(i, dl, tile)] = base + idx[i];
 }
 
 // The same over the poses of several jobs (global pose index gp of the launch).
@@ -430,6 +445,8 @@ __global__ void __launch_bounds__(1024) order_poses_jobs_kernel(const Job* __res
                                                                 int* __restrict__ order, int deal, int tile) {
     __shared__ long long key[kOrderSeg];
     __shared__ int idx[kOrderSeg];
+    __shared__ int n_scored;
+    if (threadIdx.x == 0) n_scored = 0;
     const int base = blockIdx.x * kOrderSeg;
     const int m = min(kOrderSeg, n - base);
     int len = 1;
@@ -464,7 +481,13 @@ __global__ void __launch_bounds__(1024) order_poses_jobs_kernel(const Job* __res
             }
             __syncthreads();
         }
-    for (int i = threadIdx.x; i < m; i += blockDim.x) order[base + dealt_position(i, deal, tile)] = base + idx[i];
+    // the scored poses (keys <= 0) of the segment
+    int c = 0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) c += key[i] <= 0;
+    if (c) atomicAdd(&n_scored, c);
+    __syncthreads();
+    const int dl = deal_tiles(m, n_scored, deal, tile);
+    for (int i = threadIdx.x; i < m; i += blockDim.x) order[base + dealt_position(i, dl, tile)] = base + idx[i];
 }
 
 // deal: full tiles to deal the sorted poses over (one segment only; 0 keeps the sorted order);
