@@ -1260,7 +1260,7 @@ struct fxe_batch {
     fxe_cf* d_out = nullptr;
     fxe_cf* h_out = nullptr;               // pinned
     int* d_next = nullptr;                 // pose queue of the polyhedron launch
-    int* d_order = nullptr;                // [max_poses] its order, costliest first
+    int* d_order = nullptr;                // [max_poses] its order (order_poses_jobs_kernel)
     uint8_t* d_hist = nullptr;             // face history of the polyhedron launch
     size_t hist_bytes = 0;
     int64_t launches = 0;
@@ -1477,7 +1477,7 @@ struct fxe_ga {
     int* d_run = nullptr;               // [max_jobs] running slots of the captured graph
     fxe::Job* d_eval = nullptr;         // [max_jobs] batched-evaluation table of the running slots
     int* d_next = nullptr;              // pose queue of the polyhedron launch
-    int* d_order = nullptr;             // its order, costliest first
+    int* d_order = nullptr;             // its order (order_poses_jobs_kernel)
     int order_cap = 0;
     uint8_t* d_hist = nullptr;          // face history of the polyhedron launch
     size_t hist_bytes = 0;
