@@ -28,7 +28,7 @@ cudaError_t configure_voronoi();
 size_t pose_hist_bytes();
 int pose_max_blocks_per_sm();
 int pose_warps_per_block();
-int pose_tile();
+int pose_tile_for(int, size_t, int);
 int pose_launch_blocks(int, size_t, int);
 }
 namespace f64 {
@@ -37,7 +37,7 @@ cudaError_t configure_voronoi();
 size_t pose_hist_bytes();
 int pose_max_blocks_per_sm();
 int pose_warps_per_block();
-int pose_tile();
+int pose_tile_for(int, size_t, int);
 int pose_launch_blocks(int, size_t, int);
 }
 
@@ -50,7 +50,8 @@ struct Deal {
 };
 inline Deal order_deal(int precision, int n, size_t hist_bytes, int blocks_per_sm) {
     const bool fast = precision == FXE_PRECISION_FAST;
-    const int tile = fast ? f32::pose_tile() : f64::pose_tile();
+    const int tile = fast ? f32::pose_tile_for(n, hist_bytes, blocks_per_sm)
+                          : f64::pose_tile_for(n, hist_bytes, blocks_per_sm);
     if (tile < 1) return {0, 0};
     const int blocks = fast ? f32::pose_launch_blocks(n, hist_bytes, blocks_per_sm)
                             : f64::pose_launch_blocks(n, hist_bytes, blocks_per_sm);

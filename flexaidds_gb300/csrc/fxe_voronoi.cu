@@ -1801,23 +1801,26 @@ __device__ __forceinline__ uint8_t* warp_hist(uint8_t* hist_all) {
     return hist_all ? hist_all + (size_t)(blockIdx.x * kVorWarps + (threadIdx.x >> 5)) * kHistStride : nullptr;
 }
 
+// tile: poses a lockstep block takes at a time (its first `tile` warps score them; the others
+// keep meeting the barriers); unused without lockstep.
 __global__ void __launch_bounds__(kVorWarps * 32)
-pose_kernel(DevSystem S, DevWork W, int n, int* next, uint8_t* hist_all) {
+pose_kernel(DevSystem S, DevWork W, int n, int* next, uint8_t* hist_all, int tile) {
     extern __shared__ __align__(16) unsigned char smem[];
     PoseShared& ps = reinterpret_cast<PoseShared*>(smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     uint8_t* hist = warp_hist(hist_all);
     if (kLockstep) {
-        // the block takes kVorWarps neighbouring poses of the queue at once
+        // the block takes `tile` neighbouring poses of the queue at once
         __shared__ int base_s;
         #pragma unroll 1
         for (;;) {
-            if (threadIdx.x == 0) base_s = atomicAdd(next, kVorWarps);
+            if (threadIdx.x == 0) base_s = atomicAdd(next, tile);
             __syncthreads();
             const int base = base_s;
             __syncthreads();
             if (base >= n) break;
-            const int q = base + (int)(threadIdx.x >> 5);
+            const int w = (int)(threadIdx.x >> 5);
+            const int q = w < tile ? base + w : n;
             score_pose(S, W, q < n ? W.pose_order[q] : -1, lane, ps, hist, n_mobile(S));
             __syncwarp();
         }
@@ -1834,24 +1837,25 @@ pose_kernel(DevSystem S, DevWork W, int n, int* next, uint8_t* hist_all) {
 // from the job table (they stay in L1), keeping shared memory for the polyhedron workspace.
 __global__ void __launch_bounds__(kVorWarps * 32)
 pose_kernel_jobs(const Job* __restrict__ jobs, int n_jobs, int total, int* next, const int* __restrict__ order,
-                 uint8_t* hist_all) {
+                 uint8_t* hist_all, int tile) {
     extern __shared__ __align__(16) unsigned char smem[];
     PoseShared& ps = reinterpret_cast<PoseShared*>(smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     uint8_t* hist = warp_hist(hist_all);
     if (kLockstep) {
-        // the block takes kVorWarps neighbouring poses of the queue at once and steps through as
+        // the block takes `tile` neighbouring poses of the queue at once and steps through as
         // many atoms as the largest of them has
         __shared__ int base_s, steps_s;
         #pragma unroll 1
         for (;;) {
             if (threadIdx.x == 0) {
-                base_s = atomicAdd(next, kVorWarps);
+                base_s = atomicAdd(next, tile);
                 steps_s = 0;
             }
             __syncthreads();
             const int base = base_s;
-            const int q = base + (int)(threadIdx.x >> 5);
+            const int w = (int)(threadIdx.x >> 5);
+            const int q = w < tile ? base + w : total;
             int gp = -1, j = 0;
             if (q < total) {
                 gp = order[q];
@@ -1886,21 +1890,43 @@ static int g_sms = 0, g_per_sm = 0;  // SMs, and blocks of pose_kernel one SM ho
 // Blocks of a launch over n poses: no more than the device holds at once (the warps take poses
 // from a queue), no more than blocks_per_sm per SM when that is set (> 0; the autotuner's
 // occupancy cap), and no more than the face history holds (hist_bytes; 0: no history).
-static unsigned pose_blocks(int n, size_t hist_bytes, int blocks_per_sm) {
-    int b = (n + kVorWarps - 1) / kVorWarps;
-    if (g_resident_blocks > 0 && g_resident_blocks < b) b = g_resident_blocks;
+// Blocks a launch may run at once: as many as the device holds, no more than blocks_per_sm per
+// SM when that is set (> 0), no more than the face history holds (hist_bytes; 0: no history).
+static int pose_max_blocks(size_t hist_bytes, int blocks_per_sm) {
+    int b = g_resident_blocks > 0 ? g_resident_blocks : 1;
     if (blocks_per_sm > 0 && g_sms > 0 && blocks_per_sm < g_per_sm && g_sms * blocks_per_sm < b)
         b = g_sms * blocks_per_sm;
     if (hist_bytes) {
         const size_t cap = hist_bytes / (kVorWarps * kHistStride);
         if ((size_t)b > cap) b = (int)cap;
     }
-    return (unsigned)b;
+    return b > 0 ? b : 1;
+}
+
+// Poses a lockstep block takes at a time (0 without lockstep): all its warps' worth, or fewer
+// when the launch's poses would not reach every block the device runs at once, so that they
+// spread over more SMs (a pose's time is its chain of atoms, shorter with fewer warps sharing the
+// SM's double-precision pipe).
+int pose_tile_for(int n, size_t hist_bytes, int blocks_per_sm) {
+    if (!kLockstep) return 0;
+    if (hist_bytes < kVorWarps * kHistStride) hist_bytes = 0;
+    const int r = pose_max_blocks(hist_bytes, blocks_per_sm);
+    const int t = (int)(((long long)n + r - 1) / r);
+    return t < 1 ? 1 : (t > kVorWarps ? kVorWarps : t);
+}
+
+// Blocks of a launch over n poses: one per tile of poses (per kVorWarps poses without lockstep),
+// no more than pose_max_blocks.
+static unsigned pose_blocks(int n, size_t hist_bytes, int blocks_per_sm) {
+    const int per = kLockstep ? pose_tile_for(n, hist_bytes, blocks_per_sm) : kVorWarps;
+    int b = (n + per - 1) / per;
+    const int r = pose_max_blocks(hist_bytes, blocks_per_sm);
+    if (b > r) b = r;
+    return (unsigned)(b > 0 ? b : 1);
 }
 
 size_t pose_hist_bytes() { return (size_t)g_resident_blocks * kVorWarps * kHistStride; }
-// Poses per lockstep block (0: the warps take poses one at a time), and the blocks of a launch.
-int pose_tile() { return kLockstep ? kVorWarps : 0; }
+// The blocks of a launch.
 int pose_launch_blocks(int n, size_t hist_bytes, int blocks_per_sm) {
     if (hist_bytes < kVorWarps * kHistStride) hist_bytes = 0;
     return (int)pose_blocks(n, hist_bytes, blocks_per_sm);
@@ -1915,8 +1941,8 @@ void launch_poses(const DevSystem& S, const DevWork& W, int n, int* next, uint8_
     if (hist_bytes < kVorWarps * kHistStride) hist = nullptr;
     if (!hist) hist_bytes = 0;
     cudaMemsetAsync(next, 0, sizeof(int), st);
-    pose_kernel<<<pose_blocks(n, hist_bytes, blocks_per_sm), kVorWarps * 32, pose_smem_bytes(), st>>>(S, W, n, next,
-                                                                                                       hist);
+    pose_kernel<<<pose_blocks(n, hist_bytes, blocks_per_sm), kVorWarps * 32, pose_smem_bytes(), st>>>(
+        S, W, n, next, hist, pose_tile_for(n, hist_bytes, blocks_per_sm));
 }
 
 void launch_poses_jobs(const Job* jobs, int n_jobs, int total, int* next, const int* order, uint8_t* hist,
@@ -1925,7 +1951,7 @@ void launch_poses_jobs(const Job* jobs, int n_jobs, int total, int* next, const 
     if (!hist) hist_bytes = 0;
     cudaMemsetAsync(next, 0, sizeof(int), st);
     pose_kernel_jobs<<<pose_blocks(total, hist_bytes, blocks_per_sm), kVorWarps * 32, pose_jobs_smem_bytes(), st>>>(
-        jobs, n_jobs, total, next, order, hist);
+        jobs, n_jobs, total, next, order, hist, pose_tile_for(total, hist_bytes, blocks_per_sm));
 }
 
 cudaError_t configure_voronoi() {
